@@ -1,0 +1,80 @@
+/* TEST ORACLE -- not part of the product.
+ *
+ * CPU restatement (C11 + OpenMP, IEEE binary64, no implicit FMA) of the
+ * reference's sequential NOSB step (src/main_seq.cpp:386-470, with the
+ * bond-associated weights at n1 = n2 = 0, i.e. the classic correspondence
+ * model) plus the critical-stretch bond mask and damage that the drop-in
+ * adds.  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg
+ * may load it, and only as the checker / CPU baseline.
+ *
+ * It is pinned against the reference itself: oracle/_ref (the reference's own
+ * main_seq.cpp + SetupParticleSystem.cpp + matrix.cpp compiled by
+ * oracle/Makefile) reproduces the reference's shipped golden files
+ * byte-for-byte, and tests/golden/ holds full-precision outputs of that
+ * build which this restatement must match (tests/test_oracle_golden.py).
+ *
+ * The operation sequence here is canonical: the CUDA FP64 kernels perform
+ * the same IEEE operations in the same order (explicit fma() where written,
+ * no contraction elsewhere), so the two agree bit-for-bit.
+ */
+#ifndef PD_ORACLE_H
+#define PD_ORACLE_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { PDO_BC_NONE = 0, PDO_BC_VELOCITY = 1, PDO_BC_FIXED = 2 };
+
+typedef struct pdo_problem {
+  int64_t n;               /* particles */
+  const double* x;         /* [n][2] reference positions */
+  const double* vol;       /* [n] volumes */
+  const int64_t* row_ptr;  /* [n+1] family CSR */
+  const int32_t* col;      /* [row_ptr[n]] neighbour ids, ascending per row */
+  const uint8_t* bc;       /* [n] 0 = free, g >= 1 = BC group g-1 (may be NULL) */
+  int32_t n_groups;        /* BC groups */
+  const int32_t* group_kind; /* [n_groups] PDO_BC_VELOCITY / PDO_BC_FIXED */
+  const double* group_val;   /* [n_groups][2] prescribed velocity (VELOCITY) */
+  double E, nu, rho, dt;
+  double s_c;              /* critical stretch; <= 0 disables breaking */
+  double det_guard;        /* relative det(K) guard, e.g. 1e-10 */
+  int32_t nthreads;        /* OpenMP threads, <= 0: runtime default */
+} pdo_problem;
+
+typedef struct pdo_state {
+  double* u;          /* [n][2] displacements (current position - x) */
+  double* v;          /* [n][2] velocities */
+  double* f;          /* [n][2] net force density (reference netF) */
+  uint8_t* alive;     /* [nnz] 1 = bond intact */
+  int32_t* broken;    /* [n] broken-bond count */
+  double* damage;     /* [n] broken / family size */
+  double* kinv;       /* [n][3] K^-1 (11, 12, 22) of the alive bonds */
+  double* mt;         /* [n][2] (sum_j V_j xi_ij) / V_i */
+  double* w;          /* [n][4] V_i * S_i, S = sigma K^-1 (row-major 2x2) */
+  uint8_t* singular;  /* [n] 1 if det guard tripped (S_i = 0) */
+} pdo_state;
+
+/* Families within `cutoff` (strict: sqrt(d2) < cutoff, as
+ * src/SetupParticleSystem.cpp:100-121), ascending neighbour id, minus bonds
+ * that properly cross any crack segment cracks[c] = (ax, ay, bx, by).
+ * Two-call protocol: col == NULL returns the bond count in *nnz_out.
+ * Returns 0 on success, -1 if cap is too small. */
+int pdo_build_families(int64_t n, const double* x, double cutoff, int32_t n_cracks, const double* cracks,
+                       int64_t* row_ptr, int32_t* col, int64_t cap, int64_t* nnz_out, int32_t nthreads);
+
+/* u = v = f = 0, all bonds alive, K^-1 / mt from the full families. */
+int pdo_init(const pdo_problem* pb, pdo_state* st);
+
+/* nsteps reference steps (src/main_seq.cpp:686-699 order).  Returns the
+ * number of bonds broken during these steps (>= 0). */
+int64_t pdo_step(const pdo_problem* pb, pdo_state* st, int32_t nsteps);
+
+/* Plane-stress constants exactly as the device receives them:
+ * c[0] = C11 = C22, c[1] = C12, c[2] = C33 (src/main_seq.cpp:180-201). */
+void pdo_stiffness(double E, double nu, double c[3]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
