@@ -1,0 +1,635 @@
+// C ABI of the GB300 NOSB step (include/pd_gb300.h): context, device-resident
+// state, family/bond set-up, step launches captured in CUDA graphs.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "pd_internal.h"
+
+using pd::Fp64Args;
+
+struct pd_ctx {
+  pd_params p{};
+  cudaStream_t stream = nullptr;
+  std::string err;
+  int64_t n = 0;
+  bool has_particles = false, has_families = false;
+  std::vector<double> h_x;  // host copy of the reference positions (cell-list bbox)
+
+  // per particle
+  double2 *x = nullptr, *u = nullptr, *v = nullptr, *f = nullptr, *acc = nullptr;
+  double *vol = nullptr, *kinv22 = nullptr, *damage = nullptr;
+  double2 *w01 = nullptr, *w23 = nullptr, *kinv01 = nullptr, *mt = nullptr;
+  uint8_t *bc = nullptr, *singular = nullptr;
+  int32_t *broken = nullptr, *fam = nullptr;
+  // BC groups
+  int32_t* gkind = nullptr;
+  double2* gval = nullptr;
+  // families
+  int64_t nnz = 0;
+  int64_t* row_ptr = nullptr;
+  int32_t* col = nullptr;
+  pd::SellLayout sell;
+  double2 *bxi = nullptr, *bgeo = nullptr;
+  double* blim = nullptr;
+  // counters (device) + host mirror of steps
+  unsigned long long* counters = nullptr;
+  int64_t steps = 0;
+  // graphs per step count
+  std::map<int32_t, cudaGraphExec_t> graphs;
+  // drop-in staging (pinned)
+  std::vector<void*> scratch;
+};
+
+namespace {
+
+thread_local std::string g_create_err;
+
+int fail(pd_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+int cuda_fail(pd_ctx* c, cudaError_t e, const char* where) {
+  return fail(c, PD_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define PD_CK(ctx, call)                                  \
+  do {                                                    \
+    cudaError_t e_ = (call);                              \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+  } while (0)
+
+template <typename T>
+void dfree(T*& p) {
+  if (p) cudaFree(p);
+  p = nullptr;
+}
+
+void clear_graphs(pd_ctx* c) {
+  for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+  c->graphs.clear();
+}
+
+void free_families(pd_ctx* c) {
+  dfree(c->row_ptr);
+  dfree(c->col);
+  dfree(c->sell.chunk_base);
+  dfree(c->sell.chunk_w);
+  dfree(c->sell.nbr);
+  dfree(c->bxi);
+  dfree(c->bgeo);
+  dfree(c->blim);
+  c->sell = pd::SellLayout{};
+  c->nnz = 0;
+  c->has_families = false;
+  clear_graphs(c);
+}
+
+void free_particles(pd_ctx* c) {
+  free_families(c);
+  dfree(c->x); dfree(c->u); dfree(c->v); dfree(c->f); dfree(c->acc);
+  dfree(c->vol); dfree(c->kinv22); dfree(c->damage);
+  dfree(c->w01); dfree(c->w23); dfree(c->kinv01); dfree(c->mt);
+  dfree(c->bc); dfree(c->singular); dfree(c->broken); dfree(c->fam);
+  c->n = 0;
+  c->has_particles = false;
+}
+
+double stretch_factor(double s_c) { return s_c > 0.0 ? s_c * (2.0 + s_c) : INFINITY; }
+
+int check_params(pd_ctx* c, const pd_params* p) {
+  if (!p) return fail(c, PD_ERR_ARG, "params is NULL");
+  if (p->precision != PD_FP64 && p->precision != PD_MIXED) return fail(c, PD_ERR_ARG, "unknown precision");
+  if (!(p->rho > 0.0) || !(p->dt > 0.0) || !std::isfinite(p->E) || !(p->nu > -1.0 && p->nu < 1.0) ||
+      !(p->det_guard >= 0.0))
+    return fail(c, PD_ERR_ARG, "invalid material / time-step parameters");
+  if (p->singular_policy != PD_SINGULAR_ZERO && p->singular_policy != PD_SINGULAR_ERROR)
+    return fail(c, PD_ERR_ARG, "unknown singular_policy");
+  return PD_OK;
+}
+
+Fp64Args fp64_args(pd_ctx* c) {
+  Fp64Args a{};
+  a.n = c->n;
+  a.x = c->x; a.vol = c->vol; a.u = c->u; a.v = c->v; a.f = c->f; a.acc = c->acc;
+  a.w01 = c->w01; a.w23 = c->w23; a.kinv01 = c->kinv01; a.kinv22 = c->kinv22; a.mt = c->mt;
+  a.bc = c->bc; a.gkind = c->gkind; a.gval = c->gval;
+  a.broken = c->broken; a.damage = c->damage; a.singular = c->singular; a.fam = c->fam;
+  a.chunk_base = c->sell.chunk_base; a.chunk_w = c->sell.chunk_w; a.nbr = c->sell.nbr;
+  a.bxi = c->bxi; a.bgeo = c->bgeo; a.blim = c->blim;
+  const double E = c->p.E, nu = c->p.nu;
+  const double pre = E / (1.0 - nu * nu);  // getStiffnessTensor, src/main_seq.cpp:185-187
+  a.c11 = pre;
+  a.c12 = nu * pre;
+  a.c33 = (1.0 - nu) * pre;
+  a.dt = c->p.dt;
+  a.dt2 = c->p.dt * c->p.dt;
+  a.inv_rho = 1.0 / c->p.rho;
+  a.det_guard = c->p.det_guard;
+  a.counters = c->counters;
+  return a;
+}
+
+__global__ void k_fam_from_rowptr(int64_t n, const int64_t* rp, int32_t* fam) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) fam[i] = (int32_t)(rp[i + 1] - rp[i]);
+}
+
+// After row_ptr/col exist: SELL layout, bond geometry, per-particle geometry, reset.
+int finish_families(pd_ctx* c) {
+  cudaStream_t s = c->stream;
+  std::string msg;
+  PD_CK(c, cudaMemsetAsync(c->counters, 0, pd::CNT_N * sizeof(unsigned long long), s));
+  int rc = pd::build_sell(c->n, c->row_ptr, c->col, s, &c->sell, c->counters, &msg);
+  if (rc != PD_OK) return fail(c, rc, msg);
+  unsigned long long h[pd::CNT_N];
+  PD_CK(c, cudaMemcpy(h, c->counters, sizeof(h), cudaMemcpyDeviceToHost));
+  if (h[pd::CNT_ERROR])
+    return fail(c, PD_ERR_ARG, "invalid family: neighbour id out of range or a self bond (error word " +
+                                   std::to_string(h[pd::CNT_ERROR]) + ")");
+  const size_t ns = (size_t)(c->sell.nslots > 0 ? c->sell.nslots : 1);
+  PD_CK(c, cudaMalloc(&c->bxi, ns * sizeof(double2)));
+  PD_CK(c, cudaMalloc(&c->bgeo, ns * sizeof(double2)));
+  PD_CK(c, cudaMalloc(&c->blim, ns * sizeof(double)));
+  pd::launch_bond_geometry_fp64(c->n, c->x, c->vol, c->sell, c->row_ptr, stretch_factor(c->p.s_c), c->bxi, c->bgeo,
+                                c->blim, s);
+  if (c->n > 0) k_fam_from_rowptr<<<(unsigned)pd::blocks_for(c->n), pd::kBlock, 0, s>>>(c->n, c->row_ptr, c->fam);
+  PD_CK(c, cudaGetLastError());
+  c->has_families = true;
+  return pd_reset(c);
+}
+
+}  // namespace
+
+extern "C" {
+
+int pd_abi_version(void) { return PD_ABI_VERSION; }
+
+void pd_default_params(pd_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->precision = PD_FP64;
+  p->device = 0;
+  p->E = 72e9;
+  p->nu = 0.33;
+  p->rho = 2440.0;
+  p->dt = 1e-8;
+  p->s_c = 0.0;
+  p->det_guard = 1e-10;
+  p->singular_policy = PD_SINGULAR_ZERO;
+}
+
+int pd_create(const pd_params* p, pd_ctx** out) {
+  if (!out) {
+    g_create_err = "out is NULL";
+    return PD_ERR_ARG;
+  }
+  *out = nullptr;
+  std::unique_ptr<pd_ctx> c(new (std::nothrow) pd_ctx());
+  if (!c) {
+    g_create_err = "out of host memory";
+    return PD_ERR_CAPACITY;
+  }
+  int rc = check_params(c.get(), p);
+  if (rc != PD_OK) {
+    g_create_err = c->err;
+    return rc;
+  }
+  c->p = *p;
+  cudaError_t e = cudaSetDevice(p->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&c->counters, pd::CNT_N * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemset(c->counters, 0, pd::CNT_N * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&c->gkind, PD_MAX_BC_GROUPS * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&c->gval, PD_MAX_BC_GROUPS * sizeof(double2));
+  if (e == cudaSuccess) e = cudaMemset(c->gkind, 0, PD_MAX_BC_GROUPS * sizeof(int32_t));
+  if (e != cudaSuccess) {
+    g_create_err = std::string("pd_create: ") + cudaGetErrorString(e);
+    pd_destroy(c.release());
+    return PD_ERR_CUDA;
+  }
+  *out = c.release();
+  return PD_OK;
+}
+
+int pd_destroy(pd_ctx* c) {
+  if (!c) return PD_OK;
+  cudaSetDevice(c->p.device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  free_particles(c);
+  dfree(c->counters);
+  dfree(c->gkind);
+  dfree(c->gval);
+  for (void* q : c->scratch) cudaFreeHost(q);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return PD_OK;
+}
+
+const char* pd_last_error(const pd_ctx* c) { return c ? c->err.c_str() : g_create_err.c_str(); }
+
+int pd_set_params(pd_ctx* c, const pd_params* p) {
+  if (!c) return PD_ERR_ARG;
+  int rc = check_params(c, p);
+  if (rc != PD_OK) return rc;
+  if (p->device != c->p.device || p->precision != c->p.precision)
+    return fail(c, PD_ERR_ARG, "device and precision are fixed at pd_create");
+  PD_CK(c, cudaSetDevice(c->p.device));
+  const bool s_changed = p->s_c != c->p.s_c;
+  c->p = *p;
+  clear_graphs(c);
+  if (c->has_families && s_changed) {
+    pd::launch_bond_limit_fp64(c->sell.nslots, c->bxi, stretch_factor(c->p.s_c), c->sell.nbr, c->blim, c->stream);
+    PD_CK(c, cudaGetLastError());
+    PD_CK(c, cudaStreamSynchronize(c->stream));
+  }
+  return PD_OK;
+}
+
+int pd_get_params(const pd_ctx* c, pd_params* p) {
+  if (!c || !p) return PD_ERR_ARG;
+  *p = c->p;
+  return PD_OK;
+}
+
+int pd_set_particles(pd_ctx* c, int64_t n, const double* x, const double* vol) {
+  if (!c) return PD_ERR_ARG;
+  if (n < 0 || n > (int64_t)INT32_MAX - 2) return fail(c, PD_ERR_ARG, "n out of range");
+  if (n > 0 && (!x || !vol)) return fail(c, PD_ERR_ARG, "x / vol is NULL");
+  for (int64_t i = 0; i < 2 * n; ++i)
+    if (!std::isfinite(x[i])) return fail(c, PD_ERR_ARG, "non-finite reference position");
+  for (int64_t i = 0; i < n; ++i)
+    if (!(vol[i] > 0.0) || !std::isfinite(vol[i])) return fail(c, PD_ERR_ARG, "volumes must be positive");
+  PD_CK(c, cudaSetDevice(c->p.device));
+  PD_CK(c, cudaStreamSynchronize(c->stream));
+  free_particles(c);
+  c->n = n;
+  const size_t nn = (size_t)(n > 0 ? n : 1);
+  PD_CK(c, cudaMalloc(&c->x, nn * sizeof(double2)));
+  PD_CK(c, cudaMalloc(&c->u, nn * sizeof(double2)));
+  PD_CK(c, cudaMalloc(&c->v, nn * sizeof(double2)));
+  PD_CK(c, cudaMalloc(&c->f, nn * sizeof(double2)));
+  PD_CK(c, cudaMalloc(&c->acc, nn * sizeof(double2)));
+  PD_CK(c, cudaMalloc(&c->w01, nn * sizeof(double2)));
+  PD_CK(c, cudaMalloc(&c->w23, nn * sizeof(double2)));
+  PD_CK(c, cudaMalloc(&c->kinv01, nn * sizeof(double2)));
+  PD_CK(c, cudaMalloc(&c->mt, nn * sizeof(double2)));
+  PD_CK(c, cudaMalloc(&c->vol, nn * sizeof(double)));
+  PD_CK(c, cudaMalloc(&c->kinv22, nn * sizeof(double)));
+  PD_CK(c, cudaMalloc(&c->damage, nn * sizeof(double)));
+  PD_CK(c, cudaMalloc(&c->bc, nn));
+  PD_CK(c, cudaMalloc(&c->singular, nn));
+  PD_CK(c, cudaMalloc(&c->broken, nn * sizeof(int32_t)));
+  PD_CK(c, cudaMalloc(&c->fam, nn * sizeof(int32_t)));
+  PD_CK(c, cudaMemset(c->bc, 0, nn));
+  if (n > 0) {
+    PD_CK(c, cudaMemcpy(c->x, x, (size_t)n * sizeof(double2), cudaMemcpyHostToDevice));
+    PD_CK(c, cudaMemcpy(c->vol, vol, (size_t)n * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  c->h_x.assign(x, x + 2 * n);
+  c->has_particles = true;
+  return PD_OK;
+}
+
+int pd_build_families(pd_ctx* c, double cutoff, int32_t n_cracks, const double* cracks) {
+  if (!c) return PD_ERR_ARG;
+  if (!c->has_particles) return fail(c, PD_ERR_ORDER, "pd_set_particles first");
+  if (n_cracks > 0 && !cracks) return fail(c, PD_ERR_ARG, "cracks is NULL");
+  PD_CK(c, cudaSetDevice(c->p.device));
+  free_families(c);
+  pd::FamilyBuild fb;
+  std::string msg;
+  int rc = pd::build_families_gpu(c->n, c->x, c->h_x.data(), cutoff, n_cracks, cracks, c->stream, &fb, &msg);
+  c->row_ptr = fb.row_ptr;
+  c->col = fb.col;
+  c->nnz = fb.nnz;
+  if (rc != PD_OK) return fail(c, rc, msg);
+  return finish_families(c);
+}
+
+int pd_set_families(pd_ctx* c, const int64_t* row_ptr, const int32_t* col) {
+  if (!c) return PD_ERR_ARG;
+  if (!c->has_particles) return fail(c, PD_ERR_ORDER, "pd_set_particles first");
+  if (!row_ptr) return fail(c, PD_ERR_ARG, "row_ptr is NULL");
+  const int64_t n = c->n;
+  if (row_ptr[0] != 0) return fail(c, PD_ERR_ARG, "row_ptr[0] must be 0");
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t d = row_ptr[i + 1] - row_ptr[i];
+    if (d < 0) return fail(c, PD_ERR_ARG, "row_ptr must be non-decreasing");
+    if (d > PD_MAX_FAMILY) return fail(c, PD_ERR_CAPACITY, "a family exceeds PD_MAX_FAMILY bonds");
+  }
+  const int64_t nnz = row_ptr[n];
+  if (nnz > 0 && !col) return fail(c, PD_ERR_ARG, "col is NULL");
+  PD_CK(c, cudaSetDevice(c->p.device));
+  free_families(c);
+  c->nnz = nnz;
+  PD_CK(c, cudaMalloc(&c->row_ptr, (size_t)(n + 1) * sizeof(int64_t)));
+  PD_CK(c, cudaMalloc(&c->col, (size_t)(nnz > 0 ? nnz : 1) * sizeof(int32_t)));
+  PD_CK(c, cudaMemcpy(c->row_ptr, row_ptr, (size_t)(n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
+  if (nnz > 0) PD_CK(c, cudaMemcpy(c->col, col, (size_t)nnz * sizeof(int32_t), cudaMemcpyHostToDevice));
+  return finish_families(c);
+}
+
+int pd_num_bonds(const pd_ctx* c, int64_t* nnz) {
+  if (!c || !nnz) return PD_ERR_ARG;
+  *nnz = c->nnz;
+  return PD_OK;
+}
+
+int pd_get_families(pd_ctx* c, int64_t* row_ptr, int32_t* col) {
+  if (!c) return PD_ERR_ARG;
+  if (!c->has_families) return fail(c, PD_ERR_ORDER, "no families");
+  PD_CK(c, cudaSetDevice(c->p.device));
+  PD_CK(c, cudaStreamSynchronize(c->stream));
+  if (row_ptr) PD_CK(c, cudaMemcpy(row_ptr, c->row_ptr, (size_t)(c->n + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost));
+  if (col && c->nnz > 0) PD_CK(c, cudaMemcpy(col, c->col, (size_t)c->nnz * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  return PD_OK;
+}
+
+int pd_set_bc(pd_ctx* c, int32_t n_groups, const int32_t* kind, const double* value, const uint8_t* group_of) {
+  if (!c) return PD_ERR_ARG;
+  if (!c->has_particles) return fail(c, PD_ERR_ORDER, "pd_set_particles first");
+  if (n_groups < 0 || n_groups > PD_MAX_BC_GROUPS) return fail(c, PD_ERR_ARG, "n_groups out of range");
+  if (n_groups > 0 && (!kind || !value)) return fail(c, PD_ERR_ARG, "kind / value is NULL");
+  for (int g = 0; g < n_groups; ++g)
+    if (kind[g] != PD_BC_NONE && kind[g] != PD_BC_VELOCITY && kind[g] != PD_BC_FIXED)
+      return fail(c, PD_ERR_ARG, "unknown BC kind");
+  if (group_of)
+    for (int64_t i = 0; i < c->n; ++i)
+      if (group_of[i] > n_groups) return fail(c, PD_ERR_ARG, "group_of refers to a missing group");
+  PD_CK(c, cudaSetDevice(c->p.device));
+  PD_CK(c, cudaStreamSynchronize(c->stream));
+  std::vector<int32_t> k(PD_MAX_BC_GROUPS, PD_BC_NONE);
+  std::vector<double> val(2 * PD_MAX_BC_GROUPS, 0.0);
+  for (int g = 0; g < n_groups; ++g) {
+    k[g] = kind[g];
+    val[2 * g] = value[2 * g];
+    val[2 * g + 1] = value[2 * g + 1];
+  }
+  PD_CK(c, cudaMemcpy(c->gkind, k.data(), k.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+  PD_CK(c, cudaMemcpy(c->gval, val.data(), val.size() * sizeof(double), cudaMemcpyHostToDevice));
+  if (c->n > 0) {
+    if (group_of)
+      PD_CK(c, cudaMemcpy(c->bc, group_of, (size_t)c->n, cudaMemcpyHostToDevice));
+    else
+      PD_CK(c, cudaMemset(c->bc, 0, (size_t)c->n));
+  }
+  return PD_OK;
+}
+
+int pd_reset(pd_ctx* c) {
+  if (!c) return PD_ERR_ARG;
+  if (!c->has_families) return fail(c, PD_ERR_ORDER, "families first");
+  PD_CK(c, cudaSetDevice(c->p.device));
+  cudaStream_t s = c->stream;
+  const size_t nn = (size_t)(c->n > 0 ? c->n : 1);
+  PD_CK(c, cudaMemsetAsync(c->u, 0, nn * sizeof(double2), s));
+  PD_CK(c, cudaMemsetAsync(c->v, 0, nn * sizeof(double2), s));
+  PD_CK(c, cudaMemsetAsync(c->f, 0, nn * sizeof(double2), s));
+  PD_CK(c, cudaMemsetAsync(c->acc, 0, nn * sizeof(double2), s));
+  PD_CK(c, cudaMemsetAsync(c->w01, 0, nn * sizeof(double2), s));
+  PD_CK(c, cudaMemsetAsync(c->w23, 0, nn * sizeof(double2), s));
+  PD_CK(c, cudaMemsetAsync(c->broken, 0, nn * sizeof(int32_t), s));
+  PD_CK(c, cudaMemsetAsync(c->damage, 0, nn * sizeof(double), s));
+  PD_CK(c, cudaMemsetAsync(c->counters, 0, pd::CNT_N * sizeof(unsigned long long), s));
+  pd::launch_sell_reset(c->n, c->row_ptr, c->col, c->sell, s);
+  Fp64Args a = fp64_args(c);
+  pd::launch_init_geometry_fp64(a, s);
+  PD_CK(c, cudaGetLastError());
+  PD_CK(c, cudaStreamSynchronize(s));
+  c->steps = 0;
+  return PD_OK;
+}
+
+int pd_set_state(pd_ctx* c, const double* u, const double* v, const double* f) {
+  if (!c) return PD_ERR_ARG;
+  if (!c->has_particles) return fail(c, PD_ERR_ORDER, "pd_set_particles first");
+  PD_CK(c, cudaSetDevice(c->p.device));
+  PD_CK(c, cudaStreamSynchronize(c->stream));
+  const size_t b = (size_t)c->n * sizeof(double2);
+  if (b == 0) return PD_OK;
+  if (u) PD_CK(c, cudaMemcpy(c->u, u, b, cudaMemcpyHostToDevice));
+  if (v) PD_CK(c, cudaMemcpy(c->v, v, b, cudaMemcpyHostToDevice));
+  if (f) PD_CK(c, cudaMemcpy(c->f, f, b, cudaMemcpyHostToDevice));
+  return PD_OK;
+}
+
+int pd_get_state(pd_ctx* c, double* u, double* v, double* f) {
+  if (!c) return PD_ERR_ARG;
+  if (!c->has_particles) return fail(c, PD_ERR_ORDER, "pd_set_particles first");
+  PD_CK(c, cudaSetDevice(c->p.device));
+  PD_CK(c, cudaStreamSynchronize(c->stream));
+  const size_t b = (size_t)c->n * sizeof(double2);
+  if (b == 0) return PD_OK;
+  if (u) PD_CK(c, cudaMemcpy(u, c->u, b, cudaMemcpyDeviceToHost));
+  if (v) PD_CK(c, cudaMemcpy(v, c->v, b, cudaMemcpyDeviceToHost));
+  if (f) PD_CK(c, cudaMemcpy(f, c->f, b, cudaMemcpyDeviceToHost));
+  return PD_OK;
+}
+
+int pd_get_damage(pd_ctx* c, double* damage) {
+  if (!c || !damage) return PD_ERR_ARG;
+  if (!c->has_families) return fail(c, PD_ERR_ORDER, "families first");
+  PD_CK(c, cudaSetDevice(c->p.device));
+  PD_CK(c, cudaStreamSynchronize(c->stream));
+  if (c->n > 0) PD_CK(c, cudaMemcpy(damage, c->damage, (size_t)c->n * sizeof(double), cudaMemcpyDeviceToHost));
+  return PD_OK;
+}
+
+int pd_get_bond_mask(pd_ctx* c, uint8_t* alive) {
+  if (!c || !alive) return PD_ERR_ARG;
+  if (!c->has_families) return fail(c, PD_ERR_ORDER, "families first");
+  PD_CK(c, cudaSetDevice(c->p.device));
+  if (c->nnz == 0) return PD_OK;
+  uint8_t* d = nullptr;
+  PD_CK(c, cudaMallocAsync(&d, (size_t)c->nnz, c->stream));
+  pd::launch_mask_out(c->n, c->row_ptr, c->sell, d, c->stream);
+  PD_CK(c, cudaGetLastError());
+  PD_CK(c, cudaMemcpyAsync(alive, d, (size_t)c->nnz, cudaMemcpyDeviceToHost, c->stream));
+  PD_CK(c, cudaFreeAsync(d, c->stream));
+  PD_CK(c, cudaStreamSynchronize(c->stream));
+  return PD_OK;
+}
+
+int pd_get_counters(pd_ctx* c, pd_counters* out) {
+  if (!c || !out) return PD_ERR_ARG;
+  PD_CK(c, cudaSetDevice(c->p.device));
+  PD_CK(c, cudaStreamSynchronize(c->stream));
+  unsigned long long h[pd::CNT_N];
+  PD_CK(c, cudaMemcpy(h, c->counters, sizeof(h), cudaMemcpyDeviceToHost));
+  out->bonds_broken = (int64_t)h[pd::CNT_BROKEN];
+  out->singular_events = (int64_t)h[pd::CNT_SINGULAR];
+  out->steps = c->steps;
+  out->device_error = (int32_t)h[pd::CNT_ERROR];
+  out->reserved = 0;
+  return PD_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Launch sequence of nsteps steps on stream s (graph-capturable).
+void enqueue_steps(pd_ctx* c, int32_t nsteps, cudaStream_t s) {
+  const Fp64Args a = fp64_args(c);
+  const bool brk = c->p.s_c > 0.0;
+  pd::launch_drift_fp64(a, s);
+  for (int32_t k = 0; k < nsteps; ++k) {
+    pd::launch_pass_a_fp64(a, brk, s);
+    pd::launch_pass_b_fp64(a, k + 1 < nsteps ? 1 : 0, s);
+  }
+}
+
+int check_after_step(pd_ctx* c) {
+  if (c->p.singular_policy != PD_SINGULAR_ERROR) return PD_OK;
+  unsigned long long h = 0;
+  PD_CK(c, cudaMemcpyAsync(&h, c->counters + pd::CNT_SINGULAR, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  PD_CK(c, cudaStreamSynchronize(c->stream));
+  if (h) return fail(c, PD_ERR_SINGULAR, "det(K) guard tripped for " + std::to_string(h) + " particle update(s)");
+  return PD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pd_step(pd_ctx* c, int32_t nsteps) {
+  if (!c) return PD_ERR_ARG;
+  if (!c->has_families) return fail(c, PD_ERR_ORDER, "families first");
+  if (nsteps < 0) return fail(c, PD_ERR_ARG, "nsteps < 0");
+  if (nsteps == 0 || c->n == 0) return PD_OK;
+  PD_CK(c, cudaSetDevice(c->p.device));
+  auto it = c->graphs.find(nsteps);
+  if (it == c->graphs.end()) {
+    cudaGraph_t g;
+    PD_CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_steps(c, nsteps, c->stream);
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (e != cudaSuccess) return cuda_fail(c, e, "graph capture");
+    cudaGraphExec_t ge;
+    e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(c, e, "graph instantiate");
+    if (c->graphs.size() > 16) clear_graphs(c);
+    it = c->graphs.emplace(nsteps, ge).first;
+  }
+  PD_CK(c, cudaGraphLaunch(it->second, c->stream));
+  c->steps += nsteps;
+  return check_after_step(c);
+}
+
+int pd_synchronize(pd_ctx* c) {
+  if (!c) return PD_ERR_ARG;
+  PD_CK(c, cudaSetDevice(c->p.device));
+  PD_CK(c, cudaStreamSynchronize(c->stream));
+  return PD_OK;
+}
+
+int pd_compute_velocity(pd_ctx* c, const double* u, double* velocity, double* acce, double* netF) {
+  if (!c) return PD_ERR_ARG;
+  if (!c->has_families) return fail(c, PD_ERR_ORDER, "families first");
+  if (!u || !velocity || !acce || !netF) return fail(c, PD_ERR_ARG, "NULL buffer");
+  if (c->n == 0) return PD_OK;
+  PD_CK(c, cudaSetDevice(c->p.device));
+  const size_t b = (size_t)c->n * sizeof(double2);
+  cudaStream_t s = c->stream;
+  PD_CK(c, cudaMemcpyAsync(c->u, u, b, cudaMemcpyHostToDevice, s));
+  PD_CK(c, cudaMemcpyAsync(c->v, velocity, b, cudaMemcpyHostToDevice, s));
+  PD_CK(c, cudaMemcpyAsync(c->acc, acce, b, cudaMemcpyHostToDevice, s));
+  const Fp64Args a = fp64_args(c);
+  pd::launch_pass_a_fp64(a, c->p.s_c > 0.0, s);
+  pd::launch_pass_b_fp64(a, 2, s);
+  PD_CK(c, cudaGetLastError());
+  PD_CK(c, cudaMemcpyAsync(velocity, c->v, b, cudaMemcpyDeviceToHost, s));
+  PD_CK(c, cudaMemcpyAsync(acce, c->acc, b, cudaMemcpyDeviceToHost, s));
+  PD_CK(c, cudaMemcpyAsync(netF, c->f, b, cudaMemcpyDeviceToHost, s));
+  PD_CK(c, cudaStreamSynchronize(s));
+  c->steps += 1;
+  return check_after_step(c);
+}
+
+int pd_step_timed(pd_ctx* c, int32_t nsteps, float* ms) {
+  if (!c || !ms) return PD_ERR_ARG;
+  PD_CK(c, cudaSetDevice(c->p.device));
+  cudaEvent_t e0, e1;
+  PD_CK(c, cudaEventCreate(&e0));
+  PD_CK(c, cudaEventCreate(&e1));
+  PD_CK(c, cudaEventRecord(e0, c->stream));
+  int rc = pd_step(c, nsteps);
+  cudaEventRecord(e1, c->stream);
+  cudaEventSynchronize(e1);
+  cudaEventElapsedTime(ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
+}
+
+int pd_profile_steps(pd_ctx* c, int32_t nsteps, double* ms, int64_t* launches) {
+  if (!c || !ms || !launches) return PD_ERR_ARG;
+  if (!c->has_families) return fail(c, PD_ERR_ORDER, "families first");
+  PD_CK(c, cudaSetDevice(c->p.device));
+  for (int k = 0; k < PD_NUM_KERNELS; ++k) {
+    ms[k] = 0.0;
+    launches[k] = 0;
+  }
+  if (nsteps <= 0 || c->n == 0) return PD_OK;
+  const int nev = 2 * (1 + 2 * nsteps);
+  std::vector<cudaEvent_t> ev(nev);
+  for (auto& e : ev) PD_CK(c, cudaEventCreate(&e));
+  std::vector<int> kind;
+  const Fp64Args a = fp64_args(c);
+  const bool brk = c->p.s_c > 0.0;
+  cudaStream_t s = c->stream;
+  int q = 0;
+  cudaEventRecord(ev[q++], s);
+  pd::launch_drift_fp64(a, s);
+  cudaEventRecord(ev[q++], s);
+  kind.push_back(PD_KERNEL_DRIFT);
+  for (int32_t k = 0; k < nsteps; ++k) {
+    cudaEventRecord(ev[q++], s);
+    pd::launch_pass_a_fp64(a, brk, s);
+    cudaEventRecord(ev[q++], s);
+    kind.push_back(PD_KERNEL_PASS_A);
+    cudaEventRecord(ev[q++], s);
+    pd::launch_pass_b_fp64(a, k + 1 < nsteps ? 1 : 0, s);
+    cudaEventRecord(ev[q++], s);
+    kind.push_back(PD_KERNEL_PASS_B);
+  }
+  PD_CK(c, cudaGetLastError());
+  PD_CK(c, cudaStreamSynchronize(s));
+  for (size_t k = 0; k < kind.size(); ++k) {
+    float t = 0.f;
+    cudaEventElapsedTime(&t, ev[2 * k], ev[2 * k + 1]);
+    ms[kind[k]] += t;
+    launches[kind[k]] += 1;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  c->steps += nsteps;
+  return check_after_step(c);
+}
+
+int pd_host_alloc(int64_t bytes, void** p) {
+  if (!p || bytes < 0) return PD_ERR_ARG;
+  *p = nullptr;
+  if (cudaMallocHost(p, (size_t)(bytes > 0 ? bytes : 1)) != cudaSuccess) return PD_ERR_CUDA;
+  return PD_OK;
+}
+
+int pd_host_free(void* p) {
+  if (p && cudaFreeHost(p) != cudaSuccess) return PD_ERR_CUDA;
+  return PD_OK;
+}
+
+int pd_model_bytes(const pd_ctx* c, double* bytes) {
+  if (!c || !bytes) return PD_ERR_ARG;
+  const double per_particle = c->p.precision == PD_FP64 ? 248.0 : 148.0;
+  *bytes = per_particle * (double)c->n + 11.0 * (double)c->nnz;
+  return PD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,222 @@
+// FP64 explicit NOSB step (the plain form).  Compiled with --fmad=false: the
+// only fused multiply-adds are the explicit fma() calls, written in the same
+// places as the oracle's restatement, so results are bit-identical to it.
+//
+// One thread per particle, bonds walked in family order through the SELL-32
+// layout (every slot load of a warp is one coalesced line).  Per-particle sums
+// are sequential in family order, with no atomics, so results are
+// deterministic and independent of the launch shape.
+//
+// Reference correspondence (src/main_seq.cpp):
+//   k_drift / pass B tail : applyVelocityBC :28-36, updatePositions :386-393,
+//                           applyFixedBC :38-46
+//   k_pass_a              : computeShapeTensors :71-156 (n1=n2=0: one K per
+//                           particle), computeStressTensor :204-268,
+//                           S = sigma K^-1 of computeForceDensityStates :355
+//   k_pass_b              : computeVelocity :396-470 in gather form
+//                           f_i = sum_j V_j (S_i + S_j) xi_ij (= T_ij - T_ji)
+// FP64 operations per bond: pass A 11 (d 2, stretch test 5, D 4), pass B 4.
+#include "pd_internal.h"
+
+namespace pd {
+
+namespace {
+
+__device__ __forceinline__ int64_t slot0(const Fp64Args& a, int64_t i, int* w) {
+  const int64_t c = i >> 5;
+  *w = a.chunk_w[c];
+  return a.chunk_base[c] + (i & 31);
+}
+
+// K^-1 and m/V of particle i over its intact bonds (oracle: kinv_of).
+__device__ void kinv_update(const Fp64Args& a, int64_t i) {
+  int w;
+  const int64_t s0 = slot0(a, i, &w);
+  double k11 = 0.0, k12 = 0.0, k22 = 0.0, mx = 0.0, my = 0.0;
+  int nal = 0;
+  for (int k = 0; k < w; ++k) {
+    const int64_t s = s0 + (int64_t)k * kChunk;
+    if (a.nbr[s] < 0) continue;
+    const double2 e = a.bxi[s];
+    const double2 t = a.bgeo[s];
+    k11 = fma(t.x, e.x, k11);
+    k12 = fma(t.x, e.y, k12);
+    k22 = fma(t.y, e.y, k22);
+    mx = mx + t.x;
+    my = my + t.y;
+    ++nal;
+  }
+  const double det = fma(k11, k22, -(k12 * k12));
+  if (nal == 0 || !(det > a.det_guard * (k11 * k22))) {
+    a.kinv01[i] = make_double2(0.0, 0.0);
+    a.kinv22[i] = 0.0;
+    a.mt[i] = make_double2(0.0, 0.0);
+    a.singular[i] = 1;
+    atomicAdd(a.counters + CNT_SINGULAR, 1ull);
+    return;
+  }
+  const double r = 1.0 / det;
+  a.kinv01[i] = make_double2(k22 * r, -k12 * r);
+  a.kinv22[i] = k11 * r;
+  const double rv = 1.0 / a.vol[i];
+  a.mt[i] = make_double2(mx * rv, my * rv);
+  a.singular[i] = 0;
+}
+
+__global__ void __launch_bounds__(kBlock) k_init_geometry(Fp64Args a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  kinv_update(a, i);
+}
+
+// Velocity BC, drift, fixed BC of particle i; an = f_i / rho.
+__device__ __forceinline__ void drift_one(const Fp64Args& a, int64_t i, double2& v, double2& u, double anx,
+                                          double any) {
+  const int g = a.bc[i];
+  const int kind = g ? a.gkind[g - 1] : PD_BC_NONE;
+  if (kind == PD_BC_VELOCITY) v = a.gval[g - 1];
+  u.x = u.x + (v.x * a.dt + (0.5 * anx) * a.dt2);
+  u.y = u.y + (v.y * a.dt + (0.5 * any) * a.dt2);
+  if (kind == PD_BC_FIXED) u = make_double2(0.0, 0.0);
+}
+
+__global__ void __launch_bounds__(kBlock) k_drift(Fp64Args a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  double2 v = a.v[i], u = a.u[i];
+  const double2 f = a.f[i];
+  drift_one(a, i, v, u, f.x * a.inv_rho, f.y * a.inv_rho);
+  a.v[i] = v;
+  a.u[i] = u;
+}
+
+template <bool BREAK>
+__global__ void __launch_bounds__(kBlock) k_pass_a(Fp64Args a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  int w;
+  const int64_t s0 = slot0(a, i, &w);
+  const double2 ui = a.u[i];
+  double d11 = 0.0, d12 = 0.0, d21 = 0.0, d22 = 0.0;
+  int newly = 0;
+  for (int k = 0; k < w; ++k) {
+    const int64_t s = s0 + (int64_t)k * kChunk;
+    const int j = a.nbr[s];
+    if (j < 0) continue;
+    const double2 uj = a.u[j];
+    const double dx = uj.x - ui.x, dy = uj.y - ui.y;
+    if (BREAK) {
+      const double2 e = __ldcs(&a.bxi[s]);
+      const double q = fma(dx, fma(2.0, e.x, dx), dy * fma(2.0, e.y, dy));
+      if (q > __ldcs(&a.blim[s])) {
+        a.nbr[s] = -2 - j;
+        ++newly;
+        continue;
+      }
+    }
+    const double2 t = __ldcs(&a.bgeo[s]);
+    d11 = fma(dx, t.x, d11);
+    d12 = fma(dx, t.y, d12);
+    d21 = fma(dy, t.x, d21);
+    d22 = fma(dy, t.y, d22);
+  }
+  if (BREAK && newly) {
+    atomicAdd(a.counters + CNT_BROKEN, (unsigned long long)newly);
+    const int32_t b = a.broken[i] + newly;
+    a.broken[i] = b;
+    a.damage[i] = (double)b / (double)a.fam[i];
+    kinv_update(a, i);
+  }
+  if (a.singular[i]) {
+    a.w01[i] = make_double2(0.0, 0.0);
+    a.w23[i] = make_double2(0.0, 0.0);
+    return;
+  }
+  const double2 k01 = a.kinv01[i];
+  const double k11 = k01.x, k12 = k01.y, k22 = a.kinv22[i];
+  // G = D K^-1 = F - I
+  const double g11 = fma(d11, k11, d12 * k12), g12 = fma(d11, k12, d12 * k22);
+  const double g21 = fma(d21, k11, d22 * k12), g22 = fma(d21, k12, d22 * k22);
+  const double e11 = g11, e22 = g22, e12 = 0.5 * (g12 + g21);
+  const double s11 = fma(a.c11, e11, a.c12 * e22);
+  const double s22 = fma(a.c12, e11, a.c11 * e22);
+  const double s12 = a.c33 * e12;
+  const double vi = a.vol[i];
+  a.w01[i] = make_double2(vi * fma(s11, k11, s12 * k12), vi * fma(s11, k12, s12 * k22));
+  a.w23[i] = make_double2(vi * fma(s12, k11, s22 * k12), vi * fma(s12, k12, s22 * k22));
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kBlock) k_pass_b(Fp64Args a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  int w;
+  const int64_t s0 = slot0(a, i, &w);
+  const double2 wa = a.w01[i], wb = a.w23[i], m = a.mt[i];
+  double fx = fma(wa.x, m.x, wa.y * m.y);
+  double fy = fma(wb.x, m.x, wb.y * m.y);
+  for (int k = 0; k < w; ++k) {
+    const int64_t s = s0 + (int64_t)k * kChunk;
+    const int j = a.nbr[s];
+    if (j < 0) continue;
+    const double2 e = __ldcs(&a.bxi[s]);
+    const double2 ja = a.w01[j], jb = a.w23[j];
+    fx = fma(ja.x, e.x, fx);
+    fx = fma(ja.y, e.y, fx);
+    fy = fma(jb.x, e.x, fy);
+    fy = fma(jb.y, e.y, fy);
+  }
+  double2 v = a.v[i];
+  double aox, aoy;
+  if (MODE == 2) {
+    const double2 ao = a.acc[i];
+    aox = ao.x;
+    aoy = ao.y;
+  } else {
+    const double2 fo = a.f[i];
+    aox = fo.x * a.inv_rho;
+    aoy = fo.y * a.inv_rho;
+  }
+  const double anx = fx * a.inv_rho, any = fy * a.inv_rho;
+  v.x = v.x + (0.5 * (aox + anx)) * a.dt;
+  v.y = v.y + (0.5 * (aoy + any)) * a.dt;
+  a.f[i] = make_double2(fx, fy);
+  if (MODE == 2) a.acc[i] = make_double2(anx, any);
+  if (MODE == 1) {
+    double2 u = a.u[i];
+    drift_one(a, i, v, u, anx, any);
+    a.u[i] = u;
+  }
+  a.v[i] = v;
+}
+
+}  // namespace
+
+void launch_init_geometry_fp64(const Fp64Args& a, cudaStream_t s) {
+  if (a.n > 0) k_init_geometry<<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
+}
+
+void launch_drift_fp64(const Fp64Args& a, cudaStream_t s) {
+  if (a.n > 0) k_drift<<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
+}
+
+void launch_pass_a_fp64(const Fp64Args& a, bool breaking, cudaStream_t s) {
+  if (a.n <= 0) return;
+  if (breaking)
+    k_pass_a<true><<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
+  else
+    k_pass_a<false><<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
+}
+
+void launch_pass_b_fp64(const Fp64Args& a, int mode, cudaStream_t s) {
+  if (a.n <= 0) return;
+  const unsigned nb = (unsigned)blocks_for(a.n);
+  if (mode == 0)
+    k_pass_b<0><<<nb, kBlock, 0, s>>>(a);
+  else if (mode == 1)
+    k_pass_b<1><<<nb, kBlock, 0, s>>>(a);
+  else
+    k_pass_b<2><<<nb, kBlock, 0, s>>>(a);
+}
+
+}  // namespace pd

@@ -1,0 +1,105 @@
+// Internal types of the GB300 NOSB library (not installed; see include/pd_gb300.h).
+//
+// Device data layout (HBM), one context = one plate:
+//   per particle (n):  x double2, vol double, u/v/f double2 (FP64 state),
+//                      w01/w23 double2 (W = V sigma K^-1, rows), kinv01 double2
+//                      + kinv22 double (K^-1), mt double2 (m / V), bc uint8,
+//                      broken int32, damage double, singular uint8, fam int32.
+//   per bond:          SELL-32 ("sliced ELL", chunk = 32 consecutive particles
+//                      = one warp, column-major inside a chunk): slot k of
+//                      particle i lives at chunk_base[i/32] + 32*k + (i%32),
+//                      so each bond slot of a warp is one coalesced 128 B (int)
+//                      or 512 B (double2) line.  nbr int32 (j, -1 padding,
+//                      -2-j broken), bxi double2 (xi = x_j - x_i), bgeo double2
+//                      (V_j xi), blim double (((1+s_c)^2-1) |xi|^2).
+//   Precomputing the bond geometry trades HBM bytes for FP64 operations: on
+//   GB300 one FP64 operation costs as much time as ~12 bytes of HBM traffic.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "pd_gb300.h"
+
+namespace pd {
+
+constexpr int kChunk = 32;
+constexpr int kBlock = 256;
+
+// Counters word layout (device int64 array).
+enum { CNT_BROKEN = 0, CNT_SINGULAR = 1, CNT_ERROR = 2, CNT_N = 4 };
+// Device error bits (CNT_ERROR).
+enum { ERR_FAMILY_OVERFLOW = 1, ERR_BAD_NEIGHBOR = 2, ERR_SELF_BOND = 4 };
+
+struct Fp64Args {
+  int64_t n;
+  const double2* __restrict__ x;
+  const double* __restrict__ vol;
+  double2* u;
+  double2* v;
+  double2* f;
+  double2* acc;  // drop-in mode only (pd_compute_velocity)
+  double2* w01;
+  double2* w23;
+  double2* kinv01;
+  double* kinv22;
+  double2* mt;
+  const uint8_t* __restrict__ bc;
+  const int32_t* __restrict__ gkind;
+  const double2* __restrict__ gval;
+  int32_t* broken;
+  double* damage;
+  uint8_t* singular;
+  const int32_t* __restrict__ fam;
+  const int64_t* __restrict__ chunk_base;
+  const int32_t* __restrict__ chunk_w;
+  int32_t* nbr;
+  const double2* __restrict__ bxi;
+  const double2* __restrict__ bgeo;
+  const double* __restrict__ blim;
+  double c11, c12, c33;
+  double dt, dt2, inv_rho, det_guard;
+  unsigned long long* counters;
+};
+
+// ---- family build (pd_family.cu)
+struct FamilyBuild {
+  int64_t nnz = 0;
+  int64_t* row_ptr = nullptr;  // device, n+1
+  int32_t* col = nullptr;      // device, nnz
+};
+// GPU cell list -> CSR.  Returns PD_OK or an error code with msg set.
+int build_families_gpu(int64_t n, const double2* d_x, const double* h_x, double cutoff, int n_cracks,
+                       const double* h_cracks, cudaStream_t s, FamilyBuild* out, std::string* msg);
+// SELL-32 layout of a CSR family (+ FP64 bond geometry).  d_* are device pointers.
+struct SellLayout {
+  int64_t nchunks = 0, nslots = 0;
+  int64_t* chunk_base = nullptr;
+  int32_t* chunk_w = nullptr;
+  int32_t* nbr = nullptr;
+};
+int build_sell(int64_t n, const int64_t* d_row_ptr, const int32_t* d_col, cudaStream_t s, SellLayout* out,
+               unsigned long long* d_counters, std::string* msg);
+void launch_bond_geometry_fp64(int64_t n, const double2* x, const double* vol, const SellLayout& L,
+                               const int64_t* row_ptr, double s2, double2* bxi, double2* bgeo, double* blim,
+                               cudaStream_t s);
+void launch_bond_limit_fp64(int64_t nslots, const double2* bxi, double s2, const int32_t* nbr, double* blim,
+                            cudaStream_t s);
+void launch_mask_out(int64_t n, const int64_t* row_ptr, const SellLayout& L, uint8_t* alive, cudaStream_t s);
+void launch_sell_reset(int64_t n, const int64_t* row_ptr, const int32_t* col, const SellLayout& L, cudaStream_t s);
+// exclusive scan of int64 in[0..n) -> out[0..n], out[n] = total (device)
+void scan_exclusive_i64(const int64_t* in, int64_t* out, int64_t n, cudaStream_t s);
+
+// ---- FP64 step (pd_fp64.cu)
+void launch_init_geometry_fp64(const Fp64Args& a, cudaStream_t s);
+void launch_drift_fp64(const Fp64Args& a, cudaStream_t s);
+void launch_pass_a_fp64(const Fp64Args& a, bool breaking, cudaStream_t s);
+// mode 0: kick; 1: kick + next step's drift; 2: drop-in kick (acc array in/out)
+void launch_pass_b_fp64(const Fp64Args& a, int mode, cudaStream_t s);
+
+inline int64_t blocks_for(int64_t n, int64_t per = kBlock) { return (n + per - 1) / per; }
+
+}  // namespace pd

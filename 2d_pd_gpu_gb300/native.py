@@ -1,0 +1,287 @@
+"""ctypes binding of the C ABI in include/pd_gb300.h (libpd_gb300.so).
+
+The library is the product: there is no CPU fallback.  If it is missing or a
+CUDA device is unavailable, every call fails loudly.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_build", "libpd_gb300.so")
+
+PD_OK = 0
+PD_FP64, PD_MIXED = 0, 1
+PD_BC_NONE, PD_BC_VELOCITY, PD_BC_FIXED = 0, 1, 2
+PD_SINGULAR_ZERO, PD_SINGULAR_ERROR = 0, 1
+PD_KERNEL_NAMES = ("drift", "pass_a", "pass_b")
+PD_ERRORS = {-1: "PD_ERR_ARG", -2: "PD_ERR_CUDA", -3: "PD_ERR_ORDER", -4: "PD_ERR_CAPACITY",
+             -5: "PD_ERR_SINGULAR", -6: "PD_ERR_DEVICE", -7: "PD_ERR_TIMEOUT"}
+
+
+class PdError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{PD_ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Params(ctypes.Structure):
+    _fields_ = [
+        ("precision", ctypes.c_int32),
+        ("device", ctypes.c_int32),
+        ("E", ctypes.c_double),
+        ("nu", ctypes.c_double),
+        ("rho", ctypes.c_double),
+        ("dt", ctypes.c_double),
+        ("s_c", ctypes.c_double),
+        ("det_guard", ctypes.c_double),
+        ("singular_policy", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+    ]
+
+
+class Counters(ctypes.Structure):
+    _fields_ = [
+        ("bonds_broken", ctypes.c_int64),
+        ("singular_events", ctypes.c_int64),
+        ("steps", ctypes.c_int64),
+        ("device_error", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+    ]
+
+
+_vp = ctypes.c_void_p
+_lib = None
+
+# name -> argtypes (restype int unless listed in _RESTYPES)
+_SIGS = {
+    "pd_abi_version": [],
+    "pd_default_params": [ctypes.POINTER(Params)],
+    "pd_create": [ctypes.POINTER(Params), ctypes.POINTER(_vp)],
+    "pd_destroy": [_vp],
+    "pd_last_error": [_vp],
+    "pd_set_params": [_vp, ctypes.POINTER(Params)],
+    "pd_get_params": [_vp, ctypes.POINTER(Params)],
+    "pd_set_particles": [_vp, ctypes.c_int64, _vp, _vp],
+    "pd_build_families": [_vp, ctypes.c_double, ctypes.c_int32, _vp],
+    "pd_set_families": [_vp, _vp, _vp],
+    "pd_num_bonds": [_vp, ctypes.POINTER(ctypes.c_int64)],
+    "pd_get_families": [_vp, _vp, _vp],
+    "pd_set_bc": [_vp, ctypes.c_int32, _vp, _vp, _vp],
+    "pd_reset": [_vp],
+    "pd_set_state": [_vp, _vp, _vp, _vp],
+    "pd_get_state": [_vp, _vp, _vp, _vp],
+    "pd_get_damage": [_vp, _vp],
+    "pd_get_bond_mask": [_vp, _vp],
+    "pd_get_counters": [_vp, ctypes.POINTER(Counters)],
+    "pd_step": [_vp, ctypes.c_int32],
+    "pd_synchronize": [_vp],
+    "pd_compute_velocity": [_vp, _vp, _vp, _vp, _vp],
+    "pd_step_timed": [_vp, ctypes.c_int32, ctypes.POINTER(ctypes.c_float)],
+    "pd_profile_steps": [_vp, ctypes.c_int32, _vp, _vp],
+    "pd_model_bytes": [_vp, ctypes.POINTER(ctypes.c_double)],
+    "pd_host_alloc": [ctypes.c_int64, ctypes.POINTER(_vp)],
+    "pd_host_free": [_vp],
+}
+_RESTYPES = {"pd_default_params": None, "pd_last_error": ctypes.c_char_p}
+
+EXPORTED = tuple(_SIGS)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with __graft_entry__.build() "
+                               "(the CUDA extension is required; there is no CPU fallback)")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, args in _SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = _RESTYPES.get(name, ctypes.c_int)
+        _lib = L
+    return _lib
+
+
+def ptr(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+class PinnedArray:
+    """numpy view of a page-locked host buffer (pd_host_alloc)."""
+
+    def __init__(self, shape, dtype=np.float64):
+        self.nbytes = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        self._p = _vp()
+        rc = lib().pd_host_alloc(self.nbytes, ctypes.byref(self._p))
+        if rc != PD_OK:
+            raise PdError(rc, "pd_host_alloc failed")
+        buf = (ctypes.c_char * max(self.nbytes, 1)).from_address(self._p.value)
+        self.array = np.frombuffer(buf, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
+
+    def free(self):
+        if self._p:
+            self.array = None
+            lib().pd_host_free(self._p)
+            self._p = _vp()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def default_params(**kw):
+    p = Params()
+    lib().pd_default_params(ctypes.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+class Context:
+    """One device-resident plate (a pd_ctx)."""
+
+    def __init__(self, params: Params):
+        self._h = _vp()
+        self._params = params
+        rc = lib().pd_create(ctypes.byref(params), ctypes.byref(self._h))
+        if rc != PD_OK:
+            raise PdError(rc, lib().pd_last_error(None).decode())
+        self.n = 0
+        self.nnz = 0
+
+    # -- plumbing
+    def _ck(self, rc):
+        if rc != PD_OK:
+            raise PdError(rc, lib().pd_last_error(self._h).decode())
+        return rc
+
+    def close(self):
+        if self._h:
+            lib().pd_destroy(self._h)
+            self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    # -- set-up
+    def set_params(self, **kw):
+        p = Params()
+        self._ck(lib().pd_get_params(self._h, ctypes.byref(p)))
+        for k, v in kw.items():
+            setattr(p, k, v)
+        self._ck(lib().pd_set_params(self._h, ctypes.byref(p)))
+
+    def set_particles(self, x, vol):
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 2)
+        vol = np.ascontiguousarray(vol, dtype=np.float64).reshape(-1)
+        self._ck(lib().pd_set_particles(self._h, x.shape[0], ptr(x), ptr(vol)))
+        self.n = x.shape[0]
+
+    def build_families(self, cutoff, cracks=None):
+        cr = np.ascontiguousarray(np.zeros((0, 4)) if cracks is None else cracks, dtype=np.float64).reshape(-1, 4)
+        self._ck(lib().pd_build_families(self._h, float(cutoff), cr.shape[0], ptr(cr) if cr.size else None))
+        self._refresh_nnz()
+
+    def set_families(self, row_ptr, col):
+        rp = np.ascontiguousarray(row_ptr, dtype=np.int64)
+        cl = np.ascontiguousarray(col, dtype=np.int32)
+        self._ck(lib().pd_set_families(self._h, ptr(rp), ptr(cl) if cl.size else None))
+        self._refresh_nnz()
+
+    def _refresh_nnz(self):
+        v = ctypes.c_int64(0)
+        self._ck(lib().pd_num_bonds(self._h, ctypes.byref(v)))
+        self.nnz = v.value
+
+    def families(self):
+        rp = np.zeros(self.n + 1, dtype=np.int64)
+        col = np.zeros(max(self.nnz, 1), dtype=np.int32)
+        self._ck(lib().pd_get_families(self._h, ptr(rp), ptr(col)))
+        return rp, col[: self.nnz]
+
+    def set_bc(self, kinds, values, group_of):
+        k = np.ascontiguousarray(kinds, dtype=np.int32)
+        v = np.ascontiguousarray(values, dtype=np.float64).reshape(-1, 2)
+        g = np.ascontiguousarray(group_of, dtype=np.uint8)
+        self._ck(lib().pd_set_bc(self._h, k.size, ptr(k), ptr(v), ptr(g)))
+
+    # -- state
+    def reset(self):
+        self._ck(lib().pd_reset(self._h))
+
+    def set_state(self, u=None, v=None, f=None):
+        c = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float64).reshape(-1, 2)
+        u, v, f = c(u), c(v), c(f)
+        self._ck(lib().pd_set_state(self._h, ptr(u), ptr(v), ptr(f)))
+
+    def state(self):
+        u = np.zeros((self.n, 2))
+        v = np.zeros((self.n, 2))
+        f = np.zeros((self.n, 2))
+        self._ck(lib().pd_get_state(self._h, ptr(u), ptr(v), ptr(f)))
+        return u, v, f
+
+    def damage(self):
+        d = np.zeros(self.n)
+        self._ck(lib().pd_get_damage(self._h, ptr(d)))
+        return d
+
+    def bond_mask(self):
+        m = np.zeros(max(self.nnz, 1), dtype=np.uint8)
+        self._ck(lib().pd_get_bond_mask(self._h, ptr(m)))
+        return m[: self.nnz]
+
+    def counters(self):
+        c = Counters()
+        self._ck(lib().pd_get_counters(self._h, ctypes.byref(c)))
+        return {"bonds_broken": c.bonds_broken, "singular_events": c.singular_events, "steps": c.steps,
+                "device_error": c.device_error}
+
+    # -- stepping
+    def step(self, nsteps=1):
+        self._ck(lib().pd_step(self._h, int(nsteps)))
+
+    def synchronize(self):
+        self._ck(lib().pd_synchronize(self._h))
+
+    def compute_velocity(self, u, velocity, acce):
+        """The reference GPU wrapper's one-call contract on host arrays (in place)."""
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        netf = np.zeros_like(velocity)
+        self._ck(lib().pd_compute_velocity(self._h, ptr(u), ptr(velocity), ptr(acce), ptr(netf)))
+        return netf
+
+    def step_timed(self, nsteps):
+        ms = ctypes.c_float(0.0)
+        self._ck(lib().pd_step_timed(self._h, int(nsteps), ctypes.byref(ms)))
+        return ms.value
+
+    def profile_steps(self, nsteps):
+        ms = np.zeros(3)
+        launches = np.zeros(3, dtype=np.int64)
+        self._ck(lib().pd_profile_steps(self._h, int(nsteps), ptr(ms), ptr(launches)))
+        return {k: (float(ms[i]), int(launches[i])) for i, k in enumerate(PD_KERNEL_NAMES)}
+
+    def model_bytes(self):
+        b = ctypes.c_double(0.0)
+        self._ck(lib().pd_model_bytes(self._h, ctypes.byref(b)))
+        return b.value

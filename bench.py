@@ -1,0 +1,316 @@
+"""Throughput of the explicit NOSB step on GB300 (bond-updates/s).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (N=1): the 1000 x 1000 FP64 plate -- 1,000,000 particles, ~27.9M
+directed bonds, seeded +-0.01 dx jitter, a pre-crack of seeded length in
+[0.2, 0.5] width at a seeded height, E=72 GPa, nu=0.33, rho=2440 kg/m^3,
+s_c=5e-4 (bond breaking on), top/bottom 3 rows at +-1 m/s, dt = 0.8 CFL.
+One bench step = one time step of the whole plate (drift, pass A, pass B).
+Synthetic data (there is no public dataset for this path).  The state
+(~2 GB of per-particle and per-bond arrays) is far larger than the 129 MB L2,
+so no flush is needed between steps.
+
+Reported: value = bond-updates/s over the timed K steps (CUDA events on the
+context's stream, one graph of K steps); roofline of the dominant kernel
+(per-kernel CUDA events over a second K-step pass); e2e = the same metric
+through the public API with pinned host buffers (state uploaded before and
+downloaded after every step); cpu_baseline = the oracle's C restatement
+(OpenMP, all host cores) on a bounded sample of the same plate.  With
+--impl reference, the reference arm: that CPU restatement alone.
+
+Multi-GPU: independent replicas (the step is not sharded), one per rank,
+launched by torch.distributed.run; value aggregates all ranks over the max
+rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+MEASURED_FP64_DFMA_PER_S = 5.98e11  # DFMA warp-lane issue rate measured on this GB300 (profiles/fp64_alu_peak.md)
+
+
+def load_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clock and throttle reasons during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.gpu)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            for k, nm in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class Comm:
+    """Host-side barrier / max over ranks (gloo); a no-op at N=1."""
+
+    def __init__(self):
+        self.rank, self.world, self.local = dist_env()
+        self.dist = None
+        if self.world > 1:
+            import torch.distributed as dist
+
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, v):
+        if not self.dist:
+            return v
+        import torch
+
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v):
+        if not self.dist:
+            return v
+        import torch
+
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.dist:
+            self.dist.destroy_process_group()
+
+
+def byte_model(precision, n, nb):
+    """Algorithmic bytes per launch (each array once per pass that must touch it)."""
+    if precision == "fp64":
+        return {"pass_a": 88.0 * n + 6.0 * nb, "pass_b": 160.0 * n + 5.0 * nb, "drift": 64.0 * n,
+                "step": 248.0 * n + 11.0 * nb}
+    return {"pass_a": 56.0 * n + 6.0 * nb, "pass_b": 92.0 * n + 5.0 * nb, "drift": 40.0 * n,
+            "step": 148.0 * n + 11.0 * nb}
+
+
+def fp64_ops(n, nb):
+    """FP64 operations per step of the FP64 form (pass A 11/bond + ~35/particle,
+    pass B 4/bond + ~30/particle), for the FP64-ALU fraction."""
+    return 15.0 * nb + 65.0 * n
+
+
+def cpu_step_rate(plate, steps, nthreads, s_c=None):
+    import pd_oracle as po
+
+    rp, col = po.build_families(plate.x, plate.cutoff, plate.cracks, nthreads=nthreads)
+    sim = po.OracleSim(plate.x, plate.vol, rp, col, E=plate.material.E, nu=plate.material.nu,
+                       rho=plate.material.rho, dt=plate.dt, s_c=plate.material.s_c if s_c is None else s_c,
+                       bc=plate.group_of, group_kind=plate.group_kind, group_val=plate.group_val, nthreads=nthreads)
+    sim.step(1)  # first touch
+    t0 = time.perf_counter()
+    sim.step(steps)
+    dt = time.perf_counter() - t0
+    return int(rp[-1]), dt
+
+
+def run_reference(args, comm):
+    """Reference arm: the oracle's C restatement of the reference step, all host cores."""
+    if comm.rank != 0:
+        return
+    pdg = importlib.import_module("2d_pd_gpu_gb300")
+    plate = pdg.plates.config_plate_scale(side=args.side, seed=args.seed)
+    nth = os.cpu_count() or 1
+    import pd_oracle as po
+
+    rp, col = po.build_families(plate.x, plate.cutoff, plate.cracks, nthreads=nth)
+    sim = po.OracleSim(plate.x, plate.vol, rp, col, E=plate.material.E, nu=plate.material.nu,
+                       rho=plate.material.rho, dt=plate.dt, s_c=plate.material.s_c, bc=plate.group_of,
+                       group_kind=plate.group_kind, group_val=plate.group_val, nthreads=nth)
+    nb = int(rp[-1])
+    sim.step(max(args.warmup, 1))
+    t0 = time.perf_counter()
+    sim.step(args.steps)
+    secs = time.perf_counter() - t0
+    v = nb * args.steps / secs
+    sample = f"{args.steps} full steps of the {args.side}x{args.side} FP64 plate ({nb} bonds), {nth} threads"
+    print(json.dumps({
+        "impl": "reference", "metric": "bond-updates/s", "value": v, "unit": "bond-updates/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"plate{args.side}x{args.side}-fp64-crack-sc5e-4", "particles": plate.n, "bonds": nb,
+                   "precision": "fp64", "parallelism": "host threads"},
+        "cpu_baseline": {"value": v, "unit": "bond-updates/s", "cores": nth, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": "bond-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def run_ours(args, comm):
+    pdg = importlib.import_module("2d_pd_gpu_gb300")
+    nat = pdg.native
+    prec = args.precision
+    plate = pdg.plates.config_plate_scale(side=args.side, seed=args.seed + comm.rank)
+    device = comm.local
+    ctx = plate.context(precision=nat.PD_FP64 if prec == "fp64" else nat.PD_MIXED, device=device)
+    n, nb = ctx.n, ctx.nnz
+    sampler = ClockSampler(device)
+    sampler.start()
+    ctx.step(args.warmup)
+    ctx.synchronize()
+    comm.barrier()
+    ms = ctx.step_timed(args.steps)
+    comm.barrier()
+    ms_max = comm.max(ms)
+    bonds_all = comm.sum(nb * args.steps)
+    value = bonds_all / (ms_max / 1e3)
+    # per-kernel durations (CUDA events around each launch on the context stream)
+    prof = ctx.profile_steps(args.steps)
+    clocks = sampler.stop()
+    model = byte_model(prec, n, nb)
+    share = {k: prof[k][0] for k in prof}
+    tot = sum(share.values())
+    dom = max(("pass_a", "pass_b"), key=lambda k: share[k])
+    avg_ms = prof[dom][0] / max(prof[dom][1], 1)
+    peaks, peak_kind = load_peaks()
+    achieved = model[dom] / (avg_ms / 1e3) / 1e9
+    kernels = {k: {"launches": prof[k][1], "avg_ms": prof[k][0] / max(prof[k][1], 1),
+                   "share": prof[k][0] / tot if tot else None,
+                   "achieved_gbs": (model[k] / (prof[k][0] / max(prof[k][1], 1) / 1e3) / 1e9) if prof[k][1] else None}
+               for k in prof}
+    step_ms = ms_max / args.steps
+    result = {
+        "metric": "bond-updates/s", "value": value, "unit": "bond-updates/s", "n_gpus": comm.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32+f64",
+        "data": "synthetic (seeded plate generator)",
+        "config": {"workload": f"plate{args.side}x{args.side}-{prec}-crack-sc5e-4", "particles": n, "bonds": nb,
+                   "precision": prec, "parallelism": f"replicas x{comm.world}",
+                   "l2": "inputs larger than L2 (~2 GB state vs 129 MB L2)"},
+        "gpu_launches": 1 + 2 * args.steps,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                     "algorithmic_bytes_per_launch": model[dom]},
+        "kernels": kernels,
+        "clocks": clocks,
+    }
+    if prec == "fp64":
+        ops = fp64_ops(n, nb) / (step_ms / 1e3)
+        result["fp64_alu"] = {"ops_per_s": ops, "peak_ops_per_s": MEASURED_FP64_DFMA_PER_S,
+                              "frac": ops / MEASURED_FP64_DFMA_PER_S, "ops_per_step": fp64_ops(n, nb)}
+    # end to end through the public API with pinned host buffers, every step
+    if not args.no_e2e:
+        esteps = min(args.steps, args.e2e_steps)
+        bufs = [nat.PinnedArray((n, 2)) for _ in range(3)]
+        u, v, f = (b.array for b in bufs)
+        got = ctx.state()
+        u[:], v[:], f[:] = got
+        comm.barrier()
+        t0 = time.perf_counter()
+        for _ in range(esteps):
+            ctx._ck(nat.lib().pd_set_state(ctx.handle, nat.ptr(u), nat.ptr(v), nat.ptr(f)))
+            ctx._ck(nat.lib().pd_step(ctx.handle, 1))
+            ctx._ck(nat.lib().pd_get_state(ctx.handle, nat.ptr(u), nat.ptr(v), nat.ptr(f)))
+        secs = comm.max(time.perf_counter() - t0)
+        result["e2e"] = {"value": comm.sum(nb * esteps) / secs, "unit": "bond-updates/s",
+                         "h2d_bytes_per_step": 3 * 16 * n, "d2h_bytes_per_step": 3 * 16 * n, "steps": esteps,
+                         "api": "pd_set_state(u,v,f) -> pd_step(1) -> pd_get_state(u,v,f), pinned host buffers"}
+        for b in bufs:
+            b.free()
+    ctx.close()
+    if comm.rank == 0 and not args.no_cpu:
+        nth = os.cpu_count() or 1
+        nbc, secs = cpu_step_rate(plate, args.cpu_steps, nth)
+        result["cpu_baseline"] = {"value": nbc * args.cpu_steps / secs, "unit": "bond-updates/s", "cores": nth,
+                                  "kind": "port",
+                                  "sample": f"{args.cpu_steps} steps of the same {args.side}x{args.side} plate "
+                                            f"({nbc} bonds), oracle C restatement, OpenMP {nth} threads"}
+    if comm.rank == 0:
+        print(json.dumps(result), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--side", type=int, default=1000)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    comm = Comm()
+    try:
+        if args.impl == "reference":
+            run_reference(args, comm)
+        else:
+            run_ours(args, comm)
+    finally:
+        comm.close()
+
+
+if __name__ == "__main__":
+    main()

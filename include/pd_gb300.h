@@ -1,0 +1,189 @@
+/* pd_gb300.h -- C ABI of the GB300 (sm_103a) explicit NOSB peridynamics step.
+ *
+ * This is the drop-in boundary that replaces the reference's mechanics call
+ * surface (EricYJA/2D_PD_GPU).  Every entry point below names the reference
+ * interface it stands in for.  Plain C types only; every call returns an int
+ * status (PD_OK = 0, negative on error) and pd_last_error() explains it.  The
+ * reference has no return codes (errors go to cout, src/main_seq.cpp:61).
+ *
+ * Model: 2-D plane-stress classic NOSB (correspondence) peridynamics,
+ * influence function 1, critical-stretch bond breaking, velocity Verlet in
+ * the reference's step order (src/main_seq.cpp:686-699):
+ *     velocity BC -> drift (updatePositions) -> fixed BC -> force + kick.
+ * State lives on the device (one context = one plate = one CUDA stream);
+ * the host only crosses at set-up, explicit get/set, and step launches.
+ *
+ * Units are the caller's (the reference uses mm/s/kg/MPa, the plate
+ * workloads SI).  Positions are [n][2] interleaved doubles, as the
+ * reference's Particle::initialPositions.
+ */
+#ifndef PD_GB300_H
+#define PD_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PD_ABI_VERSION 1
+
+/* status codes */
+#define PD_OK 0
+#define PD_ERR_ARG (-1)       /* bad argument (size, pointer, value) */
+#define PD_ERR_CUDA (-2)      /* CUDA runtime error (see pd_last_error) */
+#define PD_ERR_ORDER (-3)     /* call out of order (e.g. step before families) */
+#define PD_ERR_CAPACITY (-4)  /* a family exceeds PD_MAX_FAMILY, or out of memory */
+#define PD_ERR_SINGULAR (-5)  /* det(K) guard tripped and policy is PD_SINGULAR_ERROR */
+#define PD_ERR_DEVICE (-6)    /* a device-side check failed (error word set) */
+#define PD_ERR_TIMEOUT (-7)   /* a bounded device wait gave up */
+
+#define PD_MAX_FAMILY 128     /* bonds per particle */
+#define PD_MAX_BC_GROUPS 255
+#define PD_MAX_CRACKS 64
+
+/* numerical form */
+#define PD_FP64 0   /* IEEE binary64 throughout; bit-identical to the oracle */
+#define PD_MIXED 1  /* FP32 bond arithmetic, FP64 K^-1 + det guard, compensated sums */
+
+/* boundary-condition group kinds (src/main_seq.cpp:15-46) */
+#define PD_BC_NONE 0
+#define PD_BC_VELOCITY 1  /* applyVelocityBC: v := value at the start of each step */
+#define PD_BC_FIXED 2     /* applyFixedBC: position := reference position after the drift */
+
+/* what a singular shape tensor does (the reference GPU path substitutes the
+ * identity, include/mechanics.cuh:29-37; its CPU path divides by zero,
+ * src/matrix.cpp:121-126) */
+#define PD_SINGULAR_ZERO 0   /* S_i := 0 for that particle, counted in pd_counters */
+#define PD_SINGULAR_ERROR 1  /* pd_step returns PD_ERR_SINGULAR */
+
+typedef struct pd_ctx pd_ctx;
+
+typedef struct pd_params {
+  int32_t precision;       /* PD_FP64 or PD_MIXED */
+  int32_t device;          /* CUDA device ordinal */
+  double E;                /* Young's modulus */
+  double nu;               /* Poisson ratio (plane stress, src/main_seq.cpp:180-188) */
+  double rho;              /* mass density (src/main_seq.cpp:389 massDensity) */
+  double dt;               /* time step (src/main_seq.cpp:657 stepSize) */
+  double s_c;              /* critical stretch; <= 0 disables bond breaking */
+  double det_guard;        /* singular if det(K) <= det_guard * K11 * K22 */
+  int32_t singular_policy; /* PD_SINGULAR_ZERO / PD_SINGULAR_ERROR */
+  int32_t reserved;
+} pd_params;
+
+typedef struct pd_counters {
+  int64_t bonds_broken;    /* total bonds broken since pd_reset */
+  int64_t singular_events; /* det-guard trips since pd_reset */
+  int64_t steps;           /* steps taken since pd_reset */
+  int32_t device_error;    /* device error word (0 = none) */
+  int32_t reserved;
+} pd_counters;
+
+/* ---------------------------------------------------------------- context */
+
+int pd_abi_version(void);
+void pd_default_params(pd_params* p);
+
+/* Creates a context (device buffers are allocated by later calls).  There is
+ * no reference counterpart: the reference GPU wrapper allocates, copies and
+ * frees everything on every call (include/mechanics.cuh:963-1135). */
+int pd_create(const pd_params* p, pd_ctx** out);
+int pd_destroy(pd_ctx* ctx);
+/* Message for the last failing call on ctx (ctx == NULL: last pd_create). */
+const char* pd_last_error(const pd_ctx* ctx);
+/* Material / time-step / stretch update; bond data is refreshed in place. */
+int pd_set_params(pd_ctx* ctx, const pd_params* p);
+int pd_get_params(const pd_ctx* ctx, pd_params* p);
+
+/* --------------------------------------------------------------- problem */
+
+/* Reference positions x[n][2] and volumes vol[n].  Replaces the particle
+ * arrays built by computeInitialPositions / readMeshFile
+ * (include/SetupParticleSystem.h:24-25) and the per-call H2D copies of
+ * include/mechanics.cuh:1050-1060. */
+int pd_set_particles(pd_ctx* ctx, int64_t n, const double* x, const double* vol);
+
+/* Families on the GPU: every j != i with sqrt(|x_j - x_i|^2) < cutoff,
+ * ascending j, minus bonds that properly cross one of the n_cracks crack
+ * segments cracks[c] = (ax, ay, bx, by).  Replaces findNeighbor
+ * (src/SetupParticleSystem.cpp:100-121; the reference passes
+ * cutoff = 1.01 * dx * horizon) and buildLocalNeighborlist
+ * (src/main_seq.cpp:49-68).  Resets the state. */
+int pd_build_families(pd_ctx* ctx, double cutoff, int32_t n_cracks, const double* cracks);
+
+/* Families from the host, CSR (row_ptr[n+1] int64, col[row_ptr[n]] int32,
+ * ascending per row), e.g. the reference's Particle::neighbors.  Resets. */
+int pd_set_families(pd_ctx* ctx, const int64_t* row_ptr, const int32_t* col);
+
+int pd_num_bonds(const pd_ctx* ctx, int64_t* nnz);
+int pd_get_families(pd_ctx* ctx, int64_t* row_ptr, int32_t* col);
+
+/* Boundary-condition groups: group_of[i] = 0 (free) or g in 1..n_groups;
+ * group g-1 has kind[g-1] and value[g-1][2] (velocity for PD_BC_VELOCITY).
+ * Replaces the index sets of defineBoundarySet
+ * (src/SetupParticleSystem.cpp:513-529) as used by applyVelocityBC /
+ * applyFixedBC (src/main_seq.cpp:28-46).  A particle is in at most one group. */
+int pd_set_bc(pd_ctx* ctx, int32_t n_groups, const int32_t* kind, const double* value,
+              const uint8_t* group_of);
+
+/* ----------------------------------------------------------------- state */
+
+/* u = v = f = 0, every family bond intact, damage 0, counters 0. */
+int pd_reset(pd_ctx* ctx);
+/* Any pointer may be NULL (left unchanged).  u = current - reference position. */
+int pd_set_state(pd_ctx* ctx, const double* u, const double* v, const double* f);
+int pd_get_state(pd_ctx* ctx, double* u, double* v, double* f);
+/* damage[n] = broken / family size (the reference's Particle::damageStatus,
+ * src/main_seq.cpp:588, with the critical-stretch law instead of Mazars). */
+int pd_get_damage(pd_ctx* ctx, double* damage);
+/* alive[nnz] in family (CSR) order, 1 = intact. */
+int pd_get_bond_mask(pd_ctx* ctx, uint8_t* alive);
+int pd_get_counters(pd_ctx* ctx, pd_counters* c);
+
+/* ------------------------------------------------------------------ step */
+
+/* nsteps full steps on the device (one CUDA graph per distinct nsteps).
+ * Equivalent to nsteps passes of the reference loop body
+ * src/main_seq.cpp:686-699 (applyVelocityBC, updatePositions, applyFixedBC,
+ * computeVelocity).  Asynchronous unless an error check needs the host. */
+int pd_step(pd_ctx* ctx, int32_t nsteps);
+int pd_synchronize(pd_ctx* ctx);
+
+/* One force + kick with host buffers, the reference GPU wrapper's contract
+ * (compute_velocity_GPU_host, include/mechanics.cuh:867-1136, called from
+ * src/main.cu:628): reads the displacement u[n][2] (current position minus
+ * reference position), velocity[n][2] and acce[n][2]; writes
+ * velocity += 0.5 (acce + f/rho) dt, acce = f/rho and netF = f.  Device
+ * buffers stay allocated between calls.  The bond mask persists across calls
+ * and breaks bonds as in pd_step when s_c > 0. */
+int pd_compute_velocity(pd_ctx* ctx, const double* u, double* velocity, double* acce, double* netF);
+
+/* Page-locked host buffers for pd_set_state / pd_get_state /
+ * pd_compute_velocity (full-bandwidth host<->device copies).  No reference
+ * counterpart (the reference copies from pageable std::vector storage,
+ * include/mechanics.cuh:976-991). */
+int pd_host_alloc(int64_t bytes, void** p);
+int pd_host_free(void* p);
+
+/* ---------------------------------------------------------- measurement */
+
+/* pd_step(nsteps) bracketed by CUDA events on the context's stream;
+ * *ms = elapsed device time. */
+int pd_step_timed(pd_ctx* ctx, int32_t nsteps, float* ms);
+
+#define PD_KERNEL_DRIFT 0
+#define PD_KERNEL_PASS_A 1   /* stretch test, D, stress, W = V sigma K^-1 */
+#define PD_KERNEL_PASS_B 2   /* force gather + kick (+ next drift) */
+#define PD_NUM_KERNELS 3
+/* nsteps steps launched kernel by kernel with an event pair around every
+ * launch; ms[k] = summed device time of kernel k, launches[k] = launch count. */
+int pd_profile_steps(pd_ctx* ctx, int32_t nsteps, double* ms, int64_t* launches);
+
+/* Algorithmic bytes per step of the dominant kernels (fixed byte model:
+ * FP64 248 B/particle + 11 B/bond, mixed 148 B/particle + 11 B/bond). */
+int pd_model_bytes(const pd_ctx* ctx, double* bytes_per_step);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PD_GB300_H */

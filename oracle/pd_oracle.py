@@ -214,7 +214,7 @@ def read_ref_output(path, n_hint=None, hassa=False):
         o += 4
         arr = np.frombuffer(b, "<f8", 8 * n, o).reshape(4, n, 2).copy()
         o += 64 * n
-        steps[s] = {"y": arr[0], "v": arr[1], "f": arr[2], "a": arr[3]}
+        steps[s] = {"u": arr[0], "v": arr[1], "f": arr[2], "a": arr[3]}
     out["steps"] = steps
     return out
 

@@ -7,7 +7,7 @@
 // functions in the order of the reference's step loop
 // (src/main_seq.cpp:680-715):
 //     applyVelocityBC -> updatePositions -> applyFixedBC -> computeVelocity
-// and dumps positions, velocities, net force and acceleration at full
+// and dumps displacements, velocities, net force and acceleration at full
 // precision (binary doubles), so that the project's C restatement (oracle/
 // pd_oracle.c) and the CUDA path can be checked against the reference itself.
 //
@@ -77,11 +77,14 @@ struct Writer {
   }
 };
 
-// Dump one step: int32 step, then y, v, netF, acce as N x 2 doubles each.
+// Dump one step: int32 step, then u, v, netF, acce as N x 2 doubles each.
+// u = currentPositions - initialPositions is formed in long double before the
+// rounding to double, so it keeps the reference's full precision.
 void dump_step(Writer& w, int step, const vector<Particle>& P, const vector<vector<long double>>& v,
                const vector<vector<long double>>& f, const vector<vector<long double>>& a) {
   w.put<int32_t>(step);
-  for (const auto& p : P) { w.put<double>((double)p.currentPositions[0]); w.put<double>((double)p.currentPositions[1]); }
+  for (const auto& p : P)
+    for (int m = 0; m < 2; ++m) w.put<double>((double)(p.currentPositions[m] - p.initialPositions[m]));
   w.vec2(v); w.vec2(f); w.vec2(a);
 }
 

@@ -1,0 +1,191 @@
+"""FP64 CUDA path (through the C ABI) vs the oracle and the reference fixtures.
+
+The FP64 kernels perform the oracle's IEEE operations in the oracle's order
+(--fmad=false + the same explicit fma() calls), so the bar here is bit
+equality for displacements, velocities, forces, the bond mask and damage;
+against the reference's own outputs the bar is the benchmark spec's 1e-10
+(normwise) on velocities/displacements, see test_oracle_golden.py for the
+reference's long-double floor on the Hassa mesh.
+"""
+import numpy as np
+import pytest
+
+from conftest import hassa_oracle, normwise, plate_oracle
+from test_oracle_golden import F_TOL, V_TOL, u_tol
+
+pytestmark = pytest.mark.gpu
+
+
+def _hassa_ctx(pdg, h):
+    n = h["x"].shape[0]
+    dx, hor, E, nu, rho, dt = h["params"]
+    ctx = pdg.native.Context(pdg.default_params(E=E, nu=nu, rho=rho, dt=dt, s_c=0.0))
+    ctx.set_particles(h["x"], h["vol"])
+    ctx.build_families(1.01 * dx * hor)
+    g = np.zeros(n, np.uint8)
+    g[h["top"]] = 1
+    g[h["bottom"]] = 2
+    ctx.set_bc([pdg.native.PD_BC_VELOCITY, pdg.native.PD_BC_FIXED], [[0.0, 5.0], [0.0, 0.0]], g)
+    return ctx
+
+
+def _assert_same(ctx, sim):
+    u, v, f = ctx.state()
+    assert np.array_equal(u, sim.u), f"u differs: {np.abs(u - sim.u).max()}"
+    assert np.array_equal(v, sim.v), f"v differs: {np.abs(v - sim.v).max()}"
+    assert np.array_equal(f, sim.f), f"f differs: {np.abs(f - sim.f).max()}"
+    assert np.array_equal(ctx.bond_mask(), sim.mask)
+    assert np.array_equal(ctx.damage(), sim.damage)
+
+
+def test_gpu_families_hassa_match_reference(pdg, hassa):
+    ctx = _hassa_ctx(pdg, hassa)
+    rp, col = ctx.families()
+    assert np.array_equal(rp, hassa["row_ptr"]) and np.array_equal(col, hassa["col"])
+
+
+def test_gpu_families_plate_with_crack_match_oracle(pdg, po):
+    p = pdg.plates.config_plate_100(seed=5)
+    ctx = p.context()
+    rp, col = ctx.families()
+    orp, ocol = po.build_families(p.x, p.cutoff, p.cracks)
+    assert np.array_equal(rp, orp) and np.array_equal(col, ocol)
+    assert int(np.diff(rp).max()) == 28
+
+
+def test_gpu_hassa_matches_reference_fixture(pdg, po, hassa):
+    ctx = _hassa_ctx(pdg, hassa)
+    ctx.step(1)
+    u, v, f = ctx.state()
+    assert normwise(v, hassa["c_v1"]) < V_TOL
+    assert normwise(u, hassa["c_u1"]) < u_tol(hassa["x"], hassa["c_u1"])
+    assert normwise(f, hassa["c_f1"]) < F_TOL
+    ctx.step(2)
+    u, v, f = ctx.state()
+    assert normwise(v, hassa["c_v3"]) < V_TOL
+    assert normwise(u, hassa["c_u3"]) < u_tol(hassa["x"], hassa["c_u3"])
+    assert normwise(f, hassa["c_f3"]) < F_TOL
+    sim = hassa_oracle(po, hassa)
+    sim.step(3)
+    _assert_same(ctx, sim)
+
+
+def test_gpu_plate30_matches_reference_fixture(pdg, plate30_ref):
+    p = pdg.plates.make_plate(30, seed=3, crack="centre-half")
+    ctx = p.context(s_c=0.0)
+    rp, col = ctx.families()
+    assert np.array_equal(rp, plate30_ref["row_ptr"]) and np.array_equal(col, plate30_ref["col"])
+    ctx.step(1)
+    u, v, f = ctx.state()
+    assert normwise(u, plate30_ref["u1"]) < V_TOL and normwise(v, plate30_ref["v1"]) < V_TOL
+    assert normwise(f, plate30_ref["f1"]) < F_TOL
+    ctx.step(3)
+    u, v, f = ctx.state()
+    assert normwise(u, plate30_ref["u4"]) < V_TOL and normwise(v, plate30_ref["v4"]) < V_TOL
+    assert normwise(f, plate30_ref["f4"]) < F_TOL
+
+
+@pytest.mark.parametrize("side,seed,s_c,steps", [(48, 1, 5e-4, 60), (64, 2, 2e-4, 40), (33, 4, 0.0, 10)])
+def test_gpu_fp64_bit_exact_vs_oracle(pdg, po, side, seed, s_c, steps):
+    p = pdg.plates.make_plate(side, seed=seed, crack="centre-half")
+    ctx = p.context(s_c=s_c)
+    sim = plate_oracle(po, p, s_c=s_c)
+    done = 0
+    for chunk in (1, 2, steps - 3):  # graph per distinct step count, state carried across calls
+        ctx.step(chunk)
+        sim.step(chunk)
+        done += chunk
+        _assert_same(ctx, sim)
+    if s_c > 0:
+        assert sim.mask.min() == 0, "the case is meant to break bonds"
+        assert ctx.counters()["bonds_broken"] == int((sim.mask == 0).sum())
+
+
+def test_gpu_config1_plate_100_steps_bit_exact(pdg, po):
+    """Config 1 (100x100, centred half-width crack, s_c = 5e-4, 100 steps)."""
+    p = pdg.plates.config_plate_100(seed=0)
+    ctx = p.context()
+    sim = plate_oracle(po, p)
+    ctx.step(100)
+    sim.step(100)
+    _assert_same(ctx, sim)
+
+
+def test_gpu_compute_velocity_dropin_matches_oracle(pdg, po):
+    """pd_compute_velocity (compute_velocity_GPU_host contract) after a host drift."""
+    p = pdg.plates.make_plate(40, seed=9, crack="centre-half")
+    ctx = p.context(s_c=0.0)
+    sim = plate_oracle(po, p, s_c=0.0)
+    sim.step(3)
+    # host-side drift of the next step, as the reference host loop does
+    u, v, f = sim.u.copy(), sim.v.copy(), sim.f.copy()
+    top, bot = p.group_of == 1, p.group_of == 2
+    v[top] = p.group_val[0]
+    v[bot] = p.group_val[1]
+    a = f * (1.0 / p.material.rho)
+    u = u + (v * p.dt + (0.5 * a) * (p.dt * p.dt))
+    vel, acc = v.copy(), a.copy()
+    ctx.set_state(u=u, v=v, f=f)
+    netf = ctx.compute_velocity(u, vel, acc)
+    sim.step(1)
+    assert np.array_equal(netf, sim.f)
+    assert np.array_equal(vel, sim.v)
+    assert np.array_equal(acc, sim.f * (1.0 / p.material.rho))
+
+
+def test_gpu_reset_and_determinism(pdg):
+    p = pdg.plates.make_plate(80, seed=6, crack="centre-half")
+    ctx = p.context(s_c=3e-4)
+    ctx.step(30)
+    a = ctx.state()
+    m = ctx.bond_mask()
+    ctx.reset()
+    ctx.step(30)
+    b = ctx.state()
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+    assert np.array_equal(m, ctx.bond_mask())
+
+
+def test_gpu_set_families_from_host(pdg, po):
+    p = pdg.plates.make_plate(24, seed=8, crack="centre-half")
+    rp, col = po.build_families(p.x, p.cutoff, p.cracks)
+    ctx = pdg.native.Context(p.params())
+    ctx.set_particles(p.x, p.vol)
+    ctx.set_families(rp, col)
+    ctx.set_bc(p.group_kind, p.group_val, p.group_of)
+    sim = plate_oracle(po, p, families=(rp, col))
+    ctx.step(5)
+    sim.step(5)
+    _assert_same(ctx, sim)
+
+
+def test_gpu_rejects_bad_families(pdg):
+    p = pdg.plates.make_plate(8, seed=1)
+    ctx = pdg.native.Context(p.params())
+    ctx.set_particles(p.x, p.vol)
+    rp = np.arange(p.n + 1, dtype=np.int64)
+    col = np.full(p.n, p.n + 5, dtype=np.int32)  # out of range
+    with pytest.raises(pdg.PdError) as e:
+        ctx.set_families(rp, col)
+    assert e.value.code == -1
+    with pytest.raises(pdg.PdError):
+        ctx.step(1)  # no families -> PD_ERR_ORDER
+
+
+def test_gpu_singular_policy(pdg):
+    """Two collinear bonds only: det(K) = 0; ZERO policy gives S = 0, ERROR policy fails the step."""
+    x = np.array([[0.0, 0.0], [1.0, 0.0], [2.0, 0.0]])
+    vol = np.ones(3)
+    for policy, expect_err in ((0, False), (1, True)):
+        ctx = pdg.native.Context(pdg.default_params(E=1.0, nu=0.2, rho=1.0, dt=1e-3, singular_policy=policy))
+        ctx.set_particles(x, vol)
+        ctx.build_families(1.5)
+        if expect_err:
+            with pytest.raises(pdg.PdError) as e:
+                ctx.step(1)
+            assert e.value.code == -5
+        else:
+            ctx.step(2)
+            u, v, f = ctx.state()
+            assert np.all(f == 0.0) and ctx.counters()["singular_events"] == 3
