@@ -30,6 +30,7 @@ NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "
 CUDA_UNITS = [
     ("pd_family.cu", ["--fmad=false"]),
     ("pd_fp64.cu", ["--fmad=false"]),
+    ("pd_mixed.cu", []),
     ("pd_api.cu", []),
 ]
 DROPIN_UNITS = ["pd_dropin.cpp"]

@@ -14,6 +14,8 @@ using pd::Fp64Args;
 
 struct pd_ctx {
   pd_params p{};
+  bool c_override = false;
+  double c11 = 0.0, c12 = 0.0, c33 = 0.0;
   cudaStream_t stream = nullptr;
   std::string err;
   int64_t n = 0;
@@ -124,9 +126,9 @@ Fp64Args fp64_args(pd_ctx* c) {
   a.bxi = c->bxi; a.bgeo = c->bgeo; a.blim = c->blim;
   const double E = c->p.E, nu = c->p.nu;
   const double pre = E / (1.0 - nu * nu);  // getStiffnessTensor, src/main_seq.cpp:185-187
-  a.c11 = pre;
-  a.c12 = nu * pre;
-  a.c33 = (1.0 - nu) * pre;
+  a.c11 = c->c_override ? c->c11 : pre;
+  a.c12 = c->c_override ? c->c12 : nu * pre;
+  a.c33 = c->c_override ? c->c33 : (1.0 - nu) * pre;
   a.dt = c->p.dt;
   a.dt2 = c->p.dt * c->p.dt;
   a.inv_rho = 1.0 / c->p.rho;
@@ -242,12 +244,27 @@ int pd_set_params(pd_ctx* c, const pd_params* p) {
   PD_CK(c, cudaSetDevice(c->p.device));
   const bool s_changed = p->s_c != c->p.s_c;
   c->p = *p;
+  c->c_override = false;
   clear_graphs(c);
   if (c->has_families && s_changed) {
     pd::launch_bond_limit_fp64(c->sell.nslots, c->bxi, stretch_factor(c->p.s_c), c->sell.nbr, c->blim, c->stream);
     PD_CK(c, cudaGetLastError());
     PD_CK(c, cudaStreamSynchronize(c->stream));
   }
+  return PD_OK;
+}
+
+int pd_set_stiffness(pd_ctx* c, const double* C) {
+  if (!c || !C) return PD_ERR_ARG;
+  for (int k = 0; k < 9; ++k)
+    if (!std::isfinite(C[k])) return fail(c, PD_ERR_ARG, "non-finite stiffness");
+  if (C[0] != C[4] || C[1] != C[3] || C[2] != 0.0 || C[5] != 0.0 || C[6] != 0.0 || C[7] != 0.0)
+    return fail(c, PD_ERR_ARG, "stiffness is not of the plane-stress pattern");
+  c->c_override = true;
+  c->c11 = C[0];
+  c->c12 = C[1];
+  c->c33 = C[8];
+  clear_graphs(c);
   return PD_OK;
 }
 

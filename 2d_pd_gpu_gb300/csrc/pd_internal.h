@@ -65,6 +65,35 @@ struct Fp64Args {
   unsigned long long* counters;
 };
 
+// Mixed form (pd_mixed.cu): scaled two-float state, FP32 bond arithmetic.
+struct MixedArgs {
+  int64_t n;
+  const double2* __restrict__ x;    // FP64 reference positions (K^-1 recompute)
+  const double* __restrict__ vol;   // FP64 volumes
+  float4* xs;                       // x^ two-float {hi.x, hi.y, lo.x, lo.y}
+  float* vh;                        // V^
+  float4* us;                       // u^ two-float
+  float4* vs;                       // v^ = v dt / Ls, two-float
+  float2* fs;                       // f^ = f Ls / Es
+  float4* ws;                       // W^ = V^ sigma^ K^-1 (row-major 2x2)
+  float4* geo;                      // {K^-1 11, 12, 22, V^_i}
+  float2* mh;                       // m^ / V^_i
+  const uint8_t* __restrict__ bc;
+  const int32_t* __restrict__ gkind;
+  const float4* __restrict__ gvel;  // prescribed v^ per group, two-float
+  int32_t* broken;
+  double* damage;
+  uint8_t* singular;
+  const int32_t* __restrict__ fam;
+  const int64_t* __restrict__ chunk_base;
+  const int32_t* __restrict__ chunk_w;
+  int32_t* nbr;
+  float c11, c12, c33;  // C / Es
+  float s2, tau2;       // stretch limit factor, Es dt^2 / (rho Ls^2)
+  double inv_ls, inv_vs, v_scale, f_scale, det_guard;
+  unsigned long long* counters;
+};
+
 // ---- family build (pd_family.cu)
 struct FamilyBuild {
   int64_t nnz = 0;
@@ -99,6 +128,14 @@ void launch_drift_fp64(const Fp64Args& a, cudaStream_t s);
 void launch_pass_a_fp64(const Fp64Args& a, bool breaking, cudaStream_t s);
 // mode 0: kick; 1: kick + next step's drift; 2: drop-in kick (acc array in/out)
 void launch_pass_b_fp64(const Fp64Args& a, int mode, cudaStream_t s);
+
+// ---- mixed step (pd_mixed.cu)
+void launch_init_geometry_mixed(const MixedArgs& a, cudaStream_t s);
+void launch_drift_mixed(const MixedArgs& a, cudaStream_t s);
+void launch_pass_a_mixed(const MixedArgs& a, bool breaking, cudaStream_t s);
+void launch_pass_b_mixed(const MixedArgs& a, bool drift, cudaStream_t s);
+void launch_to_mixed(const MixedArgs& a, const double2* u, const double2* v, const double2* f, cudaStream_t s);
+void launch_from_mixed(const MixedArgs& a, double2* u, double2* v, double2* f, cudaStream_t s);
 
 inline int64_t blocks_for(int64_t n, int64_t per = kBlock) { return (n + per - 1) / per; }
 

@@ -1,0 +1,308 @@
+// Mixed-precision NOSB step (PD_MIXED): FP32 bond arithmetic, FP64 shape-
+// tensor inversion + determinant guard, compensated FP32 force sums.
+//
+// Variables are scaled so that FP32 works on O(1e-4..1) numbers whatever the
+// caller's units: lengths by Ls (the family cutoff), volumes by Vs (mean
+// volume), stresses by Es (C11), and the Verlet update is written in
+// per-step units:
+//   x^ = x/Ls, u^ = u/Ls, V^ = V/Vs,  v^ = v dt/Ls,  a^ = a dt^2/Ls,
+//   K^ = sum V^ xi^ (x) xi^,  D^ = sum V^ du^ (x) xi^,  G = D^ K^-1 = F - I,
+//   sigma^ = (C/Es) eps,  W^ = V^ sigma^ K^-1,  f^ = W^_i m^_i + sum_j W^_j xi^_ij,
+//   a^ = tau2 f^ with tau2 = Es dt^2 / (rho Ls^2).
+// Reference positions, displacements, velocities and prescribed velocities
+// are two-float pairs (hi + lo, ~48-bit significand): neighbour differences
+// (hi_j - hi_i) + (lo_j - lo_i) keep full FP32 relative precision even when
+// |u| >> |u_j - u_i|.  The FP64 K^-1 is rounded to FP32 for the per-step
+// products.  Nothing here is bit-identical to the FP64 form; its error is
+// measured against it (tests/test_gpu_mixed.py, bench.py).
+#include "pd_internal.h"
+
+namespace pd {
+
+namespace {
+
+__device__ __forceinline__ float2 two_sum(float a, float b) {
+  const float s = a + b;
+  const float z = s - a;
+  const float e = (a - (s - z)) + (b - z);
+  return make_float2(s, e);
+}
+
+// (hi, lo) + d  -> renormalised pair
+__device__ __forceinline__ void tf_add(float& hi, float& lo, float d) {
+  const float2 s = two_sum(hi, d);
+  const float l = s.y + lo;
+  hi = s.x + l;
+  lo = l - (hi - s.x);
+}
+
+// (hi, lo) + (dh, dl)
+__device__ __forceinline__ void tf_add2(float& hi, float& lo, float dh, float dl) {
+  const float2 s = two_sum(hi, dh);
+  const float l = s.y + (lo + dl);
+  hi = s.x + l;
+  lo = l - (hi - s.x);
+}
+
+__device__ __forceinline__ float tf_diff(float hj, float lj, float hi, float li) { return (hj - hi) + (lj - li); }
+
+__device__ __forceinline__ int64_t slot0(const MixedArgs& a, int64_t i, int* w) {
+  const int64_t c = i >> 5;
+  *w = a.chunk_w[c];
+  return a.chunk_base[c] + (i & 31);
+}
+
+// K^-1 (FP64 inversion + guard) and m^ from the FP64 reference positions.
+__device__ void kinv_update_mixed(const MixedArgs& a, int64_t i) {
+  int w;
+  const int64_t s0 = slot0(a, i, &w);
+  const double2 xi = a.x[i];
+  double k11 = 0.0, k12 = 0.0, k22 = 0.0, mx = 0.0, my = 0.0;
+  int nal = 0;
+  for (int k = 0; k < w; ++k) {
+    const int64_t s = s0 + (int64_t)k * kChunk;
+    const int j = a.nbr[s];
+    if (j < 0) continue;
+    const double2 xj = a.x[j];
+    const double ex = (xj.x - xi.x) * a.inv_ls, ey = (xj.y - xi.y) * a.inv_ls;
+    const double vj = a.vol[j] * a.inv_vs;
+    const double t0 = vj * ex, t1 = vj * ey;
+    k11 = fma(t0, ex, k11);
+    k12 = fma(t0, ey, k12);
+    k22 = fma(t1, ey, k22);
+    mx += t0;
+    my += t1;
+    ++nal;
+  }
+  const double det = fma(k11, k22, -(k12 * k12));
+  const double vi = a.vol[i] * a.inv_vs;
+  if (nal == 0 || !(det > a.det_guard * (k11 * k22))) {
+    a.geo[i] = make_float4(0.f, 0.f, 0.f, (float)vi);
+    a.mh[i] = make_float2(0.f, 0.f);
+    a.singular[i] = 1;
+    atomicAdd(a.counters + CNT_SINGULAR, 1ull);
+    return;
+  }
+  const double r = 1.0 / det;
+  a.geo[i] = make_float4((float)(k22 * r), (float)(-k12 * r), (float)(k11 * r), (float)vi);
+  a.mh[i] = make_float2((float)(mx / vi), (float)(my / vi));
+  a.singular[i] = 0;
+}
+
+__global__ void __launch_bounds__(kBlock) k_init_geometry_mixed(MixedArgs a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < a.n) kinv_update_mixed(a, i);
+}
+
+// BC + drift of particle i in scaled per-step units; an = a^ of the new force.
+__device__ __forceinline__ void drift_mixed(const MixedArgs& a, int64_t i, float4& v, float4& u, float anx,
+                                            float any) {
+  const int g = a.bc[i];
+  const int kind = g ? a.gkind[g - 1] : PD_BC_NONE;
+  if (kind == PD_BC_VELOCITY) v = a.gvel[g - 1];
+  // u += v + a/2   (v two-float, a/2 FP32)
+  tf_add2(u.x, u.z, v.x, v.z);
+  tf_add2(u.y, u.w, v.y, v.w);
+  tf_add(u.x, u.z, 0.5f * anx);
+  tf_add(u.y, u.w, 0.5f * any);
+  if (kind == PD_BC_FIXED) u = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+__global__ void __launch_bounds__(kBlock) k_drift_mixed(MixedArgs a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  float4 v = a.vs[i], u = a.us[i];
+  const float2 f = a.fs[i];
+  drift_mixed(a, i, v, u, a.tau2 * f.x, a.tau2 * f.y);
+  a.vs[i] = v;
+  a.us[i] = u;
+}
+
+template <bool BREAK>
+__global__ void __launch_bounds__(kBlock) k_pass_a_mixed(MixedArgs a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  int w;
+  const int64_t s0 = slot0(a, i, &w);
+  const float4 ui = a.us[i], xi = a.xs[i];
+  float d11 = 0.f, d12 = 0.f, d21 = 0.f, d22 = 0.f;
+  int newly = 0;
+  for (int k = 0; k < w; ++k) {
+    const int64_t s = s0 + (int64_t)k * kChunk;
+    const int j = __ldcs(&a.nbr[s]);
+    if (j < 0) continue;
+    const float4 uj = a.us[j], xj = a.xs[j];
+    const float vj = a.vh[j];
+    const float ex = tf_diff(xj.x, xj.z, xi.x, xi.z), ey = tf_diff(xj.y, xj.w, xi.y, xi.w);
+    const float dx = tf_diff(uj.x, uj.z, ui.x, ui.z), dy = tf_diff(uj.y, uj.w, ui.y, ui.w);
+    if (BREAK) {
+      const float q = fmaf(dx, fmaf(2.f, ex, dx), dy * fmaf(2.f, ey, dy));
+      if (q > a.s2 * fmaf(ex, ex, ey * ey)) {
+        a.nbr[s] = -2 - j;
+        ++newly;
+        continue;
+      }
+    }
+    const float t0 = vj * ex, t1 = vj * ey;
+    d11 = fmaf(dx, t0, d11);
+    d12 = fmaf(dx, t1, d12);
+    d21 = fmaf(dy, t0, d21);
+    d22 = fmaf(dy, t1, d22);
+  }
+  if (BREAK && newly) {
+    atomicAdd(a.counters + CNT_BROKEN, (unsigned long long)newly);
+    const int32_t b = a.broken[i] + newly;
+    a.broken[i] = b;
+    a.damage[i] = (double)b / (double)a.fam[i];
+    kinv_update_mixed(a, i);
+  }
+  if (a.singular[i]) {
+    a.ws[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    return;
+  }
+  const float4 g = a.geo[i];
+  const float k11 = g.x, k12 = g.y, k22 = g.z, vi = g.w;
+  const float g11 = fmaf(d11, k11, d12 * k12), g12 = fmaf(d11, k12, d12 * k22);
+  const float g21 = fmaf(d21, k11, d22 * k12), g22 = fmaf(d21, k12, d22 * k22);
+  const float e11 = g11, e22 = g22, e12 = 0.5f * (g12 + g21);
+  const float s11 = fmaf(a.c11, e11, a.c12 * e22);
+  const float s22 = fmaf(a.c12, e11, a.c11 * e22);
+  const float s12 = a.c33 * e12;
+  a.ws[i] = make_float4(vi * fmaf(s11, k11, s12 * k12), vi * fmaf(s11, k12, s12 * k22),
+                        vi * fmaf(s12, k11, s22 * k12), vi * fmaf(s12, k12, s22 * k22));
+}
+
+template <bool DRIFT>
+__global__ void __launch_bounds__(kBlock) k_pass_b_mixed(MixedArgs a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  int w;
+  const int64_t s0 = slot0(a, i, &w);
+  const float4 wi = a.ws[i], xi = a.xs[i];
+  const float2 m = a.mh[i];
+  // compensated sums (value, correction) per component
+  float sx = fmaf(wi.x, m.x, wi.y * m.y), cx = 0.f;
+  float sy = fmaf(wi.z, m.x, wi.w * m.y), cy = 0.f;
+  for (int k = 0; k < w; ++k) {
+    const int64_t s = s0 + (int64_t)k * kChunk;
+    const int j = __ldcs(&a.nbr[s]);
+    if (j < 0) continue;
+    const float4 xj = a.xs[j], wj = a.ws[j];
+    const float ex = tf_diff(xj.x, xj.z, xi.x, xi.z), ey = tf_diff(xj.y, xj.w, xi.y, xi.w);
+    const float px = fmaf(wj.x, ex, wj.y * ey);
+    const float py = fmaf(wj.z, ex, wj.w * ey);
+    const float2 tx = two_sum(sx, px), ty = two_sum(sy, py);
+    sx = tx.x;
+    cx += tx.y;
+    sy = ty.x;
+    cy += ty.y;
+  }
+  const float fx = sx + cx, fy = sy + cy;
+  const float2 fo = a.fs[i];
+  const float aox = a.tau2 * fo.x, aoy = a.tau2 * fo.y;
+  const float anx = a.tau2 * fx, any = a.tau2 * fy;
+  float4 v = a.vs[i];
+  tf_add(v.x, v.z, 0.5f * (aox + anx));
+  tf_add(v.y, v.w, 0.5f * (aoy + any));
+  a.fs[i] = make_float2(fx, fy);
+  if (DRIFT) {
+    float4 u = a.us[i];
+    drift_mixed(a, i, v, u, anx, any);
+    a.us[i] = u;
+  }
+  a.vs[i] = v;
+}
+
+// FP64 <-> scaled two-float conversions (set/get state; not per step)
+__device__ __forceinline__ void split2(double v, float& hi, float& lo) {
+  hi = (float)v;
+  lo = (float)(v - (double)hi);
+}
+
+__global__ void k_to_mixed(MixedArgs a, const double2* u, const double2* v, const double2* f) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  float4 o;
+  if (u) {
+    const double2 q = u[i];
+    split2(q.x * a.inv_ls, o.x, o.z);
+    split2(q.y * a.inv_ls, o.y, o.w);
+    a.us[i] = o;
+  }
+  if (v) {
+    const double2 q = v[i];
+    split2(q.x * a.v_scale, o.x, o.z);
+    split2(q.y * a.v_scale, o.y, o.w);
+    a.vs[i] = o;
+  }
+  if (f) {
+    const double2 q = f[i];
+    a.fs[i] = make_float2((float)(q.x * a.f_scale), (float)(q.y * a.f_scale));
+  }
+}
+
+__global__ void k_from_mixed(MixedArgs a, double2* u, double2* v, double2* f) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  if (u) {
+    const float4 q = a.us[i];
+    u[i] = make_double2(((double)q.x + (double)q.z) / a.inv_ls, ((double)q.y + (double)q.w) / a.inv_ls);
+  }
+  if (v) {
+    const float4 q = a.vs[i];
+    v[i] = make_double2(((double)q.x + (double)q.z) / a.v_scale, ((double)q.y + (double)q.w) / a.v_scale);
+  }
+  if (f) {
+    const float2 q = a.fs[i];
+    f[i] = make_double2((double)q.x / a.f_scale, (double)q.y / a.f_scale);
+  }
+}
+
+__global__ void k_positions_mixed(MixedArgs a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const double2 q = a.x[i];
+  float4 o;
+  split2(q.x * a.inv_ls, o.x, o.z);
+  split2(q.y * a.inv_ls, o.y, o.w);
+  a.xs[i] = o;
+  a.vh[i] = (float)(a.vol[i] * a.inv_vs);
+}
+
+}  // namespace
+
+void launch_init_geometry_mixed(const MixedArgs& a, cudaStream_t s) {
+  if (a.n <= 0) return;
+  k_positions_mixed<<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
+  k_init_geometry_mixed<<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
+}
+
+void launch_drift_mixed(const MixedArgs& a, cudaStream_t s) {
+  if (a.n > 0) k_drift_mixed<<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
+}
+
+void launch_pass_a_mixed(const MixedArgs& a, bool breaking, cudaStream_t s) {
+  if (a.n <= 0) return;
+  if (breaking)
+    k_pass_a_mixed<true><<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
+  else
+    k_pass_a_mixed<false><<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
+}
+
+void launch_pass_b_mixed(const MixedArgs& a, bool drift, cudaStream_t s) {
+  if (a.n <= 0) return;
+  if (drift)
+    k_pass_b_mixed<true><<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
+  else
+    k_pass_b_mixed<false><<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
+}
+
+void launch_to_mixed(const MixedArgs& a, const double2* u, const double2* v, const double2* f, cudaStream_t s) {
+  if (a.n > 0) k_to_mixed<<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a, u, v, f);
+}
+
+void launch_from_mixed(const MixedArgs& a, double2* u, double2* v, double2* f, cudaStream_t s) {
+  if (a.n > 0) k_from_mixed<<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a, u, v, f);
+}
+
+}  // namespace pd

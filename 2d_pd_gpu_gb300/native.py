@@ -65,6 +65,7 @@ _SIGS = {
     "pd_last_error": [_vp],
     "pd_set_params": [_vp, ctypes.POINTER(Params)],
     "pd_get_params": [_vp, ctypes.POINTER(Params)],
+    "pd_set_stiffness": [_vp, _vp],
     "pd_set_particles": [_vp, ctypes.c_int64, _vp, _vp],
     "pd_build_families": [_vp, ctypes.c_double, ctypes.c_int32, _vp],
     "pd_set_families": [_vp, _vp, _vp],

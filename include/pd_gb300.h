@@ -94,6 +94,12 @@ const char* pd_last_error(const pd_ctx* ctx);
 /* Material / time-step / stretch update; bond data is refreshed in place. */
 int pd_set_params(pd_ctx* ctx, const pd_params* p);
 int pd_get_params(const pd_ctx* ctx, pd_params* p);
+/* Plane-stress stiffness given as the reference's 3x3 Voigt matrix
+ * C[9] (row-major, sigma = C [e11, e22, e12], getStiffnessTensor
+ * src/main_seq.cpp:180-201) instead of (E, nu).  Requires the plane-stress
+ * pattern C[0] == C[4], C[1] == C[3], C[2] == C[5] == C[6] == C[7] == 0.
+ * Stays in force until the next pd_set_params. */
+int pd_set_stiffness(pd_ctx* ctx, const double* C);
 
 /* --------------------------------------------------------------- problem */
 
