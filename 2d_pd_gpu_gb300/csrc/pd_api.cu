@@ -1,5 +1,6 @@
 // C ABI of the GB300 NOSB step (include/pd_gb300.h): context, device-resident
 // state, family/bond set-up, step launches captured in CUDA graphs.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -20,7 +21,11 @@ struct pd_ctx {
   std::string err;
   int64_t n = 0;
   bool has_particles = false, has_families = false;
-  std::vector<double> h_x;  // host copy of the reference positions (cell-list bbox)
+  std::vector<double> h_x;    // host copy of the reference positions (cell-list bbox, scales)
+  std::vector<double> h_vol;  // host copy of the volumes
+  double cutoff = 0.0;        // family cutoff (0 if families came from the host)
+  // mixed-form scales: lengths / Ls, volumes / Vs, stresses / Es
+  double ls = 1.0, vs_scale = 1.0;
 
   // per particle
   double2 *x = nullptr, *u = nullptr, *v = nullptr, *f = nullptr, *acc = nullptr;
@@ -28,9 +33,15 @@ struct pd_ctx {
   double2 *w01 = nullptr, *w23 = nullptr, *kinv01 = nullptr, *mt = nullptr;
   uint8_t *bc = nullptr, *singular = nullptr;
   int32_t *broken = nullptr, *fam = nullptr;
+  // mixed form (PD_MIXED)
+  float4 *xs = nullptr, *us = nullptr, *vsm = nullptr, *ws = nullptr, *geo = nullptr;
+  float2 *fs = nullptr, *mh = nullptr;
+  float* vh = nullptr;
   // BC groups
   int32_t* gkind = nullptr;
   double2* gval = nullptr;
+  float4* gvel = nullptr;  // mixed: scaled two-float prescribed velocities
+  std::vector<double> h_gval = std::vector<double>(2 * PD_MAX_BC_GROUPS, 0.0);
   // families
   int64_t nnz = 0;
   int64_t* row_ptr = nullptr;
@@ -98,6 +109,8 @@ void free_particles(pd_ctx* c) {
   dfree(c->vol); dfree(c->kinv22); dfree(c->damage);
   dfree(c->w01); dfree(c->w23); dfree(c->kinv01); dfree(c->mt);
   dfree(c->bc); dfree(c->singular); dfree(c->broken); dfree(c->fam);
+  dfree(c->xs); dfree(c->us); dfree(c->vsm); dfree(c->ws); dfree(c->geo);
+  dfree(c->fs); dfree(c->mh); dfree(c->vh);
   c->n = 0;
   c->has_particles = false;
 }
@@ -115,6 +128,8 @@ int check_params(pd_ctx* c, const pd_params* p) {
   return PD_OK;
 }
 
+void stiffness(const pd_ctx* c, double* c11, double* c12, double* c33);
+
 Fp64Args fp64_args(pd_ctx* c) {
   Fp64Args a{};
   a.n = c->n;
@@ -124,17 +139,64 @@ Fp64Args fp64_args(pd_ctx* c) {
   a.broken = c->broken; a.damage = c->damage; a.singular = c->singular; a.fam = c->fam;
   a.chunk_base = c->sell.chunk_base; a.chunk_w = c->sell.chunk_w; a.nbr = c->sell.nbr;
   a.bxi = c->bxi; a.bgeo = c->bgeo; a.blim = c->blim;
-  const double E = c->p.E, nu = c->p.nu;
-  const double pre = E / (1.0 - nu * nu);  // getStiffnessTensor, src/main_seq.cpp:185-187
-  a.c11 = c->c_override ? c->c11 : pre;
-  a.c12 = c->c_override ? c->c12 : nu * pre;
-  a.c33 = c->c_override ? c->c33 : (1.0 - nu) * pre;
+  stiffness(c, &a.c11, &a.c12, &a.c33);  // getStiffnessTensor, src/main_seq.cpp:185-187
   a.dt = c->p.dt;
   a.dt2 = c->p.dt * c->p.dt;
   a.inv_rho = 1.0 / c->p.rho;
   a.det_guard = c->p.det_guard;
   a.counters = c->counters;
   return a;
+}
+
+bool mixed(const pd_ctx* c) { return c->p.precision == PD_MIXED; }
+
+void stiffness(const pd_ctx* c, double* c11, double* c12, double* c33) {
+  const double E = c->p.E, nu = c->p.nu;
+  const double pre = E / (1.0 - nu * nu);
+  *c11 = c->c_override ? c->c11 : pre;
+  *c12 = c->c_override ? c->c12 : nu * pre;
+  *c33 = c->c_override ? c->c33 : (1.0 - nu) * pre;
+}
+
+pd::MixedArgs mixed_args(pd_ctx* c) {
+  pd::MixedArgs a{};
+  a.n = c->n;
+  a.x = c->x; a.vol = c->vol;
+  a.xs = c->xs; a.vh = c->vh; a.us = c->us; a.vs = c->vsm; a.fs = c->fs; a.ws = c->ws; a.geo = c->geo; a.mh = c->mh;
+  a.bc = c->bc; a.gkind = c->gkind; a.gvel = c->gvel;
+  a.broken = c->broken; a.damage = c->damage; a.singular = c->singular; a.fam = c->fam;
+  a.chunk_base = c->sell.chunk_base; a.chunk_w = c->sell.chunk_w; a.nbr = c->sell.nbr;
+  double c11, c12, c33;
+  stiffness(c, &c11, &c12, &c33);
+  const double es = c11 != 0.0 ? c11 : 1.0;
+  a.c11 = (float)(c11 / es);
+  a.c12 = (float)(c12 / es);
+  a.c33 = (float)(c33 / es);
+  a.s2 = c->p.s_c > 0.0 ? (float)(c->p.s_c * (2.0 + c->p.s_c)) : INFINITY;
+  a.tau2 = (float)(es * c->p.dt * c->p.dt / (c->p.rho * c->ls * c->ls));
+  a.inv_ls = 1.0 / c->ls;
+  a.inv_vs = 1.0 / c->vs_scale;
+  a.v_scale = c->p.dt / c->ls;
+  a.f_scale = c->ls / es;
+  a.det_guard = c->p.det_guard;
+  a.counters = c->counters;
+  return a;
+}
+
+// Scaled two-float prescribed velocities for the mixed form.
+int upload_gvel(pd_ctx* c) {
+  if (!mixed(c) || !c->gvel) return PD_OK;
+  std::vector<float> g(4 * PD_MAX_BC_GROUPS, 0.f);
+  const double sc = c->p.dt / c->ls;
+  for (int k = 0; k < PD_MAX_BC_GROUPS; ++k)
+    for (int m = 0; m < 2; ++m) {
+      const double v = c->h_gval[2 * k + m] * sc;
+      const float hi = (float)v;
+      g[4 * k + m] = hi;
+      g[4 * k + 2 + m] = (float)(v - (double)hi);
+    }
+  PD_CK(c, cudaMemcpy(c->gvel, g.data(), g.size() * sizeof(float), cudaMemcpyHostToDevice));
+  return PD_OK;
 }
 
 __global__ void k_fam_from_rowptr(int64_t n, const int64_t* rp, int32_t* fam) {
@@ -154,12 +216,37 @@ int finish_families(pd_ctx* c) {
   if (h[pd::CNT_ERROR])
     return fail(c, PD_ERR_ARG, "invalid family: neighbour id out of range or a self bond (error word " +
                                    std::to_string(h[pd::CNT_ERROR]) + ")");
-  const size_t ns = (size_t)(c->sell.nslots > 0 ? c->sell.nslots : 1);
-  PD_CK(c, cudaMalloc(&c->bxi, ns * sizeof(double2)));
-  PD_CK(c, cudaMalloc(&c->bgeo, ns * sizeof(double2)));
-  PD_CK(c, cudaMalloc(&c->blim, ns * sizeof(double)));
-  pd::launch_bond_geometry_fp64(c->n, c->x, c->vol, c->sell, c->row_ptr, stretch_factor(c->p.s_c), c->bxi, c->bgeo,
-                                c->blim, s);
+  if (!mixed(c)) {
+    const size_t ns = (size_t)(c->sell.nslots > 0 ? c->sell.nslots : 1);
+    PD_CK(c, cudaMalloc(&c->bxi, ns * sizeof(double2)));
+    PD_CK(c, cudaMalloc(&c->bgeo, ns * sizeof(double2)));
+    PD_CK(c, cudaMalloc(&c->blim, ns * sizeof(double)));
+    pd::launch_bond_geometry_fp64(c->n, c->x, c->vol, c->sell, c->row_ptr, stretch_factor(c->p.s_c), c->bxi,
+                                  c->bgeo, c->blim, s);
+  } else {
+    // mixed-form scales: Ls = the family cutoff (or the longest bond), Vs = mean volume
+    double ls = c->cutoff;
+    if (!(ls > 0.0)) {
+      std::vector<int64_t> rp(c->n + 1);
+      std::vector<int32_t> col((size_t)(c->nnz > 0 ? c->nnz : 1));
+      PD_CK(c, cudaMemcpy(rp.data(), c->row_ptr, rp.size() * sizeof(int64_t), cudaMemcpyDeviceToHost));
+      if (c->nnz > 0)
+        PD_CK(c, cudaMemcpy(col.data(), c->col, (size_t)c->nnz * sizeof(int32_t), cudaMemcpyDeviceToHost));
+      double m2 = 0.0;
+      for (int64_t i = 0; i < c->n; ++i)
+        for (int64_t k = rp[i]; k < rp[i + 1]; ++k) {
+          const double ex = c->h_x[2 * col[k]] - c->h_x[2 * i], ey = c->h_x[2 * col[k] + 1] - c->h_x[2 * i + 1];
+          m2 = std::max(m2, ex * ex + ey * ey);
+        }
+      ls = m2 > 0.0 ? std::sqrt(m2) : 1.0;
+    }
+    double vsum = 0.0;
+    for (double v : c->h_vol) vsum += v;
+    c->ls = ls;
+    c->vs_scale = c->n > 0 ? vsum / (double)c->n : 1.0;
+    int rc2 = upload_gvel(c);
+    if (rc2 != PD_OK) return rc2;
+  }
   if (c->n > 0) k_fam_from_rowptr<<<(unsigned)pd::blocks_for(c->n), pd::kBlock, 0, s>>>(c->n, c->row_ptr, c->fam);
   PD_CK(c, cudaGetLastError());
   c->has_families = true;
@@ -210,6 +297,8 @@ int pd_create(const pd_params* p, pd_ctx** out) {
   if (e == cudaSuccess) e = cudaMalloc(&c->gkind, PD_MAX_BC_GROUPS * sizeof(int32_t));
   if (e == cudaSuccess) e = cudaMalloc(&c->gval, PD_MAX_BC_GROUPS * sizeof(double2));
   if (e == cudaSuccess) e = cudaMemset(c->gkind, 0, PD_MAX_BC_GROUPS * sizeof(int32_t));
+  if (e == cudaSuccess && p->precision == PD_MIXED) e = cudaMalloc(&c->gvel, PD_MAX_BC_GROUPS * sizeof(float4));
+  if (e == cudaSuccess && c->gvel) e = cudaMemset(c->gvel, 0, PD_MAX_BC_GROUPS * sizeof(float4));
   if (e != cudaSuccess) {
     g_create_err = std::string("pd_create: ") + cudaGetErrorString(e);
     pd_destroy(c.release());
@@ -227,6 +316,7 @@ int pd_destroy(pd_ctx* c) {
   dfree(c->counters);
   dfree(c->gkind);
   dfree(c->gval);
+  dfree(c->gvel);
   for (void* q : c->scratch) cudaFreeHost(q);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -246,7 +336,11 @@ int pd_set_params(pd_ctx* c, const pd_params* p) {
   c->p = *p;
   c->c_override = false;
   clear_graphs(c);
-  if (c->has_families && s_changed) {
+  if (c->has_families) {
+    int rc2 = upload_gvel(c);
+    if (rc2 != PD_OK) return rc2;
+  }
+  if (c->has_families && s_changed && !mixed(c)) {
     pd::launch_bond_limit_fp64(c->sell.nslots, c->bxi, stretch_factor(c->p.s_c), c->sell.nbr, c->blim, c->stream);
     PD_CK(c, cudaGetLastError());
     PD_CK(c, cudaStreamSynchronize(c->stream));
@@ -291,13 +385,24 @@ int pd_set_particles(pd_ctx* c, int64_t n, const double* x, const double* vol) {
   PD_CK(c, cudaMalloc(&c->u, nn * sizeof(double2)));
   PD_CK(c, cudaMalloc(&c->v, nn * sizeof(double2)));
   PD_CK(c, cudaMalloc(&c->f, nn * sizeof(double2)));
-  PD_CK(c, cudaMalloc(&c->acc, nn * sizeof(double2)));
-  PD_CK(c, cudaMalloc(&c->w01, nn * sizeof(double2)));
-  PD_CK(c, cudaMalloc(&c->w23, nn * sizeof(double2)));
-  PD_CK(c, cudaMalloc(&c->kinv01, nn * sizeof(double2)));
-  PD_CK(c, cudaMalloc(&c->mt, nn * sizeof(double2)));
   PD_CK(c, cudaMalloc(&c->vol, nn * sizeof(double)));
-  PD_CK(c, cudaMalloc(&c->kinv22, nn * sizeof(double)));
+  if (mixed(c)) {
+    PD_CK(c, cudaMalloc(&c->xs, nn * sizeof(float4)));
+    PD_CK(c, cudaMalloc(&c->us, nn * sizeof(float4)));
+    PD_CK(c, cudaMalloc(&c->vsm, nn * sizeof(float4)));
+    PD_CK(c, cudaMalloc(&c->ws, nn * sizeof(float4)));
+    PD_CK(c, cudaMalloc(&c->geo, nn * sizeof(float4)));
+    PD_CK(c, cudaMalloc(&c->fs, nn * sizeof(float2)));
+    PD_CK(c, cudaMalloc(&c->mh, nn * sizeof(float2)));
+    PD_CK(c, cudaMalloc(&c->vh, nn * sizeof(float)));
+  } else {
+    PD_CK(c, cudaMalloc(&c->acc, nn * sizeof(double2)));
+    PD_CK(c, cudaMalloc(&c->w01, nn * sizeof(double2)));
+    PD_CK(c, cudaMalloc(&c->w23, nn * sizeof(double2)));
+    PD_CK(c, cudaMalloc(&c->kinv01, nn * sizeof(double2)));
+    PD_CK(c, cudaMalloc(&c->mt, nn * sizeof(double2)));
+    PD_CK(c, cudaMalloc(&c->kinv22, nn * sizeof(double)));
+  }
   PD_CK(c, cudaMalloc(&c->damage, nn * sizeof(double)));
   PD_CK(c, cudaMalloc(&c->bc, nn));
   PD_CK(c, cudaMalloc(&c->singular, nn));
@@ -309,6 +414,7 @@ int pd_set_particles(pd_ctx* c, int64_t n, const double* x, const double* vol) {
     PD_CK(c, cudaMemcpy(c->vol, vol, (size_t)n * sizeof(double), cudaMemcpyHostToDevice));
   }
   c->h_x.assign(x, x + 2 * n);
+  c->h_vol.assign(vol, vol + n);
   c->has_particles = true;
   return PD_OK;
 }
@@ -321,6 +427,7 @@ int pd_build_families(pd_ctx* c, double cutoff, int32_t n_cracks, const double* 
   free_families(c);
   pd::FamilyBuild fb;
   std::string msg;
+  c->cutoff = cutoff;
   int rc = pd::build_families_gpu(c->n, c->x, c->h_x.data(), cutoff, n_cracks, cracks, c->stream, &fb, &msg);
   c->row_ptr = fb.row_ptr;
   c->col = fb.col;
@@ -344,6 +451,7 @@ int pd_set_families(pd_ctx* c, const int64_t* row_ptr, const int32_t* col) {
   if (nnz > 0 && !col) return fail(c, PD_ERR_ARG, "col is NULL");
   PD_CK(c, cudaSetDevice(c->p.device));
   free_families(c);
+  c->cutoff = 0.0;
   c->nnz = nnz;
   PD_CK(c, cudaMalloc(&c->row_ptr, (size_t)(n + 1) * sizeof(int64_t)));
   PD_CK(c, cudaMalloc(&c->col, (size_t)(nnz > 0 ? nnz : 1) * sizeof(int32_t)));
@@ -390,6 +498,11 @@ int pd_set_bc(pd_ctx* c, int32_t n_groups, const int32_t* kind, const double* va
   }
   PD_CK(c, cudaMemcpy(c->gkind, k.data(), k.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
   PD_CK(c, cudaMemcpy(c->gval, val.data(), val.size() * sizeof(double), cudaMemcpyHostToDevice));
+  c->h_gval = val;
+  if (c->has_families) {
+    int rc = upload_gvel(c);
+    if (rc != PD_OK) return rc;
+  }
   if (c->n > 0) {
     if (group_of)
       PD_CK(c, cudaMemcpy(c->bc, group_of, (size_t)c->n, cudaMemcpyHostToDevice));
@@ -408,15 +521,22 @@ int pd_reset(pd_ctx* c) {
   PD_CK(c, cudaMemsetAsync(c->u, 0, nn * sizeof(double2), s));
   PD_CK(c, cudaMemsetAsync(c->v, 0, nn * sizeof(double2), s));
   PD_CK(c, cudaMemsetAsync(c->f, 0, nn * sizeof(double2), s));
-  PD_CK(c, cudaMemsetAsync(c->acc, 0, nn * sizeof(double2), s));
-  PD_CK(c, cudaMemsetAsync(c->w01, 0, nn * sizeof(double2), s));
-  PD_CK(c, cudaMemsetAsync(c->w23, 0, nn * sizeof(double2), s));
   PD_CK(c, cudaMemsetAsync(c->broken, 0, nn * sizeof(int32_t), s));
   PD_CK(c, cudaMemsetAsync(c->damage, 0, nn * sizeof(double), s));
   PD_CK(c, cudaMemsetAsync(c->counters, 0, pd::CNT_N * sizeof(unsigned long long), s));
   pd::launch_sell_reset(c->n, c->row_ptr, c->col, c->sell, s);
-  Fp64Args a = fp64_args(c);
-  pd::launch_init_geometry_fp64(a, s);
+  if (mixed(c)) {
+    PD_CK(c, cudaMemsetAsync(c->us, 0, nn * sizeof(float4), s));
+    PD_CK(c, cudaMemsetAsync(c->vsm, 0, nn * sizeof(float4), s));
+    PD_CK(c, cudaMemsetAsync(c->ws, 0, nn * sizeof(float4), s));
+    PD_CK(c, cudaMemsetAsync(c->fs, 0, nn * sizeof(float2), s));
+    pd::launch_init_geometry_mixed(mixed_args(c), s);
+  } else {
+    PD_CK(c, cudaMemsetAsync(c->acc, 0, nn * sizeof(double2), s));
+    PD_CK(c, cudaMemsetAsync(c->w01, 0, nn * sizeof(double2), s));
+    PD_CK(c, cudaMemsetAsync(c->w23, 0, nn * sizeof(double2), s));
+    pd::launch_init_geometry_fp64(fp64_args(c), s);
+  }
   PD_CK(c, cudaGetLastError());
   PD_CK(c, cudaStreamSynchronize(s));
   c->steps = 0;
@@ -433,6 +553,12 @@ int pd_set_state(pd_ctx* c, const double* u, const double* v, const double* f) {
   if (u) PD_CK(c, cudaMemcpy(c->u, u, b, cudaMemcpyHostToDevice));
   if (v) PD_CK(c, cudaMemcpy(c->v, v, b, cudaMemcpyHostToDevice));
   if (f) PD_CK(c, cudaMemcpy(c->f, f, b, cudaMemcpyHostToDevice));
+  if (mixed(c)) {
+    if (!c->has_families) return fail(c, PD_ERR_ORDER, "mixed form: families first (they fix the scales)");
+    pd::launch_to_mixed(mixed_args(c), u ? c->u : nullptr, v ? c->v : nullptr, f ? c->f : nullptr, c->stream);
+    PD_CK(c, cudaGetLastError());
+    PD_CK(c, cudaStreamSynchronize(c->stream));
+  }
   return PD_OK;
 }
 
@@ -443,6 +569,12 @@ int pd_get_state(pd_ctx* c, double* u, double* v, double* f) {
   PD_CK(c, cudaStreamSynchronize(c->stream));
   const size_t b = (size_t)c->n * sizeof(double2);
   if (b == 0) return PD_OK;
+  if (mixed(c)) {
+    if (!c->has_families) return fail(c, PD_ERR_ORDER, "mixed form: families first (they fix the scales)");
+    pd::launch_from_mixed(mixed_args(c), u ? c->u : nullptr, v ? c->v : nullptr, f ? c->f : nullptr, c->stream);
+    PD_CK(c, cudaGetLastError());
+    PD_CK(c, cudaStreamSynchronize(c->stream));
+  }
   if (u) PD_CK(c, cudaMemcpy(u, c->u, b, cudaMemcpyDeviceToHost));
   if (v) PD_CK(c, cudaMemcpy(v, c->v, b, cudaMemcpyDeviceToHost));
   if (f) PD_CK(c, cudaMemcpy(f, c->f, b, cudaMemcpyDeviceToHost));
@@ -492,13 +624,36 @@ int pd_get_counters(pd_ctx* c, pd_counters* out) {
 namespace {
 
 // Launch sequence of nsteps steps on stream s (graph-capturable).
+// One launcher per kernel kind, so graph capture and per-kernel profiling
+// issue the same sequence.
+struct Launcher {
+  pd_ctx* c;
+  Fp64Args f;
+  pd::MixedArgs m;
+  bool brk;
+  explicit Launcher(pd_ctx* ctx) : c(ctx), brk(ctx->p.s_c > 0.0) {
+    if (mixed(ctx))
+      m = mixed_args(ctx);
+    else
+      f = fp64_args(ctx);
+  }
+  void drift(cudaStream_t s) {
+    if (mixed(c)) pd::launch_drift_mixed(m, s); else pd::launch_drift_fp64(f, s);
+  }
+  void pass_a(cudaStream_t s) {
+    if (mixed(c)) pd::launch_pass_a_mixed(m, brk, s); else pd::launch_pass_a_fp64(f, brk, s);
+  }
+  void pass_b(bool next_drift, cudaStream_t s) {
+    if (mixed(c)) pd::launch_pass_b_mixed(m, next_drift, s); else pd::launch_pass_b_fp64(f, next_drift ? 1 : 0, s);
+  }
+};
+
 void enqueue_steps(pd_ctx* c, int32_t nsteps, cudaStream_t s) {
-  const Fp64Args a = fp64_args(c);
-  const bool brk = c->p.s_c > 0.0;
-  pd::launch_drift_fp64(a, s);
+  Launcher L(c);
+  L.drift(s);
   for (int32_t k = 0; k < nsteps; ++k) {
-    pd::launch_pass_a_fp64(a, brk, s);
-    pd::launch_pass_b_fp64(a, k + 1 < nsteps ? 1 : 0, s);
+    L.pass_a(s);
+    L.pass_b(k + 1 < nsteps, s);
   }
 }
 
@@ -551,6 +706,7 @@ int pd_compute_velocity(pd_ctx* c, const double* u, double* velocity, double* ac
   if (!c) return PD_ERR_ARG;
   if (!c->has_families) return fail(c, PD_ERR_ORDER, "families first");
   if (!u || !velocity || !acce || !netF) return fail(c, PD_ERR_ARG, "NULL buffer");
+  if (mixed(c)) return fail(c, PD_ERR_ARG, "pd_compute_velocity is the FP64 drop-in; create the context with PD_FP64");
   if (c->n == 0) return PD_OK;
   PD_CK(c, cudaSetDevice(c->p.device));
   const size_t b = (size_t)c->n * sizeof(double2);
@@ -599,21 +755,20 @@ int pd_profile_steps(pd_ctx* c, int32_t nsteps, double* ms, int64_t* launches) {
   std::vector<cudaEvent_t> ev(nev);
   for (auto& e : ev) PD_CK(c, cudaEventCreate(&e));
   std::vector<int> kind;
-  const Fp64Args a = fp64_args(c);
-  const bool brk = c->p.s_c > 0.0;
+  Launcher L(c);
   cudaStream_t s = c->stream;
   int q = 0;
   cudaEventRecord(ev[q++], s);
-  pd::launch_drift_fp64(a, s);
+  L.drift(s);
   cudaEventRecord(ev[q++], s);
   kind.push_back(PD_KERNEL_DRIFT);
   for (int32_t k = 0; k < nsteps; ++k) {
     cudaEventRecord(ev[q++], s);
-    pd::launch_pass_a_fp64(a, brk, s);
+    L.pass_a(s);
     cudaEventRecord(ev[q++], s);
     kind.push_back(PD_KERNEL_PASS_A);
     cudaEventRecord(ev[q++], s);
-    pd::launch_pass_b_fp64(a, k + 1 < nsteps ? 1 : 0, s);
+    L.pass_b(k + 1 < nsteps, s);
     cudaEventRecord(ev[q++], s);
     kind.push_back(PD_KERNEL_PASS_B);
   }

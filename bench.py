@@ -202,59 +202,83 @@ def run_reference(args, comm):
     }), flush=True)
 
 
-def run_ours(args, comm):
-    pdg = importlib.import_module("2d_pd_gpu_gb300")
-    nat = pdg.native
-    prec = args.precision
-    plate = pdg.plates.config_plate_scale(side=args.side, seed=args.seed + comm.rank)
-    device = comm.local
-    ctx = plate.context(precision=nat.PD_FP64 if prec == "fp64" else nat.PD_MIXED, device=device)
+def measure(ctx, prec, args, comm, sampler=None):
+    """Warm up, time K steps (one graph), then time every kernel of K more steps."""
     n, nb = ctx.n, ctx.nnz
-    sampler = ClockSampler(device)
-    sampler.start()
     ctx.step(args.warmup)
     ctx.synchronize()
     comm.barrier()
     ms = ctx.step_timed(args.steps)
     comm.barrier()
     ms_max = comm.max(ms)
-    bonds_all = comm.sum(nb * args.steps)
-    value = bonds_all / (ms_max / 1e3)
-    # per-kernel durations (CUDA events around each launch on the context stream)
+    value = comm.sum(nb * args.steps) / (ms_max / 1e3)
     prof = ctx.profile_steps(args.steps)
-    clocks = sampler.stop()
     model = byte_model(prec, n, nb)
-    share = {k: prof[k][0] for k in prof}
-    tot = sum(share.values())
-    dom = max(("pass_a", "pass_b"), key=lambda k: share[k])
+    tot = sum(v[0] for v in prof.values())
+    dom = max(("pass_a", "pass_b"), key=lambda k: prof[k][0])
     avg_ms = prof[dom][0] / max(prof[dom][1], 1)
     peaks, peak_kind = load_peaks()
     achieved = model[dom] / (avg_ms / 1e3) / 1e9
     kernels = {k: {"launches": prof[k][1], "avg_ms": prof[k][0] / max(prof[k][1], 1),
                    "share": prof[k][0] / tot if tot else None,
-                   "achieved_gbs": (model[k] / (prof[k][0] / max(prof[k][1], 1) / 1e3) / 1e9) if prof[k][1] else None}
+                   "achieved_gbs": (model[k] / (prof[k][0] / max(prof[k][1], 1) / 1e3) / 1e9) if prof[k][1] else None,
+                   "algorithmic_bytes": model[k]}
                for k in prof}
-    step_ms = ms_max / args.steps
+    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)", "algorithmic_bytes_per_launch": model[dom]}
+    return value, ms_max / args.steps, kernels, roof
+
+
+def accuracy(pdg, plate, device, checkpoints=(100, 500, 1000)):
+    """Mixed vs FP64 from the same initial state: max / RMS displacement error
+    (normwise), velocity error, and bond-mask mismatches at each checkpoint."""
+    nat = pdg.native
+    a = plate.context(precision=nat.PD_FP64, device=device)
+    b = plate.context(precision=nat.PD_MIXED, device=device)
+    out, done = {}, 0
+    for t in checkpoints:
+        a.step(t - done)
+        b.step(t - done)
+        done = t
+        ua, va, _ = a.state()
+        ub, vb, _ = b.state()
+        ma, mb = a.bond_mask(), b.bond_mask()
+        out[str(t)] = {"u_max_rel": float(np.abs(ub - ua).max() / np.abs(ua).max()),
+                       "u_rms_rel": float(np.sqrt(((ub - ua) ** 2).mean() / (ua ** 2).mean())),
+                       "v_max_rel": float(np.abs(vb - va).max() / np.abs(va).max()),
+                       "mask_mismatch": int((ma != mb).sum()), "bonds_broken_fp64": int((ma == 0).sum())}
+    a.close()
+    b.close()
+    return out
+
+
+def run_ours(args, comm):
+    pdg = importlib.import_module("2d_pd_gpu_gb300")
+    nat = pdg.native
+    plate = pdg.plates.config_plate_scale(side=args.side, seed=args.seed + comm.rank)
+    device = comm.local
+    sampler = ClockSampler(device)
+    sampler.start()
+    ctx = plate.context(precision=nat.PD_FP64, device=device)
+    n, nb = ctx.n, ctx.nnz
+    value, step_ms, kernels, roof = measure(ctx, "fp64", args, comm)
     result = {
         "metric": "bond-updates/s", "value": value, "unit": "bond-updates/s", "n_gpus": comm.world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f32+f64",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded plate generator)",
-        "config": {"workload": f"plate{args.side}x{args.side}-{prec}-crack-sc5e-4", "particles": n, "bonds": nb,
-                   "precision": prec, "parallelism": f"replicas x{comm.world}",
+        "config": {"workload": f"plate{args.side}x{args.side}-fp64-crack-sc5e-4", "particles": n, "bonds": nb,
+                   "precision": "fp64", "parallelism": f"replicas x{comm.world}",
                    "l2": "inputs larger than L2 (~2 GB state vs 129 MB L2)"},
         "gpu_launches": 1 + 2 * args.steps,
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                     "frac": achieved / peaks["hbm_gbs"], "traffic": None,
-                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                     "algorithmic_bytes_per_launch": model[dom]},
+        "roofline": roof,
         "kernels": kernels,
-        "clocks": clocks,
     }
-    if prec == "fp64":
-        ops = fp64_ops(n, nb) / (step_ms / 1e3)
-        result["fp64_alu"] = {"ops_per_s": ops, "peak_ops_per_s": MEASURED_FP64_DFMA_PER_S,
-                              "frac": ops / MEASURED_FP64_DFMA_PER_S, "ops_per_step": fp64_ops(n, nb)}
+    ops = fp64_ops(n, nb) / (step_ms / 1e3)
+    result["fp64_alu"] = {"ops_per_s": ops, "peak_ops_per_s": MEASURED_FP64_DFMA_PER_S,
+                          "frac": ops / MEASURED_FP64_DFMA_PER_S, "ops_per_step": fp64_ops(n, nb),
+                          "peak_source": "measured DFMA issue rate on this GB300 (profiles/fp64_alu_peak.md)"}
     # end to end through the public API with pinned host buffers, every step
     if not args.no_e2e:
         esteps = min(args.steps, args.e2e_steps)
@@ -275,6 +299,16 @@ def run_ours(args, comm):
         for b in bufs:
             b.free()
     ctx.close()
+    if not args.no_mixed:
+        mctx = plate.context(precision=nat.PD_MIXED, device=device)
+        mvalue, mstep_ms, mkernels, mroof = measure(mctx, "mixed", args, comm)
+        mctx.close()
+        result["mixed"] = {"value": mvalue, "unit": "bond-updates/s", "ms_per_step": mstep_ms,
+                           "speedup_vs_fp64": mvalue / value, "dtype": "f32 bonds + f64 K^-1/det",
+                           "roofline": mroof, "kernels": mkernels, "gpu_launches": 1 + 2 * args.steps}
+        if not args.no_accuracy and comm.rank == 0:
+            result["mixed"]["accuracy_vs_fp64"] = accuracy(pdg, plate, device)
+    result["clocks"] = sampler.stop()
     if comm.rank == 0 and not args.no_cpu:
         nth = os.cpu_count() or 1
         nbc, secs = cpu_step_rate(plate, args.cpu_steps, nth)
@@ -292,13 +326,14 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--side", type=int, default=1000)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
