@@ -30,12 +30,12 @@ struct pd_ctx {
   // per particle
   double2 *x = nullptr, *u = nullptr, *v = nullptr, *f = nullptr, *acc = nullptr;
   double *vol = nullptr, *kinv22 = nullptr, *damage = nullptr;
-  double2 *w01 = nullptr, *w23 = nullptr, *kinv01 = nullptr, *mt = nullptr;
+  double2 *w01 = nullptr, *w23 = nullptr, *kinv01 = nullptr, *mt = nullptr, *hg = nullptr;
   uint8_t *bc = nullptr, *singular = nullptr;
   int32_t *broken = nullptr, *fam = nullptr;
   // mixed form (PD_MIXED)
   float4 *xs = nullptr, *us = nullptr, *vsm = nullptr, *ws = nullptr, *geo = nullptr;
-  float2 *fs = nullptr, *mh = nullptr;
+  float2 *fs = nullptr, *mh = nullptr, *hgs = nullptr;
   float* vh = nullptr;
   // BC groups
   int32_t* gkind = nullptr;
@@ -107,7 +107,7 @@ void free_particles(pd_ctx* c) {
   free_families(c);
   dfree(c->x); dfree(c->u); dfree(c->v); dfree(c->f); dfree(c->acc);
   dfree(c->vol); dfree(c->kinv22); dfree(c->damage);
-  dfree(c->w01); dfree(c->w23); dfree(c->kinv01); dfree(c->mt);
+  dfree(c->w01); dfree(c->w23); dfree(c->kinv01); dfree(c->mt); dfree(c->hg); dfree(c->hgs);
   dfree(c->bc); dfree(c->singular); dfree(c->broken); dfree(c->fam);
   dfree(c->xs); dfree(c->us); dfree(c->vsm); dfree(c->ws); dfree(c->geo);
   dfree(c->fs); dfree(c->mh); dfree(c->vh);
@@ -121,7 +121,7 @@ int check_params(pd_ctx* c, const pd_params* p) {
   if (!p) return fail(c, PD_ERR_ARG, "params is NULL");
   if (p->precision != PD_FP64 && p->precision != PD_MIXED) return fail(c, PD_ERR_ARG, "unknown precision");
   if (!(p->rho > 0.0) || !(p->dt > 0.0) || !std::isfinite(p->E) || !(p->nu > -1.0 && p->nu < 1.0) ||
-      !(p->det_guard >= 0.0))
+      !(p->det_guard >= 0.0) || !(p->k_hg >= 0.0) || !std::isfinite(p->k_hg))
     return fail(c, PD_ERR_ARG, "invalid material / time-step parameters");
   if (p->singular_policy != PD_SINGULAR_ZERO && p->singular_policy != PD_SINGULAR_ERROR)
     return fail(c, PD_ERR_ARG, "unknown singular_policy");
@@ -134,7 +134,7 @@ Fp64Args fp64_args(pd_ctx* c) {
   Fp64Args a{};
   a.n = c->n;
   a.x = c->x; a.vol = c->vol; a.u = c->u; a.v = c->v; a.f = c->f; a.acc = c->acc;
-  a.w01 = c->w01; a.w23 = c->w23; a.kinv01 = c->kinv01; a.kinv22 = c->kinv22; a.mt = c->mt;
+  a.w01 = c->w01; a.w23 = c->w23; a.kinv01 = c->kinv01; a.kinv22 = c->kinv22; a.mt = c->mt; a.hg = c->hg;
   a.bc = c->bc; a.gkind = c->gkind; a.gval = c->gval;
   a.broken = c->broken; a.damage = c->damage; a.singular = c->singular; a.fam = c->fam;
   a.chunk_base = c->sell.chunk_base; a.chunk_w = c->sell.chunk_w; a.nbr = c->sell.nbr;
@@ -144,6 +144,7 @@ Fp64Args fp64_args(pd_ctx* c) {
   a.dt2 = c->p.dt * c->p.dt;
   a.inv_rho = 1.0 / c->p.rho;
   a.det_guard = c->p.det_guard;
+  a.k_hg = c->p.k_hg;
   a.counters = c->counters;
   return a;
 }
@@ -163,6 +164,7 @@ pd::MixedArgs mixed_args(pd_ctx* c) {
   a.n = c->n;
   a.x = c->x; a.vol = c->vol;
   a.xs = c->xs; a.vh = c->vh; a.us = c->us; a.vs = c->vsm; a.fs = c->fs; a.ws = c->ws; a.geo = c->geo; a.mh = c->mh;
+  a.hgs = c->hgs;
   a.bc = c->bc; a.gkind = c->gkind; a.gvel = c->gvel;
   a.broken = c->broken; a.damage = c->damage; a.singular = c->singular; a.fam = c->fam;
   a.chunk_base = c->sell.chunk_base; a.chunk_w = c->sell.chunk_w; a.nbr = c->sell.nbr;
@@ -174,6 +176,7 @@ pd::MixedArgs mixed_args(pd_ctx* c) {
   a.c33 = (float)(c33 / es);
   a.s2 = c->p.s_c > 0.0 ? (float)(c->p.s_c * (2.0 + c->p.s_c)) : INFINITY;
   a.tau2 = (float)(es * c->p.dt * c->p.dt / (c->p.rho * c->ls * c->ls));
+  a.k_hg = (float)(c->p.k_hg * c->vs_scale * c->ls * c->ls / es);
   a.inv_ls = 1.0 / c->ls;
   a.inv_vs = 1.0 / c->vs_scale;
   a.v_scale = c->p.dt / c->ls;
@@ -270,6 +273,7 @@ void pd_default_params(pd_params* p) {
   p->dt = 1e-8;
   p->s_c = 0.0;
   p->det_guard = 1e-10;
+  p->k_hg = 0.0;
   p->singular_policy = PD_SINGULAR_ZERO;
 }
 
@@ -394,6 +398,7 @@ int pd_set_particles(pd_ctx* c, int64_t n, const double* x, const double* vol) {
     PD_CK(c, cudaMalloc(&c->geo, nn * sizeof(float4)));
     PD_CK(c, cudaMalloc(&c->fs, nn * sizeof(float2)));
     PD_CK(c, cudaMalloc(&c->mh, nn * sizeof(float2)));
+    PD_CK(c, cudaMalloc(&c->hgs, nn * sizeof(float2)));
     PD_CK(c, cudaMalloc(&c->vh, nn * sizeof(float)));
   } else {
     PD_CK(c, cudaMalloc(&c->acc, nn * sizeof(double2)));
@@ -401,6 +406,7 @@ int pd_set_particles(pd_ctx* c, int64_t n, const double* x, const double* vol) {
     PD_CK(c, cudaMalloc(&c->w23, nn * sizeof(double2)));
     PD_CK(c, cudaMalloc(&c->kinv01, nn * sizeof(double2)));
     PD_CK(c, cudaMalloc(&c->mt, nn * sizeof(double2)));
+    PD_CK(c, cudaMalloc(&c->hg, nn * sizeof(double2)));
     PD_CK(c, cudaMalloc(&c->kinv22, nn * sizeof(double)));
   }
   PD_CK(c, cudaMalloc(&c->damage, nn * sizeof(double)));
@@ -530,11 +536,13 @@ int pd_reset(pd_ctx* c) {
     PD_CK(c, cudaMemsetAsync(c->vsm, 0, nn * sizeof(float4), s));
     PD_CK(c, cudaMemsetAsync(c->ws, 0, nn * sizeof(float4), s));
     PD_CK(c, cudaMemsetAsync(c->fs, 0, nn * sizeof(float2), s));
+    PD_CK(c, cudaMemsetAsync(c->hgs, 0, nn * sizeof(float2), s));
     pd::launch_init_geometry_mixed(mixed_args(c), s);
   } else {
     PD_CK(c, cudaMemsetAsync(c->acc, 0, nn * sizeof(double2), s));
     PD_CK(c, cudaMemsetAsync(c->w01, 0, nn * sizeof(double2), s));
     PD_CK(c, cudaMemsetAsync(c->w23, 0, nn * sizeof(double2), s));
+    PD_CK(c, cudaMemsetAsync(c->hg, 0, nn * sizeof(double2), s));
     pd::launch_init_geometry_fp64(fp64_args(c), s);
   }
   PD_CK(c, cudaGetLastError());

@@ -15,7 +15,8 @@
 //                           S = sigma K^-1 of computeForceDensityStates :355
 //   k_pass_b              : computeVelocity :396-470 in gather form
 //                           f_i = sum_j V_j (S_i + S_j) xi_ij (= T_ij - T_ji)
-// FP64 operations per bond: pass A 11 (d 2, stretch test 5, D 4), pass B 4.
+// FP64 operations per bond: pass A 11 (d 2, stretch test 5, D 4) + 2 with the
+// zero-energy-mode penalty (sum V_j d), pass B 4.
 #include "pd_internal.h"
 
 namespace pd {
@@ -90,14 +91,14 @@ __global__ void __launch_bounds__(kBlock) k_drift(Fp64Args a) {
   a.u[i] = u;
 }
 
-template <bool BREAK>
+template <bool BREAK, bool HG>
 __global__ void __launch_bounds__(kBlock) k_pass_a(Fp64Args a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   int w;
   const int64_t s0 = slot0(a, i, &w);
   const double2 ui = a.u[i];
-  double d11 = 0.0, d12 = 0.0, d21 = 0.0, d22 = 0.0;
+  double d11 = 0.0, d12 = 0.0, d21 = 0.0, d22 = 0.0, ax = 0.0, ay = 0.0;
   int newly = 0;
   for (int k = 0; k < w; ++k) {
     const int64_t s = s0 + (int64_t)k * kChunk;
@@ -119,6 +120,15 @@ __global__ void __launch_bounds__(kBlock) k_pass_a(Fp64Args a) {
     d12 = fma(dx, t.y, d12);
     d21 = fma(dy, t.x, d21);
     d22 = fma(dy, t.y, d22);
+    if (HG) {
+      const double vj = a.vol[j];
+      ax = fma(vj, dx, ax);
+      ay = fma(vj, dy, ay);
+    }
+  }
+  if (HG) {
+    const double k2 = 2.0 * a.k_hg;
+    a.hg[i] = make_double2(k2 * ax, k2 * ay);
   }
   if (BREAK && newly) {
     atomicAdd(a.counters + CNT_BROKEN, (unsigned long long)newly);
@@ -142,19 +152,32 @@ __global__ void __launch_bounds__(kBlock) k_pass_a(Fp64Args a) {
   const double s22 = fma(a.c12, e11, a.c11 * e22);
   const double s12 = a.c33 * e12;
   const double vi = a.vol[i];
-  a.w01[i] = make_double2(vi * fma(s11, k11, s12 * k12), vi * fma(s11, k12, s12 * k22));
-  a.w23[i] = make_double2(vi * fma(s12, k11, s22 * k12), vi * fma(s12, k12, s22 * k22));
+  if (HG) {  // W = V (sigma K^-1 - k G)
+    const double kh = -a.k_hg;
+    a.w01[i] = make_double2(vi * fma(kh, g11, fma(s11, k11, s12 * k12)), vi * fma(kh, g12, fma(s11, k12, s12 * k22)));
+    a.w23[i] = make_double2(vi * fma(kh, g21, fma(s12, k11, s22 * k12)), vi * fma(kh, g22, fma(s12, k12, s22 * k22)));
+  } else {
+    a.w01[i] = make_double2(vi * fma(s11, k11, s12 * k12), vi * fma(s11, k12, s12 * k22));
+    a.w23[i] = make_double2(vi * fma(s12, k11, s22 * k12), vi * fma(s12, k12, s22 * k22));
+  }
 }
 
-template <int MODE>
+template <int MODE, bool HG>
 __global__ void __launch_bounds__(kBlock) k_pass_b(Fp64Args a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   int w;
   const int64_t s0 = slot0(a, i, &w);
   const double2 wa = a.w01[i], wb = a.w23[i], m = a.mt[i];
-  double fx = fma(wa.x, m.x, wa.y * m.y);
-  double fy = fma(wb.x, m.x, wb.y * m.y);
+  double fx, fy;
+  if (HG) {
+    const double2 h = a.hg[i];
+    fx = fma(wa.x, m.x, fma(wa.y, m.y, h.x));
+    fy = fma(wb.x, m.x, fma(wb.y, m.y, h.y));
+  } else {
+    fx = fma(wa.x, m.x, wa.y * m.y);
+    fy = fma(wb.x, m.x, wb.y * m.y);
+  }
   for (int k = 0; k < w; ++k) {
     const int64_t s = s0 + (int64_t)k * kChunk;
     const int j = a.nbr[s];
@@ -202,21 +225,31 @@ void launch_drift_fp64(const Fp64Args& a, cudaStream_t s) {
 
 void launch_pass_a_fp64(const Fp64Args& a, bool breaking, cudaStream_t s) {
   if (a.n <= 0) return;
+  const unsigned nb = (unsigned)blocks_for(a.n);
+  const bool hg = a.k_hg != 0.0;
   if (breaking)
-    k_pass_a<true><<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
+    hg ? k_pass_a<true, true><<<nb, kBlock, 0, s>>>(a) : k_pass_a<true, false><<<nb, kBlock, 0, s>>>(a);
   else
-    k_pass_a<false><<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
+    hg ? k_pass_a<false, true><<<nb, kBlock, 0, s>>>(a) : k_pass_a<false, false><<<nb, kBlock, 0, s>>>(a);
+}
+
+template <int MODE>
+void launch_b(const Fp64Args& a, unsigned nb, cudaStream_t s) {
+  if (a.k_hg != 0.0)
+    k_pass_b<MODE, true><<<nb, kBlock, 0, s>>>(a);
+  else
+    k_pass_b<MODE, false><<<nb, kBlock, 0, s>>>(a);
 }
 
 void launch_pass_b_fp64(const Fp64Args& a, int mode, cudaStream_t s) {
   if (a.n <= 0) return;
   const unsigned nb = (unsigned)blocks_for(a.n);
   if (mode == 0)
-    k_pass_b<0><<<nb, kBlock, 0, s>>>(a);
+    launch_b<0>(a, nb, s);
   else if (mode == 1)
-    k_pass_b<1><<<nb, kBlock, 0, s>>>(a);
+    launch_b<1>(a, nb, s);
   else
-    k_pass_b<2><<<nb, kBlock, 0, s>>>(a);
+    launch_b<2>(a, nb, s);
 }
 
 }  // namespace pd

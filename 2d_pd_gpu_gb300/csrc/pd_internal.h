@@ -60,8 +60,9 @@ struct Fp64Args {
   const double2* __restrict__ bxi;
   const double2* __restrict__ bgeo;
   const double* __restrict__ blim;
+  double2* hg;  // 2 k_hg sum_j V_j (u_j - u_i), pass A -> pass B
   double c11, c12, c33;
-  double dt, dt2, inv_rho, det_guard;
+  double dt, dt2, inv_rho, det_guard, k_hg;
   unsigned long long* counters;
 };
 
@@ -78,6 +79,7 @@ struct MixedArgs {
   float4* ws;                       // W^ = V^ sigma^ K^-1 (row-major 2x2)
   float4* geo;                      // {K^-1 11, 12, 22, V^_i}
   float2* mh;                       // m^ / V^_i
+  float2* hgs;                      // 2 k^ sum_j V^_j du^ (pass A -> pass B)
   const uint8_t* __restrict__ bc;
   const int32_t* __restrict__ gkind;
   const float4* __restrict__ gvel;  // prescribed v^ per group, two-float
@@ -90,6 +92,7 @@ struct MixedArgs {
   int32_t* nbr;
   float c11, c12, c33;  // C / Es
   float s2, tau2;       // stretch limit factor, Es dt^2 / (rho Ls^2)
+  float k_hg;           // k Vs Ls^2 / Es
   double inv_ls, inv_vs, v_scale, f_scale, det_guard;
   unsigned long long* counters;
 };
@@ -125,7 +128,7 @@ void scan_exclusive_i64(const int64_t* in, int64_t* out, int64_t n, cudaStream_t
 // ---- FP64 step (pd_fp64.cu)
 void launch_init_geometry_fp64(const Fp64Args& a, cudaStream_t s);
 void launch_drift_fp64(const Fp64Args& a, cudaStream_t s);
-void launch_pass_a_fp64(const Fp64Args& a, bool breaking, cudaStream_t s);
+void launch_pass_a_fp64(const Fp64Args& a, bool breaking, cudaStream_t s);  // hourglass term if a.k_hg != 0
 // mode 0: kick; 1: kick + next step's drift; 2: drop-in kick (acc array in/out)
 void launch_pass_b_fp64(const Fp64Args& a, int mode, cudaStream_t s);
 

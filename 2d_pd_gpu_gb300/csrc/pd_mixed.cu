@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(kBlock) k_pass_a_mixed(MixedArgs a) {
   int w;
   const int64_t s0 = slot0(a, i, &w);
   const float4 ui = a.us[i], xi = a.xs[i];
-  float d11 = 0.f, d12 = 0.f, d21 = 0.f, d22 = 0.f;
+  float d11 = 0.f, d12 = 0.f, d21 = 0.f, d22 = 0.f, ax = 0.f, ay = 0.f;
   int newly = 0;
   for (int k = 0; k < w; ++k) {
     const int64_t s = s0 + (int64_t)k * kChunk;
@@ -148,7 +148,10 @@ __global__ void __launch_bounds__(kBlock) k_pass_a_mixed(MixedArgs a) {
     d12 = fmaf(dx, t1, d12);
     d21 = fmaf(dy, t0, d21);
     d22 = fmaf(dy, t1, d22);
+    ax = fmaf(vj, dx, ax);
+    ay = fmaf(vj, dy, ay);
   }
+  a.hgs[i] = make_float2(2.f * a.k_hg * ax, 2.f * a.k_hg * ay);
   if (BREAK && newly) {
     atomicAdd(a.counters + CNT_BROKEN, (unsigned long long)newly);
     const int32_t b = a.broken[i] + newly;
@@ -168,8 +171,9 @@ __global__ void __launch_bounds__(kBlock) k_pass_a_mixed(MixedArgs a) {
   const float s11 = fmaf(a.c11, e11, a.c12 * e22);
   const float s22 = fmaf(a.c12, e11, a.c11 * e22);
   const float s12 = a.c33 * e12;
-  a.ws[i] = make_float4(vi * fmaf(s11, k11, s12 * k12), vi * fmaf(s11, k12, s12 * k22),
-                        vi * fmaf(s12, k11, s22 * k12), vi * fmaf(s12, k12, s22 * k22));
+  const float kh = -a.k_hg;  // W^ = V^ (sigma^ K^-1 - k^ G)
+  a.ws[i] = make_float4(vi * fmaf(kh, g11, fmaf(s11, k11, s12 * k12)), vi * fmaf(kh, g12, fmaf(s11, k12, s12 * k22)),
+                        vi * fmaf(kh, g21, fmaf(s12, k11, s22 * k12)), vi * fmaf(kh, g22, fmaf(s12, k12, s22 * k22)));
 }
 
 template <bool DRIFT>
@@ -179,10 +183,10 @@ __global__ void __launch_bounds__(kBlock) k_pass_b_mixed(MixedArgs a) {
   int w;
   const int64_t s0 = slot0(a, i, &w);
   const float4 wi = a.ws[i], xi = a.xs[i];
-  const float2 m = a.mh[i];
+  const float2 m = a.mh[i], h = a.hgs[i];
   // compensated sums (value, correction) per component
-  float sx = fmaf(wi.x, m.x, wi.y * m.y), cx = 0.f;
-  float sy = fmaf(wi.z, m.x, wi.w * m.y), cy = 0.f;
+  float sx = fmaf(wi.x, m.x, fmaf(wi.y, m.y, h.x)), cx = 0.f;
+  float sy = fmaf(wi.z, m.x, fmaf(wi.w, m.y, h.y)), cy = 0.f;
   for (int k = 0; k < w; ++k) {
     const int64_t s = s0 + (int64_t)k * kChunk;
     const int j = __ldcs(&a.nbr[s]);

@@ -38,6 +38,7 @@ class Params(ctypes.Structure):
         ("dt", ctypes.c_double),
         ("s_c", ctypes.c_double),
         ("det_guard", ctypes.c_double),
+        ("k_hg", ctypes.c_double),
         ("singular_policy", ctypes.c_int32),
         ("reserved", ctypes.c_int32),
     ]

@@ -11,6 +11,11 @@ bottom `bc_rows` rows carry prescribed +-y velocity (the reference selects one
 row per face with defineBoundarySet, src/SetupParticleSystem.cpp:513-529; the
 plate workloads ask for three).  Random numbers come from a counter-based
 splitmix64 stream, so every consumer regenerates identical inputs.
+
+The plates run with a zero-energy-mode penalty (G_s = 0.25): the classic
+correspondence model alone lets the velocity loading grow hourglass modes
+until bonds fail spuriously and the run diverges (pass hourglass=0 or
+k_hg=0 for the reference's model).
 """
 from __future__ import annotations
 
@@ -67,19 +72,28 @@ class Plate:
     steps: int
     name: str = ""
     meta: dict = field(default_factory=dict)
+    hourglass: float = 0.25  # G_s of the zero-energy-mode penalty (0: the reference's model)
 
     @property
     def n(self):
         return self.x.shape[0]
 
-    def params(self, precision=native.PD_FP64, device=0, s_c=None, det_guard=1e-10):
+    @property
+    def k_hg(self):
+        """Zero-energy-mode penalty coefficient k = G_s C11 / (mean V * cutoff^2)."""
+        m = self.material
+        c11 = m.E / (1.0 - m.nu * m.nu)
+        return self.hourglass * c11 / (float(self.vol.mean()) * self.cutoff * self.cutoff)
+
+    def params(self, precision=native.PD_FP64, device=0, s_c=None, det_guard=1e-10, k_hg=None):
         m = self.material
         return native.default_params(precision=precision, device=device, E=m.E, nu=m.nu, rho=m.rho, dt=self.dt,
-                                     s_c=m.s_c if s_c is None else s_c, det_guard=det_guard)
+                                     s_c=m.s_c if s_c is None else s_c, det_guard=det_guard,
+                                     k_hg=self.k_hg if k_hg is None else k_hg)
 
-    def context(self, precision=native.PD_FP64, device=0, s_c=None):
+    def context(self, precision=native.PD_FP64, device=0, s_c=None, k_hg=None):
         """A device context with particles, GPU-built families and BCs set."""
-        ctx = native.Context(self.params(precision, device, s_c))
+        ctx = native.Context(self.params(precision, device, s_c, k_hg=k_hg))
         ctx.set_particles(self.x, self.vol)
         ctx.build_families(self.cutoff, self.cracks)
         ctx.set_bc(self.group_kind, self.group_val, self.group_of)

@@ -67,6 +67,16 @@ typedef struct pd_params {
   double dt;               /* time step (src/main_seq.cpp:657 stepSize) */
   double s_c;              /* critical stretch; <= 0 disables bond breaking */
   double det_guard;        /* singular if det(K) <= det_guard * K11 * K22 */
+  /* Zero-energy-mode (hourglass) penalty coefficient k (force density per
+   * volume per length^2; 0 = the reference's correspondence model exactly).
+   * Adds T_ij += k (eta_ij - F_i xi_ij) to every bond, so the force gains
+   * 2k sum_j V_j (u_j - u_i) - k G_i m_i - k sum_j V_j G_j xi_ij (G = F - I).
+   * The classic model has zero-energy modes (the reference has no control,
+   * its bond-associated n1/n2 weights aside); without this, the plate
+   * workloads' velocity loading grows them until bonds fail spuriously and
+   * the run diverges.  A common choice is k = G_s C11 / (mean V * cutoff^2)
+   * with G_s ~ 0.25 at dt = 0.8 CFL. */
+  double k_hg;
   int32_t singular_policy; /* PD_SINGULAR_ZERO / PD_SINGULAR_ERROR */
   int32_t reserved;
 } pd_params;

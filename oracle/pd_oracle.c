@@ -237,6 +237,7 @@ int pdo_init(const pdo_problem* pb, pdo_state* st) {
   memset(st->broken, 0, (size_t)n * sizeof(int32_t));
   memset(st->damage, 0, (size_t)n * sizeof(double));
   memset(st->w, 0, (size_t)n * 4 * sizeof(double));
+  memset(st->hg, 0, (size_t)n * 2 * sizeof(double));
 #pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < n; ++i) kinv_of(pb, st, i);
   return 0;
@@ -281,7 +282,7 @@ static int64_t pass_a(const pdo_problem* pb, pdo_state* st) {
   for (int64_t i = 0; i < pb->n; ++i) {
     const double xi = pb->x[2 * i], yi = pb->x[2 * i + 1];
     const double ui = st->u[2 * i], wi = st->u[2 * i + 1];
-    double d11 = 0.0, d12 = 0.0, d21 = 0.0, d22 = 0.0;
+    double d11 = 0.0, d12 = 0.0, d21 = 0.0, d22 = 0.0, ax = 0.0, ay = 0.0;
     int32_t newly = 0;
     for (int64_t s = pb->row_ptr[i]; s < pb->row_ptr[i + 1]; ++s) {
       if (!st->alive[s]) continue;
@@ -300,6 +301,13 @@ static int64_t pass_a(const pdo_problem* pb, pdo_state* st) {
       d12 = fma(dx, t1, d12);
       d21 = fma(dy, t0, d21);
       d22 = fma(dy, t1, d22);
+      ax = fma(pb->vol[j], dx, ax);
+      ay = fma(pb->vol[j], dy, ay);
+    }
+    {
+      const double k2 = 2.0 * pb->k_hg;
+      st->hg[2 * i] = k2 * ax;
+      st->hg[2 * i + 1] = k2 * ay;
     }
     if (newly) {
       st->broken[i] += newly;
@@ -322,11 +330,13 @@ static int64_t pass_a(const pdo_problem* pb, pdo_state* st) {
     const double s11 = fma(c[0], e11, c[1] * e22);
     const double s22 = fma(c[1], e11, c[0] * e22);
     const double s12 = c[2] * e12;
-    const double vi = pb->vol[i];
-    w[0] = vi * fma(s11, k11, s12 * k12);
-    w[1] = vi * fma(s11, k12, s12 * k22);
-    w[2] = vi * fma(s12, k11, s22 * k12);
-    w[3] = vi * fma(s12, k12, s22 * k22);
+    const double vi = pb->vol[i], kh = -pb->k_hg;
+    /* W = V (sigma K^-1 - k_hg G): correspondence stress plus the
+       zero-energy-mode penalty's -k G xi part */
+    w[0] = vi * fma(kh, g11, fma(s11, k11, s12 * k12));
+    w[1] = vi * fma(kh, g12, fma(s11, k12, s12 * k22));
+    w[2] = vi * fma(kh, g21, fma(s12, k11, s22 * k12));
+    w[3] = vi * fma(kh, g22, fma(s12, k12, s22 * k22));
   }
   return nbroke;
 }
@@ -339,8 +349,8 @@ static void pass_b(const pdo_problem* pb, pdo_state* st) {
     const double xi = pb->x[2 * i], yi = pb->x[2 * i + 1];
     const double* wi = st->w + 4 * i;
     const double* mt = st->mt + 2 * i;
-    double fx = fma(wi[0], mt[0], wi[1] * mt[1]);
-    double fy = fma(wi[2], mt[0], wi[3] * mt[1]);
+    double fx = fma(wi[0], mt[0], fma(wi[1], mt[1], st->hg[2 * i]));
+    double fy = fma(wi[2], mt[0], fma(wi[3], mt[1], st->hg[2 * i + 1]));
     for (int64_t s = pb->row_ptr[i]; s < pb->row_ptr[i + 1]; ++s) {
       if (!st->alive[s]) continue;
       const int64_t j = pb->col[s];

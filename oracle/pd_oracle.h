@@ -39,6 +39,7 @@ typedef struct pdo_problem {
   double E, nu, rho, dt;
   double s_c;              /* critical stretch; <= 0 disables breaking */
   double det_guard;        /* relative det(K) guard, e.g. 1e-10 */
+  double k_hg;             /* zero-energy-mode penalty coefficient (0: the reference's model) */
   int32_t nthreads;        /* OpenMP threads, <= 0: runtime default */
 } pdo_problem;
 
@@ -51,7 +52,8 @@ typedef struct pdo_state {
   double* damage;     /* [n] broken / family size */
   double* kinv;       /* [n][3] K^-1 (11, 12, 22) of the alive bonds */
   double* mt;         /* [n][2] (sum_j V_j xi_ij) / V_i */
-  double* w;          /* [n][4] V_i * S_i, S = sigma K^-1 (row-major 2x2) */
+  double* w;          /* [n][4] V_i (S_i - k_hg G_i), S = sigma K^-1, G = F - I */
+  double* hg;         /* [n][2] 2 k_hg sum_j V_j (u_j - u_i) */
   uint8_t* singular;  /* [n] 1 if det guard tripped (S_i = 0) */
 } pdo_state;
 

@@ -46,6 +46,7 @@ class _Problem(ctypes.Structure):
         ("dt", ctypes.c_double),
         ("s_c", ctypes.c_double),
         ("det_guard", ctypes.c_double),
+        ("k_hg", ctypes.c_double),
         ("nthreads", ctypes.c_int32),
     ]
 
@@ -61,6 +62,7 @@ class _State(ctypes.Structure):
         ("kinv", _f64p),
         ("mt", _f64p),
         ("w", _f64p),
+        ("hg", _f64p),
         ("singular", _u8p),
     ]
 
@@ -131,6 +133,7 @@ class OracleSim:
     dt: float
     s_c: float = 0.0
     det_guard: float = 1e-10
+    k_hg: float = 0.0
     bc: np.ndarray | None = None
     group_kind: np.ndarray | None = None
     group_val: np.ndarray | None = None
@@ -161,13 +164,14 @@ class OracleSim:
         self.mt = np.zeros((n, 2))
         self.w = np.zeros((n, 4))
         self.singular = np.zeros(n, dtype=np.uint8)
+        self.hg = np.zeros((n, 2))
         self._pb = _Problem(n, _p(self.x, _f64p), _p(self.vol, _f64p), _p(self.row_ptr, _i64p),
                             _p(self.col, _i32p), _p(self.bc, _u8p), self.group_kind.size,
                             _p(self.group_kind, _i32p), _p(self.group_val, _f64p), self.E, self.nu, self.rho,
-                            self.dt, self.s_c, self.det_guard, self.nthreads)
+                            self.dt, self.s_c, self.det_guard, self.k_hg, self.nthreads)
         self._st = _State(_p(self.u, _f64p), _p(self.v, _f64p), _p(self.f, _f64p), _p(self.alive, _u8p),
                           _p(self.broken, _i32p), _p(self.damage, _f64p), _p(self.kinv, _f64p),
-                          _p(self.mt, _f64p), _p(self.w, _f64p), _p(self.singular, _u8p))
+                          _p(self.mt, _f64p), _p(self.w, _f64p), _p(self.hg, _f64p), _p(self.singular, _u8p))
         lib().pdo_init(ctypes.byref(self._pb), ctypes.byref(self._st))
 
     def step(self, nsteps=1):

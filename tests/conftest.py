@@ -70,8 +70,8 @@ def hassa_oracle(po, h, n1n2_zero=True):
                         group_val=np.array([[0.0, 5.0], [0.0, 0.0]]))
 
 
-def plate_oracle(po, p, s_c=None, families=None):
+def plate_oracle(po, p, s_c=None, families=None, k_hg=None):
     rp, col = families if families is not None else po.build_families(p.x, p.cutoff, p.cracks)
     return po.OracleSim(p.x, p.vol, rp, col, E=p.material.E, nu=p.material.nu, rho=p.material.rho, dt=p.dt,
-                        s_c=p.material.s_c if s_c is None else s_c, bc=p.group_of, group_kind=p.group_kind,
-                        group_val=p.group_val)
+                        s_c=p.material.s_c if s_c is None else s_c, k_hg=p.k_hg if k_hg is None else k_hg,
+                        bc=p.group_of, group_kind=p.group_kind, group_val=p.group_val)

@@ -72,7 +72,7 @@ def test_gpu_hassa_matches_reference_fixture(pdg, po, hassa):
 
 def test_gpu_plate30_matches_reference_fixture(pdg, plate30_ref):
     p = pdg.plates.make_plate(30, seed=3, crack="centre-half")
-    ctx = p.context(s_c=0.0)
+    ctx = p.context(s_c=0.0, k_hg=0.0)  # the reference's model (no zero-energy-mode penalty)
     rp, col = ctx.families()
     assert np.array_equal(rp, plate30_ref["row_ptr"]) and np.array_equal(col, plate30_ref["col"])
     ctx.step(1)

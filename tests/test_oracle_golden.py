@@ -73,7 +73,7 @@ def test_plate30_steps_match_reference(po, pdg, plate30_ref):
     fam = (plate30_ref["row_ptr"], plate30_ref["col"])
     rp, col = po.build_families(p.x, p.cutoff, p.cracks)
     assert np.array_equal(rp, fam[0]) and np.array_equal(col, fam[1])
-    sim = plate_oracle(po, p, s_c=0.0, families=fam)
+    sim = plate_oracle(po, p, s_c=0.0, families=fam, k_hg=0.0)  # the reference's model
     sim.step(1)
     assert normwise(sim.v, plate30_ref["v1"]) < V_TOL
     assert normwise(sim.u, plate30_ref["u1"]) < V_TOL
