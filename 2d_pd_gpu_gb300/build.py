@@ -31,6 +31,7 @@ CUDA_UNITS = [
     ("pd_family.cu", ["--fmad=false"]),
     ("pd_fp64.cu", ["--fmad=false"]),
     ("pd_mixed.cu", []),
+    ("pd_probe.cu", []),
     ("pd_api.cu", []),
 ]
 DROPIN_UNITS = ["pd_dropin.cpp"]

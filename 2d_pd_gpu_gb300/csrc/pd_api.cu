@@ -49,6 +49,8 @@ struct pd_ctx {
   pd::SellLayout sell;
   double2 *bxi = nullptr, *bgeo = nullptr;
   double* blim = nullptr;
+  float* br2 = nullptr;
+  float2* u32 = nullptr;
   // counters (device) + host mirror of steps
   unsigned long long* counters = nullptr;
   int64_t steps = 0;
@@ -56,6 +58,29 @@ struct pd_ctx {
   std::map<int32_t, cudaGraphExec_t> graphs;
   // drop-in staging (pinned)
   std::vector<void*> scratch;
+  // batch membership (pd_batch_add)
+  pd_batch* batch = nullptr;
+};
+
+struct pd_batch {
+  int32_t device = 0, precision = PD_FP64;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;
+  std::string err;
+  std::vector<pd_ctx*> members;
+  pd::BatchLaunch cfg;
+  int tile = 1024;
+  int nsm = 0;
+  bool dirty = true;
+  void* d_plates = nullptr;
+  size_t plates_bytes = 0;
+  pd::BatchTile* d_tiles = nullptr;
+  size_t tiles_cap = 0;
+  int ntiles = 0;
+  pd::GridBarrier* d_bar = nullptr;
+  int64_t particles = 0, bonds = 0;
+  std::map<int32_t, cudaGraphExec_t> graphs;
+  bool direct = false;  // persistent kernel launched directly (its capture was refused)
 };
 
 namespace {
@@ -83,9 +108,19 @@ void dfree(T*& p) {
   p = nullptr;
 }
 
+void clear_batch_graphs(pd_batch* b) {
+  for (auto& kv : b->graphs) cudaGraphExecDestroy(kv.second);
+  b->graphs.clear();
+}
+
+// Captured kernel arguments are stale: drop the graphs (and the batch tables).
 void clear_graphs(pd_ctx* c) {
   for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
   c->graphs.clear();
+  if (c->batch) {
+    c->batch->dirty = true;
+    clear_batch_graphs(c->batch);
+  }
 }
 
 void free_families(pd_ctx* c) {
@@ -97,6 +132,7 @@ void free_families(pd_ctx* c) {
   dfree(c->bxi);
   dfree(c->bgeo);
   dfree(c->blim);
+  dfree(c->br2);
   c->sell = pd::SellLayout{};
   c->nnz = 0;
   c->has_families = false;
@@ -109,19 +145,19 @@ void free_particles(pd_ctx* c) {
   dfree(c->vol); dfree(c->kinv22); dfree(c->damage);
   dfree(c->w01); dfree(c->w23); dfree(c->kinv01); dfree(c->mt); dfree(c->hg); dfree(c->hgs);
   dfree(c->bc); dfree(c->singular); dfree(c->broken); dfree(c->fam);
+  dfree(c->u32);
   dfree(c->xs); dfree(c->us); dfree(c->vsm); dfree(c->ws); dfree(c->geo);
   dfree(c->fs); dfree(c->mh); dfree(c->vh);
   c->n = 0;
   c->has_particles = false;
 }
 
-double stretch_factor(double s_c) { return s_c > 0.0 ? s_c * (2.0 + s_c) : INFINITY; }
 
 int check_params(pd_ctx* c, const pd_params* p) {
   if (!p) return fail(c, PD_ERR_ARG, "params is NULL");
   if (p->precision != PD_FP64 && p->precision != PD_MIXED) return fail(c, PD_ERR_ARG, "unknown precision");
   if (!(p->rho > 0.0) || !(p->dt > 0.0) || !std::isfinite(p->E) || !(p->nu > -1.0 && p->nu < 1.0) ||
-      !(p->det_guard >= 0.0) || !(p->k_hg >= 0.0) || !std::isfinite(p->k_hg))
+      !(p->det_guard >= 0.0) || !(p->k_hg >= 0.0) || !std::isfinite(p->k_hg) || !(p->damage_fail >= 0.0))
     return fail(c, PD_ERR_ARG, "invalid material / time-step parameters");
   if (p->singular_policy != PD_SINGULAR_ZERO && p->singular_policy != PD_SINGULAR_ERROR)
     return fail(c, PD_ERR_ARG, "unknown singular_policy");
@@ -138,14 +174,16 @@ Fp64Args fp64_args(pd_ctx* c) {
   a.bc = c->bc; a.gkind = c->gkind; a.gval = c->gval;
   a.broken = c->broken; a.damage = c->damage; a.singular = c->singular; a.fam = c->fam;
   a.chunk_base = c->sell.chunk_base; a.chunk_w = c->sell.chunk_w; a.nbr = c->sell.nbr;
-  a.bxi = c->bxi; a.bgeo = c->bgeo; a.blim = c->blim;
+  a.bxi = c->bxi; a.bgeo = c->bgeo; a.blim = c->blim; a.br2 = c->br2; a.u32 = c->u32;
   stiffness(c, &a.c11, &a.c12, &a.c33);  // getStiffnessTensor, src/main_seq.cpp:185-187
   a.dt = c->p.dt;
   a.dt2 = c->p.dt * c->p.dt;
   a.inv_rho = 1.0 / c->p.rho;
   a.det_guard = c->p.det_guard;
   a.k_hg = c->p.k_hg;
+  a.damage_fail = c->p.damage_fail;
   a.counters = c->counters;
+  a.brk = c->p.s_c > 0.0;
   return a;
 }
 
@@ -182,7 +220,9 @@ pd::MixedArgs mixed_args(pd_ctx* c) {
   a.v_scale = c->p.dt / c->ls;
   a.f_scale = c->ls / es;
   a.det_guard = c->p.det_guard;
+  a.damage_fail = c->p.damage_fail;
   a.counters = c->counters;
+  a.brk = c->p.s_c > 0.0;
   return a;
 }
 
@@ -224,8 +264,9 @@ int finish_families(pd_ctx* c) {
     PD_CK(c, cudaMalloc(&c->bxi, ns * sizeof(double2)));
     PD_CK(c, cudaMalloc(&c->bgeo, ns * sizeof(double2)));
     PD_CK(c, cudaMalloc(&c->blim, ns * sizeof(double)));
-    pd::launch_bond_geometry_fp64(c->n, c->x, c->vol, c->sell, c->row_ptr, stretch_factor(c->p.s_c), c->bxi,
-                                  c->bgeo, c->blim, s);
+    PD_CK(c, cudaMalloc(&c->br2, ns * sizeof(float)));
+    pd::launch_bond_geometry_fp64(c->n, c->x, c->vol, c->sell, c->row_ptr, c->p.s_c, c->bxi, c->bgeo, c->blim,
+                                  c->br2, s);
   } else {
     // mixed-form scales: Ls = the family cutoff (or the longest bond), Vs = mean volume
     double ls = c->cutoff;
@@ -274,6 +315,7 @@ void pd_default_params(pd_params* p) {
   p->s_c = 0.0;
   p->det_guard = 1e-10;
   p->k_hg = 0.0;
+  p->damage_fail = 1.0;
   p->singular_policy = PD_SINGULAR_ZERO;
 }
 
@@ -314,6 +356,7 @@ int pd_create(const pd_params* p, pd_ctx** out) {
 
 int pd_destroy(pd_ctx* c) {
   if (!c) return PD_OK;
+  if (c->batch) pd_batch_remove(c->batch, c);
   cudaSetDevice(c->p.device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   free_particles(c);
@@ -345,7 +388,7 @@ int pd_set_params(pd_ctx* c, const pd_params* p) {
     if (rc2 != PD_OK) return rc2;
   }
   if (c->has_families && s_changed && !mixed(c)) {
-    pd::launch_bond_limit_fp64(c->sell.nslots, c->bxi, stretch_factor(c->p.s_c), c->sell.nbr, c->blim, c->stream);
+    pd::launch_bond_limit_fp64(c->sell.nslots, c->bxi, c->p.s_c, c->sell.nbr, c->blim, c->br2, c->stream);
     PD_CK(c, cudaGetLastError());
     PD_CK(c, cudaStreamSynchronize(c->stream));
   }
@@ -407,6 +450,7 @@ int pd_set_particles(pd_ctx* c, int64_t n, const double* x, const double* vol) {
     PD_CK(c, cudaMalloc(&c->kinv01, nn * sizeof(double2)));
     PD_CK(c, cudaMalloc(&c->mt, nn * sizeof(double2)));
     PD_CK(c, cudaMalloc(&c->hg, nn * sizeof(double2)));
+    PD_CK(c, cudaMalloc(&c->u32, nn * sizeof(float2)));
     PD_CK(c, cudaMalloc(&c->kinv22, nn * sizeof(double)));
   }
   PD_CK(c, cudaMalloc(&c->damage, nn * sizeof(double)));
@@ -543,6 +587,7 @@ int pd_reset(pd_ctx* c) {
     PD_CK(c, cudaMemsetAsync(c->w01, 0, nn * sizeof(double2), s));
     PD_CK(c, cudaMemsetAsync(c->w23, 0, nn * sizeof(double2), s));
     PD_CK(c, cudaMemsetAsync(c->hg, 0, nn * sizeof(double2), s));
+    PD_CK(c, cudaMemsetAsync(c->u32, 0, nn * sizeof(float2), s));
     pd::launch_init_geometry_fp64(fp64_args(c), s);
   }
   PD_CK(c, cudaGetLastError());
@@ -564,6 +609,10 @@ int pd_set_state(pd_ctx* c, const double* u, const double* v, const double* f) {
   if (mixed(c)) {
     if (!c->has_families) return fail(c, PD_ERR_ORDER, "mixed form: families first (they fix the scales)");
     pd::launch_to_mixed(mixed_args(c), u ? c->u : nullptr, v ? c->v : nullptr, f ? c->f : nullptr, c->stream);
+    PD_CK(c, cudaGetLastError());
+    PD_CK(c, cudaStreamSynchronize(c->stream));
+  } else if (u && c->has_families) {
+    pd::launch_shadow_fp64(fp64_args(c), c->stream);
     PD_CK(c, cudaGetLastError());
     PD_CK(c, cudaStreamSynchronize(c->stream));
   }
@@ -723,6 +772,7 @@ int pd_compute_velocity(pd_ctx* c, const double* u, double* velocity, double* ac
   PD_CK(c, cudaMemcpyAsync(c->v, velocity, b, cudaMemcpyHostToDevice, s));
   PD_CK(c, cudaMemcpyAsync(c->acc, acce, b, cudaMemcpyHostToDevice, s));
   const Fp64Args a = fp64_args(c);
+  pd::launch_shadow_fp64(a, s);
   pd::launch_pass_a_fp64(a, c->p.s_c > 0.0, s);
   pd::launch_pass_b_fp64(a, 2, s);
   PD_CK(c, cudaGetLastError());
@@ -810,6 +860,271 @@ int pd_model_bytes(const pd_ctx* c, double* bytes) {
   const double per_particle = c->p.precision == PD_FP64 ? 248.0 : 148.0;
   *bytes = per_particle * (double)c->n + 11.0 * (double)c->nnz;
   return PD_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ batches
+
+namespace {
+
+int bfail(pd_batch* b, int code, const std::string& m) {
+  if (b) b->err = m;
+  return code;
+}
+
+#define PD_BCK(b, call)                                                          \
+  do {                                                                           \
+    cudaError_t e_ = (call);                                                     \
+    if (e_ != cudaSuccess) return bfail(b, PD_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+int batch_refresh(pd_batch* b) {
+  if (!b->dirty) return PD_OK;
+  std::vector<pd::BatchTile> tiles;
+  std::vector<unsigned char> plates;
+  const size_t asz = b->precision == PD_MIXED ? sizeof(pd::MixedArgs) : sizeof(Fp64Args);
+  plates.resize(asz * (b->members.empty() ? 1 : b->members.size()));
+  b->particles = 0;
+  b->bonds = 0;
+  for (size_t k = 0; k < b->members.size(); ++k) {
+    pd_ctx* c = b->members[k];
+    if (!c->has_families) return bfail(b, PD_ERR_ORDER, "a member has no families");
+    if (b->precision == PD_MIXED) {
+      const pd::MixedArgs m = mixed_args(c);
+      std::memcpy(plates.data() + k * asz, &m, asz);
+    } else {
+      const Fp64Args f = fp64_args(c);
+      std::memcpy(plates.data() + k * asz, &f, asz);
+    }
+    for (int64_t first = 0; first < c->n; first += b->tile)
+      tiles.push_back(pd::BatchTile{(int32_t)k, (int32_t)std::min<int64_t>(b->tile, c->n - first), first});
+    b->particles += c->n;
+    b->bonds += c->nnz;
+  }
+  if (plates.size() > b->plates_bytes) {
+    if (b->d_plates) cudaFree(b->d_plates);
+    b->d_plates = nullptr;
+    PD_BCK(b, cudaMalloc(&b->d_plates, plates.size()));
+    b->plates_bytes = plates.size();
+  }
+  if (tiles.size() > b->tiles_cap || !b->d_tiles) {
+    if (b->d_tiles) cudaFree(b->d_tiles);
+    b->d_tiles = nullptr;
+    const size_t cap = std::max<size_t>(tiles.size(), 1);
+    PD_BCK(b, cudaMalloc(&b->d_tiles, cap * sizeof(pd::BatchTile)));
+    b->tiles_cap = cap;
+  }
+  PD_BCK(b, cudaMemcpyAsync(b->d_plates, plates.data(), plates.size(), cudaMemcpyHostToDevice, b->stream));
+  if (!tiles.empty())
+    PD_BCK(b, cudaMemcpyAsync(b->d_tiles, tiles.data(), tiles.size() * sizeof(pd::BatchTile), cudaMemcpyHostToDevice,
+                              b->stream));
+  PD_BCK(b, cudaStreamSynchronize(b->stream));
+  b->ntiles = (int)tiles.size();
+  clear_batch_graphs(b);
+  b->dirty = false;
+  return PD_OK;
+}
+
+cudaError_t batch_enqueue(pd_batch* b, int32_t nsteps) {
+  if (b->precision == PD_MIXED)
+    return pd::launch_batch_mixed(static_cast<const pd::MixedArgs*>(b->d_plates), b->d_tiles, b->ntiles, nsteps,
+                                  b->cfg, b->d_bar, b->nsm, b->stream);
+  return pd::launch_batch_fp64(static_cast<const Fp64Args*>(b->d_plates), b->d_tiles, b->ntiles, nsteps, b->cfg,
+                               b->d_bar, b->nsm, b->stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+int pd_batch_create(int32_t device, int32_t precision, pd_batch** out) {
+  if (!out) return PD_ERR_ARG;
+  *out = nullptr;
+  if (precision != PD_FP64 && precision != PD_MIXED) {
+    g_create_err = "pd_batch_create: unknown precision";
+    return PD_ERR_ARG;
+  }
+  std::unique_ptr<pd_batch> b(new (std::nothrow) pd_batch());
+  if (!b) return PD_ERR_CAPACITY;
+  b->device = device;
+  b->precision = precision;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_bar, sizeof(pd::GridBarrier));
+  if (e == cudaSuccess) e = cudaMemset(b->d_bar, 0, sizeof(pd::GridBarrier));
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->nsm, cudaDevAttrMultiProcessorCount, device);
+  if (e != cudaSuccess) {
+    g_create_err = std::string("pd_batch_create: ") + cudaGetErrorString(e);
+    pd_batch_destroy(b.release());
+    return PD_ERR_CUDA;
+  }
+  *out = b.release();
+  return PD_OK;
+}
+
+int pd_batch_destroy(pd_batch* b) {
+  if (!b) return PD_OK;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  for (pd_ctx* c : b->members) c->batch = nullptr;
+  clear_batch_graphs(b);
+  if (b->d_plates) cudaFree(b->d_plates);
+  if (b->d_tiles) cudaFree(b->d_tiles);
+  if (b->d_bar) cudaFree(b->d_bar);
+  if (b->done) cudaEventDestroy(b->done);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return PD_OK;
+}
+
+const char* pd_batch_last_error(const pd_batch* b) { return b ? b->err.c_str() : g_create_err.c_str(); }
+
+int pd_batch_add(pd_batch* b, pd_ctx* c) {
+  if (!b || !c) return PD_ERR_ARG;
+  if (c->batch) return bfail(b, PD_ERR_ARG, "the context is already in a batch");
+  if (c->p.device != b->device || c->p.precision != b->precision)
+    return bfail(b, PD_ERR_ARG, "batch members share the batch's device and precision");
+  if (!c->has_families) return bfail(b, PD_ERR_ORDER, "set particles and families before adding a context");
+  PD_BCK(b, cudaSetDevice(b->device));
+  PD_BCK(b, cudaStreamSynchronize(b->stream));
+  b->members.push_back(c);
+  c->batch = b;
+  b->dirty = true;
+  clear_batch_graphs(b);
+  return PD_OK;
+}
+
+int pd_batch_remove(pd_batch* b, pd_ctx* c) {
+  if (!b || !c) return PD_ERR_ARG;
+  auto it = std::find(b->members.begin(), b->members.end(), c);
+  if (it == b->members.end()) return bfail(b, PD_ERR_ARG, "not a member");
+  cudaSetDevice(b->device);
+  cudaStreamSynchronize(b->stream);
+  b->members.erase(it);
+  c->batch = nullptr;
+  b->dirty = true;
+  clear_batch_graphs(b);
+  return PD_OK;
+}
+
+int pd_batch_info(const pd_batch* b, int32_t* nplates, int64_t* particles, int64_t* bonds) {
+  if (!b) return PD_ERR_ARG;
+  int64_t np = 0, nb = 0;
+  for (const pd_ctx* c : b->members) {
+    np += c->n;
+    nb += c->nnz;
+  }
+  if (nplates) *nplates = (int32_t)b->members.size();
+  if (particles) *particles = np;
+  if (bonds) *bonds = nb;
+  return PD_OK;
+}
+
+int pd_batch_set_config(pd_batch* b, const pd_batch_config* cfg) {
+  if (!b || !cfg) return PD_ERR_ARG;
+  if (cfg->block < 32 || cfg->block > 256 || cfg->block % 32 || cfg->tile < 32 || cfg->tile % 32 ||
+      cfg->blocks_per_sm < 1 || (cfg->persistent != 0 && cfg->persistent != 1))
+    return bfail(b, PD_ERR_ARG, "invalid batch configuration");
+  PD_BCK(b, cudaSetDevice(b->device));
+  PD_BCK(b, cudaStreamSynchronize(b->stream));
+  b->cfg.block = cfg->block;
+  b->cfg.blocks_per_sm = cfg->blocks_per_sm;
+  b->cfg.persistent = cfg->persistent;
+  if (cfg->tile != b->tile) b->dirty = true;
+  b->tile = cfg->tile;
+  clear_batch_graphs(b);
+  return PD_OK;
+}
+
+int pd_batch_get_config(const pd_batch* b, pd_batch_config* cfg) {
+  if (!b || !cfg) return PD_ERR_ARG;
+  cfg->block = b->cfg.block;
+  cfg->blocks_per_sm = b->cfg.blocks_per_sm;
+  cfg->persistent = b->cfg.persistent;
+  cfg->tile = b->tile;
+  return PD_OK;
+}
+
+int pd_batch_step(pd_batch* b, int32_t nsteps) {
+  if (!b) return PD_ERR_ARG;
+  if (nsteps < 0) return bfail(b, PD_ERR_ARG, "nsteps < 0");
+  if (nsteps == 0 || b->members.empty()) return PD_OK;
+  PD_BCK(b, cudaSetDevice(b->device));
+  int rc = batch_refresh(b);
+  if (rc != PD_OK) return rc;
+  // order after every member's pending work
+  for (pd_ctx* c : b->members) {
+    PD_BCK(b, cudaEventRecord(b->done, c->stream));
+    PD_BCK(b, cudaStreamWaitEvent(b->stream, b->done, 0));
+  }
+  if (b->cfg.persistent && b->direct) {
+    PD_BCK(b, batch_enqueue(b, nsteps));
+  } else {
+    auto it = b->graphs.find(nsteps);
+    if (it == b->graphs.end()) {
+      cudaGraph_t g;
+      PD_BCK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+      cudaError_t le = batch_enqueue(b, nsteps);
+      cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+      if (le != cudaSuccess || ce != cudaSuccess) {
+        if (ce == cudaSuccess) cudaGraphDestroy(g);
+        cudaGetLastError();
+        if (!b->cfg.persistent)
+          return bfail(b, PD_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(le != cudaSuccess ? le : ce));
+        b->direct = true;  // this runtime does not capture cooperative launches: launch directly
+        PD_BCK(b, batch_enqueue(b, nsteps));
+      } else {
+        cudaGraphExec_t ge;
+        cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) return bfail(b, PD_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(ie));
+        if (b->graphs.size() > 16) clear_batch_graphs(b);
+        it = b->graphs.emplace(nsteps, ge).first;
+      }
+    }
+    if (!(b->cfg.persistent && b->direct)) PD_BCK(b, cudaGraphLaunch(it->second, b->stream));
+  }
+  PD_BCK(b, cudaEventRecord(b->done, b->stream));
+  for (pd_ctx* c : b->members) {
+    PD_BCK(b, cudaStreamWaitEvent(c->stream, b->done, 0));
+    c->steps += nsteps;
+  }
+  return PD_OK;
+}
+
+int pd_batch_synchronize(pd_batch* b) {
+  if (!b) return PD_ERR_ARG;
+  PD_BCK(b, cudaSetDevice(b->device));
+  PD_BCK(b, cudaStreamSynchronize(b->stream));
+  pd::GridBarrier h;
+  PD_BCK(b, cudaMemcpy(&h, b->d_bar, sizeof(h), cudaMemcpyDeviceToHost));
+  if (h.err) return bfail(b, PD_ERR_TIMEOUT, "a grid-barrier wait of the persistent batch kernel gave up");
+  return PD_OK;
+}
+
+int pd_batch_step_timed(pd_batch* b, int32_t nsteps, float* ms) {
+  if (!b || !ms) return PD_ERR_ARG;
+  PD_BCK(b, cudaSetDevice(b->device));
+  int rc = batch_refresh(b);
+  if (rc != PD_OK) return rc;
+  cudaEvent_t e0, e1;
+  PD_BCK(b, cudaEventCreate(&e0));
+  PD_BCK(b, cudaEventCreate(&e1));
+  for (pd_ctx* c : b->members) {
+    PD_BCK(b, cudaEventRecord(b->done, c->stream));
+    PD_BCK(b, cudaStreamWaitEvent(b->stream, b->done, 0));
+  }
+  PD_BCK(b, cudaEventRecord(e0, b->stream));
+  rc = pd_batch_step(b, nsteps);
+  cudaEventRecord(e1, b->stream);
+  cudaEventSynchronize(e1);
+  cudaEventElapsedTime(ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != PD_OK) return rc;
+  return pd_batch_synchronize(b);
 }
 
 }  // extern "C"

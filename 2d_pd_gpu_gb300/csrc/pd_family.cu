@@ -223,10 +223,19 @@ __global__ void k_sell_fill(int64_t n, const int64_t* __restrict__ row_ptr, cons
   }
 }
 
+// Stretch limits of a bond: the exact FP64 one, and the FP32 certificate
+// threshold (s_c |xi|)^2 (1 - 1e-5) rounded toward zero (never above the truth).
+__device__ __forceinline__ void bond_limits(double ex, double ey, double s_c, double* lim, float* r2) {
+  const double ee = fma(ex, ex, ey * ey);
+  const double s2 = s_c > 0.0 ? s_c * (2.0 + s_c) : INFINITY;
+  *lim = s2 * ee;
+  *r2 = s_c > 0.0 ? __double2float_rz(((s_c * s_c) * ee) * (1.0 - 1e-5)) : 0.0f;
+}
+
 __global__ void k_bond_geometry(int64_t n, const double2* __restrict__ x, const double* __restrict__ vol,
                                 const int64_t* __restrict__ chunk_base, const int32_t* __restrict__ chunk_w,
-                                const int32_t* __restrict__ nbr, double s2, double2* bxi, double2* bgeo,
-                                double* blim) {
+                                const int32_t* __restrict__ nbr, double s_c, double2* bxi, double2* bgeo,
+                                double* blim, float* br2) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int64_t c = i / kChunk;
@@ -241,6 +250,7 @@ __global__ void k_bond_geometry(int64_t n, const double2* __restrict__ x, const 
       bxi[s] = make_double2(0.0, 0.0);
       bgeo[s] = make_double2(0.0, 0.0);
       blim[s] = 0.0;
+      br2[s] = 0.0f;
       continue;
     }
     const double2 pj = x[j];
@@ -248,16 +258,21 @@ __global__ void k_bond_geometry(int64_t n, const double2* __restrict__ x, const 
     const double vj = vol[j];
     bxi[s] = make_double2(ex, ey);
     bgeo[s] = make_double2(vj * ex, vj * ey);
-    blim[s] = s2 * fma(ex, ex, ey * ey);
+    bond_limits(ex, ey, s_c, &blim[s], &br2[s]);
   }
 }
 
-__global__ void k_bond_limit(int64_t nslots, const double2* __restrict__ bxi, double s2,
-                             const int32_t* __restrict__ nbr, double* blim) {
+__global__ void k_bond_limit(int64_t nslots, const double2* __restrict__ bxi, double s_c,
+                             const int32_t* __restrict__ nbr, double* blim, float* br2) {
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nslots) return;
   const double2 e = bxi[s];
-  blim[s] = nbr[s] == -1 ? 0.0 : s2 * fma(e.x, e.x, e.y * e.y);
+  if (nbr[s] == -1) {
+    blim[s] = 0.0;
+    br2[s] = 0.0f;
+  } else {
+    bond_limits(e.x, e.y, s_c, &blim[s], &br2[s]);
+  }
 }
 
 __global__ void k_mask_out(int64_t n, const int64_t* __restrict__ row_ptr, const int64_t* __restrict__ chunk_base,
@@ -418,16 +433,16 @@ int build_sell(int64_t n, const int64_t* d_row_ptr, const int32_t* d_col, cudaSt
 }
 
 void launch_bond_geometry_fp64(int64_t n, const double2* x, const double* vol, const SellLayout& L,
-                               const int64_t* /*row_ptr*/, double s2, double2* bxi, double2* bgeo, double* blim,
-                               cudaStream_t s) {
+                               const int64_t* /*row_ptr*/, double s_c, double2* bxi, double2* bgeo, double* blim,
+                               float* br2, cudaStream_t s) {
   if (n > 0)
-    k_bond_geometry<<<(unsigned)blocks_for(n), kBlock, 0, s>>>(n, x, vol, L.chunk_base, L.chunk_w, L.nbr, s2, bxi,
-                                                              bgeo, blim);
+    k_bond_geometry<<<(unsigned)blocks_for(n), kBlock, 0, s>>>(n, x, vol, L.chunk_base, L.chunk_w, L.nbr, s_c, bxi,
+                                                              bgeo, blim, br2);
 }
 
-void launch_bond_limit_fp64(int64_t nslots, const double2* bxi, double s2, const int32_t* nbr, double* blim,
-                            cudaStream_t s) {
-  if (nslots > 0) k_bond_limit<<<(unsigned)blocks_for(nslots), kBlock, 0, s>>>(nslots, bxi, s2, nbr, blim);
+void launch_bond_limit_fp64(int64_t nslots, const double2* bxi, double s_c, const int32_t* nbr, double* blim,
+                            float* br2, cudaStream_t s) {
+  if (nslots > 0) k_bond_limit<<<(unsigned)blocks_for(nslots), kBlock, 0, s>>>(nslots, bxi, s_c, nbr, blim, br2);
 }
 
 void launch_mask_out(int64_t n, const int64_t* row_ptr, const SellLayout& L, uint8_t* alive, cudaStream_t s) {

@@ -16,7 +16,9 @@
 //   k_pass_b              : computeVelocity :396-470 in gather form
 //                           f_i = sum_j V_j (S_i + S_j) xi_ij (= T_ij - T_ji)
 // FP64 operations per bond: pass A 11 (d 2, stretch test 5, D 4) + 2 with the
-// zero-energy-mode penalty (sum V_j d), pass B 4.
+// zero-energy-mode penalty (sum V_j d), pass B 4.  The stretch test runs in
+// FP64 only for bonds an FP32 bound cannot prove intact (surely_intact), so
+// pass A costs 8 FP64 operations for almost every bond.
 #include "pd_internal.h"
 
 namespace pd {
@@ -48,7 +50,9 @@ __device__ void kinv_update(const Fp64Args& a, int64_t i) {
     ++nal;
   }
   const double det = fma(k11, k22, -(k12 * k12));
-  if (nal == 0 || !(det > a.det_guard * (k11 * k22))) {
+  const int32_t fam = a.fam[i];
+  const bool failed = fam > 0 && (double)a.broken[i] / (double)fam > a.damage_fail;
+  if (nal == 0 || failed || !(det > a.det_guard * (k11 * k22))) {
     a.kinv01[i] = make_double2(0.0, 0.0);
     a.kinv22[i] = 0.0;
     a.mt[i] = make_double2(0.0, 0.0);
@@ -81,23 +85,48 @@ __device__ __forceinline__ void drift_one(const Fp64Args& a, int64_t i, double2&
   if (kind == PD_BC_FIXED) u = make_double2(0.0, 0.0);
 }
 
-__global__ void __launch_bounds__(kBlock) k_drift(Fp64Args a) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
+__device__ __forceinline__ void drift_particle(const Fp64Args& a, int64_t i) {
   double2 v = a.v[i], u = a.u[i];
   const double2 f = a.f[i];
   drift_one(a, i, v, u, f.x * a.inv_rho, f.y * a.inv_rho);
   a.v[i] = v;
   a.u[i] = u;
+  a.u32[i] = make_float2((float)u.x, (float)u.y);
 }
 
-template <bool BREAK, bool HG>
-__global__ void __launch_bounds__(kBlock) k_pass_a(Fp64Args a) {
+__global__ void __launch_bounds__(kBlock) k_drift(Fp64Args a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < a.n) drift_particle(a, i);
+}
+
+__global__ void __launch_bounds__(kBlock) k_shadow(Fp64Args a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
+  const double2 u = a.u[i];
+  a.u32[i] = make_float2((float)u.x, (float)u.y);
+}
+
+// FP32 certificate that a bond is intact: an upper bound B on the FP64
+// |d| = |fl64(u_j - u_i)| from the FP32 shadows (|u - fl32(u)| <= 2^-24 |u|,
+// FP32 rounding of the difference and of B itself covered by the 6e-8 and
+// 1.000001 factors) with B^2 <= (s_c |xi|)^2 (1 - 1e-5).  Then
+// d.(2 xi + d) <= 2|xi|B + B^2 < ((1 + s_c)^2 - 1)|xi|^2 by a relative
+// margin >= 5e-6, far above the FP64 evaluation error of the exact test, so
+// the FP64 test would say "intact": skipping it cannot change any result.
+__device__ __forceinline__ bool surely_intact(float2 ui, float2 uj, float r2) {
+  const float fx = uj.x - ui.x, fy = uj.y - ui.y;
+  const float bx = fabsf(fx) + 6.0e-8f * (fabsf(uj.x) + fabsf(ui.x) + fabsf(fx));
+  const float by = fabsf(fy) + 6.0e-8f * (fabsf(uj.y) + fabsf(ui.y) + fabsf(fy));
+  return fmaf(bx, bx, by * by) * 1.000001f <= r2;
+}
+
+// Pass A of particle i (stretch tests, D, penalty sum, stress, W).
+template <bool BREAK, bool HG>
+__device__ __forceinline__ void pass_a_particle(const Fp64Args& a, int64_t i) {
   int w;
   const int64_t s0 = slot0(a, i, &w);
   const double2 ui = a.u[i];
+  const float2 ui32 = a.u32[i];
   double d11 = 0.0, d12 = 0.0, d21 = 0.0, d22 = 0.0, ax = 0.0, ay = 0.0;
   int newly = 0;
   for (int k = 0; k < w; ++k) {
@@ -106,7 +135,7 @@ __global__ void __launch_bounds__(kBlock) k_pass_a(Fp64Args a) {
     if (j < 0) continue;
     const double2 uj = a.u[j];
     const double dx = uj.x - ui.x, dy = uj.y - ui.y;
-    if (BREAK) {
+    if (BREAK && !surely_intact(ui32, a.u32[j], __ldcs(&a.br2[s]))) {
       const double2 e = __ldcs(&a.bxi[s]);
       const double q = fma(dx, fma(2.0, e.x, dx), dy * fma(2.0, e.y, dy));
       if (q > __ldcs(&a.blim[s])) {
@@ -162,10 +191,16 @@ __global__ void __launch_bounds__(kBlock) k_pass_a(Fp64Args a) {
   }
 }
 
-template <int MODE, bool HG>
-__global__ void __launch_bounds__(kBlock) k_pass_b(Fp64Args a) {
+template <bool BREAK, bool HG>
+__global__ void __launch_bounds__(kBlock) k_pass_a(Fp64Args a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
+  if (i < a.n) pass_a_particle<BREAK, HG>(a, i);
+}
+
+// Pass B of particle i (force gather, kick; MODE 1 adds the next drift,
+// MODE 2 is the drop-in kick with acce in/out).
+template <int MODE, bool HG>
+__device__ __forceinline__ void pass_b_particle(const Fp64Args& a, int64_t i) {
   int w;
   const int64_t s0 = slot0(a, i, &w);
   const double2 wa = a.w01[i], wb = a.w23[i], m = a.mt[i];
@@ -209,10 +244,101 @@ __global__ void __launch_bounds__(kBlock) k_pass_b(Fp64Args a) {
     double2 u = a.u[i];
     drift_one(a, i, v, u, anx, any);
     a.u[i] = u;
+    a.u32[i] = make_float2((float)u.x, (float)u.y);
   }
   a.v[i] = v;
 }
 
+template <int MODE, bool HG>
+__global__ void __launch_bounds__(kBlock) k_pass_b(Fp64Args a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < a.n) pass_b_particle<MODE, HG>(a, i);
+}
+
+// ---- batched plates: phase 0 drift, 1 pass A, 2 pass B + next drift, 3 pass B
+__device__ __forceinline__ void batch_particle(const Fp64Args& p, int64_t i, int phase) {
+  const bool hg = p.k_hg != 0.0;
+  if (phase == 0) {
+    drift_particle(p, i);
+  } else if (phase == 1) {
+    if (p.brk)
+      hg ? pass_a_particle<true, true>(p, i) : pass_a_particle<true, false>(p, i);
+    else
+      hg ? pass_a_particle<false, true>(p, i) : pass_a_particle<false, false>(p, i);
+  } else if (phase == 2) {
+    hg ? pass_b_particle<1, true>(p, i) : pass_b_particle<1, false>(p, i);
+  } else {
+    hg ? pass_b_particle<0, true>(p, i) : pass_b_particle<0, false>(p, i);
+  }
+}
+
+__device__ __forceinline__ void batch_phase(const Fp64Args* __restrict__ plates, const BatchTile* __restrict__ tiles,
+                                            int ntiles, int phase) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const BatchTile T = tiles[t];
+    const Fp64Args& p = plates[T.plate];
+    for (int k = threadIdx.x; k < T.count; k += blockDim.x) batch_particle(p, T.first + k, phase);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_batch_persistent(const Fp64Args* __restrict__ plates,
+                                                          const BatchTile* __restrict__ tiles, int ntiles, int nsteps,
+                                                          GridBarrier* bar) {
+  const unsigned nb = gridDim.x;
+  batch_phase(plates, tiles, ntiles, 0);
+  for (int s = 0; s < nsteps; ++s) {
+    if (!grid_sync(bar, nb)) return;
+    batch_phase(plates, tiles, ntiles, 1);
+    if (!grid_sync(bar, nb)) return;
+    batch_phase(plates, tiles, ntiles, s + 1 < nsteps ? 2 : 3);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_batch_phase(const Fp64Args* __restrict__ plates,
+                                                     const BatchTile* __restrict__ tiles, int ntiles, int phase) {
+  batch_phase(plates, tiles, ntiles, phase);
+}
+
+}  // namespace
+
+int batch_occupancy_fp64(const BatchLaunch& cfg) {
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch_persistent, cfg.block, 0) != cudaSuccess) return 0;
+  return nb;
+}
+
+cudaError_t launch_batch_fp64(const Fp64Args* d_plates, const BatchTile* d_tiles, int ntiles, int nsteps,
+                              const BatchLaunch& cfg, GridBarrier* d_bar, int nsm, cudaStream_t s) {
+  if (ntiles <= 0 || nsteps <= 0) return cudaSuccess;
+  if (!cfg.persistent) {
+    const unsigned g = (unsigned)ntiles;
+    k_batch_phase<<<g, cfg.block, 0, s>>>(d_plates, d_tiles, ntiles, 0);
+    for (int k = 0; k < nsteps; ++k) {
+      k_batch_phase<<<g, cfg.block, 0, s>>>(d_plates, d_tiles, ntiles, 1);
+      k_batch_phase<<<g, cfg.block, 0, s>>>(d_plates, d_tiles, ntiles, k + 1 < nsteps ? 2 : 3);
+    }
+    return cudaGetLastError();
+  }
+  int occ = batch_occupancy_fp64(cfg);
+  int bps = cfg.blocks_per_sm < occ ? cfg.blocks_per_sm : occ;
+  if (bps < 1) return cudaErrorInvalidConfiguration;
+  int grid = nsm * bps;
+  if (grid > ntiles) grid = ntiles;
+  cudaError_t e = cudaMemsetAsync(d_bar, 0, sizeof(GridBarrier), s);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t lc = {};
+  lc.gridDim = dim3((unsigned)grid);
+  lc.blockDim = dim3((unsigned)cfg.block);
+  lc.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  lc.attrs = at;
+  lc.numAttrs = 1;
+  return cudaLaunchKernelEx(&lc, k_batch_persistent, d_plates, d_tiles, ntiles, nsteps, d_bar);
+}
+
+namespace {
 }  // namespace
 
 void launch_init_geometry_fp64(const Fp64Args& a, cudaStream_t s) {
@@ -221,6 +347,10 @@ void launch_init_geometry_fp64(const Fp64Args& a, cudaStream_t s) {
 
 void launch_drift_fp64(const Fp64Args& a, cudaStream_t s) {
   if (a.n > 0) k_drift<<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
+}
+
+void launch_shadow_fp64(const Fp64Args& a, cudaStream_t s) {
+  if (a.n > 0) k_shadow<<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
 }
 
 void launch_pass_a_fp64(const Fp64Args& a, bool breaking, cudaStream_t s) {

@@ -22,6 +22,7 @@
 #include <string>
 #include <vector>
 
+#include "pd_batch.cuh"
 #include "pd_gb300.h"
 
 namespace pd {
@@ -60,10 +61,14 @@ struct Fp64Args {
   const double2* __restrict__ bxi;
   const double2* __restrict__ bgeo;
   const double* __restrict__ blim;
+  const float* __restrict__ br2;  // (s_c |xi|)^2 (1 - 1e-5), rounded toward 0: FP32 stretch certificate
+  float2* u32;                    // u rounded to FP32 (shadow for the certificate)
   double2* hg;  // 2 k_hg sum_j V_j (u_j - u_i), pass A -> pass B
   double c11, c12, c33;
-  double dt, dt2, inv_rho, det_guard, k_hg;
+  double dt, dt2, inv_rho, det_guard, k_hg, damage_fail;
   unsigned long long* counters;
+  int32_t brk;  // bond breaking on (s_c > 0)
+  int32_t pad;
 };
 
 // Mixed form (pd_mixed.cu): scaled two-float state, FP32 bond arithmetic.
@@ -93,8 +98,10 @@ struct MixedArgs {
   float c11, c12, c33;  // C / Es
   float s2, tau2;       // stretch limit factor, Es dt^2 / (rho Ls^2)
   float k_hg;           // k Vs Ls^2 / Es
-  double inv_ls, inv_vs, v_scale, f_scale, det_guard;
+  double inv_ls, inv_vs, v_scale, f_scale, det_guard, damage_fail;
   unsigned long long* counters;
+  int32_t brk;  // bond breaking on (s_c > 0)
+  int32_t pad;
 };
 
 // ---- family build (pd_family.cu)
@@ -116,10 +123,10 @@ struct SellLayout {
 int build_sell(int64_t n, const int64_t* d_row_ptr, const int32_t* d_col, cudaStream_t s, SellLayout* out,
                unsigned long long* d_counters, std::string* msg);
 void launch_bond_geometry_fp64(int64_t n, const double2* x, const double* vol, const SellLayout& L,
-                               const int64_t* row_ptr, double s2, double2* bxi, double2* bgeo, double* blim,
-                               cudaStream_t s);
-void launch_bond_limit_fp64(int64_t nslots, const double2* bxi, double s2, const int32_t* nbr, double* blim,
-                            cudaStream_t s);
+                               const int64_t* row_ptr, double s_c, double2* bxi, double2* bgeo, double* blim,
+                               float* br2, cudaStream_t s);
+void launch_bond_limit_fp64(int64_t nslots, const double2* bxi, double s_c, const int32_t* nbr, double* blim,
+                            float* br2, cudaStream_t s);
 void launch_mask_out(int64_t n, const int64_t* row_ptr, const SellLayout& L, uint8_t* alive, cudaStream_t s);
 void launch_sell_reset(int64_t n, const int64_t* row_ptr, const int32_t* col, const SellLayout& L, cudaStream_t s);
 // exclusive scan of int64 in[0..n) -> out[0..n], out[n] = total (device)
@@ -128,9 +135,15 @@ void scan_exclusive_i64(const int64_t* in, int64_t* out, int64_t n, cudaStream_t
 // ---- FP64 step (pd_fp64.cu)
 void launch_init_geometry_fp64(const Fp64Args& a, cudaStream_t s);
 void launch_drift_fp64(const Fp64Args& a, cudaStream_t s);
+void launch_shadow_fp64(const Fp64Args& a, cudaStream_t s);  // u32 := (float)u
 void launch_pass_a_fp64(const Fp64Args& a, bool breaking, cudaStream_t s);  // hourglass term if a.k_hg != 0
 // mode 0: kick; 1: kick + next step's drift; 2: drop-in kick (acc array in/out)
 void launch_pass_b_fp64(const Fp64Args& a, int mode, cudaStream_t s);
+
+// batched steps (BatchLaunch / BatchTile / GridBarrier in pd_batch.cuh)
+cudaError_t launch_batch_fp64(const Fp64Args* d_plates, const BatchTile* d_tiles, int ntiles, int nsteps,
+                              const BatchLaunch& cfg, GridBarrier* d_bar, int nsm, cudaStream_t s);
+int batch_occupancy_fp64(const BatchLaunch& cfg);  // resident persistent blocks per SM
 
 // ---- mixed step (pd_mixed.cu)
 void launch_init_geometry_mixed(const MixedArgs& a, cudaStream_t s);
@@ -139,6 +152,9 @@ void launch_pass_a_mixed(const MixedArgs& a, bool breaking, cudaStream_t s);
 void launch_pass_b_mixed(const MixedArgs& a, bool drift, cudaStream_t s);
 void launch_to_mixed(const MixedArgs& a, const double2* u, const double2* v, const double2* f, cudaStream_t s);
 void launch_from_mixed(const MixedArgs& a, double2* u, double2* v, double2* f, cudaStream_t s);
+cudaError_t launch_batch_mixed(const MixedArgs* d_plates, const BatchTile* d_tiles, int ntiles, int nsteps,
+                               const BatchLaunch& cfg, GridBarrier* d_bar, int nsm, cudaStream_t s);
+int batch_occupancy_mixed(const BatchLaunch& cfg);
 
 inline int64_t blocks_for(int64_t n, int64_t per = kBlock) { return (n + per - 1) / per; }
 

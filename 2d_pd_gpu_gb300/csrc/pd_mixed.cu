@@ -76,7 +76,9 @@ __device__ void kinv_update_mixed(const MixedArgs& a, int64_t i) {
   }
   const double det = fma(k11, k22, -(k12 * k12));
   const double vi = a.vol[i] * a.inv_vs;
-  if (nal == 0 || !(det > a.det_guard * (k11 * k22))) {
+  const int32_t fam = a.fam[i];
+  const bool failed = fam > 0 && (double)a.broken[i] / (double)fam > a.damage_fail;
+  if (nal == 0 || failed || !(det > a.det_guard * (k11 * k22))) {
     a.geo[i] = make_float4(0.f, 0.f, 0.f, (float)vi);
     a.mh[i] = make_float2(0.f, 0.f);
     a.singular[i] = 1;
@@ -108,9 +110,7 @@ __device__ __forceinline__ void drift_mixed(const MixedArgs& a, int64_t i, float
   if (kind == PD_BC_FIXED) u = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
-__global__ void __launch_bounds__(kBlock) k_drift_mixed(MixedArgs a) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
+__device__ __forceinline__ void drift_particle_mixed(const MixedArgs& a, int64_t i) {
   float4 v = a.vs[i], u = a.us[i];
   const float2 f = a.fs[i];
   drift_mixed(a, i, v, u, a.tau2 * f.x, a.tau2 * f.y);
@@ -118,10 +118,13 @@ __global__ void __launch_bounds__(kBlock) k_drift_mixed(MixedArgs a) {
   a.us[i] = u;
 }
 
-template <bool BREAK>
-__global__ void __launch_bounds__(kBlock) k_pass_a_mixed(MixedArgs a) {
+__global__ void __launch_bounds__(kBlock) k_drift_mixed(MixedArgs a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
+  if (i < a.n) drift_particle_mixed(a, i);
+}
+
+template <bool BREAK>
+__device__ __forceinline__ void pass_a_particle_mixed(const MixedArgs& a, int64_t i) {
   int w;
   const int64_t s0 = slot0(a, i, &w);
   const float4 ui = a.us[i], xi = a.xs[i];
@@ -176,10 +179,14 @@ __global__ void __launch_bounds__(kBlock) k_pass_a_mixed(MixedArgs a) {
                         vi * fmaf(kh, g21, fmaf(s12, k11, s22 * k12)), vi * fmaf(kh, g22, fmaf(s12, k12, s22 * k22)));
 }
 
-template <bool DRIFT>
-__global__ void __launch_bounds__(kBlock) k_pass_b_mixed(MixedArgs a) {
+template <bool BREAK>
+__global__ void __launch_bounds__(kBlock) k_pass_a_mixed(MixedArgs a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
+  if (i < a.n) pass_a_particle_mixed<BREAK>(a, i);
+}
+
+template <bool DRIFT>
+__device__ __forceinline__ void pass_b_particle_mixed(const MixedArgs& a, int64_t i) {
   int w;
   const int64_t s0 = slot0(a, i, &w);
   const float4 wi = a.ws[i], xi = a.xs[i];
@@ -215,6 +222,51 @@ __global__ void __launch_bounds__(kBlock) k_pass_b_mixed(MixedArgs a) {
     a.us[i] = u;
   }
   a.vs[i] = v;
+}
+
+template <bool DRIFT>
+__global__ void __launch_bounds__(kBlock) k_pass_b_mixed(MixedArgs a) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < a.n) pass_b_particle_mixed<DRIFT>(a, i);
+}
+
+// ---- batched plates (see pd_batch.cuh): phase 0 drift, 1 pass A, 2 pass B + drift, 3 pass B
+__device__ __forceinline__ void batch_particle_mixed(const MixedArgs& p, int64_t i, int phase) {
+  if (phase == 0)
+    drift_particle_mixed(p, i);
+  else if (phase == 1)
+    p.brk ? pass_a_particle_mixed<true>(p, i) : pass_a_particle_mixed<false>(p, i);
+  else if (phase == 2)
+    pass_b_particle_mixed<true>(p, i);
+  else
+    pass_b_particle_mixed<false>(p, i);
+}
+
+__device__ __forceinline__ void batch_phase_mixed(const MixedArgs* __restrict__ plates,
+                                                  const BatchTile* __restrict__ tiles, int ntiles, int phase) {
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const BatchTile T = tiles[t];
+    const MixedArgs& p = plates[T.plate];
+    for (int k = threadIdx.x; k < T.count; k += blockDim.x) batch_particle_mixed(p, T.first + k, phase);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_batch_persistent_mixed(const MixedArgs* __restrict__ plates,
+                                                                const BatchTile* __restrict__ tiles, int ntiles,
+                                                                int nsteps, GridBarrier* bar) {
+  const unsigned nb = gridDim.x;
+  batch_phase_mixed(plates, tiles, ntiles, 0);
+  for (int s = 0; s < nsteps; ++s) {
+    if (!grid_sync(bar, nb)) return;
+    batch_phase_mixed(plates, tiles, ntiles, 1);
+    if (!grid_sync(bar, nb)) return;
+    batch_phase_mixed(plates, tiles, ntiles, s + 1 < nsteps ? 2 : 3);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_batch_phase_mixed(const MixedArgs* __restrict__ plates,
+                                                           const BatchTile* __restrict__ tiles, int ntiles, int phase) {
+  batch_phase_mixed(plates, tiles, ntiles, phase);
 }
 
 // FP64 <-> scaled two-float conversions (set/get state; not per step)
@@ -274,6 +326,44 @@ __global__ void k_positions_mixed(MixedArgs a) {
 }
 
 }  // namespace
+
+int batch_occupancy_mixed(const BatchLaunch& cfg) {
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch_persistent_mixed, cfg.block, 0) != cudaSuccess)
+    return 0;
+  return nb;
+}
+
+cudaError_t launch_batch_mixed(const MixedArgs* d_plates, const BatchTile* d_tiles, int ntiles, int nsteps,
+                               const BatchLaunch& cfg, GridBarrier* d_bar, int nsm, cudaStream_t s) {
+  if (ntiles <= 0 || nsteps <= 0) return cudaSuccess;
+  if (!cfg.persistent) {
+    const unsigned g = (unsigned)ntiles;
+    k_batch_phase_mixed<<<g, cfg.block, 0, s>>>(d_plates, d_tiles, ntiles, 0);
+    for (int k = 0; k < nsteps; ++k) {
+      k_batch_phase_mixed<<<g, cfg.block, 0, s>>>(d_plates, d_tiles, ntiles, 1);
+      k_batch_phase_mixed<<<g, cfg.block, 0, s>>>(d_plates, d_tiles, ntiles, k + 1 < nsteps ? 2 : 3);
+    }
+    return cudaGetLastError();
+  }
+  const int occ = batch_occupancy_mixed(cfg);
+  const int bps = cfg.blocks_per_sm < occ ? cfg.blocks_per_sm : occ;
+  if (bps < 1) return cudaErrorInvalidConfiguration;
+  int grid = nsm * bps;
+  if (grid > ntiles) grid = ntiles;
+  cudaError_t e = cudaMemsetAsync(d_bar, 0, sizeof(GridBarrier), s);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t lc = {};
+  lc.gridDim = dim3((unsigned)grid);
+  lc.blockDim = dim3((unsigned)cfg.block);
+  lc.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  lc.attrs = at;
+  lc.numAttrs = 1;
+  return cudaLaunchKernelEx(&lc, k_batch_persistent_mixed, d_plates, d_tiles, ntiles, nsteps, d_bar);
+}
 
 void launch_init_geometry_mixed(const MixedArgs& a, cudaStream_t s) {
   if (a.n <= 0) return;

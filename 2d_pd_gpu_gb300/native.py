@@ -39,6 +39,7 @@ class Params(ctypes.Structure):
         ("s_c", ctypes.c_double),
         ("det_guard", ctypes.c_double),
         ("k_hg", ctypes.c_double),
+        ("damage_fail", ctypes.c_double),
         ("singular_policy", ctypes.c_int32),
         ("reserved", ctypes.c_int32),
     ]
@@ -51,6 +52,15 @@ class Counters(ctypes.Structure):
         ("steps", ctypes.c_int64),
         ("device_error", ctypes.c_int32),
         ("reserved", ctypes.c_int32),
+    ]
+
+
+class BatchConfig(ctypes.Structure):
+    _fields_ = [
+        ("block", ctypes.c_int32),
+        ("blocks_per_sm", ctypes.c_int32),
+        ("persistent", ctypes.c_int32),
+        ("tile", ctypes.c_int32),
     ]
 
 
@@ -85,10 +95,23 @@ _SIGS = {
     "pd_step_timed": [_vp, ctypes.c_int32, ctypes.POINTER(ctypes.c_float)],
     "pd_profile_steps": [_vp, ctypes.c_int32, _vp, _vp],
     "pd_model_bytes": [_vp, ctypes.POINTER(ctypes.c_double)],
+    "pd_batch_create": [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(_vp)],
+    "pd_batch_destroy": [_vp],
+    "pd_batch_last_error": [_vp],
+    "pd_batch_add": [_vp, _vp],
+    "pd_batch_remove": [_vp, _vp],
+    "pd_batch_info": [_vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int64),
+                      ctypes.POINTER(ctypes.c_int64)],
+    "pd_batch_set_config": [_vp, ctypes.POINTER(BatchConfig)],
+    "pd_batch_get_config": [_vp, ctypes.POINTER(BatchConfig)],
+    "pd_batch_step": [_vp, ctypes.c_int32],
+    "pd_batch_synchronize": [_vp],
+    "pd_batch_step_timed": [_vp, ctypes.c_int32, ctypes.POINTER(ctypes.c_float)],
+    "pd_probe_fma_rates": [ctypes.c_int32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
     "pd_host_alloc": [ctypes.c_int64, ctypes.POINTER(_vp)],
     "pd_host_free": [_vp],
 }
-_RESTYPES = {"pd_default_params": None, "pd_last_error": ctypes.c_char_p}
+_RESTYPES = {"pd_default_params": None, "pd_last_error": ctypes.c_char_p, "pd_batch_last_error": ctypes.c_char_p}
 
 EXPORTED = tuple(_SIGS)
 
@@ -143,6 +166,15 @@ def default_params(**kw):
     for k, v in kw.items():
         setattr(p, k, v)
     return p
+
+
+def probe_fma_rates(device=0):
+    """Measured (fp64, fp32) FMA lane-operations per second of the device."""
+    a, b = ctypes.c_double(), ctypes.c_double()
+    rc = lib().pd_probe_fma_rates(device, ctypes.byref(a), ctypes.byref(b))
+    if rc != PD_OK:
+        raise PdError(rc, "pd_probe_fma_rates failed")
+    return a.value, b.value
 
 
 class Context:
@@ -287,3 +319,69 @@ class Context:
         b = ctypes.c_double(0.0)
         self._ck(lib().pd_model_bytes(self._h, ctypes.byref(b)))
         return b.value
+
+
+class Batch:
+    """Many contexts stepped together (pd_batch): one persistent kernel or one
+    graph of phase kernels advances every member; results equal solo runs."""
+
+    def __init__(self, precision=PD_FP64, device=0):
+        self._h = _vp()
+        rc = lib().pd_batch_create(device, precision, ctypes.byref(self._h))
+        if rc != PD_OK:
+            raise PdError(rc, lib().pd_batch_last_error(None).decode())
+        self.members = []
+
+    def _ck(self, rc):
+        if rc != PD_OK:
+            raise PdError(rc, lib().pd_batch_last_error(self._h).decode())
+        return rc
+
+    def add(self, ctx):
+        self._ck(lib().pd_batch_add(self._h, ctx.handle))
+        self.members.append(ctx)
+
+    def remove(self, ctx):
+        self._ck(lib().pd_batch_remove(self._h, ctx.handle))
+        self.members.remove(ctx)
+
+    def info(self):
+        n, p, b = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int64()
+        self._ck(lib().pd_batch_info(self._h, ctypes.byref(n), ctypes.byref(p), ctypes.byref(b)))
+        return {"plates": n.value, "particles": p.value, "bonds": b.value}
+
+    def config(self):
+        c = BatchConfig()
+        self._ck(lib().pd_batch_get_config(self._h, ctypes.byref(c)))
+        return {"block": c.block, "blocks_per_sm": c.blocks_per_sm, "persistent": c.persistent, "tile": c.tile}
+
+    def set_config(self, block=None, blocks_per_sm=None, persistent=None, tile=None):
+        cur = self.config()
+        for k, v in (("block", block), ("blocks_per_sm", blocks_per_sm), ("persistent", persistent), ("tile", tile)):
+            if v is not None:
+                cur[k] = int(v)
+        c = BatchConfig(cur["block"], cur["blocks_per_sm"], cur["persistent"], cur["tile"])
+        self._ck(lib().pd_batch_set_config(self._h, ctypes.byref(c)))
+
+    def step(self, nsteps=1):
+        self._ck(lib().pd_batch_step(self._h, int(nsteps)))
+
+    def synchronize(self):
+        self._ck(lib().pd_batch_synchronize(self._h))
+
+    def step_timed(self, nsteps):
+        ms = ctypes.c_float(0.0)
+        self._ck(lib().pd_batch_step_timed(self._h, int(nsteps), ctypes.byref(ms)))
+        return ms.value
+
+    def close(self):
+        if self._h:
+            lib().pd_batch_destroy(self._h)
+            self._h = _vp()
+            self.members = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

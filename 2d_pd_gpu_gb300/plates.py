@@ -12,10 +12,11 @@ row per face with defineBoundarySet, src/SetupParticleSystem.cpp:513-529; the
 plate workloads ask for three).  Random numbers come from a counter-based
 splitmix64 stream, so every consumer regenerates identical inputs.
 
-The plates run with a zero-energy-mode penalty (G_s = 0.25): the classic
-correspondence model alone lets the velocity loading grow hourglass modes
-until bonds fail spuriously and the run diverges (pass hourglass=0 or
-k_hg=0 for the reference's model).
+The plates run with a zero-energy-mode penalty (G_s = 0.25) and material-
+point failure at damage 0.5: the classic correspondence model alone lets the
+velocity loading grow hourglass modes until bonds fail spuriously, and
+particles held by a few bonds outgrow the time step once cracks run; both
+make the run diverge (hourglass=0, damage_fail=1 give the reference's model).
 """
 from __future__ import annotations
 
@@ -73,6 +74,7 @@ class Plate:
     name: str = ""
     meta: dict = field(default_factory=dict)
     hourglass: float = 0.25  # G_s of the zero-energy-mode penalty (0: the reference's model)
+    damage_fail: float = 0.5  # material-point failure threshold (>= 1: never)
 
     @property
     def n(self):
@@ -85,11 +87,12 @@ class Plate:
         c11 = m.E / (1.0 - m.nu * m.nu)
         return self.hourglass * c11 / (float(self.vol.mean()) * self.cutoff * self.cutoff)
 
-    def params(self, precision=native.PD_FP64, device=0, s_c=None, det_guard=1e-10, k_hg=None):
+    def params(self, precision=native.PD_FP64, device=0, s_c=None, det_guard=1e-10, k_hg=None, damage_fail=None):
         m = self.material
         return native.default_params(precision=precision, device=device, E=m.E, nu=m.nu, rho=m.rho, dt=self.dt,
                                      s_c=m.s_c if s_c is None else s_c, det_guard=det_guard,
-                                     k_hg=self.k_hg if k_hg is None else k_hg)
+                                     k_hg=self.k_hg if k_hg is None else k_hg,
+                                     damage_fail=self.damage_fail if damage_fail is None else damage_fail)
 
     def context(self, precision=native.PD_FP64, device=0, s_c=None, k_hg=None):
         """A device context with particles, GPU-built families and BCs set."""

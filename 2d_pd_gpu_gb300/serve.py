@@ -1,0 +1,215 @@
+"""Serving loop: continuous batching of fracture-solve requests on one GPU.
+
+Requests (plate size, crack, material, load, step count) arrive over time.
+A request is admitted when its estimated HBM footprint fits under the budget
+and a batch slot is free; its plate is then built on the GPU (families by
+the cell list), kept resident, and joins the running pd_batch, so its steps
+overlap with everyone else's.  The loop advances all active requests
+together in chunks (never past any request's remaining step count), retires
+finished requests between chunks (reads their result, frees their memory)
+and admits waiting ones as memory and slots free up.  Host-side plate
+generation runs on worker threads ahead of admission.
+
+Because every plate's arithmetic is independent of the batch it runs in, a
+request's result is the same alone and in the mix (bit for bit, FP64 and
+mixed alike; tests/test_gpu_serve.py).
+
+Reported: per-request latency (completion - arrival) p50/p99/mean, queueing
+delay, aggregate bond-updates/s over the makespan.
+"""
+from __future__ import annotations
+
+import hashlib
+import math
+import time
+from collections import deque
+from concurrent.futures import ThreadPoolExecutor
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import native, plates
+
+# bytes per particle and per bond slot actually allocated (pd_api.cu): state,
+# geometry, staging, CSR, SELL and per-bond data.  Used for admission.
+FOOTPRINT = {native.PD_FP64: (215.0, 4.0 + 48.0 + 4.0), native.PD_MIXED: (230.0, 4.0 + 4.0 + 4.0)}
+
+
+@dataclass
+class Request:
+    rid: int
+    arrival: float
+    nx: int
+    ny: int
+    steps: int
+    seed: int
+    material: plates.Material
+    v_load: float
+    crack: tuple
+
+    @property
+    def particles(self):
+        return self.nx * self.ny
+
+    def plate(self):
+        return plates.make_plate(self.nx, self.ny, seed=self.seed, crack=self.crack, material=self.material,
+                                 v_load=self.v_load, steps=self.steps, name=f"req{self.rid}")
+
+
+@dataclass
+class Result:
+    rid: int
+    arrival: float
+    admitted: float
+    finished: float
+    particles: int
+    bonds: int
+    steps: int
+    digest: str
+    broken: int
+
+    @property
+    def latency(self):
+        return self.finished - self.arrival
+
+
+def footprint(n, precision, bonds_per_particle=28.0):
+    per_p, per_slot = FOOTPRINT[precision]
+    return n * (per_p + per_slot * bonds_per_particle)
+
+
+def make_requests(count, seed=0, lo=1e4, hi=2e6, steps_lo=200, steps_hi=2000, rate=None, load_work=None):
+    """Seeded request stream: particle counts log-uniform in [lo, hi], square or
+    2:1 plates, random crack (0.1-0.5 width, +-30 deg) and material as the
+    batched workload, steps uniform in [steps_lo, steps_hi].  Arrivals are a
+    Poisson process of `rate` requests/s (or back to back if rate is None)."""
+    r = plates.uniform(seed, 21, np.arange(12 * count)).reshape(count, 12)
+    reqs, t = [], 0.0
+    for k in range(count):
+        n = math.exp(math.log(lo) + (math.log(hi) - math.log(lo)) * r[k, 0])
+        if r[k, 1] < 0.5:
+            nx = ny = max(8, int(round(math.sqrt(n))))
+        else:
+            ny = max(8, int(round(math.sqrt(n / 2.0))))
+            nx = 2 * ny
+        steps = int(steps_lo + (steps_hi - steps_lo) * r[k, 2])
+        mat = plates.Material(E=50e9 + 50e9 * r[k, 3], nu=0.2 + 0.15 * r[k, 4], rho=2440.0, s_c=5e-4)
+        dx = 1e-3
+        x0, y0 = -math.floor(nx / 2) * dx, -math.floor(ny / 2) * dx
+        w, h = (nx - 1) * dx, (ny - 1) * dx
+        crack = (x0 + (0.3 + 0.4 * r[k, 5]) * w, y0 + (0.3 + 0.4 * r[k, 6]) * h, (0.1 + 0.4 * r[k, 7]) * w,
+                 math.radians(-30.0 + 60.0 * r[k, 8]))
+        if rate:
+            t += -math.log(max(1e-300, 1.0 - r[k, 9])) / rate
+        reqs.append(Request(k, t, nx, ny, steps, seed * 100003 + k, mat, 0.5 + 1.5 * r[k, 10], crack))
+    return reqs
+
+
+def state_digest(ctx):
+    u, v, _ = ctx.state()
+    m = ctx.bond_mask()
+    h = hashlib.sha256()
+    for a in (u, v, m):
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest(), int((m == 0).sum())
+
+
+@dataclass
+class Server:
+    precision: int = native.PD_MIXED
+    device: int = 0
+    budget_bytes: float = 150e9
+    max_plates: int = 256
+    chunk: int = 50
+    batch_config: dict | None = None
+    workers: int = 4
+    results: list = field(default_factory=list)
+
+    def run(self, requests, stop_after=None):
+        """Serve `requests` (arrival times relative to the start); returns metrics."""
+        batch = native.Batch(precision=self.precision, device=self.device)
+        if self.batch_config:
+            batch.set_config(**self.batch_config)
+        pending = deque(sorted(requests, key=lambda q: q.arrival))
+        queue, active, used = deque(), {}, 0.0
+        pool = ThreadPoolExecutor(max_workers=self.workers)
+        futs = {}
+        t0 = time.perf_counter()
+        busy = 0.0
+        bond_steps = 0
+        done = 0
+        while pending or queue or active:
+            now = time.perf_counter() - t0
+            while pending and pending[0].arrival <= now:
+                q = pending.popleft()
+                queue.append(q)
+                futs[q.rid] = pool.submit(q.plate)
+            # prefetch the next arrivals' plates too
+            for q in list(pending)[: self.workers]:
+                if q.rid not in futs:
+                    futs[q.rid] = pool.submit(q.plate)
+            # admission: FIFO, by footprint and slots
+            while queue and len(active) < self.max_plates:
+                q = queue[0]
+                need = footprint(q.particles, self.precision)
+                if used + need > self.budget_bytes and active:
+                    break
+                if not futs[q.rid].done() and active:
+                    break  # keep the GPU busy; admit when its plate is ready
+                p = futs.pop(q.rid).result()
+                queue.popleft()
+                ctx = p.context(precision=self.precision, device=self.device)
+                batch.add(ctx)
+                used += need
+                active[q.rid] = [q, ctx, q.steps, time.perf_counter() - t0, need]
+            if not active:
+                if pending:
+                    time.sleep(max(0.0, min(0.01, pending[0].arrival - (time.perf_counter() - t0))))
+                continue
+            k = min(self.chunk, min(a[2] for a in active.values()))
+            ts = time.perf_counter()
+            batch.step(k)
+            batch.synchronize()
+            busy += time.perf_counter() - ts
+            fin = time.perf_counter() - t0
+            for rid in list(active):
+                a = active[rid]
+                a[2] -= k
+                bond_steps += a[1].nnz * k
+                if a[2] == 0:
+                    q, ctx = a[0], a[1]
+                    batch.remove(ctx)
+                    dig, broken = state_digest(ctx)
+                    self.results.append(Result(q.rid, q.arrival, a[3], fin, q.particles, ctx.nnz, q.steps, dig, broken))
+                    ctx.close()
+                    used -= a[4]
+                    del active[rid]
+                    done += 1
+            if stop_after and done >= stop_after:
+                break
+        makespan = time.perf_counter() - t0
+        pool.shutdown()
+        batch.close()
+        lat = np.array([r.latency for r in self.results])
+        wait = np.array([r.admitted - r.arrival for r in self.results])
+        return {
+            "requests": len(self.results),
+            "precision": "fp64" if self.precision == native.PD_FP64 else "mixed",
+            "p50_latency_s": float(np.percentile(lat, 50)) if lat.size else None,
+            "p99_latency_s": float(np.percentile(lat, 99)) if lat.size else None,
+            "mean_latency_s": float(lat.mean()) if lat.size else None,
+            "p50_queue_s": float(np.percentile(wait, 50)) if wait.size else None,
+            "makespan_s": makespan,
+            "gpu_busy_frac": busy / makespan if makespan > 0 else None,
+            "bond_updates_per_s": bond_steps / makespan if makespan > 0 else None,
+            "bond_updates": bond_steps,
+        }
+
+
+def solo_digest(request, precision, device=0):
+    """The same request run alone (its own context, pd_step)."""
+    ctx = request.plate().context(precision=precision, device=device)
+    ctx.step(request.steps)
+    d = state_digest(ctx)
+    ctx.close()
+    return d

@@ -152,9 +152,10 @@ def byte_model(precision, n, nb):
 
 
 def fp64_ops(n, nb):
-    """FP64 operations per step of the FP64 form (pass A 11/bond + ~35/particle,
-    pass B 4/bond + ~30/particle), for the FP64-ALU fraction."""
-    return 15.0 * nb + 65.0 * n
+    """FP64 operations per step of the FP64 form: pass A 8 per bond (d 2, D 4,
+    penalty sum 2; the stretch test is certified in FP32 for nearly all bonds)
+    + ~40 per particle, pass B 4 per bond + ~35 per particle."""
+    return 12.0 * nb + 75.0 * n
 
 
 def cpu_step_rate(plate, steps, nthreads, s_c=None):
@@ -163,7 +164,8 @@ def cpu_step_rate(plate, steps, nthreads, s_c=None):
     rp, col = po.build_families(plate.x, plate.cutoff, plate.cracks, nthreads=nthreads)
     sim = po.OracleSim(plate.x, plate.vol, rp, col, E=plate.material.E, nu=plate.material.nu,
                        rho=plate.material.rho, dt=plate.dt, s_c=plate.material.s_c if s_c is None else s_c,
-                       bc=plate.group_of, group_kind=plate.group_kind, group_val=plate.group_val, nthreads=nthreads)
+                       k_hg=plate.k_hg, damage_fail=plate.damage_fail, bc=plate.group_of,
+                       group_kind=plate.group_kind, group_val=plate.group_val, nthreads=nthreads)
     sim.step(1)  # first touch
     t0 = time.perf_counter()
     sim.step(steps)
@@ -182,8 +184,8 @@ def run_reference(args, comm):
 
     rp, col = po.build_families(plate.x, plate.cutoff, plate.cracks, nthreads=nth)
     sim = po.OracleSim(plate.x, plate.vol, rp, col, E=plate.material.E, nu=plate.material.nu,
-                       rho=plate.material.rho, dt=plate.dt, s_c=plate.material.s_c, bc=plate.group_of,
-                       group_kind=plate.group_kind, group_val=plate.group_val, nthreads=nth)
+                       rho=plate.material.rho, dt=plate.dt, s_c=plate.material.s_c, k_hg=plate.k_hg,
+                       damage_fail=plate.damage_fail, bc=plate.group_of, group_kind=plate.group_kind, group_val=plate.group_val, nthreads=nth)
     nb = int(rp[-1])
     sim.step(max(args.warmup, 1))
     t0 = time.perf_counter()
@@ -253,6 +255,65 @@ def accuracy(pdg, plate, device, checkpoints=(100, 500, 1000)):
     return out
 
 
+def run_batch(args, pdg, device):
+    """Ragged batch: 256 plates, side U[50,400], seeded crack / material / load,
+    stepped together by pd_batch with the autotuned launch shape."""
+    nat = pdg.native
+    at = importlib.import_module("2d_pd_gpu_gb300.autotune")
+    specs = pdg.plates.batch_plate_specs(args.batch_plates, seed=args.seed)
+    out = {}
+    for name, prec in (("fp64", nat.PD_FP64), ("mixed", nat.PD_MIXED)):
+        t0 = time.perf_counter()
+        ctxs = [pdg.plates.plate_from_spec(s, steps=500).context(precision=prec, device=device) for s in specs]
+        setup = time.perf_counter() - t0
+        b = nat.Batch(precision=prec, device=device)
+        for c in ctxs:
+            b.add(c)
+        info = b.info()
+        best, timings = at.tune_batch(b, steps=3, warmup=1)
+        for c in ctxs:
+            c.reset()
+        b.step(args.warmup)
+        b.synchronize()
+        ms = b.step_timed(args.batch_steps)
+        val = info["bonds"] * args.batch_steps / (ms / 1e3)
+        model = byte_model(name, info["particles"], info["bonds"])["step"]
+        peaks, _ = load_peaks()
+        ach = model / (ms / args.batch_steps / 1e3) / 1e9
+        out[name] = {"value": val, "unit": "bond-updates/s", "ms_per_step": ms / args.batch_steps,
+                     "plates": info["plates"], "particles": info["particles"], "bonds": info["bonds"],
+                     "steps": args.batch_steps, "setup_s": setup, "config": best,
+                     "candidates_ms": {k: round(v, 4) for k, v in sorted(timings.items(), key=lambda kv: kv[1])[:6]},
+                     "achieved_gbs_step_model": ach, "frac_hbm": ach / peaks["hbm_gbs"],
+                     "gpu_launches": 1 if best["persistent"] else 1 + 2 * args.batch_steps}
+        b.close()
+        for c in ctxs:
+            c.close()
+    return out
+
+
+def run_serve(args, pdg, device, capacity, configs):
+    """Served mixed workload: Poisson stream at ~80% of the measured batch
+    capacity, particle counts log-uniform 10k-2M, steps U[200,2000], admission
+    by HBM footprint under 150 GB, continuous batching."""
+    nat = pdg.native
+    serve = importlib.import_module("2d_pd_gpu_gb300.serve")
+    out = {}
+    for name, prec, count in (("mixed", nat.PD_MIXED, args.serve_requests),
+                              ("fp64", nat.PD_FP64, max(4, args.serve_requests // 4))):
+        probe = serve.make_requests(count, seed=args.seed + 17)
+        work = float(np.mean([27.9 * q.particles * q.steps for q in probe]))
+        rate = 0.8 * capacity[name] / work
+        reqs = serve.make_requests(count, seed=args.seed + 17, rate=rate)
+        srv = serve.Server(precision=prec, device=device, budget_bytes=150e9, chunk=args.serve_chunk,
+                           batch_config=configs.get(name))
+        m = srv.run(reqs)
+        m.update({"arrival_rate_per_s": rate, "offered_load": 0.8, "capacity_bond_updates_per_s": capacity[name],
+                  "particles_range": [min(q.particles for q in reqs), max(q.particles for q in reqs)]})
+        out[name] = m
+    return out
+
+
 def run_ours(args, comm):
     pdg = importlib.import_module("2d_pd_gpu_gb300")
     nat = pdg.native
@@ -276,9 +337,13 @@ def run_ours(args, comm):
         "kernels": kernels,
     }
     ops = fp64_ops(n, nb) / (step_ms / 1e3)
-    result["fp64_alu"] = {"ops_per_s": ops, "peak_ops_per_s": MEASURED_FP64_DFMA_PER_S,
-                          "frac": ops / MEASURED_FP64_DFMA_PER_S, "ops_per_step": fp64_ops(n, nb),
-                          "peak_source": "measured DFMA issue rate on this GB300 (profiles/fp64_alu_peak.md)"}
+    try:
+        peak64, peak32 = nat.probe_fma_rates(device)
+        src = "pd_probe_fma_rates on this GPU, measured in this run"
+    except Exception:
+        peak64, peak32, src = MEASURED_FP64_DFMA_PER_S, None, "recorded DFMA rate (profiles/fp64_alu_peak.md)"
+    result["fp64_alu"] = {"ops_per_s": ops, "peak_ops_per_s": peak64, "frac": ops / peak64,
+                          "ops_per_step": fp64_ops(n, nb), "peak_source": src, "fp32_fma_per_s": peak32}
     # end to end through the public API with pinned host buffers, every step
     if not args.no_e2e:
         esteps = min(args.steps, args.e2e_steps)
@@ -308,6 +373,12 @@ def run_ours(args, comm):
                            "roofline": mroof, "kernels": mkernels, "gpu_launches": 1 + 2 * args.steps}
         if not args.no_accuracy and comm.rank == 0:
             result["mixed"]["accuracy_vs_fp64"] = accuracy(pdg, plate, device)
+    if not args.no_batch and comm.rank == 0:
+        result["batch"] = run_batch(args, pdg, device)
+        if not args.no_serve:
+            cap = {k: v["value"] for k, v in result["batch"].items()}
+            cfgs = {k: v["config"] for k, v in result["batch"].items()}
+            result["serve"] = run_serve(args, pdg, device, cap, cfgs)
     result["clocks"] = sampler.stop()
     if comm.rank == 0 and not args.no_cpu:
         nth = os.cpu_count() or 1
@@ -334,6 +405,12 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--batch-plates", type=int, default=256)
+    ap.add_argument("--batch-steps", type=int, default=20)
+    ap.add_argument("--serve-requests", type=int, default=64)
+    ap.add_argument("--serve-chunk", type=int, default=50)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))

@@ -77,6 +77,12 @@ typedef struct pd_params {
    * the run diverges.  A common choice is k = G_s C11 / (mean V * cutoff^2)
    * with G_s ~ 0.25 at dt = 0.8 CFL. */
   double k_hg;
+  /* Material-point failure: a particle whose damage exceeds damage_fail
+   * carries no stress (S_i = 0; the penalty still acts on its intact bonds).
+   * A particle held by a few bonds has a small K and a correspondence
+   * stiffness the time step cannot follow; without this the plate workloads
+   * diverge once cracks grow (>= 1: never, the reference's semantics). */
+  double damage_fail;
   int32_t singular_policy; /* PD_SINGULAR_ZERO / PD_SINGULAR_ERROR */
   int32_t reserved;
 } pd_params;
@@ -174,6 +180,35 @@ int pd_synchronize(pd_ctx* ctx);
  * and breaks bonds as in pd_step when s_c > 0. */
 int pd_compute_velocity(pd_ctx* ctx, const double* u, double* velocity, double* acce, double* netF);
 
+/* ------------------------------------------------------- batched plates */
+
+/* Many independent plates (contexts) of uneven size stepped together by one
+ * persistent kernel (or one graph of phase kernels), e.g. the ragged-plate
+ * workload and the serving loop.  No reference counterpart (the reference
+ * steps one particle system per process).  Members keep their own device
+ * state and parameters; a plate's results are identical alone and in any
+ * batch.  All members share the batch's device and precision. */
+typedef struct pd_batch pd_batch;
+typedef struct pd_batch_config {
+  int32_t block;          /* threads per block (64..256) */
+  int32_t blocks_per_sm;  /* persistent grid = SMs x this (capped at occupancy) */
+  int32_t persistent;     /* 1: one cooperative persistent kernel per call; 0: phase kernels */
+  int32_t tile;           /* particles per work item (multiple of 32) */
+} pd_batch_config;
+int pd_batch_create(int32_t device, int32_t precision, pd_batch** out);
+int pd_batch_destroy(pd_batch* b);
+const char* pd_batch_last_error(const pd_batch* b);
+int pd_batch_add(pd_batch* b, pd_ctx* ctx);     /* a context is in at most one batch */
+int pd_batch_remove(pd_batch* b, pd_ctx* ctx);  /* pd_destroy also removes it */
+int pd_batch_info(const pd_batch* b, int32_t* nplates, int64_t* particles, int64_t* bonds);
+int pd_batch_set_config(pd_batch* b, const pd_batch_config* cfg);
+int pd_batch_get_config(const pd_batch* b, pd_batch_config* cfg);
+/* nsteps steps of every member (asynchronous; members' later calls are
+ * ordered after it).  PD_ERR_TIMEOUT if a grid-barrier wait gave up. */
+int pd_batch_step(pd_batch* b, int32_t nsteps);
+int pd_batch_synchronize(pd_batch* b);
+int pd_batch_step_timed(pd_batch* b, int32_t nsteps, float* ms);
+
 /* Page-locked host buffers for pd_set_state / pd_get_state /
  * pd_compute_velocity (full-bandwidth host<->device copies).  No reference
  * counterpart (the reference copies from pageable std::vector storage,
@@ -194,6 +229,11 @@ int pd_step_timed(pd_ctx* ctx, int32_t nsteps, float* ms);
 /* nsteps steps launched kernel by kernel with an event pair around every
  * launch; ms[k] = summed device time of kernel k, launches[k] = launch count. */
 int pd_profile_steps(pd_ctx* ctx, int32_t nsteps, double* ms, int64_t* launches);
+
+/* Measured FMA issue rates of the device (FMA lane-operations per second,
+ * FP64 and FP32): the FP64 form's ALU roofline denominator.  No reference
+ * counterpart. */
+int pd_probe_fma_rates(int32_t device, double* fp64_fma_per_s, double* fp32_fma_per_s);
 
 /* Algorithmic bytes per step of the dominant kernels (fixed byte model:
  * FP64 248 B/particle + 11 B/bond, mixed 148 B/particle + 11 B/bond). */

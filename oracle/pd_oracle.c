@@ -27,7 +27,9 @@
  * accumulates damage as a per-bond average, src/main_seq.cpp:588); a
  * relative determinant guard sets S_i = 0 for a particle whose remaining
  * bonds give a singular K (the reference divides by zero on the CPU,
- * src/matrix.cpp:121-126).
+ * src/matrix.cpp:121-126), and so does material-point failure: damage above
+ * damage_fail (a particle held by a few bonds has a small K and a stiffness
+ * the time step cannot follow).
  */
 #include "pd_oracle.h"
 
@@ -210,7 +212,9 @@ static int kinv_of(const pdo_problem* pb, const pdo_state* st, int64_t i) {
   const double det = fma(k11, k22, -(k12 * k12));
   double* ki = st->kinv + 3 * i;
   double* mt = st->mt + 2 * i;
-  if (nal == 0 || !(det > pb->det_guard * (k11 * k22))) {
+  const int64_t fam = pb->row_ptr[i + 1] - pb->row_ptr[i];
+  const int failed = fam > 0 && (double)st->broken[i] / (double)fam > pb->damage_fail;
+  if (nal == 0 || failed || !(det > pb->det_guard * (k11 * k22))) {
     ki[0] = ki[1] = ki[2] = 0.0;
     mt[0] = mt[1] = 0.0;
     st->singular[i] = 1;

@@ -40,6 +40,7 @@ typedef struct pdo_problem {
   double s_c;              /* critical stretch; <= 0 disables breaking */
   double det_guard;        /* relative det(K) guard, e.g. 1e-10 */
   double k_hg;             /* zero-energy-mode penalty coefficient (0: the reference's model) */
+  double damage_fail;      /* a particle with damage > this carries no stress (>= 1: never) */
   int32_t nthreads;        /* OpenMP threads, <= 0: runtime default */
 } pdo_problem;
 

@@ -47,6 +47,7 @@ class _Problem(ctypes.Structure):
         ("s_c", ctypes.c_double),
         ("det_guard", ctypes.c_double),
         ("k_hg", ctypes.c_double),
+        ("damage_fail", ctypes.c_double),
         ("nthreads", ctypes.c_int32),
     ]
 
@@ -134,6 +135,7 @@ class OracleSim:
     s_c: float = 0.0
     det_guard: float = 1e-10
     k_hg: float = 0.0
+    damage_fail: float = 1.0
     bc: np.ndarray | None = None
     group_kind: np.ndarray | None = None
     group_val: np.ndarray | None = None
@@ -168,7 +170,7 @@ class OracleSim:
         self._pb = _Problem(n, _p(self.x, _f64p), _p(self.vol, _f64p), _p(self.row_ptr, _i64p),
                             _p(self.col, _i32p), _p(self.bc, _u8p), self.group_kind.size,
                             _p(self.group_kind, _i32p), _p(self.group_val, _f64p), self.E, self.nu, self.rho,
-                            self.dt, self.s_c, self.det_guard, self.k_hg, self.nthreads)
+                            self.dt, self.s_c, self.det_guard, self.k_hg, self.damage_fail, self.nthreads)
         self._st = _State(_p(self.u, _f64p), _p(self.v, _f64p), _p(self.f, _f64p), _p(self.alive, _u8p),
                           _p(self.broken, _i32p), _p(self.damage, _f64p), _p(self.kinv, _f64p),
                           _p(self.mt, _f64p), _p(self.w, _f64p), _p(self.hg, _f64p), _p(self.singular, _u8p))

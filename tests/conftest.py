@@ -74,4 +74,4 @@ def plate_oracle(po, p, s_c=None, families=None, k_hg=None):
     rp, col = families if families is not None else po.build_families(p.x, p.cutoff, p.cracks)
     return po.OracleSim(p.x, p.vol, rp, col, E=p.material.E, nu=p.material.nu, rho=p.material.rho, dt=p.dt,
                         s_c=p.material.s_c if s_c is None else s_c, k_hg=p.k_hg if k_hg is None else k_hg,
-                        bc=p.group_of, group_kind=p.group_kind, group_val=p.group_val)
+                        damage_fail=p.damage_fail, bc=p.group_of, group_kind=p.group_kind, group_val=p.group_val)
