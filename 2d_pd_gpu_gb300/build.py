@@ -30,6 +30,7 @@ NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "
 CUDA_UNITS = [
     ("pd_family.cu", ["--fmad=false"]),
     ("pd_fp64.cu", ["--fmad=false"]),
+    ("pd_bondassoc.cu", ["--fmad=false"]),
     ("pd_mixed.cu", []),
     ("pd_probe.cu", []),
     ("pd_api.cu", []),
@@ -61,7 +62,8 @@ def _stale(target, deps):
 def build(verbose=False, force=False):
     os.makedirs(OUT, exist_ok=True)
     nv = nvcc()
-    headers = [os.path.join(CSRC, "pd_internal.h"), os.path.join(INCLUDE, "pd_gb300.h")]
+    headers = [os.path.join(CSRC, h) for h in ("pd_internal.h", "pd_walk.cuh", "pd_batch.cuh")] + \
+        [os.path.join(INCLUDE, "pd_gb300.h")]
     objs, jobs = [], []
     for src, extra in CUDA_UNITS:
         s = os.path.join(CSRC, src)

@@ -51,6 +51,10 @@ struct pd_ctx {
   double* blim = nullptr;
   float* br2 = nullptr;
   float2* u32 = nullptr;
+  // bond-associated mode
+  double2* tb = nullptr;
+  int64_t* rslot = nullptr;
+  int32_t max_family = 0;
   // counters (device) + host mirror of steps
   unsigned long long* counters = nullptr;
   int64_t steps = 0;
@@ -133,6 +137,8 @@ void free_families(pd_ctx* c) {
   dfree(c->bgeo);
   dfree(c->blim);
   dfree(c->br2);
+  dfree(c->tb);
+  dfree(c->rslot);
   c->sell = pd::SellLayout{};
   c->nnz = 0;
   c->has_families = false;
@@ -161,8 +167,17 @@ int check_params(pd_ctx* c, const pd_params* p) {
     return fail(c, PD_ERR_ARG, "invalid material / time-step parameters");
   if (p->singular_policy != PD_SINGULAR_ZERO && p->singular_policy != PD_SINGULAR_ERROR)
     return fail(c, PD_ERR_ARG, "unknown singular_policy");
+  if (p->n1 != 0.0 || p->n2 != 0.0) {
+    if (p->precision != PD_FP64) return fail(c, PD_ERR_ARG, "bond-associated weights need PD_FP64");
+    if (p->s_c > 0.0 || p->k_hg != 0.0)
+      return fail(c, PD_ERR_ARG, "bond-associated weights: no bond breaking (s_c <= 0) and k_hg = 0");
+    if (!(p->weight_len > 0.0) || !std::isfinite(p->n1) || !std::isfinite(p->n2))
+      return fail(c, PD_ERR_ARG, "bond-associated weights need weight_len > 0 and finite n1, n2");
+  }
   return PD_OK;
 }
+
+bool bond_assoc(const pd_ctx* c) { return c->p.n1 != 0.0 || c->p.n2 != 0.0; }
 
 void stiffness(const pd_ctx* c, double* c11, double* c12, double* c33);
 
@@ -185,6 +200,35 @@ Fp64Args fp64_args(pd_ctx* c) {
   a.counters = c->counters;
   a.brk = c->p.s_c > 0.0;
   return a;
+}
+
+pd::BondAssoc ba_args(pd_ctx* c) {
+  pd::BondAssoc b{};
+  b.n1 = c->p.n1;
+  b.n2 = c->p.n2;
+  b.inv_wlen = c->p.weight_len > 0.0 ? 1.0 / c->p.weight_len : 0.0;
+  b.tb = c->tb;
+  b.rslot = c->rslot;
+  return b;
+}
+
+// Buffers and reverse-slot index of the bond-associated mode.
+int ensure_ba(pd_ctx* c) {
+  if (!bond_assoc(c) || !c->has_families) return PD_OK;
+  if (c->max_family > 64) return fail(c, PD_ERR_CAPACITY, "bond-associated mode: families are limited to 64 bonds");
+  if (c->tb) return PD_OK;
+  const size_t ns = (size_t)(c->sell.nslots > 0 ? c->sell.nslots : 1);
+  PD_CK(c, cudaMalloc(&c->tb, ns * sizeof(double2)));
+  PD_CK(c, cudaMalloc(&c->rslot, ns * sizeof(int64_t)));
+  PD_CK(c, cudaMemsetAsync(c->tb, 0, ns * sizeof(double2), c->stream));
+  PD_CK(c, cudaMemsetAsync(c->counters + pd::CNT_ERROR, 0, sizeof(unsigned long long), c->stream));
+  pd::launch_ba_reverse(fp64_args(c), ba_args(c), c->stream);
+  PD_CK(c, cudaGetLastError());
+  unsigned long long err = 0;
+  PD_CK(c, cudaMemcpyAsync(&err, c->counters + pd::CNT_ERROR, sizeof(err), cudaMemcpyDeviceToHost, c->stream));
+  PD_CK(c, cudaStreamSynchronize(c->stream));
+  if (err & pd::ERR_ASYMMETRIC) return fail(c, PD_ERR_ARG, "bond-associated mode needs symmetric families");
+  return PD_OK;
 }
 
 bool mixed(const pd_ctx* c) { return c->p.precision == PD_MIXED; }
@@ -293,7 +337,16 @@ int finish_families(pd_ctx* c) {
   }
   if (c->n > 0) k_fam_from_rowptr<<<(unsigned)pd::blocks_for(c->n), pd::kBlock, 0, s>>>(c->n, c->row_ptr, c->fam);
   PD_CK(c, cudaGetLastError());
+  {
+    std::vector<int64_t> rp((size_t)c->n + 1);
+    PD_CK(c, cudaMemcpy(rp.data(), c->row_ptr, rp.size() * sizeof(int64_t), cudaMemcpyDeviceToHost));
+    int64_t m = 0;
+    for (int64_t i = 0; i < c->n; ++i) m = std::max(m, rp[i + 1] - rp[i]);
+    c->max_family = (int32_t)m;
+  }
   c->has_families = true;
+  int rcb = ensure_ba(c);
+  if (rcb != PD_OK) return rcb;
   return pd_reset(c);
 }
 
@@ -316,6 +369,9 @@ void pd_default_params(pd_params* p) {
   p->det_guard = 1e-10;
   p->k_hg = 0.0;
   p->damage_fail = 1.0;
+  p->n1 = 0.0;
+  p->n2 = 0.0;
+  p->weight_len = 1.0;
   p->singular_policy = PD_SINGULAR_ZERO;
 }
 
@@ -385,6 +441,8 @@ int pd_set_params(pd_ctx* c, const pd_params* p) {
   clear_graphs(c);
   if (c->has_families) {
     int rc2 = upload_gvel(c);
+    if (rc2 != PD_OK) return rc2;
+    rc2 = ensure_ba(c);
     if (rc2 != PD_OK) return rc2;
   }
   if (c->has_families && s_changed && !mixed(c)) {
@@ -698,10 +756,20 @@ struct Launcher {
     if (mixed(c)) pd::launch_drift_mixed(m, s); else pd::launch_drift_fp64(f, s);
   }
   void pass_a(cudaStream_t s) {
-    if (mixed(c)) pd::launch_pass_a_mixed(m, brk, s); else pd::launch_pass_a_fp64(f, brk, s);
+    if (mixed(c))
+      pd::launch_pass_a_mixed(m, brk, s);
+    else if (bond_assoc(c))
+      pd::launch_ba_pass_a(f, ba_args(c), s);
+    else
+      pd::launch_pass_a_fp64(f, brk, s);
   }
   void pass_b(bool next_drift, cudaStream_t s) {
-    if (mixed(c)) pd::launch_pass_b_mixed(m, next_drift, s); else pd::launch_pass_b_fp64(f, next_drift ? 1 : 0, s);
+    if (mixed(c))
+      pd::launch_pass_b_mixed(m, next_drift, s);
+    else if (bond_assoc(c))
+      pd::launch_ba_pass_b(f, ba_args(c), next_drift ? 1 : 0, s);
+    else
+      pd::launch_pass_b_fp64(f, next_drift ? 1 : 0, s);
   }
 };
 
@@ -772,9 +840,14 @@ int pd_compute_velocity(pd_ctx* c, const double* u, double* velocity, double* ac
   PD_CK(c, cudaMemcpyAsync(c->v, velocity, b, cudaMemcpyHostToDevice, s));
   PD_CK(c, cudaMemcpyAsync(c->acc, acce, b, cudaMemcpyHostToDevice, s));
   const Fp64Args a = fp64_args(c);
-  pd::launch_shadow_fp64(a, s);
-  pd::launch_pass_a_fp64(a, c->p.s_c > 0.0, s);
-  pd::launch_pass_b_fp64(a, 2, s);
+  if (bond_assoc(c)) {
+    pd::launch_ba_pass_a(a, ba_args(c), s);
+    pd::launch_ba_pass_b(a, ba_args(c), 2, s);
+  } else {
+    pd::launch_shadow_fp64(a, s);
+    pd::launch_pass_a_fp64(a, c->p.s_c > 0.0, s);
+    pd::launch_pass_b_fp64(a, 2, s);
+  }
   PD_CK(c, cudaGetLastError());
   PD_CK(c, cudaMemcpyAsync(velocity, c->v, b, cudaMemcpyDeviceToHost, s));
   PD_CK(c, cudaMemcpyAsync(acce, c->acc, b, cudaMemcpyDeviceToHost, s));
@@ -987,6 +1060,7 @@ int pd_batch_add(pd_batch* b, pd_ctx* c) {
   if (c->p.device != b->device || c->p.precision != b->precision)
     return bfail(b, PD_ERR_ARG, "batch members share the batch's device and precision");
   if (!c->has_families) return bfail(b, PD_ERR_ORDER, "set particles and families before adding a context");
+  if (bond_assoc(c)) return bfail(b, PD_ERR_ARG, "bond-associated contexts are stepped on their own");
   PD_BCK(b, cudaSetDevice(b->device));
   PD_BCK(b, cudaStreamSynchronize(b->stream));
   b->members.push_back(c);

@@ -1,0 +1,210 @@
+// Bond-associated NOSB (the reference's default model, n1 / n2 != 0), FP64.
+//
+// Reference: computeShapeTensors (src/main_seq.cpp:71-156) gives every bond
+// b = (i, nb) its own weighted shape tensors
+//   K_b = sum_k w(b,k) V_k xi_k (x) xi_k,   N_b = K_b + D_b (D: displacements),
+//   w(b,k) = exp(-n1 |L_b - L_k| / (horizon dx)) (0.5 + 0.5 cos(b,k))^n2,
+// computeStressTensor (:204-268) its stress sigma_b, and
+// computeForceDensityStates (:271-380) the force state
+//   T_ij = (1/V_h) sum_b w(j,b) V_b sigma_b K_b^-1 xi_ij,
+// with the net force f_i = sum_j (T_ij - T_ji) V_j (computeVelocity :396-470).
+// The reference recomputes sigma_b K_b^-1 inside the (i, j) loop (O(n^3) per
+// particle).  Here pass A forms P_b = sigma_b K_b^-1 once per bond and T_ij
+// once per bond (O(n^2) per particle, family <= 64 bonds, kept in local
+// memory), storing T per bond slot; pass B reads T_ji through the reverse
+// slot index and applies the kick (+ the next drift) as the classic form.
+// Arithmetic follows the oracle's ba_pass_a / ba_pass_b (--fmad=false, the
+// same explicit fma() calls); exp/pow are CUDA's, so the two agree to
+// rounding (not bit for bit) in this mode.  No bond breaking here (the
+// reference has none).
+#include "pd_internal.h"
+
+namespace pd {
+
+namespace {
+
+constexpr int kBaMax = 64;
+
+__device__ __forceinline__ double ba_weight(double n1, double n2, double inv_wlen, double bx, double by, double lb,
+                                            double kx, double ky, double lk) {
+  double c = (bx * kx + by * ky) / (lb * lk);
+  if (c > 1.0) c = 1.0;
+  else if (c < -1.0) c = -1.0;
+  const double lr = fabs(lb - lk) * inv_wlen;
+  return exp(-n1 * lr) * pow(0.5 + 0.5 * c, n2);
+}
+
+__global__ void __launch_bounds__(128) k_ba_pass_a(Fp64Args a, BondAssoc b) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const int64_t c0 = i >> 5;
+  const int w = a.chunk_w[c0];
+  const int64_t s0 = a.chunk_base[c0] + (i & 31);
+  double ex[kBaMax], ey[kBaMax], el[kBaMax], vv[kBaMax], dx[kBaMax], dy[kBaMax], P[kBaMax][4];
+  int64_t slot[kBaMax];
+  const double2 ui = a.u[i];
+  double vh = 0.0;
+  int n = 0;
+  for (int k = 0; k < w && n < kBaMax; ++k) {
+    const int64_t s = s0 + (int64_t)k * kChunk;
+    const int j = a.nbr[s];
+    if (j < 0) continue;
+    const double2 e = a.bxi[s];
+    const double2 uj = a.u[j];
+    ex[n] = e.x;
+    ey[n] = e.y;
+    el[n] = sqrt(e.x * e.x + e.y * e.y);
+    vv[n] = a.vol[j];
+    dx[n] = uj.x - ui.x;
+    dy[n] = uj.y - ui.y;
+    vh = vh + vv[n];
+    slot[n] = s;
+    ++n;
+  }
+  for (int q = 0; q < n; ++q) {
+    double k11 = 0.0, k12 = 0.0, k22 = 0.0, d11 = 0.0, d12 = 0.0, d21 = 0.0, d22 = 0.0;
+    for (int k = 0; k < n; ++k) {
+      const double wv = ba_weight(b.n1, b.n2, b.inv_wlen, ex[q], ey[q], el[q], ex[k], ey[k], el[k]) * vv[k];
+      const double t0 = wv * ex[k], t1 = wv * ey[k];
+      k11 = fma(t0, ex[k], k11);
+      k12 = fma(t0, ey[k], k12);
+      k22 = fma(t1, ey[k], k22);
+      d11 = fma(dx[k], t0, d11);
+      d12 = fma(dx[k], t1, d12);
+      d21 = fma(dy[k], t0, d21);
+      d22 = fma(dy[k], t1, d22);
+    }
+    const double det = fma(k11, k22, -(k12 * k12));
+    if (!(det > a.det_guard * (k11 * k22))) {
+      P[q][0] = P[q][1] = P[q][2] = P[q][3] = 0.0;
+      continue;
+    }
+    const double r = 1.0 / det;
+    const double q11 = k22 * r, q12 = -k12 * r, q22 = k11 * r;
+    const double g11 = fma(d11, q11, d12 * q12), g12 = fma(d11, q12, d12 * q22);
+    const double g21 = fma(d21, q11, d22 * q12), g22 = fma(d21, q12, d22 * q22);
+    const double e11 = g11, e22 = g22, e12 = 0.5 * (g12 + g21);
+    const double s11 = fma(a.c11, e11, a.c12 * e22);
+    const double s22 = fma(a.c12, e11, a.c11 * e22);
+    const double s12 = a.c33 * e12;
+    P[q][0] = fma(s11, q11, s12 * q12);
+    P[q][1] = fma(s11, q12, s12 * q22);
+    P[q][2] = fma(s12, q11, s22 * q12);
+    P[q][3] = fma(s12, q12, s22 * q22);
+  }
+  const double rv = 1.0 / vh;
+  for (int jj = 0; jj < n; ++jj) {
+    double m11 = 0.0, m12 = 0.0, m21 = 0.0, m22 = 0.0;
+    for (int q = 0; q < n; ++q) {
+      const double wv = ba_weight(b.n1, b.n2, b.inv_wlen, ex[jj], ey[jj], el[jj], ex[q], ey[q], el[q]) * vv[q];
+      m11 = fma(wv, P[q][0], m11);
+      m12 = fma(wv, P[q][1], m12);
+      m21 = fma(wv, P[q][2], m21);
+      m22 = fma(wv, P[q][3], m22);
+    }
+    b.tb[slot[jj]] = make_double2(fma(m11 * rv, ex[jj], (m12 * rv) * ey[jj]), fma(m21 * rv, ex[jj], (m22 * rv) * ey[jj]));
+  }
+}
+
+// Velocity BC, drift, fixed BC (as pd_fp64.cu's drift_one).
+__device__ __forceinline__ void ba_drift(const Fp64Args& a, int64_t i, double2& v, double2& u, double anx,
+                                         double any) {
+  const int g = a.bc[i];
+  const int kind = g ? a.gkind[g - 1] : PD_BC_NONE;
+  if (kind == PD_BC_VELOCITY) v = a.gval[g - 1];
+  u.x = u.x + (v.x * a.dt + (0.5 * anx) * a.dt2);
+  u.y = u.y + (v.y * a.dt + (0.5 * any) * a.dt2);
+  if (kind == PD_BC_FIXED) u = make_double2(0.0, 0.0);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kBlock) k_ba_pass_b(Fp64Args a, BondAssoc b) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const int64_t c0 = i >> 5;
+  const int w = a.chunk_w[c0];
+  const int64_t s0 = a.chunk_base[c0] + (i & 31);
+  double fx = 0.0, fy = 0.0;
+  for (int k = 0; k < w; ++k) {
+    const int64_t s = s0 + (int64_t)k * kChunk;
+    const int j = a.nbr[s];
+    if (j < 0) continue;
+    const double2 tij = b.tb[s], tji = b.tb[b.rslot[s]];
+    const double vj = a.vol[j];
+    fx = fma(tij.x - tji.x, vj, fx);
+    fy = fma(tij.y - tji.y, vj, fy);
+  }
+  double2 v = a.v[i];
+  double aox, aoy;
+  if (MODE == 2) {
+    const double2 ao = a.acc[i];
+    aox = ao.x;
+    aoy = ao.y;
+  } else {
+    const double2 fo = a.f[i];
+    aox = fo.x * a.inv_rho;
+    aoy = fo.y * a.inv_rho;
+  }
+  const double anx = fx * a.inv_rho, any = fy * a.inv_rho;
+  v.x = v.x + (0.5 * (aox + anx)) * a.dt;
+  v.y = v.y + (0.5 * (aoy + any)) * a.dt;
+  a.f[i] = make_double2(fx, fy);
+  if (MODE == 2) a.acc[i] = make_double2(anx, any);
+  if (MODE == 1) {
+    double2 u = a.u[i];
+    ba_drift(a, i, v, u, anx, any);
+    a.u[i] = u;
+  }
+  a.v[i] = v;
+}
+
+// rslot[s] = slot of (j, i) in j's SELL rows, for every slot s = (i, j).
+__global__ void k_ba_reverse(Fp64Args a, BondAssoc b, unsigned long long* counters) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const int64_t c0 = i >> 5;
+  const int w = a.chunk_w[c0];
+  const int64_t s0 = a.chunk_base[c0] + (i & 31);
+  for (int k = 0; k < w; ++k) {
+    const int64_t s = s0 + (int64_t)k * kChunk;
+    const int j = a.nbr[s];
+    if (j < 0) continue;
+    const int64_t cj = (int64_t)j >> 5;
+    const int wj = a.chunk_w[cj];
+    const int64_t sj0 = a.chunk_base[cj] + (j & 31);
+    int64_t found = -1;
+    for (int q = 0; q < wj; ++q)
+      if (a.nbr[sj0 + (int64_t)q * kChunk] == (int)i) {
+        found = sj0 + (int64_t)q * kChunk;
+        break;
+      }
+    if (found < 0) {
+      atomicOr(counters + CNT_ERROR, (unsigned long long)ERR_ASYMMETRIC);
+      found = s;  // T_ij - T_ij = 0: the bond is inert
+    }
+    b.rslot[s] = found;
+  }
+}
+
+}  // namespace
+
+void launch_ba_reverse(const Fp64Args& a, const BondAssoc& b, cudaStream_t s) {
+  if (a.n > 0) k_ba_reverse<<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a, b, a.counters);
+}
+
+void launch_ba_pass_a(const Fp64Args& a, const BondAssoc& b, cudaStream_t s) {
+  if (a.n > 0) k_ba_pass_a<<<(unsigned)blocks_for(a.n, 128), 128, 0, s>>>(a, b);
+}
+
+void launch_ba_pass_b(const Fp64Args& a, const BondAssoc& b, int mode, cudaStream_t s) {
+  if (a.n <= 0) return;
+  const unsigned nb = (unsigned)blocks_for(a.n);
+  if (mode == 0)
+    k_ba_pass_b<0><<<nb, kBlock, 0, s>>>(a, b);
+  else if (mode == 1)
+    k_ba_pass_b<1><<<nb, kBlock, 0, s>>>(a, b);
+  else
+    k_ba_pass_b<2><<<nb, kBlock, 0, s>>>(a, b);
+}
+
+}  // namespace pd

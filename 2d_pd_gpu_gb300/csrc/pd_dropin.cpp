@@ -24,7 +24,7 @@ struct Cached {
   pd_ctx* ctx = nullptr;
   const Particle* data = nullptr;
   size_t n = 0;
-  double rho = 0.0, dt = 0.0, s_c = 0.0, C[9] = {0};
+  double rho = 0.0, dt = 0.0, s_c = 0.0, n1 = 0.0, n2 = 0.0, wlen = 1.0, C[9] = {0};
   double *u = nullptr, *v = nullptr, *a = nullptr, *f = nullptr;  // pinned staging
   ~Cached() {
     pd_host_free(u);
@@ -41,7 +41,7 @@ std::map<const vector<Particle>*, std::unique_ptr<Cached>>& cache() {
 }
 
 Cached& context_for(vector<Particle>& P, const vector<vector<Particle*>>& NL, long double rho, long double dt,
-                    const matrix& Cm) {
+                    const matrix& Cm, double n1, double n2, double wlen) {
   auto& slot = cache()[&P];
   const size_t n = P.size();
   double C[9];
@@ -55,6 +55,9 @@ Cached& context_for(vector<Particle>& P, const vector<vector<Particle*>>& NL, lo
     p.rho = (double)rho;
     p.dt = (double)dt;
     p.s_c = g_s_c;
+    p.n1 = n1;
+    p.n2 = n2;
+    p.weight_len = wlen;
     check(pd_create(&p, &k.ctx), nullptr, "pd_create");
     vector<double> x(2 * n), vol(n);
     for (size_t i = 0; i < n; ++i) {
@@ -81,16 +84,26 @@ Cached& context_for(vector<Particle>& P, const vector<vector<Particle*>>& NL, lo
     k.rho = p.rho;
     k.dt = p.dt;
     k.s_c = p.s_c;
+    k.n1 = n1;
+    k.n2 = n2;
+    k.wlen = wlen;
     std::copy(C, C + 9, k.C);
     check(pd_set_stiffness(k.ctx, C), k.ctx, "pd_set_stiffness");
   }
   Cached& k = *slot;
-  if (k.rho != (double)rho || k.dt != (double)dt || k.s_c != g_s_c || !std::equal(C, C + 9, k.C)) {
+  if (k.rho != (double)rho || k.dt != (double)dt || k.s_c != g_s_c || k.n1 != n1 || k.n2 != n2 ||
+      k.wlen != wlen || !std::equal(C, C + 9, k.C)) {
     pd_params p;
     check(pd_get_params(k.ctx, &p), k.ctx, "pd_get_params");
     p.rho = (double)rho;
     p.dt = (double)dt;
     p.s_c = g_s_c;
+    p.n1 = n1;
+    p.n2 = n2;
+    p.weight_len = wlen;
+    k.n1 = n1;
+    k.n2 = n2;
+    k.wlen = wlen;
     check(pd_set_params(k.ctx, &p), k.ctx, "pd_set_params");
     check(pd_set_stiffness(k.ctx, C), k.ctx, "pd_set_stiffness");
     k.rho = p.rho;
@@ -101,13 +114,11 @@ Cached& context_for(vector<Particle>& P, const vector<vector<Particle*>>& NL, lo
   return k;
 }
 
-void gpu_velocity(double n1, double n2, long double rho, const matrix& C, long double dt,
+void gpu_velocity(double n1, double n2, double wlen, long double rho, const matrix& C, long double dt,
                   vector<vector<long double>>& velocity, vector<vector<Particle*>>& NL,
                   vector<vector<long double>>& acce, vector<vector<long double>>& netF, vector<Particle>& P,
                   bool gpu_semantics) {
-  if (n1 != 0.0 || n2 != 0.0)
-    throw std::invalid_argument("bond-associated weights (n1, n2 != 0) are not available on the GPU path");
-  Cached& k = context_for(P, NL, rho, dt, C);
+  Cached& k = context_for(P, NL, rho, dt, C, n1, n2, wlen);
   const size_t n = P.size();
   for (size_t i = 0; i < n; ++i)
     for (int m = 0; m < 2; ++m) {
@@ -440,21 +451,21 @@ void updatePositions(int ndim, vector<Particle>& P, long double dt, long double 
     }
 }
 
-void computeVelocity(int, double n1, double n2, double, double, long double massDensity, matrix& StiffnessTensor,
-                     long double stepSize, vector<vector<long double>>& velocity,
+void computeVelocity(int, double n1, double n2, double horizon, double dx, long double massDensity,
+                     matrix& StiffnessTensor, long double stepSize, vector<vector<long double>>& velocity,
                      vector<vector<Particle*>>& Neighborslist, vector<vector<long double>>& acce,
                      vector<vector<long double>>& netF, vector<Particle>& localParticles,
                      const unordered_map<int, int>&, vector<vector<double>>&) {
-  gpu_velocity(n1, n2, massDensity, StiffnessTensor, stepSize, velocity, Neighborslist, acce, netF, localParticles,
+  gpu_velocity(n1, n2, horizon * dx, massDensity, StiffnessTensor, stepSize, velocity, Neighborslist, acce, netF, localParticles,
                false);
 }
 
-void compute_velocity_GPU_host(int, double n1, double n2, double, double, double massDensity, matrix& StiffnessTensor,
-                               double stepSize, vector<vector<long double>>& velocity,
+void compute_velocity_GPU_host(int, double n1, double n2, double horizon, double dx, double massDensity,
+                               matrix& StiffnessTensor, double stepSize, vector<vector<long double>>& velocity,
                                vector<vector<Particle*>>& Neighborslist, vector<vector<long double>>& acce,
                                vector<vector<long double>>& netF, vector<Particle>& allParticles,
                                const unordered_map<int, int>&, vector<vector<double>>&) {
-  gpu_velocity(n1, n2, massDensity, StiffnessTensor, stepSize, velocity, Neighborslist, acce, netF, allParticles,
+  gpu_velocity(n1, n2, horizon * dx, massDensity, StiffnessTensor, stepSize, velocity, Neighborslist, acce, netF, allParticles,
                true);
 }
 

@@ -20,6 +20,7 @@
 // FP64 only for bonds an FP32 bound cannot prove intact (surely_intact), so
 // pass A costs 8 FP64 operations for almost every bond.
 #include "pd_internal.h"
+#include "pd_walk.cuh"
 
 namespace pd {
 
@@ -213,17 +214,18 @@ __device__ __forceinline__ void pass_b_particle(const Fp64Args& a, int64_t i) {
     fx = fma(wa.x, m.x, wa.y * m.y);
     fy = fma(wb.x, m.x, wb.y * m.y);
   }
-  for (int k = 0; k < w; ++k) {
-    const int64_t s = s0 + (int64_t)k * kChunk;
-    const int j = a.nbr[s];
-    if (j < 0) continue;
-    const double2 e = __ldcs(&a.bxi[s]);
-    const double2 ja = a.w01[j], jb = a.w23[j];
-    fx = fma(ja.x, e.x, fx);
-    fx = fma(ja.y, e.y, fx);
-    fy = fma(jb.x, e.x, fy);
-    fy = fma(jb.y, e.y, fy);
-  }
+  struct Nb {
+    double2 a, b;
+  };
+  walk_bonds<4>(
+      a.nbr, s0, w, i, [&](int64_t j) { return Nb{a.w01[j], a.w23[j]}; },
+      [&](int64_t s, int, const Nb& nb) {
+        const double2 e = __ldcs(&a.bxi[s]);
+        fx = fma(nb.a.x, e.x, fx);
+        fx = fma(nb.a.y, e.y, fx);
+        fy = fma(nb.b.x, e.x, fy);
+        fy = fma(nb.b.y, e.y, fy);
+      });
   double2 v = a.v[i];
   double aox, aoy;
   if (MODE == 2) {

@@ -33,7 +33,7 @@ constexpr int kBlock = 256;
 // Counters word layout (device int64 array).
 enum { CNT_BROKEN = 0, CNT_SINGULAR = 1, CNT_ERROR = 2, CNT_N = 4 };
 // Device error bits (CNT_ERROR).
-enum { ERR_FAMILY_OVERFLOW = 1, ERR_BAD_NEIGHBOR = 2, ERR_SELF_BOND = 4 };
+enum { ERR_FAMILY_OVERFLOW = 1, ERR_BAD_NEIGHBOR = 2, ERR_SELF_BOND = 4, ERR_ASYMMETRIC = 8 };
 
 struct Fp64Args {
   int64_t n;
@@ -69,6 +69,13 @@ struct Fp64Args {
   unsigned long long* counters;
   int32_t brk;  // bond breaking on (s_c > 0)
   int32_t pad;
+};
+
+// Bond-associated mode (pd_bondassoc.cu): weights and per-bond force states.
+struct BondAssoc {
+  double n1, n2, inv_wlen;
+  double2* tb;     // T_ij per bond slot
+  int64_t* rslot;  // slot of the reverse bond (j, i)
 };
 
 // Mixed form (pd_mixed.cu): scaled two-float state, FP32 bond arithmetic.
@@ -144,6 +151,11 @@ void launch_pass_b_fp64(const Fp64Args& a, int mode, cudaStream_t s);
 cudaError_t launch_batch_fp64(const Fp64Args* d_plates, const BatchTile* d_tiles, int ntiles, int nsteps,
                               const BatchLaunch& cfg, GridBarrier* d_bar, int nsm, cudaStream_t s);
 int batch_occupancy_fp64(const BatchLaunch& cfg);  // resident persistent blocks per SM
+
+// ---- bond-associated FP64 step (pd_bondassoc.cu); families <= 64 bonds
+void launch_ba_reverse(const Fp64Args& a, const BondAssoc& b, cudaStream_t s);
+void launch_ba_pass_a(const Fp64Args& a, const BondAssoc& b, cudaStream_t s);
+void launch_ba_pass_b(const Fp64Args& a, const BondAssoc& b, int mode, cudaStream_t s);
 
 // ---- mixed step (pd_mixed.cu)
 void launch_init_geometry_mixed(const MixedArgs& a, cudaStream_t s);

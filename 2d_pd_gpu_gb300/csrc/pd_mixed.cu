@@ -16,6 +16,7 @@
 // products.  Nothing here is bit-identical to the FP64 form; its error is
 // measured against it (tests/test_gpu_mixed.py, bench.py).
 #include "pd_internal.h"
+#include "pd_walk.cuh"
 
 namespace pd {
 
@@ -130,30 +131,32 @@ __device__ __forceinline__ void pass_a_particle_mixed(const MixedArgs& a, int64_
   const float4 ui = a.us[i], xi = a.xs[i];
   float d11 = 0.f, d12 = 0.f, d21 = 0.f, d22 = 0.f, ax = 0.f, ay = 0.f;
   int newly = 0;
-  for (int k = 0; k < w; ++k) {
-    const int64_t s = s0 + (int64_t)k * kChunk;
-    const int j = __ldcs(&a.nbr[s]);
-    if (j < 0) continue;
-    const float4 uj = a.us[j], xj = a.xs[j];
-    const float vj = a.vh[j];
-    const float ex = tf_diff(xj.x, xj.z, xi.x, xi.z), ey = tf_diff(xj.y, xj.w, xi.y, xi.w);
-    const float dx = tf_diff(uj.x, uj.z, ui.x, ui.z), dy = tf_diff(uj.y, uj.w, ui.y, ui.w);
-    if (BREAK) {
-      const float q = fmaf(dx, fmaf(2.f, ex, dx), dy * fmaf(2.f, ey, dy));
-      if (q > a.s2 * fmaf(ex, ex, ey * ey)) {
-        a.nbr[s] = -2 - j;
-        ++newly;
-        continue;
-      }
-    }
-    const float t0 = vj * ex, t1 = vj * ey;
-    d11 = fmaf(dx, t0, d11);
-    d12 = fmaf(dx, t1, d12);
-    d21 = fmaf(dy, t0, d21);
-    d22 = fmaf(dy, t1, d22);
-    ax = fmaf(vj, dx, ax);
-    ay = fmaf(vj, dy, ay);
-  }
+  struct Nb {
+    float4 u, x;
+    float v;
+  };
+  walk_bonds<4>(
+      a.nbr, s0, w, i, [&](int64_t j) { return Nb{a.us[j], a.xs[j], a.vh[j]}; },
+      [&](int64_t s, int j, const Nb& nb) {
+        const float ex = tf_diff(nb.x.x, nb.x.z, xi.x, xi.z), ey = tf_diff(nb.x.y, nb.x.w, xi.y, xi.w);
+        const float dx = tf_diff(nb.u.x, nb.u.z, ui.x, ui.z), dy = tf_diff(nb.u.y, nb.u.w, ui.y, ui.w);
+        if (BREAK) {
+          const float q = fmaf(dx, fmaf(2.f, ex, dx), dy * fmaf(2.f, ey, dy));
+          if (q > a.s2 * fmaf(ex, ex, ey * ey)) {
+            a.nbr[s] = -2 - j;
+            ++newly;
+            return;
+          }
+        }
+        const float vj = nb.v;
+        const float t0 = vj * ex, t1 = vj * ey;
+        d11 = fmaf(dx, t0, d11);
+        d12 = fmaf(dx, t1, d12);
+        d21 = fmaf(dy, t0, d21);
+        d22 = fmaf(dy, t1, d22);
+        ax = fmaf(vj, dx, ax);
+        ay = fmaf(vj, dy, ay);
+      });
   a.hgs[i] = make_float2(2.f * a.k_hg * ax, 2.f * a.k_hg * ay);
   if (BREAK && newly) {
     atomicAdd(a.counters + CNT_BROKEN, (unsigned long long)newly);
@@ -194,20 +197,21 @@ __device__ __forceinline__ void pass_b_particle_mixed(const MixedArgs& a, int64_
   // compensated sums (value, correction) per component
   float sx = fmaf(wi.x, m.x, fmaf(wi.y, m.y, h.x)), cx = 0.f;
   float sy = fmaf(wi.z, m.x, fmaf(wi.w, m.y, h.y)), cy = 0.f;
-  for (int k = 0; k < w; ++k) {
-    const int64_t s = s0 + (int64_t)k * kChunk;
-    const int j = __ldcs(&a.nbr[s]);
-    if (j < 0) continue;
-    const float4 xj = a.xs[j], wj = a.ws[j];
-    const float ex = tf_diff(xj.x, xj.z, xi.x, xi.z), ey = tf_diff(xj.y, xj.w, xi.y, xi.w);
-    const float px = fmaf(wj.x, ex, wj.y * ey);
-    const float py = fmaf(wj.z, ex, wj.w * ey);
-    const float2 tx = two_sum(sx, px), ty = two_sum(sy, py);
-    sx = tx.x;
-    cx += tx.y;
-    sy = ty.x;
-    cy += ty.y;
-  }
+  struct Nb {
+    float4 x, w;
+  };
+  walk_bonds<4>(
+      a.nbr, s0, w, i, [&](int64_t j) { return Nb{a.xs[j], a.ws[j]}; },
+      [&](int64_t, int, const Nb& nb) {
+        const float ex = tf_diff(nb.x.x, nb.x.z, xi.x, xi.z), ey = tf_diff(nb.x.y, nb.x.w, xi.y, xi.w);
+        const float px = fmaf(nb.w.x, ex, nb.w.y * ey);
+        const float py = fmaf(nb.w.z, ex, nb.w.w * ey);
+        const float2 tx = two_sum(sx, px), ty = two_sum(sy, py);
+        sx = tx.x;
+        cx += tx.y;
+        sy = ty.x;
+        cy += ty.y;
+      });
   const float fx = sx + cx, fy = sy + cy;
   const float2 fo = a.fs[i];
   const float aox = a.tau2 * fo.x, aoy = a.tau2 * fo.y;

@@ -1,0 +1,39 @@
+// Bond walk with memory-level parallelism.
+//
+// A particle's bonds are walked U slots at a time: the U neighbour indices
+// are loaded first, then the U neighbour gathers are issued (slots that are
+// padding or broken gather the particle itself, a valid address whose data
+// is discarded), then the per-bond bodies run in slot order.  The gathers
+// are the latency-bound part of every pass (dependent index -> data loads
+// from L1/L2); U independent chains per thread keep U times more of them in
+// flight.  The body order is the sequential slot order, so sums are
+// bit-identical to the one-slot-at-a-time loop.
+#pragma once
+#include <cstdint>
+
+namespace pd {
+
+template <int U, typename Gather, typename Body>
+__device__ __forceinline__ void walk_bonds(const int32_t* nbr, int64_t s0, int w, int64_t self, Gather gather,
+                                           Body body) {
+  using G = decltype(gather(0));
+  int k = 0;
+  for (; k + U <= w; k += U) {
+    int j[U];
+#pragma unroll
+    for (int q = 0; q < U; ++q) j[q] = __ldcs(&nbr[s0 + (int64_t)(k + q) * 32]);
+    G g[U];
+#pragma unroll
+    for (int q = 0; q < U; ++q) g[q] = gather(j[q] < 0 ? self : (int64_t)j[q]);
+#pragma unroll
+    for (int q = 0; q < U; ++q)
+      if (j[q] >= 0) body(s0 + (int64_t)(k + q) * 32, j[q], g[q]);
+  }
+  for (; k < w; ++k) {
+    const int64_t s = s0 + (int64_t)k * 32;
+    const int jj = __ldcs(&nbr[s]);
+    if (jj >= 0) body(s, jj, gather((int64_t)jj));
+  }
+}
+
+}  // namespace pd

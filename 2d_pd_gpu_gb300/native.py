@@ -40,6 +40,9 @@ class Params(ctypes.Structure):
         ("det_guard", ctypes.c_double),
         ("k_hg", ctypes.c_double),
         ("damage_fail", ctypes.c_double),
+        ("n1", ctypes.c_double),
+        ("n2", ctypes.c_double),
+        ("weight_len", ctypes.c_double),
         ("singular_policy", ctypes.c_int32),
         ("reserved", ctypes.c_int32),
     ]

@@ -87,9 +87,10 @@ void updatePositions(int ndim, vector<Particle>& localParticles, long double ste
                      vector<vector<long double>>& velocity, vector<vector<long double>>& acce,
                      vector<vector<long double>>& netF);
 // The hot path: net force and velocity-Verlet kick on the GPU (FP64).
-// n1 = n2 = 0 selects the classic model (the only one the GPU path has);
-// other weights throw std::invalid_argument.  acce is left as given (the
-// reference CPU semantics, src/main_seq.cpp:463-466).
+// n1 = n2 = 0 selects the classic model; other weights the reference's
+// bond-associated model (per-bond shape tensors, weight length
+// horizon * dx).  acce is left as given (the reference CPU semantics,
+// src/main_seq.cpp:463-466).
 void computeVelocity(int ndim, double n1, double n2, double horizon, double dx, long double massDensity,
                      matrix& StiffnessTensor, long double stepSize, vector<vector<long double>>& velocity,
                      vector<vector<Particle*>>& Neighborslist, vector<vector<long double>>& acce,

@@ -83,6 +83,12 @@ typedef struct pd_params {
    * stiffness the time step cannot follow; without this the plate workloads
    * diverge once cracks grow (>= 1: never, the reference's semantics). */
   double damage_fail;
+  /* Bond-associated weights of the reference (computeShapeTensors,
+   * src/main_seq.cpp:114-118): w = exp(-n1 |L_b - L_k| / weight_len)
+   * (0.5 + 0.5 cos)^n2 with weight_len = horizon * dx.  n1 = n2 = 0 is the
+   * classic model; otherwise every bond gets its own shape tensor and stress
+   * (FP64 only, families <= 64 bonds, no bond breaking, k_hg = 0). */
+  double n1, n2, weight_len;
   int32_t singular_policy; /* PD_SINGULAR_ZERO / PD_SINGULAR_ERROR */
   int32_t reserved;
 } pd_params;

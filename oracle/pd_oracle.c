@@ -376,13 +376,147 @@ static void pass_b(const pdo_problem* pb, pdo_state* st) {
   }
 }
 
+/* ------------------------------------------------- bond-associated mode
+ * The reference's default model (n1, n2 != 0; src/main_seq.cpp:71-156,
+ * :271-380): every bond b = (i, nb) has its own shape tensors
+ *   K_b = sum_k w(b,k) V_k xi_k (x) xi_k,  N_b = K_b + D_b,
+ *   w(b,k) = exp(-n1 |L_b - L_k| / (horizon dx)) (0.5 + 0.5 cos(b,k))^n2,
+ * its own stress sigma_b (F_b = N_b K_b^-1) and P_b = sigma_b K_b^-1, and
+ *   T_ij = (1/V_h) sum_b w(j,b) V_b P_b xi_ij,   f_i = sum_j (T_ij - T_ji) V_j.
+ * The reference re-derives P_b for every (i, j, b) triple (O(n^3) per
+ * particle); here P_b is formed once per bond and T once per bond (O(n^2)).
+ * No bond breaking or penalty in this mode (the reference has neither). */
+static double ba_weight(const pdo_problem* pb, double bx, double by, double lb, double kx, double ky, double lk) {
+  double c = (bx * kx + by * ky) / (lb * lk);
+  if (c > 1.0) c = 1.0;
+  else if (c < -1.0) c = -1.0;
+  const double lr = fabs(lb - lk) / pb->wlen;
+  return exp(-pb->n1 * lr) * pow(0.5 + 0.5 * c, pb->n2);
+}
+
+static void ba_pass_a(const pdo_problem* pb, pdo_state* st) {
+  double c[3];
+  pdo_stiffness(pb->E, pb->nu, c);
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < pb->n; ++i) {
+    const int64_t r0 = pb->row_ptr[i], n = pb->row_ptr[i + 1] - r0;
+    if (n == 0) continue;
+    double ex[256], ey[256], el[256], vv[256], dx[256], dy[256], P[256][4];
+    if (n > 256) continue; /* caller checks the family size */
+    const double xi = pb->x[2 * i], yi = pb->x[2 * i + 1], ui = st->u[2 * i], wi = st->u[2 * i + 1];
+    double vh = 0.0;
+    for (int64_t k = 0; k < n; ++k) {
+      const int64_t j = pb->col[r0 + k];
+      ex[k] = pb->x[2 * j] - xi;
+      ey[k] = pb->x[2 * j + 1] - yi;
+      el[k] = sqrt(ex[k] * ex[k] + ey[k] * ey[k]);
+      vv[k] = pb->vol[j];
+      dx[k] = st->u[2 * j] - ui;
+      dy[k] = st->u[2 * j + 1] - wi;
+      vh = vh + vv[k];
+    }
+    for (int64_t b = 0; b < n; ++b) {
+      double k11 = 0.0, k12 = 0.0, k22 = 0.0, d11 = 0.0, d12 = 0.0, d21 = 0.0, d22 = 0.0;
+      for (int64_t k = 0; k < n; ++k) {
+        const double wv = ba_weight(pb, ex[b], ey[b], el[b], ex[k], ey[k], el[k]) * vv[k];
+        const double t0 = wv * ex[k], t1 = wv * ey[k];
+        k11 = fma(t0, ex[k], k11);
+        k12 = fma(t0, ey[k], k12);
+        k22 = fma(t1, ey[k], k22);
+        d11 = fma(dx[k], t0, d11);
+        d12 = fma(dx[k], t1, d12);
+        d21 = fma(dy[k], t0, d21);
+        d22 = fma(dy[k], t1, d22);
+      }
+      const double det = fma(k11, k22, -(k12 * k12));
+      if (!(det > pb->det_guard * (k11 * k22))) {
+        P[b][0] = P[b][1] = P[b][2] = P[b][3] = 0.0;
+        continue;
+      }
+      const double r = 1.0 / det;
+      const double q11 = k22 * r, q12 = -k12 * r, q22 = k11 * r;
+      const double g11 = fma(d11, q11, d12 * q12), g12 = fma(d11, q12, d12 * q22);
+      const double g21 = fma(d21, q11, d22 * q12), g22 = fma(d21, q12, d22 * q22);
+      const double e11 = g11, e22 = g22, e12 = 0.5 * (g12 + g21);
+      const double s11 = fma(c[0], e11, c[1] * e22);
+      const double s22 = fma(c[1], e11, c[0] * e22);
+      const double s12 = c[2] * e12;
+      P[b][0] = fma(s11, q11, s12 * q12);
+      P[b][1] = fma(s11, q12, s12 * q22);
+      P[b][2] = fma(s12, q11, s22 * q12);
+      P[b][3] = fma(s12, q12, s22 * q22);
+    }
+    const double rv = 1.0 / vh;
+    for (int64_t jj = 0; jj < n; ++jj) {
+      double m11 = 0.0, m12 = 0.0, m21 = 0.0, m22 = 0.0;
+      for (int64_t b = 0; b < n; ++b) {
+        const double wv = ba_weight(pb, ex[jj], ey[jj], el[jj], ex[b], ey[b], el[b]) * vv[b];
+        m11 = fma(wv, P[b][0], m11);
+        m12 = fma(wv, P[b][1], m12);
+        m21 = fma(wv, P[b][2], m21);
+        m22 = fma(wv, P[b][3], m22);
+      }
+      double* t = st->tb + 2 * (r0 + jj);
+      t[0] = fma(m11 * rv, ex[jj], (m12 * rv) * ey[jj]);
+      t[1] = fma(m21 * rv, ex[jj], (m22 * rv) * ey[jj]);
+    }
+  }
+}
+
+static void ba_pass_b(const pdo_problem* pb, pdo_state* st) {
+  const double dt = pb->dt, inv_rho = 1.0 / pb->rho;
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < pb->n; ++i) {
+    double fx = 0.0, fy = 0.0;
+    for (int64_t s = pb->row_ptr[i]; s < pb->row_ptr[i + 1]; ++s) {
+      const int64_t j = pb->col[s], r = st->rev[s];
+      const double vj = pb->vol[j];
+      fx = fma(st->tb[2 * s] - st->tb[2 * r], vj, fx);
+      fy = fma(st->tb[2 * s + 1] - st->tb[2 * r + 1], vj, fy);
+    }
+    double* f = st->f + 2 * i;
+    double* v = st->v + 2 * i;
+    const double ao0 = f[0] * inv_rho, ao1 = f[1] * inv_rho;
+    const double an0 = fx * inv_rho, an1 = fy * inv_rho;
+    v[0] = v[0] + (0.5 * (ao0 + an0)) * dt;
+    v[1] = v[1] + (0.5 * (ao1 + an1)) * dt;
+    f[0] = fx;
+    f[1] = fy;
+  }
+}
+
+int pdo_reverse_bonds(int64_t n, const int64_t* row_ptr, const int32_t* col, int64_t* rev) {
+  int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad)
+  for (int64_t i = 0; i < n; ++i)
+    for (int64_t s = row_ptr[i]; s < row_ptr[i + 1]; ++s) {
+      const int64_t j = col[s];
+      int64_t lo = row_ptr[j], hi = row_ptr[j + 1], found = -1;
+      while (lo < hi) {
+        const int64_t mid = lo + (hi - lo) / 2;
+        if (col[mid] < i) lo = mid + 1;
+        else if (col[mid] > i) hi = mid;
+        else { found = mid; break; }
+      }
+      rev[s] = found;
+      if (found < 0) bad |= 1;
+    }
+  return bad ? -1 : 0;
+}
+
 int64_t pdo_step(const pdo_problem* pb, pdo_state* st, int32_t nsteps) {
   set_threads(pb->nthreads);
   int64_t nb = 0;
+  const int ba = pb->n1 != 0.0 || pb->n2 != 0.0;
   for (int32_t s = 0; s < nsteps; ++s) {
     drift(pb, st);
-    nb += pass_a(pb, st);
-    pass_b(pb, st);
+    if (ba) {
+      ba_pass_a(pb, st);
+      ba_pass_b(pb, st);
+    } else {
+      nb += pass_a(pb, st);
+      pass_b(pb, st);
+    }
   }
   return nb;
 }

@@ -41,6 +41,8 @@ typedef struct pdo_problem {
   double det_guard;        /* relative det(K) guard, e.g. 1e-10 */
   double k_hg;             /* zero-energy-mode penalty coefficient (0: the reference's model) */
   double damage_fail;      /* a particle with damage > this carries no stress (>= 1: never) */
+  double n1, n2;           /* bond-associated weights (0, 0: classic) */
+  double wlen;             /* length scale of the weight's length ratio (horizon * dx) */
   int32_t nthreads;        /* OpenMP threads, <= 0: runtime default */
 } pdo_problem;
 
@@ -56,6 +58,8 @@ typedef struct pdo_state {
   double* w;          /* [n][4] V_i (S_i - k_hg G_i), S = sigma K^-1, G = F - I */
   double* hg;         /* [n][2] 2 k_hg sum_j V_j (u_j - u_i) */
   uint8_t* singular;  /* [n] 1 if det guard tripped (S_i = 0) */
+  double* tb;         /* [nnz][2] bond-associated force states T_ij (n1, n2 != 0 only) */
+  int64_t* rev;       /* [nnz] family position of the reverse bond (j, i) (n1, n2 != 0 only) */
 } pdo_state;
 
 /* Families within `cutoff` (strict: sqrt(d2) < cutoff, as
@@ -72,6 +76,10 @@ int pdo_init(const pdo_problem* pb, pdo_state* st);
 /* nsteps reference steps (src/main_seq.cpp:686-699 order).  Returns the
  * number of bonds broken during these steps (>= 0). */
 int64_t pdo_step(const pdo_problem* pb, pdo_state* st, int32_t nsteps);
+
+/* rev[s] = family position of bond (j, i) for every bond s = (i, j); the
+ * families must be symmetric (returns -1 otherwise). */
+int pdo_reverse_bonds(int64_t n, const int64_t* row_ptr, const int32_t* col, int64_t* rev);
 
 /* Plane-stress constants exactly as the device receives them:
  * c[0] = C11 = C22, c[1] = C12, c[2] = C33 (src/main_seq.cpp:180-201). */

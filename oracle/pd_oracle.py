@@ -48,6 +48,9 @@ class _Problem(ctypes.Structure):
         ("det_guard", ctypes.c_double),
         ("k_hg", ctypes.c_double),
         ("damage_fail", ctypes.c_double),
+        ("n1", ctypes.c_double),
+        ("n2", ctypes.c_double),
+        ("wlen", ctypes.c_double),
         ("nthreads", ctypes.c_int32),
     ]
 
@@ -65,6 +68,8 @@ class _State(ctypes.Structure):
         ("w", _f64p),
         ("hg", _f64p),
         ("singular", _u8p),
+        ("tb", _f64p),
+        ("rev", _i64p),
     ]
 
 
@@ -84,6 +89,8 @@ def lib():
         L.pdo_init.argtypes = [ctypes.POINTER(_Problem), ctypes.POINTER(_State)]
         L.pdo_step.restype = ctypes.c_int64
         L.pdo_step.argtypes = [ctypes.POINTER(_Problem), ctypes.POINTER(_State), ctypes.c_int32]
+        L.pdo_reverse_bonds.restype = ctypes.c_int
+        L.pdo_reverse_bonds.argtypes = [ctypes.c_int64, _i64p, _i32p, _i64p]
         L.pdo_stiffness.restype = None
         L.pdo_stiffness.argtypes = [ctypes.c_double, ctypes.c_double, _f64p]
         _lib = L
@@ -136,6 +143,9 @@ class OracleSim:
     det_guard: float = 1e-10
     k_hg: float = 0.0
     damage_fail: float = 1.0
+    n1: float = 0.0
+    n2: float = 0.0
+    wlen: float = 1.0
     bc: np.ndarray | None = None
     group_kind: np.ndarray | None = None
     group_val: np.ndarray | None = None
@@ -167,13 +177,20 @@ class OracleSim:
         self.w = np.zeros((n, 4))
         self.singular = np.zeros(n, dtype=np.uint8)
         self.hg = np.zeros((n, 2))
+        self.tb = np.zeros((max(nnz, 1), 2))
+        self.rev = np.zeros(max(nnz, 1), dtype=np.int64)
+        if self.n1 != 0.0 or self.n2 != 0.0:
+            if lib().pdo_reverse_bonds(n, _p(self.row_ptr, _i64p), _p(self.col, _i32p), _p(self.rev, _i64p)) != 0:
+                raise ValueError("bond-associated mode needs symmetric families")
         self._pb = _Problem(n, _p(self.x, _f64p), _p(self.vol, _f64p), _p(self.row_ptr, _i64p),
                             _p(self.col, _i32p), _p(self.bc, _u8p), self.group_kind.size,
                             _p(self.group_kind, _i32p), _p(self.group_val, _f64p), self.E, self.nu, self.rho,
-                            self.dt, self.s_c, self.det_guard, self.k_hg, self.damage_fail, self.nthreads)
+                            self.dt, self.s_c, self.det_guard, self.k_hg, self.damage_fail, self.n1, self.n2,
+                            self.wlen, self.nthreads)
         self._st = _State(_p(self.u, _f64p), _p(self.v, _f64p), _p(self.f, _f64p), _p(self.alive, _u8p),
                           _p(self.broken, _i32p), _p(self.damage, _f64p), _p(self.kinv, _f64p),
-                          _p(self.mt, _f64p), _p(self.w, _f64p), _p(self.hg, _f64p), _p(self.singular, _u8p))
+                          _p(self.mt, _f64p), _p(self.w, _f64p), _p(self.hg, _f64p), _p(self.singular, _u8p),
+                          _p(self.tb, _f64p), _p(self.rev, _i64p))
         lib().pdo_init(ctypes.byref(self._pb), ctypes.byref(self._st))
 
     def step(self, nsteps=1):

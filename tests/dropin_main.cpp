@@ -6,7 +6,7 @@
 //   output/velocity_step_0_after_seq_ref.txt    (storeVelocity, after step 1)
 //   output/LocalParticlesPositions_rank_0step_0.txt
 //   dropin_state.bin: per step int32 step, then u, v, netF as n x 2 doubles
-// Usage: dropin_main <nsteps> <gpu|cpu-semantics 0/1>
+// Usage: dropin_main <nsteps> <gpu-wrapper 0/1> [n1 n2]
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -21,7 +21,7 @@ int main(int argc, char** argv) {
   vector<Particle> allParticles;
   int ndim = 2;
   long double dx = 1.0, horizon = 3.0;
-  double n1 = 0.0, n2 = 0.0;
+  double n1 = argc > 3 ? atof(argv[3]) : 0.0, n2 = argc > 4 ? atof(argv[4]) : 0.0;
   vector<long double> boxlimit(2 * ndim);
   allParticles = readMeshFile(boxlimit, dx);
   findNeighbor(allParticles, dx, horizon, ndim);

@@ -56,6 +56,24 @@ def test_dropin_driver_compiles(pdg, tmp_path):
 
 
 @pytest.mark.gpu
+def test_dropin_reference_default_weights(pdg, hassa, tmp_path):
+    """The reference main's own defaults, n1 = n2 = 10 (bond-associated), one
+    step: the run that produced the reference's shipped golden file."""
+    tmp = str(tmp_path)
+    exe = _build_driver(pdg, tmp)
+    _hassa_mesh(os.path.join(tmp, "2D_Hassa_test_mesh.dat"))
+    subprocess.run([exe, "1", "1", "10", "10"], cwd=tmp, check=True, capture_output=True, timeout=300)
+    b = open(os.path.join(tmp, "dropin_state.bin"), "rb").read()
+    n = struct.unpack_from("<i", b, 0)[0]
+    arr = np.frombuffer(b, "<f8", 6 * n, 8).reshape(3, n, 2)
+    assert normwise(arr[1], hassa["b_v1"]) < V_TOL
+    assert normwise(arr[2], hassa["b_f1"]) < F_TOL
+    txt = open(os.path.join(tmp, "output", "velocity_step_0_after_seq_ref.txt")).read().splitlines()
+    vals = np.array([[float(t) for t in l.split()] for l in txt])
+    assert normwise(vals, hassa["b_v1"]) < 1e-5  # the shipped golden's 6-digit format
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("gpu_wrapper", [0, 1])
 def test_dropin_reference_main_matches_reference(pdg, hassa, tmp_path, gpu_wrapper):
     tmp = str(tmp_path)

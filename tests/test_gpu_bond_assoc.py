@@ -1,0 +1,76 @@
+"""Bond-associated mode (the reference's default n1 = n2 = 10 weights) on the GPU.
+
+Against the reference's own full-precision output of that run (the run whose
+6-digit velocities are the reference's shipped golden file,
+output/velocity_step_0_after_seq_ref.txt -- tests/golden/manifest.json
+pins it), and against the oracle's O(n^2) restatement over several steps.
+exp/pow differ between CUDA and libm by rounding, so GPU vs oracle is
+compared at 1e-12 normwise instead of bit for bit.
+"""
+import numpy as np
+import pytest
+
+from conftest import normwise
+from test_oracle_golden import F_TOL, V_TOL, u_tol
+
+pytestmark = pytest.mark.gpu
+
+
+def _ctx(pdg, h, n1=10.0, n2=10.0):
+    n = h["x"].shape[0]
+    dx, hor, E, nu, rho, dt = h["params"]
+    ctx = pdg.native.Context(pdg.default_params(E=E, nu=nu, rho=rho, dt=dt, s_c=0.0, n1=n1, n2=n2,
+                                                weight_len=hor * dx))
+    ctx.set_particles(h["x"], h["vol"])
+    ctx.build_families(1.01 * dx * hor)
+    g = np.zeros(n, np.uint8)
+    g[h["top"]] = 1
+    g[h["bottom"]] = 2
+    ctx.set_bc([pdg.native.PD_BC_VELOCITY, pdg.native.PD_BC_FIXED], [[0.0, 5.0], [0.0, 0.0]], g)
+    return ctx
+
+
+def test_bond_assoc_matches_reference_default_run(pdg, hassa):
+    ctx = _ctx(pdg, hassa)
+    ctx.step(1)
+    u, v, f = ctx.state()
+    assert normwise(v, hassa["b_v1"]) < V_TOL
+    assert normwise(f, hassa["b_f1"]) < F_TOL
+
+
+def test_bond_assoc_matches_oracle_over_steps(pdg, po, hassa):
+    dx, hor, E, nu, rho, dt = hassa["params"]
+    ctx = _ctx(pdg, hassa, n1=4.0, n2=3.0)
+    n = hassa["x"].shape[0]
+    bc = np.zeros(n, np.uint8)
+    bc[hassa["top"]] = 1
+    bc[hassa["bottom"]] = 2
+    sim = po.OracleSim(hassa["x"], hassa["vol"], hassa["row_ptr"], hassa["col"], E=E, nu=nu, rho=rho, dt=dt, s_c=0.0,
+                       n1=4.0, n2=3.0, wlen=hor * dx, bc=bc,
+                       group_kind=np.array([po.BC_VELOCITY, po.BC_FIXED], np.int32),
+                       group_val=np.array([[0.0, 5.0], [0.0, 0.0]]))
+    ctx.step(4)
+    sim.step(4)
+    u, v, f = ctx.state()
+    assert normwise(u, sim.u) < 1e-12 and normwise(v, sim.v) < 1e-12 and normwise(f, sim.f) < 1e-11
+
+
+def test_bond_assoc_compute_velocity_dropin(pdg, hassa):
+    """pd_compute_velocity in the bond-associated mode after the reference's host drift."""
+    ctx = _ctx(pdg, hassa)
+    n = hassa["x"].shape[0]
+    v = np.zeros((n, 2))
+    v[hassa["top"]] = [0.0, 5.0]
+    u = v * hassa["params"][5]
+    u[hassa["bottom"]] = 0.0
+    acc = np.zeros((n, 2))
+    f = ctx.compute_velocity(u, v, acc)
+    assert normwise(v, hassa["b_v1"]) < V_TOL
+    assert normwise(f, hassa["b_f1"]) < F_TOL
+
+
+def test_bond_assoc_rejects_breaking_and_mixed(pdg):
+    with pytest.raises(pdg.PdError):
+        pdg.native.Context(pdg.default_params(n1=10.0, n2=10.0, weight_len=3.0, s_c=5e-4))
+    with pytest.raises(pdg.PdError):
+        pdg.native.Context(pdg.default_params(n1=10.0, n2=10.0, weight_len=3.0, precision=1))
