@@ -32,6 +32,7 @@ CUDA_UNITS = [
     ("pd_fp64.cu", ["--fmad=false"]),
     ("pd_bondassoc.cu", ["--fmad=false"]),
     ("pd_mixed.cu", []),
+    ("pd_noalloc.cu", ["--fmad=false"]),
     ("pd_probe.cu", []),
     ("pd_api.cu", []),
 ]

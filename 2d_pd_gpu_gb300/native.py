@@ -98,6 +98,8 @@ _SIGS = {
     "pd_step_timed": [_vp, ctypes.c_int32, ctypes.POINTER(ctypes.c_float)],
     "pd_profile_steps": [_vp, ctypes.c_int32, _vp, _vp],
     "pd_model_bytes": [_vp, ctypes.POINTER(ctypes.c_double)],
+    "pd_compute_velocity_noalloc": [ctypes.c_int64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                    ctypes.POINTER(Params), _vp, ctypes.c_char_p, ctypes.c_int],
     "pd_batch_create": [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(_vp)],
     "pd_batch_destroy": [_vp],
     "pd_batch_last_error": [_vp],

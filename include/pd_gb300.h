@@ -186,6 +186,30 @@ int pd_synchronize(pd_ctx* ctx);
  * and breaks bonds as in pd_step when s_c > 0. */
 int pd_compute_velocity(pd_ctx* ctx, const double* u, double* velocity, double* acce, double* netF);
 
+/* One FP64 force + kick, pd_compute_velocity's arithmetic, on CALLER-OWNED
+ * DEVICE buffers and without allocating any device memory.  No counterpart
+ * in the reference: it exists for callers that cannot call cudaMalloc -- a
+ * host application whose own pool owns every device allocation, or a
+ * latency-critical loop where cudaMalloc/cudaFree would synchronise the
+ * device.  All array arguments are device pointers: x[n][2], vol[n], the
+ * CSR families row_ptr[n+1] / col[row_ptr[n]] (every bond intact; no bond
+ * breaking here), u[n][2] (displacement), velocity[n][2] and acce[n][2]
+ * (read and written, as pd_compute_velocity), netF[n][2] (written).  p
+ * gives E, nu, rho, dt, det_guard, k_hg (plane stress).  stream is a cudaStream_t
+ * (NULL: the legacy default stream); the call only enqueues work, so results
+ * are ready once that stream is synchronised.  The per-particle scratch
+ * between its two kernels lives in a static device array sized for
+ * PD_NOALLOC_MAX_PARTICLES particles (4 MiB on every device that loads the
+ * library, until exit): larger n returns PD_ERR_CAPACITY.  Every call
+ * shares that array, so calls that overlap on the GPU race.  The first call
+ * on a device looks up the array's device address (cudaGetSymbolAddress);
+ * make that first call before any stream capture.  errbuf (may be NULL)
+ * receives a message on failure. */
+#define PD_NOALLOC_MAX_PARTICLES 65536
+int pd_compute_velocity_noalloc(int64_t n, const double* x, const double* vol, const int64_t* row_ptr,
+                                const int32_t* col, const double* u, double* velocity, double* acce, double* netF,
+                                const pd_params* p, void* stream, char* errbuf, int errlen);
+
 /* ------------------------------------------------------- batched plates */
 
 /* Many independent plates (contexts) of uneven size stepped together by one
