@@ -45,7 +45,17 @@ __device__ __forceinline__ void tf_add2(float& hi, float& lo, float dh, float dl
   lo = l - (hi - s.x);
 }
 
-__device__ __forceinline__ float tf_diff(float hj, float lj, float hi, float li) { return (hj - hi) + (lj - li); }
+// Packed FP32x2 (Blackwell FFMA2 / FADD2 / FMUL2): the bond math is 2-vector
+// (x, y) work, so one instruction does both components.
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+// (hi_j + lo_j) - (hi_i + lo_i) for two-float 2-vectors {hi.x, hi.y, lo.x, lo.y}
+__device__ __forceinline__ float2 tf_diff2(float4 j, float2 nhi, float2 nlo) {
+  return add2(add2(f2(j.x, j.y), nhi), add2(f2(j.z, j.w), nlo));
+}
 
 __device__ __forceinline__ int64_t slot0(const MixedArgs& a, int64_t i, int* w) {
   const int64_t c = i >> 5;
@@ -135,28 +145,34 @@ __device__ __forceinline__ void pass_a_particle_mixed(const MixedArgs& a, int64_
     float4 u, x;
     float v;
   };
+  const float2 nxh = f2(-xi.x, -xi.y), nxl = f2(-xi.z, -xi.w), nuh = f2(-ui.x, -ui.y), nul = f2(-ui.z, -ui.w);
+  float2 D1 = f2(0.f, 0.f), D2 = f2(0.f, 0.f), A = f2(0.f, 0.f);  // (d11, d12), (d21, d22), (ax, ay)
   walk_bonds<4>(
       a.nbr, s0, w, i, [&](int64_t j) { return Nb{a.us[j], a.xs[j], a.vh[j]}; },
       [&](int64_t s, int j, const Nb& nb) {
-        const float ex = tf_diff(nb.x.x, nb.x.z, xi.x, xi.z), ey = tf_diff(nb.x.y, nb.x.w, xi.y, xi.w);
-        const float dx = tf_diff(nb.u.x, nb.u.z, ui.x, ui.z), dy = tf_diff(nb.u.y, nb.u.w, ui.y, ui.w);
+        const float2 e = tf_diff2(nb.x, nxh, nxl);  // xi^
+        const float2 d = tf_diff2(nb.u, nuh, nul);  // du^
         if (BREAK) {
-          const float q = fmaf(dx, fmaf(2.f, ex, dx), dy * fmaf(2.f, ey, dy));
-          if (q > a.s2 * fmaf(ex, ex, ey * ey)) {
+          const float2 q = mul2(d, fma2(f2(2.f, 2.f), e, d));  // d . (2 xi + d)
+          const float2 ee = mul2(e, e);
+          if (q.x + q.y > a.s2 * (ee.x + ee.y)) {
             a.nbr[s] = -2 - j;
             ++newly;
             return;
           }
         }
-        const float vj = nb.v;
-        const float t0 = vj * ex, t1 = vj * ey;
-        d11 = fmaf(dx, t0, d11);
-        d12 = fmaf(dx, t1, d12);
-        d21 = fmaf(dy, t0, d21);
-        d22 = fmaf(dy, t1, d22);
-        ax = fmaf(vj, dx, ax);
-        ay = fmaf(vj, dy, ay);
+        const float2 vv = f2(nb.v, nb.v);
+        const float2 t = mul2(vv, e);
+        D1 = fma2(f2(d.x, d.x), t, D1);
+        D2 = fma2(f2(d.y, d.y), t, D2);
+        A = fma2(vv, d, A);
       });
+  d11 = D1.x;
+  d12 = D1.y;
+  d21 = D2.x;
+  d22 = D2.y;
+  ax = A.x;
+  ay = A.y;
   a.hgs[i] = make_float2(2.f * a.k_hg * ax, 2.f * a.k_hg * ay);
   if (BREAK && newly) {
     atomicAdd(a.counters + CNT_BROKEN, (unsigned long long)newly);
@@ -177,9 +193,9 @@ __device__ __forceinline__ void pass_a_particle_mixed(const MixedArgs& a, int64_
   const float s11 = fmaf(a.c11, e11, a.c12 * e22);
   const float s22 = fmaf(a.c12, e11, a.c11 * e22);
   const float s12 = a.c33 * e12;
-  const float kh = -a.k_hg;  // W^ = V^ (sigma^ K^-1 - k^ G)
-  a.ws[i] = make_float4(vi * fmaf(kh, g11, fmaf(s11, k11, s12 * k12)), vi * fmaf(kh, g12, fmaf(s11, k12, s12 * k22)),
-                        vi * fmaf(kh, g21, fmaf(s12, k11, s22 * k12)), vi * fmaf(kh, g22, fmaf(s12, k12, s22 * k22)));
+  const float kh = -a.k_hg;  // W^ = V^ (sigma^ K^-1 - k^ G), stored by columns {W11, W21, W12, W22}
+  a.ws[i] = make_float4(vi * fmaf(kh, g11, fmaf(s11, k11, s12 * k12)), vi * fmaf(kh, g21, fmaf(s12, k11, s22 * k12)),
+                        vi * fmaf(kh, g12, fmaf(s11, k12, s12 * k22)), vi * fmaf(kh, g22, fmaf(s12, k12, s22 * k22)));
 }
 
 template <bool BREAK>
@@ -194,25 +210,24 @@ __device__ __forceinline__ void pass_b_particle_mixed(const MixedArgs& a, int64_
   const int64_t s0 = slot0(a, i, &w);
   const float4 wi = a.ws[i], xi = a.xs[i];
   const float2 m = a.mh[i], h = a.hgs[i];
-  // compensated sums (value, correction) per component
-  float sx = fmaf(wi.x, m.x, fmaf(wi.y, m.y, h.x)), cx = 0.f;
-  float sy = fmaf(wi.z, m.x, fmaf(wi.w, m.y, h.y)), cy = 0.f;
+  // W columns c1 = (W11, W21), c2 = (W12, W22): W v = c1 v.x + c2 v.y
+  // compensated (TwoSum) sums S + C of both components at once
+  float2 S = fma2(f2(wi.x, wi.y), f2(m.x, m.x), fma2(f2(wi.z, wi.w), f2(m.y, m.y), h)), C = f2(0.f, 0.f);
+  const float2 nxh = f2(-xi.x, -xi.y), nxl = f2(-xi.z, -xi.w);
   struct Nb {
     float4 x, w;
   };
   walk_bonds<4>(
       a.nbr, s0, w, i, [&](int64_t j) { return Nb{a.xs[j], a.ws[j]}; },
       [&](int64_t, int, const Nb& nb) {
-        const float ex = tf_diff(nb.x.x, nb.x.z, xi.x, xi.z), ey = tf_diff(nb.x.y, nb.x.w, xi.y, xi.w);
-        const float px = fmaf(nb.w.x, ex, nb.w.y * ey);
-        const float py = fmaf(nb.w.z, ex, nb.w.w * ey);
-        const float2 tx = two_sum(sx, px), ty = two_sum(sy, py);
-        sx = tx.x;
-        cx += tx.y;
-        sy = ty.x;
-        cy += ty.y;
+        const float2 e = tf_diff2(nb.x, nxh, nxl);
+        const float2 p = fma2(f2(nb.w.x, nb.w.y), f2(e.x, e.x), mul2(f2(nb.w.z, nb.w.w), f2(e.y, e.y)));
+        const float2 s = add2(S, p);
+        const float2 z = sub2(s, S);
+        C = add2(C, add2(sub2(S, sub2(s, z)), sub2(p, z)));
+        S = s;
       });
-  const float fx = sx + cx, fy = sy + cy;
+  const float fx = S.x + C.x, fy = S.y + C.y;
   const float2 fo = a.fs[i];
   const float aox = a.tau2 * fo.x, aoy = a.tau2 * fo.y;
   const float anx = a.tau2 * fx, any = a.tau2 * fy;
