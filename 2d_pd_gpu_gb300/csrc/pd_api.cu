@@ -133,6 +133,7 @@ void free_families(pd_ctx* c) {
   dfree(c->sell.chunk_base);
   dfree(c->sell.chunk_w);
   dfree(c->sell.nbr);
+  dfree(c->sell.chunk_order);
   dfree(c->bxi);
   dfree(c->bgeo);
   dfree(c->blim);
@@ -250,6 +251,7 @@ pd::MixedArgs mixed_args(pd_ctx* c) {
   a.bc = c->bc; a.gkind = c->gkind; a.gvel = c->gvel;
   a.broken = c->broken; a.damage = c->damage; a.singular = c->singular; a.fam = c->fam;
   a.chunk_base = c->sell.chunk_base; a.chunk_w = c->sell.chunk_w; a.nbr = c->sell.nbr;
+  a.chunk_order = c->sell.chunk_order;
   double c11, c12, c33;
   stiffness(c, &c11, &c12, &c33);
   const double es = c11 != 0.0 ? c11 : 1.0;
@@ -267,6 +269,7 @@ pd::MixedArgs mixed_args(pd_ctx* c) {
   a.damage_fail = c->p.damage_fail;
   a.counters = c->counters;
   a.brk = c->p.s_c > 0.0;
+  a.wmax = c->max_family;
   return a;
 }
 
@@ -292,6 +295,73 @@ __global__ void k_fam_from_rowptr(int64_t n, const int64_t* rp, int32_t* fam) {
 }
 
 // After row_ptr/col exist: SELL layout, bond geometry, per-particle geometry, reset.
+// Visiting order of the SELL-32 chunks for the mixed passes.  A chunk is
+// 32 consecutive particles; for the usual row-major numbering it is a short
+// row segment (long axis along x).  Chunks are ordered by (band, column,
+// row) on a grid whose cells are the median chunk extent along the long axis
+// and along the short axis, with bands of 8 cells across: the 8 warps of a
+// 256-thread block then run 8 chunks stacked across their long axis (32
+// columns x 8 rows of a row-major plate), so the block's neighbour gathers
+// touch about half as many distinct particles as 8 consecutive chunks would
+// and mostly hit L1.  The particle order, and with it every array the API
+// exposes, is unchanged.
+std::vector<int32_t> chunk_visit_order(const std::vector<double>& x, int64_t n, double min_cell) {
+  const int64_t nch = (n + 31) / 32;
+  std::vector<int32_t> order((size_t)nch);
+  for (int64_t k = 0; k < nch; ++k) order[(size_t)k] = (int32_t)k;
+  if (nch <= 1) return order;
+  std::vector<double> cx((size_t)nch), cy((size_t)nch), ex((size_t)nch), ey((size_t)nch);
+  for (int64_t ch = 0; ch < nch; ++ch) {
+    const int64_t a = ch * 32, b = std::min(n, a + 32);
+    double sx = 0.0, sy = 0.0, x0 = INFINITY, x1 = -INFINITY, y0 = INFINITY, y1 = -INFINITY;
+    for (int64_t i = a; i < b; ++i) {
+      const double px = x[2 * i], py = x[2 * i + 1];
+      sx += px;
+      sy += py;
+      x0 = std::min(x0, px);
+      x1 = std::max(x1, px);
+      y0 = std::min(y0, py);
+      y1 = std::max(y1, py);
+    }
+    cx[(size_t)ch] = sx / (double)(b - a);
+    cy[(size_t)ch] = sy / (double)(b - a);
+    ex[(size_t)ch] = x1 - x0;
+    ey[(size_t)ch] = y1 - y0;
+  }
+  auto median = [](std::vector<double> v) {
+    std::nth_element(v.begin(), v.begin() + v.size() / 2, v.end());
+    return v[v.size() / 2];
+  };
+  const double mx = std::max(median(ex), min_cell), my = std::max(median(ey), min_cell);
+  const bool long_x = mx >= my;  // chunks are stacked across their long axis
+  const double ql = long_x ? mx : my, qs = long_x ? my : mx;
+  double lo_l = INFINITY, lo_s = INFINITY;
+  for (int64_t ch = 0; ch < nch; ++ch) {
+    lo_l = std::min(lo_l, long_x ? cx[(size_t)ch] : cy[(size_t)ch]);
+    lo_s = std::min(lo_s, long_x ? cy[(size_t)ch] : cx[(size_t)ch]);
+  }
+  struct Key {
+    int64_t band, col, row;
+    int32_t ch;
+    bool operator<(const Key& o) const {
+      if (band != o.band) return band < o.band;
+      if (col != o.col) return col < o.col;
+      if (row != o.row) return row < o.row;
+      return ch < o.ch;
+    }
+  };
+  std::vector<Key> key((size_t)nch);
+  for (int64_t ch = 0; ch < nch; ++ch) {
+    const double l = ((long_x ? cx[(size_t)ch] : cy[(size_t)ch]) - lo_l) / ql;
+    const double t = ((long_x ? cy[(size_t)ch] : cx[(size_t)ch]) - lo_s) / qs;
+    const int64_t row = (int64_t)std::floor(t);
+    key[(size_t)ch] = {row >> 3, (int64_t)std::floor(l), row, (int32_t)ch};
+  }
+  std::sort(key.begin(), key.end());
+  for (int64_t k = 0; k < nch; ++k) order[(size_t)k] = key[(size_t)k].ch;
+  return order;
+}
+
 int finish_families(pd_ctx* c) {
   cudaStream_t s = c->stream;
   std::string msg;
@@ -332,6 +402,10 @@ int finish_families(pd_ctx* c) {
     for (double v : c->h_vol) vsum += v;
     c->ls = ls;
     c->vs_scale = c->n > 0 ? vsum / (double)c->n : 1.0;
+    const std::vector<int32_t> order = chunk_visit_order(c->h_x, c->n, ls / 3.0);
+    PD_CK(c, cudaMalloc(&c->sell.chunk_order, (order.empty() ? 1 : order.size()) * sizeof(int32_t)));
+    if (!order.empty())
+      PD_CK(c, cudaMemcpy(c->sell.chunk_order, order.data(), order.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
     int rc2 = upload_gvel(c);
     if (rc2 != PD_OK) return rc2;
   }
@@ -824,6 +898,10 @@ int pd_synchronize(pd_ctx* c) {
   if (!c) return PD_ERR_ARG;
   PD_CK(c, cudaSetDevice(c->p.device));
   PD_CK(c, cudaStreamSynchronize(c->stream));
+  if (!c->counters) return PD_OK;
+  unsigned long long err = 0;
+  PD_CK(c, cudaMemcpy(&err, c->counters + pd::CNT_ERROR, sizeof(err), cudaMemcpyDeviceToHost));
+  if (err & pd::ERR_STAGE_TIMEOUT) return fail(c, PD_ERR_TIMEOUT, "a bounded wait for a staged bond-index copy gave up");
   return PD_OK;
 }
 

@@ -218,9 +218,9 @@ __device__ __forceinline__ void pass_b_particle(const Fp64Args& a, int64_t i) {
     double2 a, b;
   };
   walk_bonds<4>(
-      a.nbr, s0, w, i, [&](int64_t j) { return Nb{a.w01[j], a.w23[j]}; },
-      [&](int64_t s, int, const Nb& nb) {
-        const double2 e = __ldcs(&a.bxi[s]);
+      w, i, GlobalIdx{a.nbr, s0}, [&](int64_t j) { return Nb{a.w01[j], a.w23[j]}; },
+      [&](int k, int, const Nb& nb) {
+        const double2 e = __ldcs(&a.bxi[s0 + (int64_t)k * kChunk]);
         fx = fma(nb.a.x, e.x, fx);
         fx = fma(nb.a.y, e.y, fx);
         fy = fma(nb.b.x, e.x, fy);

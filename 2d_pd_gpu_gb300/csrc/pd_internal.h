@@ -33,7 +33,7 @@ constexpr int kBlock = 256;
 // Counters word layout (device int64 array).
 enum { CNT_BROKEN = 0, CNT_SINGULAR = 1, CNT_ERROR = 2, CNT_N = 4 };
 // Device error bits (CNT_ERROR).
-enum { ERR_FAMILY_OVERFLOW = 1, ERR_BAD_NEIGHBOR = 2, ERR_SELF_BOND = 4, ERR_ASYMMETRIC = 8 };
+enum { ERR_FAMILY_OVERFLOW = 1, ERR_BAD_NEIGHBOR = 2, ERR_SELF_BOND = 4, ERR_ASYMMETRIC = 8, ERR_STAGE_TIMEOUT = 16 };
 
 struct Fp64Args {
   int64_t n;
@@ -102,13 +102,14 @@ struct MixedArgs {
   const int64_t* __restrict__ chunk_base;
   const int32_t* __restrict__ chunk_w;
   int32_t* nbr;
+  const int32_t* __restrict__ chunk_order;  // warp w of a pass runs chunk chunk_order[w]
   float c11, c12, c33;  // C / Es
   float s2, tau2;       // stretch limit factor, Es dt^2 / (rho Ls^2)
   float k_hg;           // k Vs Ls^2 / Es
   double inv_ls, inv_vs, v_scale, f_scale, det_guard, damage_fail;
   unsigned long long* counters;
   int32_t brk;  // bond breaking on (s_c > 0)
-  int32_t pad;
+  int32_t wmax;  // widest SELL chunk (slot rows), sizes the staged passes' shared memory
 };
 
 // ---- family build (pd_family.cu)
@@ -126,6 +127,7 @@ struct SellLayout {
   int64_t* chunk_base = nullptr;
   int32_t* chunk_w = nullptr;
   int32_t* nbr = nullptr;
+  int32_t* chunk_order = nullptr;  // mixed form: chunks in visiting order (spatially compact blocks)
 };
 int build_sell(int64_t n, const int64_t* d_row_ptr, const int32_t* d_col, cudaStream_t s, SellLayout* out,
                unsigned long long* d_counters, std::string* msg);

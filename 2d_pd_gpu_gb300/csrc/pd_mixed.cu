@@ -16,6 +16,7 @@
 // products.  Nothing here is bit-identical to the FP64 form; its error is
 // measured against it (tests/test_gpu_mixed.py, bench.py).
 #include "pd_internal.h"
+#include "pd_stage.cuh"
 #include "pd_walk.cuh"
 
 namespace pd {
@@ -134,10 +135,9 @@ __global__ void __launch_bounds__(kBlock) k_drift_mixed(MixedArgs a) {
   if (i < a.n) drift_particle_mixed(a, i);
 }
 
-template <bool BREAK>
-__device__ __forceinline__ void pass_a_particle_mixed(const MixedArgs& a, int64_t i) {
-  int w;
-  const int64_t s0 = slot0(a, i, &w);
+// Pass A of particle i: slots s0 + 32 k, k < w, indices read through idx.
+template <bool BREAK, typename Idx>
+__device__ __forceinline__ void pass_a_particle_mixed(const MixedArgs& a, int64_t i, int w, int64_t s0, Idx idx) {
   const float4 ui = a.us[i], xi = a.xs[i];
   float d11 = 0.f, d12 = 0.f, d21 = 0.f, d22 = 0.f, ax = 0.f, ay = 0.f;
   int newly = 0;
@@ -148,15 +148,15 @@ __device__ __forceinline__ void pass_a_particle_mixed(const MixedArgs& a, int64_
   const float2 nxh = f2(-xi.x, -xi.y), nxl = f2(-xi.z, -xi.w), nuh = f2(-ui.x, -ui.y), nul = f2(-ui.z, -ui.w);
   float2 D1 = f2(0.f, 0.f), D2 = f2(0.f, 0.f), A = f2(0.f, 0.f);  // (d11, d12), (d21, d22), (ax, ay)
   walk_bonds<4>(
-      a.nbr, s0, w, i, [&](int64_t j) { return Nb{a.us[j], a.xs[j], a.vh[j]}; },
-      [&](int64_t s, int j, const Nb& nb) {
+      w, i, idx, [&](int64_t j) { return Nb{a.us[j], a.xs[j], a.vh[j]}; },
+      [&](int k, int j, const Nb& nb) {
         const float2 e = tf_diff2(nb.x, nxh, nxl);  // xi^
         const float2 d = tf_diff2(nb.u, nuh, nul);  // du^
         if (BREAK) {
           const float2 q = mul2(d, fma2(f2(2.f, 2.f), e, d));  // d . (2 xi + d)
           const float2 ee = mul2(e, e);
           if (q.x + q.y > a.s2 * (ee.x + ee.y)) {
-            a.nbr[s] = -2 - j;
+            a.nbr[s0 + (int64_t)k * kChunk] = -2 - j;
             ++newly;
             return;
           }
@@ -199,15 +199,48 @@ __device__ __forceinline__ void pass_a_particle_mixed(const MixedArgs& a, int64_
 }
 
 template <bool BREAK>
-__global__ void __launch_bounds__(kBlock) k_pass_a_mixed(MixedArgs a) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < a.n) pass_a_particle_mixed<BREAK>(a, i);
-}
-
-template <bool DRIFT>
-__device__ __forceinline__ void pass_b_particle_mixed(const MixedArgs& a, int64_t i) {
+__device__ __forceinline__ void pass_a_particle_mixed(const MixedArgs& a, int64_t i) {
   int w;
   const int64_t s0 = slot0(a, i, &w);
+  pass_a_particle_mixed<BREAK>(a, i, w, s0, GlobalIdx{a.nbr, s0});
+}
+
+// Picks the calling warp's chunk (visiting order: the 8 warps of a block run
+// chunks that are neighbours in space, so their gathers share L1) and stages
+// its indices in shared memory (pd_stage.cuh).  Returns the chunk width, or
+// -1 when the warp has nothing to do or its copy timed out (error word set).
+__device__ __forceinline__ int stage_warp(const MixedArgs& a, int32_t* stage, uint64_t* bars, int64_t* base,
+                                          int64_t* chunk) {
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if ((gw << 5) >= a.n) return -1;  // warp-uniform
+  const int64_t c = a.chunk_order[gw];
+  *chunk = c;
+  const int warp = threadIdx.x >> 5;
+  const int w = a.chunk_w[c];
+  *base = a.chunk_base[c];
+  if (!stage_chunk(stage + (int64_t)warp * a.wmax * 32, a.nbr + *base, w, &bars[warp])) {
+    if ((threadIdx.x & 31) == 0) atomicOr(a.counters + CNT_ERROR, (unsigned long long)ERR_STAGE_TIMEOUT);
+    return -1;
+  }
+  return w;
+}
+
+template <bool BREAK>
+__global__ void __launch_bounds__(kBlock) k_pass_a_mixed(MixedArgs a) {
+  extern __shared__ __align__(128) int32_t stage[];
+  __shared__ uint64_t bars[kBlock / 32];
+  int64_t base, chunk;
+  const int w = stage_warp(a, stage, bars, &base, &chunk);
+  if (w < 0) return;
+  const int lane = threadIdx.x & 31;
+  const int64_t i = chunk * 32 + lane;
+  if (i >= a.n) return;
+  pass_a_particle_mixed<BREAK>(a, i, w, base + lane, SharedIdx{stage + (threadIdx.x >> 5) * a.wmax * 32, lane});
+}
+
+// Pass B of particle i: slots s0 + 32 k, k < w, indices read through idx.
+template <bool DRIFT, typename Idx>
+__device__ __forceinline__ void pass_b_particle_mixed(const MixedArgs& a, int64_t i, int w, Idx idx) {
   const float4 wi = a.ws[i], xi = a.xs[i];
   const float2 m = a.mh[i], h = a.hgs[i];
   // W columns c1 = (W11, W21), c2 = (W12, W22): W v = c1 v.x + c2 v.y
@@ -218,8 +251,8 @@ __device__ __forceinline__ void pass_b_particle_mixed(const MixedArgs& a, int64_
     float4 x, w;
   };
   walk_bonds<4>(
-      a.nbr, s0, w, i, [&](int64_t j) { return Nb{a.xs[j], a.ws[j]}; },
-      [&](int64_t, int, const Nb& nb) {
+      w, i, idx, [&](int64_t j) { return Nb{a.xs[j], a.ws[j]}; },
+      [&](int, int, const Nb& nb) {
         const float2 e = tf_diff2(nb.x, nxh, nxl);
         const float2 p = fma2(f2(nb.w.x, nb.w.y), f2(e.x, e.x), mul2(f2(nb.w.z, nb.w.w), f2(e.y, e.y)));
         const float2 s = add2(S, p);
@@ -244,10 +277,27 @@ __device__ __forceinline__ void pass_b_particle_mixed(const MixedArgs& a, int64_
 }
 
 template <bool DRIFT>
-__global__ void __launch_bounds__(kBlock) k_pass_b_mixed(MixedArgs a) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < a.n) pass_b_particle_mixed<DRIFT>(a, i);
+__device__ __forceinline__ void pass_b_particle_mixed(const MixedArgs& a, int64_t i) {
+  int w;
+  const int64_t s0 = slot0(a, i, &w);
+  pass_b_particle_mixed<DRIFT>(a, i, w, GlobalIdx{a.nbr, s0});
 }
+
+template <bool DRIFT>
+__global__ void __launch_bounds__(kBlock) k_pass_b_mixed(MixedArgs a) {
+  extern __shared__ __align__(128) int32_t stage[];
+  __shared__ uint64_t bars[kBlock / 32];
+  int64_t base, chunk;
+  const int w = stage_warp(a, stage, bars, &base, &chunk);
+  if (w < 0) return;
+  const int lane = threadIdx.x & 31;
+  const int64_t i = chunk * 32 + lane;
+  if (i >= a.n) return;
+  pass_b_particle_mixed<DRIFT>(a, i, w, SharedIdx{stage + (threadIdx.x >> 5) * a.wmax * 32, lane});
+}
+
+// Dynamic shared memory of the staged passes: one chunk of wmax slot rows per warp.
+inline size_t stage_bytes(const MixedArgs& a) { return (size_t)(kBlock / 32) * (size_t)a.wmax * 128u; }
 
 // ---- batched plates (see pd_batch.cuh): phase 0 drift, 1 pass A, 2 pass B + drift, 3 pass B
 __device__ __forceinline__ void batch_particle_mixed(const MixedArgs& p, int64_t i, int phase) {
@@ -386,6 +436,12 @@ cudaError_t launch_batch_mixed(const MixedArgs* d_plates, const BatchTile* d_til
 
 void launch_init_geometry_mixed(const MixedArgs& a, cudaStream_t s) {
   if (a.n <= 0) return;
+  // the staged passes may take up to 8 warps x PD_MAX_FAMILY rows x 128 B of dynamic shared memory
+  const int mx = (kBlock / 32) * PD_MAX_FAMILY * 128;
+  cudaFuncSetAttribute(k_pass_a_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_pass_a_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_pass_b_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_pass_b_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   k_positions_mixed<<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
   k_init_geometry_mixed<<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
 }
@@ -396,18 +452,20 @@ void launch_drift_mixed(const MixedArgs& a, cudaStream_t s) {
 
 void launch_pass_a_mixed(const MixedArgs& a, bool breaking, cudaStream_t s) {
   if (a.n <= 0) return;
+  const size_t sm = stage_bytes(a);
   if (breaking)
-    k_pass_a_mixed<true><<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
+    k_pass_a_mixed<true><<<(unsigned)blocks_for(a.n), kBlock, sm, s>>>(a);
   else
-    k_pass_a_mixed<false><<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
+    k_pass_a_mixed<false><<<(unsigned)blocks_for(a.n), kBlock, sm, s>>>(a);
 }
 
 void launch_pass_b_mixed(const MixedArgs& a, bool drift, cudaStream_t s) {
   if (a.n <= 0) return;
+  const size_t sm = stage_bytes(a);
   if (drift)
-    k_pass_b_mixed<true><<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
+    k_pass_b_mixed<true><<<(unsigned)blocks_for(a.n), kBlock, sm, s>>>(a);
   else
-    k_pass_b_mixed<false><<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
+    k_pass_b_mixed<false><<<(unsigned)blocks_for(a.n), kBlock, sm, s>>>(a);
 }
 
 void launch_to_mixed(const MixedArgs& a, const double2* u, const double2* v, const double2* f, cudaStream_t s) {

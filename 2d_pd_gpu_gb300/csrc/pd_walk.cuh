@@ -8,32 +8,41 @@
 // from L1/L2); U independent chains per thread keep U times more of them in
 // flight.  The body order is the sequential slot order, so sums are
 // bit-identical to the one-slot-at-a-time loop.
+//
+// idx(k) returns the neighbour index of the particle's slot k (from global
+// memory or from a staged shared-memory copy); body(k, j, g) gets the slot
+// number k, the index j >= 0 and the gathered data.
 #pragma once
 #include <cstdint>
 
 namespace pd {
 
-template <int U, typename Gather, typename Body>
-__device__ __forceinline__ void walk_bonds(const int32_t* nbr, int64_t s0, int w, int64_t self, Gather gather,
-                                           Body body) {
+template <int U, typename Idx, typename Gather, typename Body>
+__device__ __forceinline__ void walk_bonds(int w, int64_t self, Idx idx, Gather gather, Body body) {
   using G = decltype(gather(0));
   int k = 0;
   for (; k + U <= w; k += U) {
     int j[U];
 #pragma unroll
-    for (int q = 0; q < U; ++q) j[q] = __ldcs(&nbr[s0 + (int64_t)(k + q) * 32]);
+    for (int q = 0; q < U; ++q) j[q] = idx(k + q);
     G g[U];
 #pragma unroll
     for (int q = 0; q < U; ++q) g[q] = gather(j[q] < 0 ? self : (int64_t)j[q]);
 #pragma unroll
     for (int q = 0; q < U; ++q)
-      if (j[q] >= 0) body(s0 + (int64_t)(k + q) * 32, j[q], g[q]);
+      if (j[q] >= 0) body(k + q, j[q], g[q]);
   }
   for (; k < w; ++k) {
-    const int64_t s = s0 + (int64_t)k * 32;
-    const int jj = __ldcs(&nbr[s]);
-    if (jj >= 0) body(s, jj, gather((int64_t)jj));
+    const int jj = idx(k);
+    if (jj >= 0) body(k, jj, gather((int64_t)jj));
   }
 }
+
+// Streaming (evict-first) load of global slot s0 + 32 k of a SELL-32 row.
+struct GlobalIdx {
+  const int32_t* nbr;
+  int64_t s0;
+  __device__ __forceinline__ int operator()(int k) const { return __ldcs(&nbr[s0 + (int64_t)k * 32]); }
+};
 
 }  // namespace pd

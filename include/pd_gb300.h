@@ -175,6 +175,9 @@ int pd_get_counters(pd_ctx* ctx, pd_counters* c);
  * src/main_seq.cpp:686-699 (applyVelocityBC, updatePositions, applyFixedBC,
  * computeVelocity).  Asynchronous unless an error check needs the host. */
 int pd_step(pd_ctx* ctx, int32_t nsteps);
+/* Waits for the context's stream.  PD_ERR_TIMEOUT if a bounded device wait
+ * (the bulk copy that stages bond indices in shared memory) gave up since the
+ * last pd_reset; the state is then not trustworthy. */
 int pd_synchronize(pd_ctx* ctx);
 
 /* One force + kick with host buffers, the reference GPU wrapper's contract
