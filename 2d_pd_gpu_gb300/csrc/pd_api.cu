@@ -47,6 +47,7 @@ struct pd_ctx {
   int64_t* row_ptr = nullptr;
   int32_t* col = nullptr;
   pd::SellLayout sell;
+  pd::HaloLayout halo;  // mixed form
   double2 *bxi = nullptr, *bgeo = nullptr;
   double* blim = nullptr;
   float* br2 = nullptr;
@@ -134,6 +135,12 @@ void free_families(pd_ctx* c) {
   dfree(c->sell.chunk_w);
   dfree(c->sell.nbr);
   dfree(c->sell.chunk_order);
+  dfree(c->halo.visit);
+  dfree(c->halo.loc);
+  dfree(c->halo.loc0);
+  dfree(c->halo.halo);
+  dfree(c->halo.halo_n);
+  c->halo = pd::HaloLayout{};
   dfree(c->bxi);
   dfree(c->bgeo);
   dfree(c->blim);
@@ -252,6 +259,12 @@ pd::MixedArgs mixed_args(pd_ctx* c) {
   a.broken = c->broken; a.damage = c->damage; a.singular = c->singular; a.fam = c->fam;
   a.chunk_base = c->sell.chunk_base; a.chunk_w = c->sell.chunk_w; a.nbr = c->sell.nbr;
   a.chunk_order = c->sell.chunk_order;
+  a.visit = c->halo.visit;
+  a.loc = c->halo.loc;
+  a.halo = c->halo.halo;
+  a.halo_n = c->halo.halo_n;
+  a.halo_cap = pd::kHaloCap;
+  a.halo_max = c->halo.halo_max;
   double c11, c12, c33;
   stiffness(c, &c11, &c12, &c33);
   const double es = c11 != 0.0 ? c11 : 1.0;
@@ -406,6 +419,8 @@ int finish_families(pd_ctx* c) {
     PD_CK(c, cudaMalloc(&c->sell.chunk_order, (order.empty() ? 1 : order.size()) * sizeof(int32_t)));
     if (!order.empty())
       PD_CK(c, cudaMemcpy(c->sell.chunk_order, order.data(), order.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    const int rch = pd::build_halo_mixed(mixed_args(c), c->sell.nslots, s, &c->halo, &msg);
+    if (rch != PD_OK) return fail(c, rch, msg);
     int rc2 = upload_gvel(c);
     if (rc2 != PD_OK) return rc2;
   }
@@ -708,6 +723,7 @@ int pd_reset(pd_ctx* c) {
   PD_CK(c, cudaMemsetAsync(c->counters, 0, pd::CNT_N * sizeof(unsigned long long), s));
   pd::launch_sell_reset(c->n, c->row_ptr, c->col, c->sell, s);
   if (mixed(c)) {
+    pd::launch_halo_relink(c->sell.nslots, c->sell.nbr, c->halo, s);
     PD_CK(c, cudaMemsetAsync(c->us, 0, nn * sizeof(float4), s));
     PD_CK(c, cudaMemsetAsync(c->vsm, 0, nn * sizeof(float4), s));
     PD_CK(c, cudaMemsetAsync(c->ws, 0, nn * sizeof(float4), s));

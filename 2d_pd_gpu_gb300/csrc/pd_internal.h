@@ -29,6 +29,10 @@ namespace pd {
 
 constexpr int kChunk = 32;
 constexpr int kBlock = 256;
+// Halo staging of the mixed passes: a block stages at most kHaloCap
+// particles whose ids span at most 32 * kHaloSpanWords.
+constexpr int kHaloCap = 2048;
+constexpr int kHaloSpanWords = 2048;
 
 // Counters word layout (device int64 array).
 enum { CNT_BROKEN = 0, CNT_SINGULAR = 1, CNT_ERROR = 2, CNT_N = 4 };
@@ -78,6 +82,12 @@ struct BondAssoc {
   int64_t* rslot;  // slot of the reverse bond (j, i)
 };
 
+// Chunk a warp runs in the mixed single-plate passes, in visiting order.
+struct alignas(16) VisitRec {
+  int32_t chunk, w;  // chunk id, width (slot rows)
+  int64_t base;      // first slot
+};
+
 // Mixed form (pd_mixed.cu): scaled two-float state, FP32 bond arithmetic.
 struct MixedArgs {
   int64_t n;
@@ -103,6 +113,11 @@ struct MixedArgs {
   const int32_t* __restrict__ chunk_w;
   int32_t* nbr;
   const int32_t* __restrict__ chunk_order;  // warp w of a pass runs chunk chunk_order[w]
+  const VisitRec* __restrict__ visit;       // the same, with the chunk's width and first slot
+  uint16_t* loc;                            // per slot: position in the block's halo (0xFFFF: padding / broken)
+  const int32_t* __restrict__ halo;         // per block: halo particle ids (halo_cap entries per block)
+  const int32_t* __restrict__ halo_n;       // per block: halo size, -1 = not staged
+  int32_t halo_cap, halo_max;               // halo_max: largest halo (multiple of 8), sizes shared memory
   float c11, c12, c33;  // C / Es
   float s2, tau2;       // stretch limit factor, Es dt^2 / (rho Ls^2)
   float k_hg;           // k Vs Ls^2 / Es
@@ -161,6 +176,18 @@ void launch_ba_pass_b(const Fp64Args& a, const BondAssoc& b, int mode, cudaStrea
 
 // ---- mixed step (pd_mixed.cu)
 void launch_init_geometry_mixed(const MixedArgs& a, cudaStream_t s);
+// per-block halos of the single-plate passes (needs chunk_order, SELL)
+struct HaloLayout {
+  int64_t nblocks = 0, staged = 0;
+  VisitRec* visit = nullptr;
+  uint16_t* loc = nullptr;   // live 16-bit indices
+  uint16_t* loc0 = nullptr;  // pristine (all bonds intact)
+  int32_t* halo = nullptr;
+  int32_t* halo_n = nullptr;
+  int32_t halo_max = 0;
+};
+int build_halo_mixed(const MixedArgs& a, int64_t nslots, cudaStream_t s, HaloLayout* out, std::string* msg);
+void launch_halo_relink(int64_t nslots, const int32_t* nbr, const HaloLayout& h, cudaStream_t s);
 void launch_drift_mixed(const MixedArgs& a, cudaStream_t s);
 void launch_pass_a_mixed(const MixedArgs& a, bool breaking, cudaStream_t s);
 void launch_pass_b_mixed(const MixedArgs& a, bool drift, cudaStream_t s);

@@ -15,6 +15,9 @@
 // |u| >> |u_j - u_i|.  The FP64 K^-1 is rounded to FP32 for the per-step
 // products.  Nothing here is bit-identical to the FP64 form; its error is
 // measured against it (tests/test_gpu_mixed.py, bench.py).
+#include <climits>
+#include <vector>
+
 #include "pd_internal.h"
 #include "pd_stage.cuh"
 #include "pd_walk.cuh"
@@ -109,6 +112,31 @@ __global__ void __launch_bounds__(kBlock) k_init_geometry_mixed(MixedArgs a) {
 }
 
 // BC + drift of particle i in scaled per-step units; an = a^ of the new force.
+// BC group of a particle, resolved (kind, prescribed v^).
+struct BcOf {
+  int kind;
+  float4 gv;
+};
+
+__device__ __forceinline__ BcOf resolve_bc(const MixedArgs& a, int g) {
+  BcOf b{PD_BC_NONE, make_float4(0.f, 0.f, 0.f, 0.f)};
+  if (g) {
+    b.kind = a.gkind[g - 1];
+    if (b.kind == PD_BC_VELOCITY) b.gv = a.gvel[g - 1];
+  }
+  return b;
+}
+
+__device__ __forceinline__ void drift_bc(const BcOf& b, float4& v, float4& u, float anx, float any) {
+  if (b.kind == PD_BC_VELOCITY) v = b.gv;
+  // u += v + a/2   (v two-float, a/2 FP32)
+  tf_add2(u.x, u.z, v.x, v.z);
+  tf_add2(u.y, u.w, v.y, v.w);
+  tf_add(u.x, u.z, 0.5f * anx);
+  tf_add(u.y, u.w, 0.5f * any);
+  if (b.kind == PD_BC_FIXED) u = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
 __device__ __forceinline__ void drift_mixed(const MixedArgs& a, int64_t i, float4& v, float4& u, float anx,
                                             float any) {
   const int g = a.bc[i];
@@ -135,57 +163,72 @@ __global__ void __launch_bounds__(kBlock) k_drift_mixed(MixedArgs a) {
   if (i < a.n) drift_particle_mixed(a, i);
 }
 
-// Pass A of particle i: slots s0 + 32 k, k < w, indices read through idx.
-template <bool BREAK, typename Idx>
-__device__ __forceinline__ void pass_a_particle_mixed(const MixedArgs& a, int64_t i, int w, int64_t s0, Idx idx) {
-  const float4 ui = a.us[i], xi = a.xs[i];
-  float d11 = 0.f, d12 = 0.f, d21 = 0.f, d22 = 0.f, ax = 0.f, ay = 0.f;
+// Neighbour data gathered by the two passes.
+struct NbA {
+  float4 u, x;
+  float v;
+};
+struct NbB {
+  float4 x, w;
+};
+
+// Pass A of particle i: slots s0 + 32 k, k < w; idx(k) gives a slot's
+// neighbour (-1: padding or broken), gather(j) its data, gid(j) its particle
+// id (j is a particle id, or a halo position when the data is staged).
+// Per-particle inputs of pass A, loaded ahead of the bond walk.
+struct PreA {
+  float4 ui, xi, geo;
+  int singular;
+};
+
+__device__ __forceinline__ PreA load_a(const MixedArgs& a, int64_t i) {
+  return PreA{a.us[i], a.xs[i], a.geo[i], a.singular[i]};
+}
+
+template <bool BREAK, typename Idx, typename Gather, typename Gid>
+__device__ __forceinline__ void pass_a_core(const MixedArgs& a, int64_t i, const PreA& pre, int w, int64_t s0, Idx idx,
+                                            Gather gather, Gid gid) {
+  const float4 ui = pre.ui, xi = pre.xi;
   int newly = 0;
-  struct Nb {
-    float4 u, x;
-    float v;
-  };
   const float2 nxh = f2(-xi.x, -xi.y), nxl = f2(-xi.z, -xi.w), nuh = f2(-ui.x, -ui.y), nul = f2(-ui.z, -ui.w);
   float2 D1 = f2(0.f, 0.f), D2 = f2(0.f, 0.f), A = f2(0.f, 0.f);  // (d11, d12), (d21, d22), (ax, ay)
-  walk_bonds<4>(
-      w, i, idx, [&](int64_t j) { return Nb{a.us[j], a.xs[j], a.vh[j]}; },
-      [&](int k, int j, const Nb& nb) {
-        const float2 e = tf_diff2(nb.x, nxh, nxl);  // xi^
-        const float2 d = tf_diff2(nb.u, nuh, nul);  // du^
-        if (BREAK) {
-          const float2 q = mul2(d, fma2(f2(2.f, 2.f), e, d));  // d . (2 xi + d)
-          const float2 ee = mul2(e, e);
-          if (q.x + q.y > a.s2 * (ee.x + ee.y)) {
-            a.nbr[s0 + (int64_t)k * kChunk] = -2 - j;
-            ++newly;
-            return;
-          }
-        }
-        const float2 vv = f2(nb.v, nb.v);
-        const float2 t = mul2(vv, e);
-        D1 = fma2(f2(d.x, d.x), t, D1);
-        D2 = fma2(f2(d.y, d.y), t, D2);
-        A = fma2(vv, d, A);
-      });
-  d11 = D1.x;
-  d12 = D1.y;
-  d21 = D2.x;
-  d22 = D2.y;
-  ax = A.x;
-  ay = A.y;
-  a.hgs[i] = make_float2(2.f * a.k_hg * ax, 2.f * a.k_hg * ay);
+  walk_bonds<4>(w, 0, idx, gather, [&](int k, int j, const NbA& nb) {
+    const float2 e = tf_diff2(nb.x, nxh, nxl);  // xi^
+    const float2 d = tf_diff2(nb.u, nuh, nul);  // du^
+    if (BREAK) {
+      const float2 q = mul2(d, fma2(f2(2.f, 2.f), e, d));  // d . (2 xi + d)
+      const float2 ee = mul2(e, e);
+      if (q.x + q.y > a.s2 * (ee.x + ee.y)) {
+        const int64_t s = s0 + (int64_t)k * kChunk;
+        a.nbr[s] = -2 - gid(j);
+        if (a.loc) a.loc[s] = 0xFFFF;
+        ++newly;
+        return;
+      }
+    }
+    const float2 vv = f2(nb.v, nb.v);
+    const float2 t = mul2(vv, e);
+    D1 = fma2(f2(d.x, d.x), t, D1);
+    D2 = fma2(f2(d.y, d.y), t, D2);
+    A = fma2(vv, d, A);
+  });
+  const float d11 = D1.x, d12 = D1.y, d21 = D2.x, d22 = D2.y;
+  a.hgs[i] = make_float2(2.f * a.k_hg * A.x, 2.f * a.k_hg * A.y);
+  float4 g = pre.geo;
+  int singular = pre.singular;
   if (BREAK && newly) {
     atomicAdd(a.counters + CNT_BROKEN, (unsigned long long)newly);
     const int32_t b = a.broken[i] + newly;
     a.broken[i] = b;
     a.damage[i] = (double)b / (double)a.fam[i];
     kinv_update_mixed(a, i);
+    g = a.geo[i];
+    singular = a.singular[i];
   }
-  if (a.singular[i]) {
+  if (singular) {
     a.ws[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     return;
   }
-  const float4 g = a.geo[i];
   const float k11 = g.x, k12 = g.y, k22 = g.z, vi = g.w;
   const float g11 = fmaf(d11, k11, d12 * k12), g12 = fmaf(d11, k12, d12 * k22);
   const float g21 = fmaf(d21, k11, d22 * k12), g22 = fmaf(d21, k12, d22 * k22);
@@ -198,106 +241,375 @@ __device__ __forceinline__ void pass_a_particle_mixed(const MixedArgs& a, int64_
                         vi * fmaf(kh, g12, fmaf(s11, k12, s12 * k22)), vi * fmaf(kh, g22, fmaf(s12, k12, s22 * k22)));
 }
 
+struct GatherA {
+  const MixedArgs* a;
+  __device__ __forceinline__ NbA operator()(int64_t j) const { return NbA{a->us[j], a->xs[j], a->vh[j]}; }
+};
+struct SelfId {
+  __device__ __forceinline__ int operator()(int j) const { return j; }
+};
+
+// Pass A of particle i with indices and data read from HBM (batched plates).
 template <bool BREAK>
 __device__ __forceinline__ void pass_a_particle_mixed(const MixedArgs& a, int64_t i) {
   int w;
   const int64_t s0 = slot0(a, i, &w);
-  pass_a_particle_mixed<BREAK>(a, i, w, s0, GlobalIdx{a.nbr, s0});
+  pass_a_core<BREAK>(a, i, load_a(a, i), w, s0, GlobalIdx{a.nbr, s0}, GatherA{&a}, SelfId{});
 }
 
-// Picks the calling warp's chunk (visiting order: the 8 warps of a block run
-// chunks that are neighbours in space, so their gathers share L1) and stages
-// its indices in shared memory (pd_stage.cuh).  Returns the chunk width, or
-// -1 when the warp has nothing to do or its copy timed out (error word set).
-__device__ __forceinline__ int stage_warp(const MixedArgs& a, int32_t* stage, uint64_t* bars, int64_t* base,
-                                          int64_t* chunk) {
-  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if ((gw << 5) >= a.n) return -1;  // warp-uniform
-  const int64_t c = a.chunk_order[gw];
-  *chunk = c;
-  const int warp = threadIdx.x >> 5;
-  const int w = a.chunk_w[c];
-  *base = a.chunk_base[c];
-  if (!stage_chunk(stage + (int64_t)warp * a.wmax * 32, a.nbr + *base, w, &bars[warp])) {
-    if ((threadIdx.x & 31) == 0) atomicOr(a.counters + CNT_ERROR, (unsigned long long)ERR_STAGE_TIMEOUT);
-    return -1;
+// Per-particle inputs of pass B, loaded ahead of the bond walk (the BC
+// group is resolved separately: resolve_bc).
+struct PreB {
+  float4 wi, xi, v, u;
+  float2 m, h, fo;
+  int g;
+};
+
+template <bool DRIFT>
+__device__ __forceinline__ PreB load_b(const MixedArgs& a, int64_t i) {
+  PreB p;
+  p.wi = a.ws[i];
+  p.xi = a.xs[i];
+  p.m = a.mh[i];
+  p.h = a.hgs[i];
+  p.fo = a.fs[i];
+  p.v = a.vs[i];
+  if (DRIFT) {
+    p.u = a.us[i];
+    p.g = a.bc[i];
   }
-  return w;
+  return p;
 }
 
-template <bool BREAK>
-__global__ void __launch_bounds__(kBlock) k_pass_a_mixed(MixedArgs a) {
-  extern __shared__ __align__(128) int32_t stage[];
-  __shared__ uint64_t bars[kBlock / 32];
-  int64_t base, chunk;
-  const int w = stage_warp(a, stage, bars, &base, &chunk);
-  if (w < 0) return;
-  const int lane = threadIdx.x & 31;
-  const int64_t i = chunk * 32 + lane;
-  if (i >= a.n) return;
-  pass_a_particle_mixed<BREAK>(a, i, w, base + lane, SharedIdx{stage + (threadIdx.x >> 5) * a.wmax * 32, lane});
-}
-
-// Pass B of particle i: slots s0 + 32 k, k < w, indices read through idx.
-template <bool DRIFT, typename Idx>
-__device__ __forceinline__ void pass_b_particle_mixed(const MixedArgs& a, int64_t i, int w, Idx idx) {
-  const float4 wi = a.ws[i], xi = a.xs[i];
-  const float2 m = a.mh[i], h = a.hgs[i];
+// Pass B of particle i (force gather, kick, optional next drift).
+template <bool DRIFT, typename Idx, typename Gather>
+__device__ __forceinline__ void pass_b_core(const MixedArgs& a, int64_t i, const PreB& pre, const BcOf& bc, int w,
+                                            Idx idx, Gather gather) {
+  const float4 wi = pre.wi, xi = pre.xi;
+  const float2 m = pre.m, h = pre.h;
   // W columns c1 = (W11, W21), c2 = (W12, W22): W v = c1 v.x + c2 v.y
   // compensated (TwoSum) sums S + C of both components at once
   float2 S = fma2(f2(wi.x, wi.y), f2(m.x, m.x), fma2(f2(wi.z, wi.w), f2(m.y, m.y), h)), C = f2(0.f, 0.f);
   const float2 nxh = f2(-xi.x, -xi.y), nxl = f2(-xi.z, -xi.w);
-  struct Nb {
-    float4 x, w;
-  };
-  walk_bonds<4>(
-      w, i, idx, [&](int64_t j) { return Nb{a.xs[j], a.ws[j]}; },
-      [&](int, int, const Nb& nb) {
-        const float2 e = tf_diff2(nb.x, nxh, nxl);
-        const float2 p = fma2(f2(nb.w.x, nb.w.y), f2(e.x, e.x), mul2(f2(nb.w.z, nb.w.w), f2(e.y, e.y)));
-        const float2 s = add2(S, p);
-        const float2 z = sub2(s, S);
-        C = add2(C, add2(sub2(S, sub2(s, z)), sub2(p, z)));
-        S = s;
-      });
+  walk_bonds<4>(w, 0, idx, gather, [&](int, int, const NbB& nb) {
+    const float2 e = tf_diff2(nb.x, nxh, nxl);
+    const float2 p = fma2(f2(nb.w.x, nb.w.y), f2(e.x, e.x), mul2(f2(nb.w.z, nb.w.w), f2(e.y, e.y)));
+    const float2 s = add2(S, p);
+    const float2 z = sub2(s, S);
+    C = add2(C, add2(sub2(S, sub2(s, z)), sub2(p, z)));
+    S = s;
+  });
   const float fx = S.x + C.x, fy = S.y + C.y;
-  const float2 fo = a.fs[i];
+  const float2 fo = pre.fo;
   const float aox = a.tau2 * fo.x, aoy = a.tau2 * fo.y;
   const float anx = a.tau2 * fx, any = a.tau2 * fy;
-  float4 v = a.vs[i];
+  float4 v = pre.v;
   tf_add(v.x, v.z, 0.5f * (aox + anx));
   tf_add(v.y, v.w, 0.5f * (aoy + any));
   a.fs[i] = make_float2(fx, fy);
   if (DRIFT) {
-    float4 u = a.us[i];
-    drift_mixed(a, i, v, u, anx, any);
+    float4 u = pre.u;
+    drift_bc(bc, v, u, anx, any);
     a.us[i] = u;
   }
   a.vs[i] = v;
 }
 
+struct GatherB {
+  const MixedArgs* a;
+  __device__ __forceinline__ NbB operator()(int64_t j) const { return NbB{a->xs[j], a->ws[j]}; }
+};
+
 template <bool DRIFT>
 __device__ __forceinline__ void pass_b_particle_mixed(const MixedArgs& a, int64_t i) {
   int w;
   const int64_t s0 = slot0(a, i, &w);
-  pass_b_particle_mixed<DRIFT>(a, i, w, GlobalIdx{a.nbr, s0});
+  const PreB pre = load_b<DRIFT>(a, i);
+  pass_b_core<DRIFT>(a, i, pre, DRIFT ? resolve_bc(a, pre.g) : BcOf{}, w, GlobalIdx{a.nbr, s0}, GatherB{&a});
+}
+
+// ---- single-plate passes.  Block b runs the chunks chunk_order[8b .. 8b+8)
+// (spatially compact, see the chunk order in pd_api.cu).  Blocks whose halo
+// -- the distinct particles their bonds reach -- was staged at setup
+// (halo_n[b] >= 0) first copy the halo's data into shared memory with
+// coalesced loads and then walk their bonds entirely out of shared memory
+// (16-bit halo indices, TMA-staged per warp); other blocks stage their int32
+// indices and gather neighbour data from L1/L2.
+
+struct HaloSmem {  // dynamic shared memory carve-up of a halo block
+  float4* q0;      // pass A: u^, pass B: x^
+  float4* q1;      // pass A: x^, pass B: W^
+  uint16_t* li;    // 8 warps x wmax x 32 halo indices
+  float* vh;       // pass A: V^
+  int32_t* hid;    // pass A: particle ids
+};
+
+__device__ __forceinline__ HaloSmem halo_smem(const MixedArgs& a, unsigned char* sm) {
+  HaloSmem h;
+  const int hm = a.halo_max;
+  h.q0 = reinterpret_cast<float4*>(sm);
+  h.q1 = h.q0 + hm;
+  h.li = reinterpret_cast<uint16_t*>(h.q1 + hm);
+  h.vh = reinterpret_cast<float*>(h.li + (kBlock / 32) * a.wmax * 32);
+  h.hid = reinterpret_cast<int32_t*>(h.vh + hm);
+  return h;
+}
+
+// The calling warp's chunk (one 16 B visit record); false if the warp has none.
+__device__ __forceinline__ bool warp_chunk(const MixedArgs& a, int64_t* chunk, int* w, int64_t* base) {
+  const int64_t gw = (int64_t)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5);
+  if ((gw << 5) >= a.n) return false;  // warp-uniform
+  if (a.visit) {
+    const VisitRec r = a.visit[gw];
+    *chunk = r.chunk;
+    *w = r.w;
+    *base = r.base;
+  } else {
+    *chunk = a.chunk_order[gw];
+    *w = a.chunk_w[*chunk];
+    *base = a.chunk_base[*chunk];
+  }
+  return true;
+}
+
+__device__ __forceinline__ void stage_timeout(const MixedArgs& a) {
+  if ((threadIdx.x & 31) == 0) atomicOr(a.counters + CNT_ERROR, (unsigned long long)ERR_STAGE_TIMEOUT);
+}
+
+// Halo blocks: lane 0 of each warp issues the TMA copy of its 16-bit index
+// chunk, then the whole block loads the halo; returns after __syncthreads.
+__device__ __forceinline__ void halo_begin(const MixedArgs& a, const HaloSmem& h, uint64_t* bars, bool has, int w,
+                                           int64_t base) {
+  const int warp = threadIdx.x >> 5;
+  if (has && w > 0 && (threadIdx.x & 31) == 0)
+    stage_issue(h.li + warp * a.wmax * 32, a.loc + base, (uint32_t)w * 64u, &bars[warp]);
+}
+
+template <bool BREAK>
+__global__ void __launch_bounds__(kBlock) k_pass_a_mixed(MixedArgs a) {
+  extern __shared__ __align__(128) unsigned char sm[];
+  __shared__ uint64_t bars[kBlock / 32];
+  int64_t chunk = 0, base = 0;
+  int w = 0;
+  const bool has = warp_chunk(a, &chunk, &w, &base);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t i = chunk * 32 + lane;
+  const int hn = a.halo_n ? a.halo_n[blockIdx.x] : -1;
+  const bool live = has && i < a.n;
+  PreA pre{};
+  if (live) pre = load_a(a, i);  // in flight during the staging below
+  if (hn < 0) {  // int32 indices staged per warp, neighbour data from L1/L2
+    if (!has) return;
+    int32_t* mine = reinterpret_cast<int32_t*>(sm) + warp * a.wmax * 32;
+    if (!stage_chunk(mine, a.nbr + base, w, &bars[warp])) return stage_timeout(a);
+    if (live) pass_a_core<BREAK>(a, i, pre, w, base + lane, SharedIdx{mine, lane}, GatherA{&a}, SelfId{});
+    return;
+  }
+  const HaloSmem h = halo_smem(a, sm);
+  halo_begin(a, h, bars, has, w, base);
+  const int32_t* H = a.halo + (int64_t)blockIdx.x * a.halo_cap;
+#pragma unroll 4
+  for (int k = threadIdx.x; k < hn; k += kBlock) {
+    const int g = H[k];
+    h.hid[k] = g;
+    h.q0[k] = a.us[g];
+    h.q1[k] = a.xs[g];
+    h.vh[k] = a.vh[g];
+  }
+  __syncthreads();
+  if (!has) return;
+  if (w > 0 && !stage_wait(&bars[warp])) return stage_timeout(a);
+  if (!live) return;
+  const float4* q0 = h.q0;
+  const float4* q1 = h.q1;
+  const float* vh = h.vh;
+  const int32_t* hid = h.hid;
+  pass_a_core<BREAK>(
+      a, i, pre, w, base + lane, SharedHaloIdx{h.li + warp * a.wmax * 32, lane},
+      [=](int64_t l) { return NbA{q0[l], q1[l], vh[l]}; }, [=](int l) { return hid[l]; });
 }
 
 template <bool DRIFT>
 __global__ void __launch_bounds__(kBlock) k_pass_b_mixed(MixedArgs a) {
-  extern __shared__ __align__(128) int32_t stage[];
+  extern __shared__ __align__(128) unsigned char sm[];
   __shared__ uint64_t bars[kBlock / 32];
-  int64_t base, chunk;
-  const int w = stage_warp(a, stage, bars, &base, &chunk);
-  if (w < 0) return;
-  const int lane = threadIdx.x & 31;
+  int64_t chunk = 0, base = 0;
+  int w = 0;
+  const bool has = warp_chunk(a, &chunk, &w, &base);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t i = chunk * 32 + lane;
-  if (i >= a.n) return;
-  pass_b_particle_mixed<DRIFT>(a, i, w, SharedIdx{stage + (threadIdx.x >> 5) * a.wmax * 32, lane});
+  const int hn = a.halo_n ? a.halo_n[blockIdx.x] : -1;
+  const bool live = has && i < a.n;
+  PreB pre{};
+  if (live) pre = load_b<DRIFT>(a, i);  // in flight during the staging below
+  if (hn < 0) {
+    if (!has) return;
+    int32_t* mine = reinterpret_cast<int32_t*>(sm) + warp * a.wmax * 32;
+    if (!stage_chunk(mine, a.nbr + base, w, &bars[warp])) return stage_timeout(a);
+    if (live)
+      pass_b_core<DRIFT>(a, i, pre, DRIFT ? resolve_bc(a, pre.g) : BcOf{}, w, SharedIdx{mine, lane}, GatherB{&a});
+    return;
+  }
+  const HaloSmem h = halo_smem(a, sm);
+  halo_begin(a, h, bars, has, w, base);
+  const int32_t* H = a.halo + (int64_t)blockIdx.x * a.halo_cap;
+#pragma unroll 4
+  for (int k = threadIdx.x; k < hn; k += kBlock) {
+    const int g = H[k];
+    h.q0[k] = a.xs[g];
+    h.q1[k] = a.ws[g];
+  }
+  BcOf bc{};
+  if (DRIFT && live) bc = resolve_bc(a, pre.g);
+  __syncthreads();
+  if (!has) return;
+  if (w > 0 && !stage_wait(&bars[warp])) return stage_timeout(a);
+  if (!live) return;
+  const float4* q0 = h.q0;
+  const float4* q1 = h.q1;
+  pass_b_core<DRIFT>(a, i, pre, bc, w, SharedHaloIdx{h.li + warp * a.wmax * 32, lane},
+                     [=](int64_t l) { return NbB{q0[l], q1[l]}; });
 }
 
-// Dynamic shared memory of the staged passes: one chunk of wmax slot rows per warp.
-inline size_t stage_bytes(const MixedArgs& a) { return (size_t)(kBlock / 32) * (size_t)a.wmax * 128u; }
+// Dynamic shared memory of the single-plate passes: the larger of the int32
+// index staging (8 warps x wmax rows x 128 B) and the halo carve-up.
+inline size_t pass_smem_bytes(const MixedArgs& a, bool pass_a) {
+  const size_t idx32 = (size_t)(kBlock / 32) * (size_t)a.wmax * 128u;
+  if (!a.halo_n) return idx32;
+  const size_t hm = (size_t)a.halo_max;
+  const size_t halo = hm * 32u + (size_t)(kBlock / 32) * (size_t)a.wmax * 64u + (pass_a ? hm * 8u : 0u);
+  return halo > idx32 ? halo : idx32;
+}
+
+// ---- halo build (setup): per block, the sorted distinct particles its
+// chunks' bonds reach (own particles included), found with a bitmap over
+// the block's id span, and every slot's position in that list.
+__device__ __forceinline__ int decode_nbr(int v) { return v >= 0 ? v : (v <= -2 ? -2 - v : -1); }
+
+__global__ void __launch_bounds__(kBlock) k_halo_build(MixedArgs a, int32_t* halo, int32_t* halo_n, uint16_t* loc,
+                                                       uint16_t* loc0) {
+  __shared__ uint32_t bits[kHaloSpanWords];
+  __shared__ int32_t pre[kHaloSpanWords];
+  __shared__ int32_t wsum[kBlock / 32];
+  __shared__ int32_t s_lo, s_hi;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  int64_t chunk = 0, base = 0;
+  int w = 0;
+  const bool has = warp_chunk(a, &chunk, &w, &base);
+  if (!has) w = 0;
+  const int64_t s0 = base + lane;
+  const int64_t i = has && chunk * 32 + lane < a.n ? chunk * 32 + lane : -1;
+  if (tid == 0) {
+    s_lo = INT_MAX;
+    s_hi = -1;
+  }
+  __syncthreads();
+  int lo = i >= 0 ? (int)i : INT_MAX, hi = (int)i;
+  for (int k = 0; k < w; ++k) {
+    const int j = decode_nbr(a.nbr[s0 + (int64_t)k * kChunk]);
+    if (j >= 0) {
+      lo = min(lo, j);
+      hi = max(hi, j);
+    }
+  }
+  for (int o = 16; o; o >>= 1) {
+    lo = min(lo, __shfl_xor_sync(~0u, lo, o));
+    hi = max(hi, __shfl_xor_sync(~0u, hi, o));
+  }
+  if (lane == 0) {
+    atomicMin(&s_lo, lo);
+    atomicMax(&s_hi, hi);
+  }
+  __syncthreads();
+  const int L = s_lo, Hi = s_hi;
+  bool fits = Hi >= L && (int64_t)Hi - L < 32LL * kHaloSpanWords;
+  if (fits) {
+    for (int k = tid; k < kHaloSpanWords; k += kBlock) bits[k] = 0u;
+    __syncthreads();
+    if (i >= 0) atomicOr(&bits[(i - L) >> 5], 1u << ((i - L) & 31));
+    for (int k = 0; k < w; ++k) {
+      const int j = decode_nbr(a.nbr[s0 + (int64_t)k * kChunk]);
+      if (j >= 0) atomicOr(&bits[(j - L) >> 5], 1u << ((j - L) & 31));
+    }
+    __syncthreads();
+    constexpr int kPer = kHaloSpanWords / kBlock;
+    int c8[kPer], cnt = 0;
+#pragma unroll
+    for (int q = 0; q < kPer; ++q) {
+      c8[q] = __popc(bits[tid * kPer + q]);
+      cnt += c8[q];
+    }
+    int incl = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(~0u, incl, o);
+      if (lane >= o) incl += t;
+    }
+    if (lane == 31) wsum[warp] = incl;
+    __syncthreads();
+    int wpre = 0, tot = 0;
+    for (int q = 0; q < kBlock / 32; ++q) {
+      if (q < warp) wpre += wsum[q];
+      tot += wsum[q];
+    }
+    int run = wpre + incl - cnt;
+#pragma unroll
+    for (int q = 0; q < kPer; ++q) {
+      pre[tid * kPer + q] = run;
+      run += c8[q];
+    }
+    __syncthreads();
+    fits = tot <= kHaloCap;
+    if (fits) {
+      if (tid == 0) halo_n[blockIdx.x] = tot;
+      int32_t* H = halo + (int64_t)blockIdx.x * kHaloCap;
+      for (int word = tid; word < kHaloSpanWords; word += kBlock) {
+        uint32_t m = bits[word];
+        int r = pre[word];
+        while (m) {
+          const int bpos = __ffs(m) - 1;
+          H[r++] = L + 32 * word + bpos;
+          m &= m - 1u;
+        }
+      }
+      for (int k = 0; k < w; ++k) {
+        const int64_t s = s0 + (int64_t)k * kChunk;
+        const int v = a.nbr[s];
+        const int j = decode_nbr(v);
+        uint16_t l = 0xFFFF;
+        if (j >= 0) {
+          const int d = j - L;
+          l = (uint16_t)(pre[d >> 5] + __popc(bits[d >> 5] & ((1u << (d & 31)) - 1u)));
+        }
+        loc0[s] = l;
+        loc[s] = v >= 0 ? l : (uint16_t)0xFFFF;
+      }
+      return;
+    }
+  }
+  // too wide or too many: the block reads neighbour data from HBM
+  if (tid == 0) halo_n[blockIdx.x] = -1;
+  for (int k = 0; k < w; ++k) {
+    const int64_t s = s0 + (int64_t)k * kChunk;
+    loc0[s] = 0xFFFF;
+    loc[s] = 0xFFFF;
+  }
+}
+
+// visit record of every warp position: {chunk, width, first slot}
+__global__ void k_visit_build(int64_t nchunks, const int32_t* __restrict__ order, const int32_t* __restrict__ chunk_w,
+                              const int64_t* __restrict__ chunk_base, VisitRec* visit) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nchunks) return;
+  const int32_t c = order[k];
+  visit[k] = VisitRec{c, chunk_w[c], chunk_base[c]};
+}
+
+// live 16-bit indices from the pristine ones and the int32 mask (after a reset)
+__global__ void k_halo_relink(int64_t nslots, const int32_t* __restrict__ nbr, const uint16_t* __restrict__ loc0,
+                              uint16_t* loc) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < nslots) loc[s] = nbr[s] >= 0 ? loc0[s] : (uint16_t)0xFFFF;
+}
 
 // ---- batched plates (see pd_batch.cuh): phase 0 drift, 1 pass A, 2 pass B + drift, 3 pass B
 __device__ __forceinline__ void batch_particle_mixed(const MixedArgs& p, int64_t i, int phase) {
@@ -436,8 +748,8 @@ cudaError_t launch_batch_mixed(const MixedArgs* d_plates, const BatchTile* d_til
 
 void launch_init_geometry_mixed(const MixedArgs& a, cudaStream_t s) {
   if (a.n <= 0) return;
-  // the staged passes may take up to 8 warps x PD_MAX_FAMILY rows x 128 B of dynamic shared memory
-  const int mx = (kBlock / 32) * PD_MAX_FAMILY * 128;
+  // the passes may take up to kHaloCap x 40 B + 8 warps x PD_MAX_FAMILY rows x 64 B of dynamic shared memory
+  const int mx = kHaloCap * 40 + (kBlock / 32) * PD_MAX_FAMILY * 64;
   cudaFuncSetAttribute(k_pass_a_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   cudaFuncSetAttribute(k_pass_a_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   cudaFuncSetAttribute(k_pass_b_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
@@ -452,7 +764,7 @@ void launch_drift_mixed(const MixedArgs& a, cudaStream_t s) {
 
 void launch_pass_a_mixed(const MixedArgs& a, bool breaking, cudaStream_t s) {
   if (a.n <= 0) return;
-  const size_t sm = stage_bytes(a);
+  const size_t sm = pass_smem_bytes(a, true);
   if (breaking)
     k_pass_a_mixed<true><<<(unsigned)blocks_for(a.n), kBlock, sm, s>>>(a);
   else
@@ -461,7 +773,7 @@ void launch_pass_a_mixed(const MixedArgs& a, bool breaking, cudaStream_t s) {
 
 void launch_pass_b_mixed(const MixedArgs& a, bool drift, cudaStream_t s) {
   if (a.n <= 0) return;
-  const size_t sm = stage_bytes(a);
+  const size_t sm = pass_smem_bytes(a, false);
   if (drift)
     k_pass_b_mixed<true><<<(unsigned)blocks_for(a.n), kBlock, sm, s>>>(a);
   else
@@ -474,6 +786,45 @@ void launch_to_mixed(const MixedArgs& a, const double2* u, const double2* v, con
 
 void launch_from_mixed(const MixedArgs& a, double2* u, double2* v, double2* f, cudaStream_t s) {
   if (a.n > 0) k_from_mixed<<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a, u, v, f);
+}
+
+int build_halo_mixed(const MixedArgs& a, int64_t nslots, cudaStream_t s, HaloLayout* h, std::string* msg) {
+  const int64_t nb = blocks_for(a.n);
+  h->nblocks = nb;
+  h->staged = 0;
+  h->halo_max = 0;
+  if (a.n <= 0) return PD_OK;
+  const size_t ns = (size_t)(nslots > 0 ? nslots : 1);
+  const int64_t nch = (a.n + kChunk - 1) / kChunk;
+  if (cudaMalloc(&h->visit, (size_t)nch * sizeof(VisitRec)) != cudaSuccess ||
+      cudaMalloc(&h->loc, ns * sizeof(uint16_t)) != cudaSuccess ||
+      cudaMalloc(&h->loc0, ns * sizeof(uint16_t)) != cudaSuccess ||
+      cudaMalloc(&h->halo, (size_t)nb * kHaloCap * sizeof(int32_t)) != cudaSuccess ||
+      cudaMalloc(&h->halo_n, (size_t)nb * sizeof(int32_t)) != cudaSuccess) {
+    *msg = "halo staging: out of device memory";
+    return PD_ERR_CUDA;
+  }
+  k_visit_build<<<(unsigned)blocks_for(nch), kBlock, 0, s>>>(nch, a.chunk_order, a.chunk_w, a.chunk_base, h->visit);
+  k_halo_build<<<(unsigned)nb, kBlock, 0, s>>>(a, h->halo, h->halo_n, h->loc, h->loc0);
+  std::vector<int32_t> cnt((size_t)nb);
+  cudaError_t e = cudaMemcpyAsync(cnt.data(), h->halo_n, (size_t)nb * sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    *msg = std::string("halo staging: ") + cudaGetErrorString(e);
+    return PD_ERR_CUDA;
+  }
+  int32_t mx = 0;
+  for (int32_t v : cnt)
+    if (v >= 0) {
+      ++h->staged;
+      mx = v > mx ? v : mx;
+    }
+  h->halo_max = (mx + 7) & ~7;
+  return PD_OK;
+}
+
+void launch_halo_relink(int64_t nslots, const int32_t* nbr, const HaloLayout& h, cudaStream_t s) {
+  if (nslots > 0 && h.loc) k_halo_relink<<<(unsigned)blocks_for(nslots), kBlock, 0, s>>>(nslots, nbr, h.loc0, h.loc);
 }
 
 }  // namespace pd

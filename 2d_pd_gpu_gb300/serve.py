@@ -31,8 +31,10 @@ import numpy as np
 from . import native, plates
 
 # bytes per particle and per bond slot actually allocated (pd_api.cu): state,
-# geometry, staging, CSR, SELL and per-bond data.  Used for admission.
-FOOTPRINT = {native.PD_FP64: (215.0, 4.0 + 48.0 + 4.0), native.PD_MIXED: (230.0, 4.0 + 4.0 + 4.0)}
+# geometry, staging, CSR, SELL and per-bond data; the mixed form adds its
+# halo lists (2048 ids per 256 particles) and two 16-bit halo indices per
+# slot.  Used for admission.
+FOOTPRINT = {native.PD_FP64: (215.0, 4.0 + 48.0 + 4.0), native.PD_MIXED: (230.0 + 32.0, 4.0 + 4.0 + 4.0 + 4.0)}
 
 
 @dataclass
