@@ -172,9 +172,6 @@ struct NbB {
   float4 x, w;
 };
 
-// Pass A of particle i: slots s0 + 32 k, k < w; idx(k) gives a slot's
-// neighbour (-1: padding or broken), gather(j) its data, gid(j) its particle
-// id (j is a particle id, or a halo position when the data is staged).
 // Per-particle inputs of pass A, loaded ahead of the bond walk.
 struct PreA {
   float4 ui, xi, geo;
@@ -185,9 +182,12 @@ __device__ __forceinline__ PreA load_a(const MixedArgs& a, int64_t i) {
   return PreA{a.us[i], a.xs[i], a.geo[i], a.singular[i]};
 }
 
-template <bool BREAK, typename Idx, typename Gather, typename Gid>
+// Pass A of particle i: slots s0 + 32 k, k < w; idx(k) gives a slot's
+// neighbour (-1: padding or broken; a particle id, or a halo position when
+// the data is staged) and gather(j) its data.
+template <bool BREAK, typename Idx, typename Gather>
 __device__ __forceinline__ void pass_a_core(const MixedArgs& a, int64_t i, const PreA& pre, int w, int64_t s0, Idx idx,
-                                            Gather gather, Gid gid) {
+                                            Gather gather) {
   const float4 ui = pre.ui, xi = pre.xi;
   int newly = 0;
   const float2 nxh = f2(-xi.x, -xi.y), nxl = f2(-xi.z, -xi.w), nuh = f2(-ui.x, -ui.y), nul = f2(-ui.z, -ui.w);
@@ -200,7 +200,7 @@ __device__ __forceinline__ void pass_a_core(const MixedArgs& a, int64_t i, const
       const float2 ee = mul2(e, e);
       if (q.x + q.y > a.s2 * (ee.x + ee.y)) {
         const int64_t s = s0 + (int64_t)k * kChunk;
-        a.nbr[s] = -2 - gid(j);
+        a.nbr[s] = -2 - a.nbr[s];  // the particle id of slot s (j may be a halo position)
         if (a.loc) a.loc[s] = 0xFFFF;
         ++newly;
         return;
@@ -245,16 +245,13 @@ struct GatherA {
   const MixedArgs* a;
   __device__ __forceinline__ NbA operator()(int64_t j) const { return NbA{a->us[j], a->xs[j], a->vh[j]}; }
 };
-struct SelfId {
-  __device__ __forceinline__ int operator()(int j) const { return j; }
-};
 
 // Pass A of particle i with indices and data read from HBM (batched plates).
 template <bool BREAK>
 __device__ __forceinline__ void pass_a_particle_mixed(const MixedArgs& a, int64_t i) {
   int w;
   const int64_t s0 = slot0(a, i, &w);
-  pass_a_core<BREAK>(a, i, load_a(a, i), w, s0, GlobalIdx{a.nbr, s0}, GatherA{&a}, SelfId{});
+  pass_a_core<BREAK>(a, i, load_a(a, i), w, s0, GlobalIdx{a.nbr, s0}, GatherA{&a});
 }
 
 // Per-particle inputs of pass B, loaded ahead of the bond walk (the BC
@@ -341,7 +338,6 @@ struct HaloSmem {  // dynamic shared memory carve-up of a halo block
   float4* q1;      // pass A: x^, pass B: W^
   uint16_t* li;    // 8 warps x wmax x 32 halo indices
   float* vh;       // pass A: V^
-  int32_t* hid;    // pass A: particle ids
 };
 
 __device__ __forceinline__ HaloSmem halo_smem(const MixedArgs& a, unsigned char* sm) {
@@ -351,9 +347,22 @@ __device__ __forceinline__ HaloSmem halo_smem(const MixedArgs& a, unsigned char*
   h.q1 = h.q0 + hm;
   h.li = reinterpret_cast<uint16_t*>(h.q1 + hm);
   h.vh = reinterpret_cast<float*>(h.li + (kBlock / 32) * a.wmax * 32);
-  h.hid = reinterpret_cast<int32_t*>(h.vh + hm);
   return h;
 }
+
+// Halo loads: each thread fetches kHaloBatch halo ids, then issues
+// asynchronous global -> shared copies (cp.async; no registers held while
+// they are in flight) for all of them, so a block's whole halo is requested
+// after one id round trip and lands after one gather round trip.
+constexpr int kHaloBatch = 4;
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 // The calling warp's chunk (one 16 B visit record); false if the warp has none.
 __device__ __forceinline__ bool warp_chunk(const MixedArgs& a, int64_t* chunk, int* w, int64_t* base) {
@@ -402,20 +411,29 @@ __global__ void __launch_bounds__(kBlock) k_pass_a_mixed(MixedArgs a) {
     if (!has) return;
     int32_t* mine = reinterpret_cast<int32_t*>(sm) + warp * a.wmax * 32;
     if (!stage_chunk(mine, a.nbr + base, w, &bars[warp])) return stage_timeout(a);
-    if (live) pass_a_core<BREAK>(a, i, pre, w, base + lane, SharedIdx{mine, lane}, GatherA{&a}, SelfId{});
+    if (live) pass_a_core<BREAK>(a, i, pre, w, base + lane, SharedIdx{mine, lane}, GatherA{&a});
     return;
   }
   const HaloSmem h = halo_smem(a, sm);
   halo_begin(a, h, bars, has, w, base);
   const int32_t* H = a.halo + (int64_t)blockIdx.x * a.halo_cap;
-#pragma unroll 4
-  for (int k = threadIdx.x; k < hn; k += kBlock) {
-    const int g = H[k];
-    h.hid[k] = g;
-    h.q0[k] = a.us[g];
-    h.q1[k] = a.xs[g];
-    h.vh[k] = a.vh[g];
+  for (int k0 = 0; k0 < hn; k0 += kHaloBatch * kBlock) {
+    int g[kHaloBatch];
+#pragma unroll
+    for (int q = 0; q < kHaloBatch; ++q) {
+      const int k = k0 + q * kBlock + threadIdx.x;
+      g[q] = k < hn ? H[k] : -1;
+    }
+#pragma unroll
+    for (int q = 0; q < kHaloBatch; ++q)
+      if (g[q] >= 0) {
+        const int k = k0 + q * kBlock + threadIdx.x;
+        cp_async16(&h.q0[k], &a.us[g[q]]);
+        cp_async16(&h.q1[k], &a.xs[g[q]]);
+        cp_async4(&h.vh[k], &a.vh[g[q]]);
+      }
   }
+  cp_async_wait_all();
   __syncthreads();
   if (!has) return;
   if (w > 0 && !stage_wait(&bars[warp])) return stage_timeout(a);
@@ -423,14 +441,12 @@ __global__ void __launch_bounds__(kBlock) k_pass_a_mixed(MixedArgs a) {
   const float4* q0 = h.q0;
   const float4* q1 = h.q1;
   const float* vh = h.vh;
-  const int32_t* hid = h.hid;
-  pass_a_core<BREAK>(
-      a, i, pre, w, base + lane, SharedHaloIdx{h.li + warp * a.wmax * 32, lane},
-      [=](int64_t l) { return NbA{q0[l], q1[l], vh[l]}; }, [=](int l) { return hid[l]; });
+  pass_a_core<BREAK>(a, i, pre, w, base + lane, SharedHaloIdx{h.li + warp * a.wmax * 32, lane},
+                     [=](int64_t l) { return NbA{q0[l], q1[l], vh[l]}; });
 }
 
 template <bool DRIFT>
-__global__ void __launch_bounds__(kBlock) k_pass_b_mixed(MixedArgs a) {
+__global__ void __launch_bounds__(kBlock, 4) k_pass_b_mixed(MixedArgs a) {
   extern __shared__ __align__(128) unsigned char sm[];
   __shared__ uint64_t bars[kBlock / 32];
   int64_t chunk = 0, base = 0;
@@ -453,14 +469,24 @@ __global__ void __launch_bounds__(kBlock) k_pass_b_mixed(MixedArgs a) {
   const HaloSmem h = halo_smem(a, sm);
   halo_begin(a, h, bars, has, w, base);
   const int32_t* H = a.halo + (int64_t)blockIdx.x * a.halo_cap;
-#pragma unroll 4
-  for (int k = threadIdx.x; k < hn; k += kBlock) {
-    const int g = H[k];
-    h.q0[k] = a.xs[g];
-    h.q1[k] = a.ws[g];
+  for (int k0 = 0; k0 < hn; k0 += kHaloBatch * kBlock) {
+    int g[kHaloBatch];
+#pragma unroll
+    for (int q = 0; q < kHaloBatch; ++q) {
+      const int k = k0 + q * kBlock + threadIdx.x;
+      g[q] = k < hn ? H[k] : -1;
+    }
+#pragma unroll
+    for (int q = 0; q < kHaloBatch; ++q)
+      if (g[q] >= 0) {
+        const int k = k0 + q * kBlock + threadIdx.x;
+        cp_async16(&h.q0[k], &a.xs[g[q]]);
+        cp_async16(&h.q1[k], &a.ws[g[q]]);
+      }
   }
   BcOf bc{};
   if (DRIFT && live) bc = resolve_bc(a, pre.g);
+  cp_async_wait_all();
   __syncthreads();
   if (!has) return;
   if (w > 0 && !stage_wait(&bars[warp])) return stage_timeout(a);
@@ -477,7 +503,7 @@ inline size_t pass_smem_bytes(const MixedArgs& a, bool pass_a) {
   const size_t idx32 = (size_t)(kBlock / 32) * (size_t)a.wmax * 128u;
   if (!a.halo_n) return idx32;
   const size_t hm = (size_t)a.halo_max;
-  const size_t halo = hm * 32u + (size_t)(kBlock / 32) * (size_t)a.wmax * 64u + (pass_a ? hm * 8u : 0u);
+  const size_t halo = hm * 32u + (size_t)(kBlock / 32) * (size_t)a.wmax * 64u + (pass_a ? hm * 4u : 0u);
   return halo > idx32 ? halo : idx32;
 }
 
@@ -748,8 +774,8 @@ cudaError_t launch_batch_mixed(const MixedArgs* d_plates, const BatchTile* d_til
 
 void launch_init_geometry_mixed(const MixedArgs& a, cudaStream_t s) {
   if (a.n <= 0) return;
-  // the passes may take up to kHaloCap x 40 B + 8 warps x PD_MAX_FAMILY rows x 64 B of dynamic shared memory
-  const int mx = kHaloCap * 40 + (kBlock / 32) * PD_MAX_FAMILY * 64;
+  // the passes may take up to kHaloCap x 36 B + 8 warps x PD_MAX_FAMILY rows x 64 B of dynamic shared memory
+  const int mx = kHaloCap * 36 + (kBlock / 32) * PD_MAX_FAMILY * 64;
   cudaFuncSetAttribute(k_pass_a_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   cudaFuncSetAttribute(k_pass_a_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   cudaFuncSetAttribute(k_pass_b_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
