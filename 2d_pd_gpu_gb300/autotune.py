@@ -2,10 +2,13 @@
 
 Chooses, by measurement on this GPU, the launch mode (one persistent
 cooperative kernel, or a graph of phase kernels), threads per block,
-particles per work tile, and persistent blocks per SM.  The tuning never
-changes the arithmetic (one thread owns one particle at a time, and the
-per-particle code is the same), so a plate's results do not depend on the
-chosen configuration -- tests/test_gpu_batch.py checks that bit for bit.
+particles per work tile, and persistent blocks per SM.  Mixed-form batches
+always run 256-thread blocks over the plates' visiting blocks (the
+shared-memory halo code of the single-plate passes), so for them only the
+launch mode and blocks per SM are searched.  The tuning never changes the
+arithmetic (one thread owns one particle at a time, and the per-particle
+code is the same), so a plate's results do not depend on the chosen
+configuration -- tests/test_gpu_batch.py checks that bit for bit.
 
 Candidates are timed on a throwaway batch built from the same plates (the
 caller passes a factory), so tuning does not advance the real simulation.
@@ -29,6 +32,12 @@ CANDIDATES = (
      for s in (1, 2, 4)]
     + [dict(persistent=0, block=b, tile=t, blocks_per_sm=1) for b in (128, 256) for t in (256, 1024)]
 )
+MIXED_CANDIDATES = ([dict(persistent=1, block=256, tile=256, blocks_per_sm=s) for s in (1, 2, 3, 4)]
+                    + [dict(persistent=0, block=256, tile=256, blocks_per_sm=1)])
+
+
+def candidates_for(precision):
+    return MIXED_CANDIDATES if precision == native.PD_MIXED else CANDIDATES
 
 
 def _gpu_name(device):
@@ -59,9 +68,10 @@ def _save(d):
     os.replace(tmp, CACHE)
 
 
-def tune(make_batch, precision, device=0, steps=4, warmup=2, candidates=CANDIDATES, use_cache=True):
+def tune(make_batch, precision, device=0, steps=4, warmup=2, candidates=None, use_cache=True):
     """make_batch() -> (Batch, [contexts]) built from the workload's plates.
     Returns (best_config, {config_key: ms_per_step})."""
+    candidates = candidates_for(precision) if candidates is None else candidates
     probe, ctxs = make_batch()
     info = probe.info()
     key = f"{_gpu_name(device)}|{precision}|{bucket(info)}"
@@ -98,10 +108,11 @@ def tune(make_batch, precision, device=0, steps=4, warmup=2, candidates=CANDIDAT
     return best, timings
 
 
-def tune_batch(batch, steps=3, warmup=1, candidates=CANDIDATES):
+def tune_batch(batch, steps=3, warmup=1, candidates=None):
     """Measure the candidates on `batch` itself (this advances its plates:
     reset them afterwards).  Returns (best_config, {config_key: ms_per_step})
     and leaves the batch set to the best configuration."""
+    candidates = candidates_for(batch.precision) if candidates is None else candidates
     timings = {}
     best, best_ms = None, math.inf
     for cfg in candidates:

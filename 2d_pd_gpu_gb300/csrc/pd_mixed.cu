@@ -246,14 +246,6 @@ struct GatherA {
   __device__ __forceinline__ NbA operator()(int64_t j) const { return NbA{a->us[j], a->xs[j], a->vh[j]}; }
 };
 
-// Pass A of particle i with indices and data read from HBM (batched plates).
-template <bool BREAK>
-__device__ __forceinline__ void pass_a_particle_mixed(const MixedArgs& a, int64_t i) {
-  int w;
-  const int64_t s0 = slot0(a, i, &w);
-  pass_a_core<BREAK>(a, i, load_a(a, i), w, s0, GlobalIdx{a.nbr, s0}, GatherA{&a});
-}
-
 // Per-particle inputs of pass B, loaded ahead of the bond walk (the BC
 // group is resolved separately: resolve_bc).
 struct PreB {
@@ -317,13 +309,6 @@ struct GatherB {
   __device__ __forceinline__ NbB operator()(int64_t j) const { return NbB{a->xs[j], a->ws[j]}; }
 };
 
-template <bool DRIFT>
-__device__ __forceinline__ void pass_b_particle_mixed(const MixedArgs& a, int64_t i) {
-  int w;
-  const int64_t s0 = slot0(a, i, &w);
-  const PreB pre = load_b<DRIFT>(a, i);
-  pass_b_core<DRIFT>(a, i, pre, DRIFT ? resolve_bc(a, pre.g) : BcOf{}, w, GlobalIdx{a.nbr, s0}, GatherB{&a});
-}
 
 // ---- single-plate passes.  Block b runs the chunks chunk_order[8b .. 8b+8)
 // (spatially compact, see the chunk order in pd_api.cu).  Blocks whose halo
@@ -365,8 +350,8 @@ __device__ __forceinline__ void cp_async4(void* dst, const void* src) {
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 // The calling warp's chunk (one 16 B visit record); false if the warp has none.
-__device__ __forceinline__ bool warp_chunk(const MixedArgs& a, int64_t* chunk, int* w, int64_t* base) {
-  const int64_t gw = (int64_t)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5);
+__device__ __forceinline__ bool warp_chunk(const MixedArgs& a, int64_t blk, int64_t* chunk, int* w, int64_t* base) {
+  const int64_t gw = blk * (kBlock / 32) + (threadIdx.x >> 5);
   if ((gw << 5) >= a.n) return false;  // warp-uniform
   if (a.visit) {
     const VisitRec r = a.visit[gw];
@@ -394,29 +379,51 @@ __device__ __forceinline__ void halo_begin(const MixedArgs& a, const HaloSmem& h
     stage_issue(h.li + warp * a.wmax * 32, a.loc + base, (uint32_t)w * 64u, &bars[warp]);
 }
 
+// Invalidates a completed stage barrier so the next tile can arm it again.
+__device__ __forceinline__ void mbar_inval(uint64_t* bar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+// Waits for the warp's staged chunk; on success the barrier is invalidated
+// (reusable).  All 32 lanes call it.  False: the copy timed out (recorded).
+__device__ __forceinline__ bool warp_stage_done(const MixedArgs& a, uint64_t* bar, int w) {
+  if (w <= 0) return true;
+  const bool ok = __all_sync(~0u, stage_wait(bar));
+  if (!ok) {
+    stage_timeout(a);
+    return false;
+  }
+  if ((threadIdx.x & 31) == 0) mbar_inval(bar);
+  __syncwarp();
+  return true;
+}
+
+// Pass A of visiting block blk (8 chunks) of plate a.  Every thread of the
+// 256-thread block calls it; sm = the pass's dynamic shared memory.  False if
+// a staged copy timed out.
 template <bool BREAK>
-__global__ void __launch_bounds__(kBlock) k_pass_a_mixed(MixedArgs a) {
-  extern __shared__ __align__(128) unsigned char sm[];
-  __shared__ uint64_t bars[kBlock / 32];
+__device__ __forceinline__ bool pass_a_block(const MixedArgs& a, int64_t blk, unsigned char* sm, uint64_t* bars) {
   int64_t chunk = 0, base = 0;
   int w = 0;
-  const bool has = warp_chunk(a, &chunk, &w, &base);
+  const bool has = warp_chunk(a, blk, &chunk, &w, &base);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t i = chunk * 32 + lane;
-  const int hn = a.halo_n ? a.halo_n[blockIdx.x] : -1;
+  const int hn = a.halo_n ? a.halo_n[blk] : -1;
   const bool live = has && i < a.n;
   PreA pre{};
   if (live) pre = load_a(a, i);  // in flight during the staging below
   if (hn < 0) {  // int32 indices staged per warp, neighbour data from L1/L2
-    if (!has) return;
+    if (!has) return true;
     int32_t* mine = reinterpret_cast<int32_t*>(sm) + warp * a.wmax * 32;
-    if (!stage_chunk(mine, a.nbr + base, w, &bars[warp])) return stage_timeout(a);
+    if (w > 0 && lane == 0) stage_issue(mine, a.nbr + base, (uint32_t)w * 128u, &bars[warp]);
+    __syncwarp();
+    if (!warp_stage_done(a, &bars[warp], w)) return false;
     if (live) pass_a_core<BREAK>(a, i, pre, w, base + lane, SharedIdx{mine, lane}, GatherA{&a});
-    return;
+    return true;
   }
   const HaloSmem h = halo_smem(a, sm);
   halo_begin(a, h, bars, has, w, base);
-  const int32_t* H = a.halo + (int64_t)blockIdx.x * a.halo_cap;
+  const int32_t* H = a.halo + blk * a.halo_cap;
   for (int k0 = 0; k0 < hn; k0 += kHaloBatch * kBlock) {
     int g[kHaloBatch];
 #pragma unroll
@@ -435,40 +442,42 @@ __global__ void __launch_bounds__(kBlock) k_pass_a_mixed(MixedArgs a) {
   }
   cp_async_wait_all();
   __syncthreads();
-  if (!has) return;
-  if (w > 0 && !stage_wait(&bars[warp])) return stage_timeout(a);
-  if (!live) return;
+  if (!has) return true;
+  if (!warp_stage_done(a, &bars[warp], w)) return false;
+  if (!live) return true;
   const float4* q0 = h.q0;
   const float4* q1 = h.q1;
   const float* vh = h.vh;
   pass_a_core<BREAK>(a, i, pre, w, base + lane, SharedHaloIdx{h.li + warp * a.wmax * 32, lane},
                      [=](int64_t l) { return NbA{q0[l], q1[l], vh[l]}; });
+  return true;
 }
 
+// Pass B (+ the next drift when DRIFT) of visiting block blk of plate a.
 template <bool DRIFT>
-__global__ void __launch_bounds__(kBlock, 4) k_pass_b_mixed(MixedArgs a) {
-  extern __shared__ __align__(128) unsigned char sm[];
-  __shared__ uint64_t bars[kBlock / 32];
+__device__ __forceinline__ bool pass_b_block(const MixedArgs& a, int64_t blk, unsigned char* sm, uint64_t* bars) {
   int64_t chunk = 0, base = 0;
   int w = 0;
-  const bool has = warp_chunk(a, &chunk, &w, &base);
+  const bool has = warp_chunk(a, blk, &chunk, &w, &base);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t i = chunk * 32 + lane;
-  const int hn = a.halo_n ? a.halo_n[blockIdx.x] : -1;
+  const int hn = a.halo_n ? a.halo_n[blk] : -1;
   const bool live = has && i < a.n;
   PreB pre{};
   if (live) pre = load_b<DRIFT>(a, i);  // in flight during the staging below
   if (hn < 0) {
-    if (!has) return;
+    if (!has) return true;
     int32_t* mine = reinterpret_cast<int32_t*>(sm) + warp * a.wmax * 32;
-    if (!stage_chunk(mine, a.nbr + base, w, &bars[warp])) return stage_timeout(a);
+    if (w > 0 && lane == 0) stage_issue(mine, a.nbr + base, (uint32_t)w * 128u, &bars[warp]);
+    __syncwarp();
+    if (!warp_stage_done(a, &bars[warp], w)) return false;
     if (live)
       pass_b_core<DRIFT>(a, i, pre, DRIFT ? resolve_bc(a, pre.g) : BcOf{}, w, SharedIdx{mine, lane}, GatherB{&a});
-    return;
+    return true;
   }
   const HaloSmem h = halo_smem(a, sm);
   halo_begin(a, h, bars, has, w, base);
-  const int32_t* H = a.halo + (int64_t)blockIdx.x * a.halo_cap;
+  const int32_t* H = a.halo + blk * a.halo_cap;
   for (int k0 = 0; k0 < hn; k0 += kHaloBatch * kBlock) {
     int g[kHaloBatch];
 #pragma unroll
@@ -488,13 +497,37 @@ __global__ void __launch_bounds__(kBlock, 4) k_pass_b_mixed(MixedArgs a) {
   if (DRIFT && live) bc = resolve_bc(a, pre.g);
   cp_async_wait_all();
   __syncthreads();
-  if (!has) return;
-  if (w > 0 && !stage_wait(&bars[warp])) return stage_timeout(a);
-  if (!live) return;
+  if (!has) return true;
+  if (!warp_stage_done(a, &bars[warp], w)) return false;
+  if (!live) return true;
   const float4* q0 = h.q0;
   const float4* q1 = h.q1;
   pass_b_core<DRIFT>(a, i, pre, bc, w, SharedHaloIdx{h.li + warp * a.wmax * 32, lane},
                      [=](int64_t l) { return NbB{q0[l], q1[l]}; });
+  return true;
+}
+
+// Drift of visiting block blk of plate a (the first drift of a batched call).
+__device__ __forceinline__ void drift_block(const MixedArgs& a, int64_t blk) {
+  int64_t chunk = 0, base = 0;
+  int w = 0;
+  if (!warp_chunk(a, blk, &chunk, &w, &base)) return;
+  const int64_t i = chunk * 32 + (threadIdx.x & 31);
+  if (i < a.n) drift_particle_mixed(a, i);
+}
+
+template <bool BREAK>
+__global__ void __launch_bounds__(kBlock) k_pass_a_mixed(MixedArgs a) {
+  extern __shared__ __align__(128) unsigned char sm[];
+  __shared__ uint64_t bars[kBlock / 32];
+  pass_a_block<BREAK>(a, blockIdx.x, sm, bars);
+}
+
+template <bool DRIFT>
+__global__ void __launch_bounds__(kBlock, 4) k_pass_b_mixed(MixedArgs a) {
+  extern __shared__ __align__(128) unsigned char sm[];
+  __shared__ uint64_t bars[kBlock / 32];
+  pass_b_block<DRIFT>(a, blockIdx.x, sm, bars);
 }
 
 // Dynamic shared memory of the single-plate passes: the larger of the int32
@@ -521,7 +554,7 @@ __global__ void __launch_bounds__(kBlock) k_halo_build(MixedArgs a, int32_t* hal
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   int64_t chunk = 0, base = 0;
   int w = 0;
-  const bool has = warp_chunk(a, &chunk, &w, &base);
+  const bool has = warp_chunk(a, blockIdx.x, &chunk, &w, &base);
   if (!has) w = 0;
   const int64_t s0 = base + lane;
   const int64_t i = has && chunk * 32 + lane < a.n ? chunk * 32 + lane : -1;
@@ -637,43 +670,57 @@ __global__ void k_halo_relink(int64_t nslots, const int32_t* __restrict__ nbr, c
   if (s < nslots) loc[s] = nbr[s] >= 0 ? loc0[s] : (uint16_t)0xFFFF;
 }
 
-// ---- batched plates (see pd_batch.cuh): phase 0 drift, 1 pass A, 2 pass B + drift, 3 pass B
-__device__ __forceinline__ void batch_particle_mixed(const MixedArgs& p, int64_t i, int phase) {
-  if (phase == 0)
-    drift_particle_mixed(p, i);
-  else if (phase == 1)
-    p.brk ? pass_a_particle_mixed<true>(p, i) : pass_a_particle_mixed<false>(p, i);
-  else if (phase == 2)
-    pass_b_particle_mixed<true>(p, i);
-  else
-    pass_b_particle_mixed<false>(p, i);
-}
-
-__device__ __forceinline__ void batch_phase_mixed(const MixedArgs* __restrict__ plates,
-                                                  const BatchTile* __restrict__ tiles, int ntiles, int phase) {
-  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+// ---- batched plates (see pd_batch.cuh): phase 0 drift, 1 pass A, 2 pass B +
+// drift, 3 pass B.  A mixed tile is one visiting block of one plate (tile.first
+// = the block index, tile.count = 256 particles at most), run by the same
+// block code as the single-plate passes, so every plate's result is the one it
+// gets alone.  False if a staged copy timed out.
+template <int PHASE>  // PHASE < 0: the phase is the runtime argument
+__device__ __forceinline__ bool batch_phase_mixed(const MixedArgs* __restrict__ plates,
+                                                  const BatchTile* __restrict__ tiles, int ntiles, int phase_rt,
+                                                  unsigned char* sm, uint64_t* bars) {
+  const int phase = PHASE < 0 ? phase_rt : PHASE;
+  bool ok = true;
+  for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
     const BatchTile T = tiles[t];
     const MixedArgs& p = plates[T.plate];
-    for (int k = threadIdx.x; k < T.count; k += blockDim.x) batch_particle_mixed(p, T.first + k, phase);
+    __syncthreads();  // the previous tile's shared memory is no longer read
+    if (phase == 0)
+      drift_block(p, T.first);
+    else if (phase == 1)
+      ok = p.brk ? pass_a_block<true>(p, T.first, sm, bars) : pass_a_block<false>(p, T.first, sm, bars);
+    else if (phase == 2)
+      ok = pass_b_block<true>(p, T.first, sm, bars);
+    else
+      ok = pass_b_block<false>(p, T.first, sm, bars);
+    ok = __syncthreads_and(ok);
   }
+  return ok;
 }
 
-__global__ void __launch_bounds__(256) k_batch_persistent_mixed(const MixedArgs* __restrict__ plates,
-                                                                const BatchTile* __restrict__ tiles, int ntiles,
-                                                                int nsteps, GridBarrier* bar) {
+__global__ void __launch_bounds__(kBlock) k_batch_persistent_mixed(const MixedArgs* __restrict__ plates,
+                                                                   const BatchTile* __restrict__ tiles, int ntiles,
+                                                                   int nsteps, GridBarrier* bar) {
+  extern __shared__ __align__(128) unsigned char sm[];
+  __shared__ uint64_t bars[kBlock / 32];
   const unsigned nb = gridDim.x;
-  batch_phase_mixed(plates, tiles, ntiles, 0);
-  for (int s = 0; s < nsteps; ++s) {
+  bool ok = batch_phase_mixed<-1>(plates, tiles, ntiles, 0, sm, bars);
+  for (int s = 0; s < nsteps && ok; ++s) {
     if (!grid_sync(bar, nb)) return;
-    batch_phase_mixed(plates, tiles, ntiles, 1);
+    ok = batch_phase_mixed<-1>(plates, tiles, ntiles, 1, sm, bars);
+    if (!ok) break;
     if (!grid_sync(bar, nb)) return;
-    batch_phase_mixed(plates, tiles, ntiles, s + 1 < nsteps ? 2 : 3);
+    ok = batch_phase_mixed<-1>(plates, tiles, ntiles, s + 1 < nsteps ? 2 : 3, sm, bars);
   }
+  if (!ok && threadIdx.x == 0) atomicExch(&bar->err, 1);  // releases the other blocks' barrier waits
 }
 
-__global__ void __launch_bounds__(256) k_batch_phase_mixed(const MixedArgs* __restrict__ plates,
-                                                           const BatchTile* __restrict__ tiles, int ntiles, int phase) {
-  batch_phase_mixed(plates, tiles, ntiles, phase);
+template <int PHASE>
+__global__ void __launch_bounds__(kBlock) k_batch_phase_mixed(const MixedArgs* __restrict__ plates,
+                                                              const BatchTile* __restrict__ tiles, int ntiles) {
+  extern __shared__ __align__(128) unsigned char sm[];
+  __shared__ uint64_t bars[kBlock / 32];
+  batch_phase_mixed<PHASE>(plates, tiles, ntiles, PHASE, sm, bars);
 }
 
 // FP64 <-> scaled two-float conversions (set/get state; not per step)
@@ -734,26 +781,37 @@ __global__ void k_positions_mixed(MixedArgs a) {
 
 }  // namespace
 
-int batch_occupancy_mixed(const BatchLaunch& cfg) {
+size_t mixed_pass_smem(const MixedArgs& a) {
+  const size_t pa = pass_smem_bytes(a, true), pb = pass_smem_bytes(a, false);
+  return pa > pb ? pa : pb;
+}
+
+int batch_occupancy_mixed(const BatchLaunch& cfg, size_t smem) {
+  (void)cfg;
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch_persistent_mixed, cfg.block, 0) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch_persistent_mixed, kBlock, smem) != cudaSuccess)
     return 0;
   return nb;
 }
 
+// Mixed batches run 256-thread blocks over visiting-block tiles; cfg.block is
+// not used.
 cudaError_t launch_batch_mixed(const MixedArgs* d_plates, const BatchTile* d_tiles, int ntiles, int nsteps,
-                               const BatchLaunch& cfg, GridBarrier* d_bar, int nsm, cudaStream_t s) {
+                               const BatchLaunch& cfg, size_t smem, GridBarrier* d_bar, int nsm, cudaStream_t s) {
   if (ntiles <= 0 || nsteps <= 0) return cudaSuccess;
   if (!cfg.persistent) {
     const unsigned g = (unsigned)ntiles;
-    k_batch_phase_mixed<<<g, cfg.block, 0, s>>>(d_plates, d_tiles, ntiles, 0);
+    k_batch_phase_mixed<0><<<g, kBlock, smem, s>>>(d_plates, d_tiles, ntiles);
     for (int k = 0; k < nsteps; ++k) {
-      k_batch_phase_mixed<<<g, cfg.block, 0, s>>>(d_plates, d_tiles, ntiles, 1);
-      k_batch_phase_mixed<<<g, cfg.block, 0, s>>>(d_plates, d_tiles, ntiles, k + 1 < nsteps ? 2 : 3);
+      k_batch_phase_mixed<1><<<g, kBlock, smem, s>>>(d_plates, d_tiles, ntiles);
+      if (k + 1 < nsteps)
+        k_batch_phase_mixed<2><<<g, kBlock, smem, s>>>(d_plates, d_tiles, ntiles);
+      else
+        k_batch_phase_mixed<3><<<g, kBlock, smem, s>>>(d_plates, d_tiles, ntiles);
     }
     return cudaGetLastError();
   }
-  const int occ = batch_occupancy_mixed(cfg);
+  const int occ = batch_occupancy_mixed(cfg, smem);
   const int bps = cfg.blocks_per_sm < occ ? cfg.blocks_per_sm : occ;
   if (bps < 1) return cudaErrorInvalidConfiguration;
   int grid = nsm * bps;
@@ -762,7 +820,8 @@ cudaError_t launch_batch_mixed(const MixedArgs* d_plates, const BatchTile* d_til
   if (e != cudaSuccess) return e;
   cudaLaunchConfig_t lc = {};
   lc.gridDim = dim3((unsigned)grid);
-  lc.blockDim = dim3((unsigned)cfg.block);
+  lc.blockDim = dim3((unsigned)kBlock);
+  lc.dynamicSmemBytes = smem;
   lc.stream = s;
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeCooperative;
@@ -780,6 +839,11 @@ void launch_init_geometry_mixed(const MixedArgs& a, cudaStream_t s) {
   cudaFuncSetAttribute(k_pass_a_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   cudaFuncSetAttribute(k_pass_b_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   cudaFuncSetAttribute(k_pass_b_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_batch_persistent_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_batch_phase_mixed<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_batch_phase_mixed<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_batch_phase_mixed<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_batch_phase_mixed<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   k_positions_mixed<<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
   k_init_geometry_mixed<<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
 }

@@ -335,6 +335,7 @@ class Batch:
         rc = lib().pd_batch_create(device, precision, ctypes.byref(self._h))
         if rc != PD_OK:
             raise PdError(rc, lib().pd_batch_last_error(None).decode())
+        self.precision = precision
         self.members = []
 
     def _ck(self, rc):
