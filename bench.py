@@ -151,6 +151,15 @@ def byte_model(precision, n, nb):
             "step": 148.0 * n + 11.0 * nb}
 
 
+# DRAM bytes (read + write) per launch per bond, from one ncu capture of each
+# pass on the 600 x 600 plate (10,031,592 bonds; profiles/passes_fp64_plate600.txt
+# and profiles/passes_mixed_plate600.txt), scaled to a launch by its bonds:
+# traffic grows with the bonds (and the particles, in the same proportion on
+# these plates).
+DRAM_BYTES_PER_BOND = {"fp64": {"pass_a": 265.45e6 / 10031592, "pass_b": 245.37e6 / 10031592},
+                       "mixed": {"pass_a": 44.70e6 / 10031592, "pass_b": 57.94e6 / 10031592}}
+
+
 def fp64_ops(n, nb):
     """FP64 operations per step of the FP64 form: pass A 8 per bond (d 2, D 4,
     penalty sum 2; the stretch test is certified in FP32 for nearly all bonds)
@@ -226,8 +235,10 @@ def measure(ctx, prec, args, comm, sampler=None):
                    "achieved_gbs": (model[k] / (prof[k][0] / max(prof[k][1], 1) / 1e3) / 1e9) if prof[k][1] else None,
                    "algorithmic_bytes": model[k]}
                for k in prof}
+    traffic = DRAM_BYTES_PER_BOND[prec][dom] * nb
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-            "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+            "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "traffic_unit": "bytes per launch",
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum on the 600 x 600 plate, scaled by bonds",
             "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)", "algorithmic_bytes_per_launch": model[dom]}
     return value, ms_max / args.steps, kernels, roof
 
