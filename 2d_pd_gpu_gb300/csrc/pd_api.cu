@@ -911,6 +911,138 @@ int pd_step(pd_ctx* c, int32_t nsteps) {
   return check_after_step(c);
 }
 
+// ---- checkpoint / restore
+namespace {
+
+struct CkptHeader {
+  char magic[8];
+  int32_t abi, precision;
+  int64_t n, nslots, nnz, steps;
+  uint64_t problem;  // FNV-1a of the reference positions, volumes, families layout and parameters
+  unsigned long long counters[pd::CNT_N];
+};
+
+uint64_t fnv1a(uint64_t h, const void* p, size_t bytes) {
+  const unsigned char* b = static_cast<const unsigned char*>(p);
+  for (size_t k = 0; k < bytes; ++k) {
+    h ^= b[k];
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
+uint64_t problem_hash(const pd_ctx* c) {
+  uint64_t h = 1469598103934665603ull;
+  h = fnv1a(h, c->h_x.data(), c->h_x.size() * sizeof(double));
+  h = fnv1a(h, c->h_vol.data(), c->h_vol.size() * sizeof(double));
+  const double p[] = {c->p.E, c->p.nu, c->p.rho, c->p.dt, c->p.s_c, c->p.k_hg, c->p.damage_fail, c->p.n1, c->p.n2};
+  h = fnv1a(h, p, sizeof(p));
+  h = fnv1a(h, &c->nnz, sizeof(c->nnz));
+  h = fnv1a(h, &c->sell.nslots, sizeof(c->sell.nslots));
+  return h;
+}
+
+// (device pointer, bytes) of every saved array, in blob order
+std::vector<std::pair<void*, size_t>> ckpt_arrays(pd_ctx* c) {
+  const size_t n = (size_t)c->n, ns = (size_t)c->sell.nslots;
+  std::vector<std::pair<void*, size_t>> a;
+  if (mixed(c)) {
+    a.push_back({c->us, n * sizeof(float4)});
+    a.push_back({c->vsm, n * sizeof(float4)});
+    a.push_back({c->fs, n * sizeof(float2)});
+  } else {
+    a.push_back({c->u, n * sizeof(double2)});
+    a.push_back({c->v, n * sizeof(double2)});
+    a.push_back({c->f, n * sizeof(double2)});
+    a.push_back({c->acc, n * sizeof(double2)});
+  }
+  a.push_back({c->broken, n * sizeof(int32_t)});
+  a.push_back({c->damage, n * sizeof(double)});
+  a.push_back({c->sell.nbr, ns * sizeof(int32_t)});
+  return a;
+}
+
+int ckpt_bytes(pd_ctx* c, int64_t* bytes) {
+  int64_t b = (int64_t)sizeof(CkptHeader);
+  for (const auto& x : ckpt_arrays(c)) b += (int64_t)x.second;
+  *bytes = b;
+  return PD_OK;
+}
+
+}  // namespace
+
+int pd_checkpoint_size(pd_ctx* c, int64_t* bytes) {
+  if (!c || !bytes) return PD_ERR_ARG;
+  if (!c->has_families) return fail(c, PD_ERR_ORDER, "families first");
+  return ckpt_bytes(c, bytes);
+}
+
+int pd_checkpoint_save(pd_ctx* c, void* buf, int64_t bytes) {
+  if (!c || !buf) return PD_ERR_ARG;
+  if (!c->has_families) return fail(c, PD_ERR_ORDER, "families first");
+  int64_t need = 0;
+  ckpt_bytes(c, &need);
+  if (bytes < need) return fail(c, PD_ERR_CAPACITY, "checkpoint buffer too small (pd_checkpoint_size)");
+  PD_CK(c, cudaSetDevice(c->p.device));
+  PD_CK(c, cudaStreamSynchronize(c->stream));
+  CkptHeader h{};
+  std::memcpy(h.magic, "PDCKPT01", 8);
+  h.abi = PD_ABI_VERSION;
+  h.precision = c->p.precision;
+  h.n = c->n;
+  h.nslots = c->sell.nslots;
+  h.nnz = c->nnz;
+  h.steps = c->steps;
+  h.problem = problem_hash(c);
+  PD_CK(c, cudaMemcpy(h.counters, c->counters, sizeof(h.counters), cudaMemcpyDeviceToHost));
+  unsigned char* o = static_cast<unsigned char*>(buf);
+  std::memcpy(o, &h, sizeof(h));
+  o += sizeof(h);
+  for (const auto& x : ckpt_arrays(c)) {
+    if (x.second) PD_CK(c, cudaMemcpy(o, x.first, x.second, cudaMemcpyDeviceToHost));
+    o += x.second;
+  }
+  return PD_OK;
+}
+
+int pd_checkpoint_load(pd_ctx* c, const void* buf, int64_t bytes) {
+  if (!c || !buf) return PD_ERR_ARG;
+  if (!c->has_families) return fail(c, PD_ERR_ORDER, "families first");
+  int64_t need = 0;
+  ckpt_bytes(c, &need);
+  CkptHeader h;
+  if (bytes < (int64_t)sizeof(h)) return fail(c, PD_ERR_ARG, "not a checkpoint (too short)");
+  std::memcpy(&h, buf, sizeof(h));
+  if (std::memcmp(h.magic, "PDCKPT01", 8) != 0 || h.abi != PD_ABI_VERSION)
+    return fail(c, PD_ERR_ARG, "not a checkpoint of this library version");
+  if (h.precision != c->p.precision) return fail(c, PD_ERR_ARG, "checkpoint precision differs from the context's");
+  if (h.n != c->n || h.nslots != c->sell.nslots || h.nnz != c->nnz || h.problem != problem_hash(c))
+    return fail(c, PD_ERR_ARG, "checkpoint of another problem (particles, families or parameters differ)");
+  if (bytes < need) return fail(c, PD_ERR_ARG, "checkpoint truncated");
+  PD_CK(c, cudaSetDevice(c->p.device));
+  PD_CK(c, cudaStreamSynchronize(c->stream));
+  const unsigned char* p = static_cast<const unsigned char*>(buf) + sizeof(h);
+  for (const auto& x : ckpt_arrays(c)) {
+    if (x.second) PD_CK(c, cudaMemcpy(x.first, p, x.second, cudaMemcpyHostToDevice));
+    p += x.second;
+  }
+  // derived data: K^-1 / m / singular flags from the restored mask and broken counts,
+  // the FP32 shadows (FP64 form) or the live halo indices (mixed form)
+  cudaStream_t s = c->stream;
+  if (mixed(c)) {
+    pd::launch_halo_relink(c->sell.nslots, c->sell.nbr, c->halo, s);
+    pd::launch_init_geometry_mixed(mixed_args(c), s);
+  } else {
+    pd::launch_init_geometry_fp64(fp64_args(c), s);
+    pd::launch_shadow_fp64(fp64_args(c), s);
+  }
+  PD_CK(c, cudaGetLastError());
+  PD_CK(c, cudaMemcpyAsync(c->counters, h.counters, sizeof(h.counters), cudaMemcpyHostToDevice, s));
+  PD_CK(c, cudaStreamSynchronize(s));
+  c->steps = h.steps;
+  return PD_OK;
+}
+
 int pd_synchronize(pd_ctx* c) {
   if (!c) return PD_ERR_ARG;
   PD_CK(c, cudaSetDevice(c->p.device));

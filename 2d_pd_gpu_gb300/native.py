@@ -92,6 +92,9 @@ _SIGS = {
     "pd_get_damage": [_vp, _vp],
     "pd_get_bond_mask": [_vp, _vp],
     "pd_get_counters": [_vp, ctypes.POINTER(Counters)],
+    "pd_checkpoint_size": [_vp, ctypes.POINTER(ctypes.c_int64)],
+    "pd_checkpoint_save": [_vp, _vp, ctypes.c_int64],
+    "pd_checkpoint_load": [_vp, _vp, ctypes.c_int64],
     "pd_step": [_vp, ctypes.c_int32],
     "pd_synchronize": [_vp],
     "pd_compute_velocity": [_vp, _vp, _vp, _vp, _vp],
@@ -294,6 +297,19 @@ class Context:
         self._ck(lib().pd_get_counters(self._h, ctypes.byref(c)))
         return {"bonds_broken": c.bonds_broken, "singular_events": c.singular_events, "steps": c.steps,
                 "device_error": c.device_error}
+
+    # -- checkpoint / restore (pd_checkpoint_*)
+    def checkpoint(self) -> bytes:
+        """The dynamic state as an opaque blob (restore into a context built from the same inputs)."""
+        nb = ctypes.c_int64()
+        self._ck(lib().pd_checkpoint_size(self._h, ctypes.byref(nb)))
+        buf = ctypes.create_string_buffer(nb.value)
+        self._ck(lib().pd_checkpoint_save(self._h, buf, nb.value))
+        return buf.raw
+
+    def restore(self, blob: bytes):
+        buf = ctypes.create_string_buffer(blob, len(blob))
+        self._ck(lib().pd_checkpoint_load(self._h, buf, len(blob)))
 
     # -- stepping
     def step(self, nsteps=1):

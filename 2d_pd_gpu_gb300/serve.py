@@ -117,7 +117,29 @@ def state_digest(ctx):
 
 
 @dataclass
+class _Parked:
+    """A preempted request: its plate and its checkpoint (pd_checkpoint_save) in host memory."""
+    request: Request
+    plate: plates.Plate
+    blob: bytes
+    remaining: int
+    admitted: float
+
+    @property
+    def rid(self):
+        return self.request.rid
+
+    @property
+    def particles(self):
+        return self.request.particles
+
+
+@dataclass
 class Server:
+    """preempt: when the request at the head of the queue does not fit the HBM
+    budget, active requests with at least `preempt_ratio` times its remaining
+    work are checkpointed to host memory (largest first), freed, and queued
+    again behind it; they resume from the checkpoint bit for bit."""
     precision: int = native.PD_MIXED
     device: int = 0
     budget_bytes: float = 150e9
@@ -125,7 +147,10 @@ class Server:
     chunk: int = 50
     batch_config: dict | None = None
     workers: int = 4
+    preempt: bool = True
+    preempt_ratio: float = 4.0
     results: list = field(default_factory=list)
+    preemptions: int = 0
 
     def run(self, requests, stop_after=None):
         """Serve `requests` (arrival times relative to the start); returns metrics."""
@@ -150,12 +175,22 @@ class Server:
             for q in list(pending)[: self.workers]:
                 if q.rid not in futs:
                     futs[q.rid] = pool.submit(q.plate)
-            # admission: FIFO, by footprint and slots
+            # admission: FIFO, by footprint and slots (preempting long requests if enabled)
             while queue and len(active) < self.max_plates:
                 q = queue[0]
                 need = footprint(q.particles, self.precision)
+                if used + need > self.budget_bytes and active and self.preempt and not isinstance(q, _Parked):
+                    used -= self._preempt_for(q, need, used, active, batch, queue)
                 if used + need > self.budget_bytes and active:
                     break
+                if isinstance(q, _Parked):
+                    queue.popleft()
+                    ctx = q.plate.context(precision=self.precision, device=self.device)
+                    ctx.restore(q.blob)
+                    batch.add(ctx)
+                    used += need
+                    active[q.rid] = [q.request, ctx, q.remaining, q.admitted, need, q.plate]
+                    continue
                 if not futs[q.rid].done() and active:
                     break  # keep the GPU busy; admit when its plate is ready
                 p = futs.pop(q.rid).result()
@@ -163,7 +198,7 @@ class Server:
                 ctx = p.context(precision=self.precision, device=self.device)
                 batch.add(ctx)
                 used += need
-                active[q.rid] = [q, ctx, q.steps, time.perf_counter() - t0, need]
+                active[q.rid] = [q, ctx, q.steps, time.perf_counter() - t0, need, p]
             if not active:
                 if pending:
                     time.sleep(max(0.0, min(0.01, pending[0].arrival - (time.perf_counter() - t0))))
@@ -205,7 +240,31 @@ class Server:
             "gpu_busy_frac": busy / makespan if makespan > 0 else None,
             "bond_updates_per_s": bond_steps / makespan if makespan > 0 else None,
             "bond_updates": bond_steps,
+            "preemptions": self.preemptions,
         }
+
+    def _preempt_for(self, q, need, used, active, batch, queue):
+        """Checkpoints and frees active requests (largest remaining work first,
+        each with >= preempt_ratio x q's work) until q fits; they are queued
+        right behind q.  Returns the bytes freed."""
+        work_q = q.steps * q.particles
+        victims = sorted(active.items(), key=lambda kv: -kv[1][2] * kv[1][0].particles)
+        freed, parked = 0.0, []
+        for rid, a in victims:
+            if used - freed + need <= self.budget_bytes:
+                break
+            if a[2] * a[0].particles < self.preempt_ratio * work_q:
+                break
+            batch.remove(a[1])
+            blob = a[1].checkpoint()
+            a[1].close()
+            parked.append(_Parked(a[0], a[5], blob, a[2], a[3]))
+            freed += a[4]
+            del active[rid]
+            self.preemptions += 1
+        for pk in reversed(parked):
+            queue.insert(1, pk)
+        return freed
 
 
 def solo_digest(request, precision, device=0):

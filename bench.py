@@ -266,6 +266,23 @@ def accuracy(pdg, plate, device, checkpoints=(100, 500, 1000)):
     return out
 
 
+def run_mixed_scale(args, pdg, device, comm):
+    """The mixed form on a scale_side x scale_side plate (16M particles at 4000):
+    how the bandwidth-class path holds up when nothing of the state fits L2."""
+    t0 = time.perf_counter()
+    plate = pdg.plates.config_plate_scale(side=args.scale_side, seed=args.seed)
+    ctx = plate.context(precision=pdg.native.PD_MIXED, device=device)
+    setup_s = time.perf_counter() - t0
+    sub = argparse.Namespace(**vars(args))
+    sub.steps = min(args.steps, 20)
+    value, step_ms, kernels, roof = measure(ctx, "mixed", sub, comm)
+    out = {"value": value, "unit": "bond-updates/s", "ms_per_step": step_ms, "steps": sub.steps,
+           "particles": plate.n, "bonds": ctx.nnz, "setup_s": setup_s, "roofline": roof, "kernels": kernels,
+           "workload": f"plate{args.scale_side}x{args.scale_side}-mixed-crack-sc5e-4"}
+    ctx.close()
+    return out
+
+
 def run_batch(args, pdg, device):
     """Ragged batch: 256 plates, side U[50,400], seeded crack / material / load,
     stepped together by pd_batch with the autotuned launch shape."""
@@ -384,6 +401,8 @@ def run_ours(args, comm):
                            "roofline": mroof, "kernels": mkernels, "gpu_launches": 1 + 2 * args.steps}
         if not args.no_accuracy and comm.rank == 0:
             result["mixed"]["accuracy_vs_fp64"] = accuracy(pdg, plate, device)
+        if args.scale_side > 0:
+            result["mixed_scale"] = run_mixed_scale(args, pdg, device, comm)
     if not args.no_batch and comm.rank == 0:
         result["batch"] = run_batch(args, pdg, device)
         if not args.no_serve:
@@ -418,6 +437,7 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--scale-side", type=int, default=4000, help="mixed form on this plate too (0: skip)")
     ap.add_argument("--batch-plates", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=20)
     ap.add_argument("--serve-requests", type=int, default=64)

@@ -168,6 +168,20 @@ int pd_get_damage(pd_ctx* ctx, double* damage);
 int pd_get_bond_mask(pd_ctx* ctx, uint8_t* alive);
 int pd_get_counters(pd_ctx* ctx, pd_counters* c);
 
+/* Checkpoint / restore of a device-resident solve (no reference counterpart;
+ * used to preempt a served request and resume it later).  The blob holds the
+ * dynamic state in the context's own precision (the mixed form's scaled
+ * two-float state as stored, so a restored run continues bit for bit): u, v,
+ * f, the drop-in acceleration, the bond mask, broken counts, damage,
+ * counters and the step count.  It does not hold the problem (particles,
+ * families, BCs, parameters): restore into a context built from the same
+ * inputs; a blob from another problem, precision or ABI is rejected with
+ * PD_ERR_ARG.  Derived data (K^-1, shadows, halo indices) is recomputed on
+ * load. */
+int pd_checkpoint_size(pd_ctx* ctx, int64_t* bytes);
+int pd_checkpoint_save(pd_ctx* ctx, void* buf, int64_t bytes);
+int pd_checkpoint_load(pd_ctx* ctx, const void* buf, int64_t bytes);
+
 /* ------------------------------------------------------------------ step */
 
 /* nsteps full steps on the device (one CUDA graph per distinct nsteps).

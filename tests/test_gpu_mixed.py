@@ -111,3 +111,41 @@ def test_mixed_shuffled_numbering_matches(pdg):
     differ = int((d_shuffled != d_rowmajor).sum())
     print("particles whose damage differs:", differ, "of", int((d_rowmajor > 0).sum()), "damaged")
     assert differ <= max(4, int((d_rowmajor > 0).sum()) // 100)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_checkpoint_restore_continues_bit_for_bit(pdg, precision):
+    """Save after 30 steps, run 25 more; a fresh context of the same plate
+    restored from the blob and run 25 steps ends in the identical state."""
+    p = pdg.plates.make_plate(72, seed=11, crack="centre-half")
+    p.material.s_c = 2e-4  # bonds break before and after the checkpoint
+    a = p.context(precision=precision)
+    a.step(30)
+    blob = a.checkpoint()
+    broken_at_save = a.counters()["bonds_broken"]
+    a.step(25)
+    b = p.context(precision=precision)
+    b.restore(blob)
+    assert b.counters()["steps"] == 30 and b.counters()["bonds_broken"] == broken_at_save
+    b.step(25)
+    for x, y in zip((*a.state(), a.bond_mask(), a.damage()), (*b.state(), b.bond_mask(), b.damage())):
+        assert np.array_equal(x, y)
+    ca, cb = a.counters(), b.counters()
+    assert ca == cb and ca["bonds_broken"] > broken_at_save > 0
+
+
+def test_checkpoint_rejects_other_problems(pdg):
+    p = pdg.plates.make_plate(40, seed=1)
+    q = pdg.plates.make_plate(40, seed=2)  # same size, other jitter
+    a = p.context(precision=pdg.native.PD_MIXED)
+    a.step(3)
+    blob = a.checkpoint()
+    with pytest.raises(pdg.PdError):
+        q.context(precision=pdg.native.PD_MIXED).restore(blob)
+    with pytest.raises(pdg.PdError):
+        p.context(precision=pdg.native.PD_FP64).restore(blob)
+    with pytest.raises(pdg.PdError):
+        p.context(precision=pdg.native.PD_MIXED).restore(blob[:-8])
+    c = p.context(precision=pdg.native.PD_MIXED)
+    c.restore(blob)  # the matching context accepts it
+    assert c.counters()["steps"] == 3

@@ -40,3 +40,25 @@ def test_served_results_equal_solo(pdg, precision):
         d, broken = serve.solo_digest(q, precision)
         assert by[q.rid].digest == d, f"request {q.rid} differs alone vs in the mix"
         assert by[q.rid].broken == broken
+
+
+@pytest.mark.gpu
+def test_preemption_by_checkpoint_keeps_results(pdg):
+    """A long request holds the memory budget when short ones arrive: it is
+    checkpointed to host memory, the short ones run, and it resumes; every
+    result still equals its solo run bit for bit."""
+    serve = __import__("importlib").import_module("2d_pd_gpu_gb300.serve")
+    mat = pdg.plates.Material()
+    big = serve.Request(0, 0.0, 160, 160, 2000, 11, mat, 1.0, None)
+    small = [serve.Request(k, 0.01 * k, 48, 48, 30, 11 + k, mat, 1.5, None) for k in (1, 2, 3)]
+    reqs = [big] + small
+    f = lambda q: serve.footprint(q.particles, pdg.native.PD_MIXED)
+    budget = f(big) + 0.5 * f(small[0])
+    srv = serve.Server(precision=pdg.native.PD_MIXED, budget_bytes=budget, max_plates=4, chunk=10, workers=2)
+    m = srv.run(reqs)
+    assert m["requests"] == 4 and m["preemptions"] >= 1
+    by = {r.rid: r for r in srv.results}
+    assert by[0].finished > max(by[k].finished for k in (1, 2, 3))  # the short ones overtook it
+    for q in reqs:
+        d, broken = serve.solo_digest(q, pdg.native.PD_MIXED)
+        assert by[q.rid].digest == d and by[q.rid].broken == broken
