@@ -520,3 +520,154 @@ int64_t pdo_step(const pdo_problem* pb, pdo_state* st, int32_t nsteps) {
   }
   return nb;
 }
+
+/* ------------------------------------------------------- Mazars damage
+ * computeDamageStatus (src/main_seq.cpp:473-598).  The 2x2 symmetric
+ * eigen-decomposition follows Eigen's SelfAdjointEigenSolver contract
+ * (ascending eigenvalues, unit eigenvector columns) in closed form:
+ * mean -+ sqrt(((p - q)/2)^2 + o^2), eigenvector (o, lambda - p) / norm, the
+ * axes when o = 0. */
+static void sym_eig2(double p, double o, double q, double lam[2], double vec[2][2]) {
+  const double mean = 0.5 * (p + q), h = 0.5 * (p - q);
+  const double rad = sqrt(h * h + o * o);
+  lam[0] = mean - rad;
+  lam[1] = mean + rad;
+  if (o == 0.0) {
+    const int swap = p > q;
+    vec[0][0] = swap ? 0.0 : 1.0;
+    vec[1][0] = swap ? 1.0 : 0.0;
+    vec[0][1] = swap ? 1.0 : 0.0;
+    vec[1][1] = swap ? 0.0 : 1.0;
+    return;
+  }
+  for (int k = 0; k < 2; ++k) {
+    const double x = o, y = lam[k] - p;
+    const double nrm = sqrt(x * x + y * y);
+    vec[0][k] = x / nrm;
+    vec[1][k] = y / nrm;
+  }
+}
+
+/* Equivalent strain and the (alpha_t, alpha_c) split of a strain e, as the
+ * reference forms them (:525-566). */
+typedef struct mz_point {
+  double eq, at, ac;
+} mz_point;
+
+static mz_point mazars_point(double e11, double e12, double e22) {
+  double lam[2], v[2][2];
+  sym_eig2(e11, e12, e22, lam, v);
+  double s2 = 0.0;
+  for (int i = 0; i < 2; ++i)
+    if (lam[i] > 0.0) s2 += lam[i] * lam[i];
+  mz_point r = {s2 > 0.0 ? sqrt(s2) : 0.0, 0.0, 0.0};
+  if (!(r.eq > 0.0)) return r;
+  double st[2][2] = {{0.0, 0.0}, {0.0, 0.0}}, sc[2][2] = {{0.0, 0.0}, {0.0, 0.0}};
+  for (int i = 0; i < 2; ++i) {
+    if (lam[i] > 0.0) {
+      for (int j = 0; j < 2; ++j)
+        for (int k = 0; k < 2; ++k) st[j][k] += lam[i] * v[j][i] * v[k][i];
+    } else if (lam[i] < 0.0) {
+      for (int j = 0; j < 2; ++j)
+        for (int k = 0; k < 2; ++k) sc[j][k] += lam[i] * v[j][i] * v[k][i];
+    }
+  }
+  double tl[2], tv[2][2], cl[2], cv[2][2];
+  sym_eig2(st[0][0], 0.5 * (st[0][1] + st[1][0]), st[1][1], tl, tv);
+  sym_eig2(sc[0][0], 0.5 * (sc[0][1] + sc[1][0]), sc[1][1], cl, cv);
+  for (int i = 0; i < 2; ++i) {
+    if (tl[i] > 0.0) r.at += tl[i] * (tl[i] + cl[i]) / (r.eq * r.eq);
+    if (cl[i] > 0.0) r.ac += cl[i] * (tl[i] + cl[i]) / (r.eq * r.eq);
+  }
+  return r;
+}
+
+/* Bond update (:539-584): only where eq exceeds the bond's threshold. */
+static void mazars_bond(const mz_point* p, const pdo_mazars* mp, double* thr, double* bd) {
+  if (!(p->eq > *thr)) return;
+  const double k = *thr;
+  const double dt = 1.0 - k * (1 - mp->a_t) / p->eq - mp->a_t / exp(mp->b_t * (p->eq - k));
+  const double dc = 1.0 - k * (1 - mp->a_c) / p->eq - mp->a_c / exp(mp->b_c * (p->eq - k));
+  *bd = p->at * dt + p->ac * dc;
+  *thr = p->eq;
+}
+
+int pdo_mazars_update(const pdo_problem* pb, const pdo_state* st, const pdo_mazars* mp, double* thr, double* bd,
+                      double* status) {
+  const int ba = pb->n1 != 0.0 || pb->n2 != 0.0;
+  int bad = 0;
+  set_threads(pb->nthreads);
+#pragma omp parallel for schedule(static) reduction(| : bad)
+  for (int64_t i = 0; i < pb->n; ++i) {
+    const int64_t r0 = pb->row_ptr[i], n = pb->row_ptr[i + 1] - r0;
+    const double xi = pb->x[2 * i], yi = pb->x[2 * i + 1], ui = st->u[2 * i], wi = st->u[2 * i + 1];
+    if (!ba) {
+      /* classic: one strain per particle, D over the intact bonds as pass A */
+      double d11 = 0.0, d12 = 0.0, d21 = 0.0, d22 = 0.0;
+      for (int64_t s = r0; s < r0 + n; ++s) {
+        if (!st->alive[s]) continue;
+        const int64_t j = pb->col[s];
+        const double ex = pb->x[2 * j] - xi, ey = pb->x[2 * j + 1] - yi;
+        const double dx = st->u[2 * j] - ui, dy = st->u[2 * j + 1] - wi;
+        const double t0 = pb->vol[j] * ex, t1 = pb->vol[j] * ey;
+        d11 = fma(dx, t0, d11);
+        d12 = fma(dx, t1, d12);
+        d21 = fma(dy, t0, d21);
+        d22 = fma(dy, t1, d22);
+      }
+      mz_point p = {0.0, 0.0, 0.0};
+      if (!st->singular[i]) {
+        const double* ki = st->kinv + 3 * i;
+        const double k11 = ki[0], k12 = ki[1], k22 = ki[2];
+        const double g11 = fma(d11, k11, d12 * k12), g12 = fma(d11, k12, d12 * k22);
+        const double g21 = fma(d21, k11, d22 * k12), g22 = fma(d21, k12, d22 * k22);
+        p = mazars_point(g11, 0.5 * (g12 + g21), g22);
+      }
+      for (int64_t s = r0; s < r0 + n; ++s) mazars_bond(&p, mp, thr + s, bd + s);
+    } else {
+      if (n > 256) {
+        bad = 1;
+        continue;
+      }
+      double ex[256], ey[256], el[256], vv[256], dx[256], dy[256];
+      for (int64_t k = 0; k < n; ++k) {
+        const int64_t j = pb->col[r0 + k];
+        ex[k] = pb->x[2 * j] - xi;
+        ey[k] = pb->x[2 * j + 1] - yi;
+        el[k] = sqrt(ex[k] * ex[k] + ey[k] * ey[k]);
+        vv[k] = pb->vol[j];
+        dx[k] = st->u[2 * j] - ui;
+        dy[k] = st->u[2 * j + 1] - wi;
+      }
+      for (int64_t b = 0; b < n; ++b) {
+        double k11 = 0.0, k12 = 0.0, k22 = 0.0, d11 = 0.0, d12 = 0.0, d21 = 0.0, d22 = 0.0;
+        for (int64_t k = 0; k < n; ++k) {
+          const double wv = ba_weight(pb, ex[b], ey[b], el[b], ex[k], ey[k], el[k]) * vv[k];
+          const double t0 = wv * ex[k], t1 = wv * ey[k];
+          k11 = fma(t0, ex[k], k11);
+          k12 = fma(t0, ey[k], k12);
+          k22 = fma(t1, ey[k], k22);
+          d11 = fma(dx[k], t0, d11);
+          d12 = fma(dx[k], t1, d12);
+          d21 = fma(dy[k], t0, d21);
+          d22 = fma(dy[k], t1, d22);
+        }
+        mz_point p = {0.0, 0.0, 0.0};
+        const double det = fma(k11, k22, -(k12 * k12));
+        if (det > pb->det_guard * (k11 * k22)) {
+          const double r = 1.0 / det;
+          const double q11 = k22 * r, q12 = -k12 * r, q22 = k11 * r;
+          const double g11 = fma(d11, q11, d12 * q12), g12 = fma(d11, q12, d12 * q22);
+          const double g21 = fma(d21, q11, d22 * q12), g22 = fma(d21, q12, d22 * q22);
+          p = mazars_point(g11, 0.5 * (g12 + g21), g22);
+        }
+        mazars_bond(&p, mp, thr + r0 + b, bd + r0 + b);
+      }
+    }
+    double sum = 0.0;
+    for (int64_t s = r0; s < r0 + n; ++s) sum += bd[s] / (double)n;
+    status[i] = sum;
+  }
+  return bad ? -1 : 0;
+}
+

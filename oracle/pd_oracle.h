@@ -81,6 +81,27 @@ int64_t pdo_step(const pdo_problem* pb, pdo_state* st, int32_t nsteps);
  * families must be symmetric (returns -1 otherwise). */
 int pdo_reverse_bonds(int64_t n, const int64_t* row_ptr, const int32_t* col, int64_t* rev);
 
+/* Mazars damage (src/main_seq.cpp:473-598, computeDamageStatus; it does not
+ * feed the forces).  kappa0 is the initial per-bond threshold (the
+ * reference's tensileStrength / E), a_t .. b_c the law's constants
+ * (src/main_seq.cpp:481: 0.87, 20000, 0.65, 2150). */
+typedef struct pdo_mazars {
+  double kappa0, a_t, b_t, a_c, b_c;
+} pdo_mazars;
+
+/* One computeDamageStatus call from the state's displacements.  Per bond
+ * (family order): thr[nnz] (the history threshold) and bd[nnz] (bond damage)
+ * are updated in place where the bond's equivalent strain exceeds thr;
+ * status[n] = sum over the family of bd / family size (Particle::damageStatus).
+ * Classic weights: the strain of bond (i, j) is particle i's
+ * sym(D K^-1) over its intact bonds; bond-associated weights (n1, n2 != 0):
+ * bond b's own sym(D_b K_b^-1).  The reference accumulates the tensile and
+ * compressive strain parts into uninitialised matrices (:509-515, :547-554);
+ * here they start at zero.  Returns 0, or -1 for a family > 256 bonds in the
+ * bond-associated mode. */
+int pdo_mazars_update(const pdo_problem* pb, const pdo_state* st, const pdo_mazars* mp, double* thr, double* bd,
+                      double* status);
+
 /* Plane-stress constants exactly as the device receives them:
  * c[0] = C11 = C22, c[1] = C12, c[2] = C33 (src/main_seq.cpp:180-201). */
 void pdo_stiffness(double E, double nu, double c[3]);

@@ -55,6 +55,11 @@ class _Problem(ctypes.Structure):
     ]
 
 
+class _Mazars(ctypes.Structure):
+    _fields_ = [("kappa0", ctypes.c_double), ("a_t", ctypes.c_double), ("b_t", ctypes.c_double),
+                ("a_c", ctypes.c_double), ("b_c", ctypes.c_double)]
+
+
 class _State(ctypes.Structure):
     _fields_ = [
         ("u", _f64p),
@@ -91,6 +96,9 @@ def lib():
         L.pdo_step.argtypes = [ctypes.POINTER(_Problem), ctypes.POINTER(_State), ctypes.c_int32]
         L.pdo_reverse_bonds.restype = ctypes.c_int
         L.pdo_reverse_bonds.argtypes = [ctypes.c_int64, _i64p, _i32p, _i64p]
+        L.pdo_mazars_update.restype = ctypes.c_int
+        L.pdo_mazars_update.argtypes = [ctypes.POINTER(_Problem), ctypes.POINTER(_State), ctypes.POINTER(_Mazars),
+                                        _f64p, _f64p, _f64p]
         L.pdo_stiffness.restype = None
         L.pdo_stiffness.argtypes = [ctypes.c_double, ctypes.c_double, _f64p]
         _lib = L
@@ -200,11 +208,52 @@ class OracleSim:
     def mask(self):
         return self.alive[: int(self.row_ptr[-1])]
 
+    def mazars(self, thr, bd, kappa0, a_t=0.87, b_t=20000.0, a_c=0.65, b_c=2150.0):
+        """One computeDamageStatus (src/main_seq.cpp:473-598) from the current
+        displacements: thr / bd (per bond, family order, float64) are updated in
+        place; returns the per-particle damage status."""
+        assert thr.dtype == np.float64 and bd.dtype == np.float64 and thr.flags.c_contiguous and bd.flags.c_contiguous
+        status = np.zeros(self.x.shape[0])
+        mp = _Mazars(kappa0, a_t, b_t, a_c, b_c)
+        if lib().pdo_mazars_update(ctypes.byref(self._pb), ctypes.byref(self._st), ctypes.byref(mp),
+                                   _p(thr, _f64p), _p(bd, _f64p), _p(status, _f64p)) != 0:
+            raise ValueError("bond-associated Mazars damage: a family has more than 256 bonds")
+        return status
+
 
 # ------------------------------------------------------------ reference build
 
 def ref_available():
     return os.path.exists(REF_HARNESS)
+
+
+def run_ref_mazars(mesh_dir, n1, n2, out):
+    """The reference's computeDamageStatus on the Hassa mesh at two imposed
+    displacement levels (oracle/ref_harness.cpp, mode `mazars`)."""
+    subprocess.run([REF_HARNESS, "mazars", mesh_dir, str(n1), str(n2), out], check=True, capture_output=True)
+    b = open(out, "rb").read()
+    o = 0
+    n = struct.unpack_from("<i", b, o)[0]
+    o += 4
+    nnz = struct.unpack_from("<q", b, o)[0]
+    o += 8
+    res = {"n": n, "row_ptr": np.frombuffer(b, "<i8", n + 1, o).copy()}
+    o += 8 * (n + 1)
+    res["col"] = np.frombuffer(b, "<i4", nnz, o).copy()
+    o += 4 * nnz
+    for _ in range(2):
+        lv = struct.unpack_from("<i", b, o)[0]
+        o += 4
+        d = {"u": np.frombuffer(b, "<f8", 2 * n, o).reshape(n, 2).copy()}
+        o += 16 * n
+        d["thr"] = np.frombuffer(b, "<f8", nnz, o).copy()
+        o += 8 * nnz
+        d["bd"] = np.frombuffer(b, "<f8", nnz, o).copy()
+        o += 8 * nnz
+        d["status"] = np.frombuffer(b, "<f8", n, o).copy()
+        o += 8 * n
+        res[lv] = d
+    return res
 
 
 def read_ref_output(path, n_hint=None, hassa=False):

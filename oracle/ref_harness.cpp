@@ -11,7 +11,7 @@
 // precision (binary doubles), so that the project's C restatement (oracle/
 // pd_oracle.c) and the CUDA path can be checked against the reference itself.
 //
-// Two input modes:
+// Three input modes:
 //   hassa <mesh_dir> <out_dir> <n1> <n2> <nsteps> <out.bin>
 //       exactly the reference main (src/main_seq.cpp:601-715): reads
 //       2D_Hassa_test_mesh.dat from <mesh_dir>, dx=1, horizon=3, dt=1e-9,
@@ -20,6 +20,12 @@
 //   plate <in.bin> <out.bin>
 //       particles, parameters, optional families and BC lists from a binary
 //       file written by tests/golden/make_golden.py (format below).
+//   mazars <mesh_dir> <n1> <n2> <out.bin>
+//       the reference's Mazars damage (computeDamageStatus, src/main_seq.cpp:
+//       473-598) on the Hassa mesh, thresholds initialised as the reference
+//       main does (tensileStrength / E, :659-673), called on two imposed
+//       displacement fields in turn (mazars_field below); dumps u, the bond
+//       thresholds, bond damage and damageStatus after each call.
 //
 // Never part of the product: only tests/ and the fixture script run it.
 #include <cstdint>
@@ -54,6 +60,10 @@ void computeVelocity(int ndim, double n1, double n2, double horizon, double dx,
                      vector<Particle>& localParticles, const unordered_map<int, int>& globalLocalIDmap,
                      vector<vector<double>>& bondDamage);
 void storeVelocity(int ndim, std::vector<std::vector<long double>>& particles, const std::string& filename);
+void computeDamageStatus(int ndim, double n1, double n2, double dx, double horizon,
+                         vector<vector<double>>& bondDamageThreshold, vector<Particle>& localParticles,
+                         const vector<vector<Particle*>>& Neighborslist, vector<vector<double>>& bondDamage,
+                         const unordered_map<int, int>& globalLocalIDmap);
 
 namespace {
 
@@ -133,6 +143,17 @@ int run_steps(Problem& pb, int nsteps, int dump_every, Writer& w, bool dump_fam)
     if ((s + 1) % dump_every == 0 || s + 1 == nsteps) dump_step(w, s + 1, pb.P, vel, netF, acce);
   }
   return 0;
+}
+
+// Imposed displacement field of the Mazars fixture, level 1 or 2 (mm): a
+// homogeneous stretch-shear plus a smooth ripple.  Part of the mesh exceeds
+// the 3 / 3.5e4 threshold at level 1; level 2 stretches more but shifts the
+// ripple, so some bonds unload (their history threshold holds) while others
+// load further.
+void mazars_field(int level, long double X, long double Y, long double* ux, long double* uy) {
+  const long double e = level == 1 ? 1.0e-4L : 1.4e-4L, a = 4.0e-4L, ph = level == 1 ? 0.0L : 1.3L;
+  *ux = e * (X + 0.3L * Y) + a * sinl(0.23L * X + 0.11L * Y + ph);
+  *uy = -0.4L * e * Y + a * cosl(0.19L * Y - 0.07L * X + ph);
 }
 
 }  // namespace
@@ -261,6 +282,52 @@ int main(int argc, char** argv) {
     Writer w{fo};
     w.put<int32_t>(n);
     run_steps(pb, nsteps, dump_every, w, true);
+    fclose(fo);
+    return 0;
+  }
+  if (mode == "mazars") {
+    if (argc != 6) { fprintf(stderr, "mazars <mesh_dir> <n1> <n2> <out.bin>\n"); return 2; }
+    const double n1 = atof(argv[3]), n2 = atof(argv[4]);
+    long double dx = 1.0, horizon = 3.0;
+    vector<long double> boxlimit(4);
+    if (chdir(argv[2]) != 0) { perror("chdir mesh_dir"); return 2; }
+    vector<Particle> P = readMeshFile(boxlimit, dx);
+    findNeighbor(P, dx, horizon, 2);
+    for (auto& p : P) p.partitionID = 0;
+    const int n = (int)P.size();
+    unordered_map<int, int> g2l;
+    defineParticleIDmap(P, g2l);
+    vector<vector<Particle*>> NL;
+    buildLocalNeighborlist(2, (double)dx, (double)horizon, P, g2l, NL);
+    // src/main_seq.cpp:659-676
+    const long double E = 3.5e4, tensileStrength = 3.0;
+    const long double damageThreshold = tensileStrength / E;
+    vector<vector<double>> bondDamage(n + 1), bondDamageThreshold(n);
+    for (int i = 0; i < n; ++i) {
+      bondDamageThreshold[i].resize(NL[i].size(), damageThreshold);
+      bondDamage[i].resize(NL[i].size(), 0.0);
+    }
+    bondDamage[n].resize(30, 0.0);
+    FILE* fo = fopen(argv[5], "wb");
+    if (!fo) { perror("out"); return 2; }
+    Writer w{fo};
+    w.put<int32_t>(n);
+    dump_families(w, P);
+    for (int level = 1; level <= 2; ++level) {
+      for (auto& p : P) {
+        long double ux, uy;
+        mazars_field(level, p.initialPositions[0], p.initialPositions[1], &ux, &uy);
+        p.currentPositions[0] = p.initialPositions[0] + ux;
+        p.currentPositions[1] = p.initialPositions[1] + uy;
+      }
+      computeDamageStatus(2, n1, n2, (double)dx, (double)horizon, bondDamageThreshold, P, NL, bondDamage, g2l);
+      w.put<int32_t>(level);
+      for (const auto& p : P)
+        for (int m = 0; m < 2; ++m) w.put<double>((double)(p.currentPositions[m] - p.initialPositions[m]));
+      for (int i = 0; i < n; ++i) for (double t : bondDamageThreshold[i]) w.put<double>(t);
+      for (int i = 0; i < n; ++i) for (size_t k = 0; k < NL[i].size(); ++k) w.put<double>(bondDamage[i][k]);
+      for (const auto& p : P) w.put<double>(p.damageStatus);
+    }
     fclose(fo);
     return 0;
   }

@@ -22,6 +22,9 @@ Steps, each recorded in manifest.json:
  4. A seeded 30 x 30 SI plate (jitter, centre crack, 3-row +-1 m/s BCs):
     the reference's findNeighbor families (no crack) and 4 reference steps
     with the crack-cut families -> plate30_ref.npz.
+ 5. The reference's Mazars damage (computeDamageStatus) on the Hassa mesh,
+    classic and n1 = n2 = 10 weights, at two imposed displacement fields in
+    turn -> mazars_ref.npz.  `--only mazars` regenerates just this one.
 """
 from __future__ import annotations
 
@@ -62,17 +65,45 @@ def sha(path):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--only", choices=["mazars"], default=None)
     args = ap.parse_args()
     ref = args.reference
     if not po.ref_available():
         sys.exit("build the reference oracle first: make -C oracle ref")
-    man = {}
+    man_path = os.path.join(HERE, "manifest.json")
+    man = json.load(open(man_path)) if args.only and os.path.exists(man_path) else {}
     with tempfile.TemporaryDirectory() as td:
         # 1. mesh by rule
         mesh_dir = os.path.join(td, "mesh")
         os.makedirs(mesh_dir)
         mesh = os.path.join(mesh_dir, "2D_Hassa_test_mesh.dat")
         open(mesh, "w").write(hassa_mesh_lines())
+        if args.only != "mazars":
+            fixtures_1_to_4(ref, td, mesh_dir, mesh, man)
+        # 5. Mazars damage, classic and bond-associated weights
+        out = {"kappa0": np.float64(np.longdouble(3.0) / np.longdouble(3.5e4))}
+        for tag, w in (("c", 0), ("b", 10)):
+            r = po.run_ref_mazars(mesh_dir, w, w, os.path.join(td, f"mz{w}.bin"))
+            for lv in (1, 2):
+                out[f"u{lv}"] = r[lv]["u"]
+                out[f"{tag}_st{lv}"] = r[lv]["status"]
+            # per-bond history after both calls (level 1 enters through the statuses)
+            out[f"{tag}_thr2"], out[f"{tag}_bd2"] = r[2]["thr"], r[2]["bd"]
+            out[f"{tag}_updated1"] = int((r[1]["thr"] > out["kappa0"]).sum())
+        np.savez_compressed(os.path.join(HERE, "mazars_ref.npz"), **out)
+        man["mazars"] = {"mesh": "hassa", "weights": ["n1=n2=0", "n1=n2=10"], "levels": [1, 2],
+                         "kappa0": "3.0L / 3.5e4L (tensileStrength / E, src/main_seq.cpp:659)",
+                         "law": "a_t=0.87 b_t=20000 a_c=0.65 b_c=2150 (src/main_seq.cpp:481)",
+                         "bonds_updated_level1": {"classic": out["c_updated1"], "bond_associated": out["b_updated1"]}}
+    json.dump(man, open(man_path, "w"), indent=1, sort_keys=True)
+    print(json.dumps(man, indent=1, sort_keys=True))
+    bad = [k for k, v in man.items() if v is False]
+    if bad:
+        sys.exit(f"pinning failed: {bad}")
+
+
+def fixtures_1_to_4(ref, td, mesh_dir, mesh, man):
+    if True:
         ref_mesh = os.path.join(ref, "2D_Hassa_test_mesh.dat")
         man["hassa_mesh_rule_matches_reference"] = filecmp.cmp(mesh, ref_mesh, shallow=False) or bool(
             np.array_equal(np.loadtxt(mesh, skiprows=1), np.loadtxt(ref_mesh, skiprows=1)))
@@ -123,11 +154,6 @@ def main():
         man["plate30"] = {"generator": "plates.make_plate(30, seed=3, crack='centre-half')", "n": int(p.n),
                           "bonds_with_crack": int(rp_c[-1]), "bonds_reference_findNeighbor": int(rn["row_ptr"][-1]),
                           "steps": [1, 4]}
-    json.dump(man, open(os.path.join(HERE, "manifest.json"), "w"), indent=1, sort_keys=True)
-    print(json.dumps(man, indent=1, sort_keys=True))
-    bad = [k for k, v in man.items() if v is False]
-    if bad:
-        sys.exit(f"pinning failed: {bad}")
 
 
 if __name__ == "__main__":

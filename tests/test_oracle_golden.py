@@ -91,3 +91,39 @@ def test_oracle_planted_mistake_is_caught(po, hassa):
     sim._pb.E = sim.E
     sim.step(1)
     assert normwise(sim.f, hassa["c_f1"]) > F_TOL
+
+
+# Mazars damage (computeDamageStatus, src/main_seq.cpp:473-598) against the
+# reference run at two imposed displacement fields (tests/golden/mazars_ref.npz).
+MZ_TOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def mazars_ref():
+    return dict(np.load(os.path.join(GOLDEN, "mazars_ref.npz")))
+
+
+def mazars_oracle(po, h, weights):
+    dx, hor, E, nu, rho, dt = h["params"]
+    return po.OracleSim(h["x"], h["vol"], h["row_ptr"], h["col"], E=E, nu=nu, rho=rho, dt=dt, n1=weights,
+                        n2=weights, wlen=hor * dx)
+
+
+@pytest.mark.parametrize("tag,weights", [("c", 0.0), ("b", 10.0)])
+def test_mazars_matches_reference(po, hassa, mazars_ref, tag, weights):
+    m = mazars_ref
+    sim = mazars_oracle(po, hassa, weights)
+    nnz = int(hassa["row_ptr"][-1])
+    k0 = float(m["kappa0"])
+    thr, bd = np.full(nnz, k0), np.zeros(nnz)
+    sim.u[:] = m["u1"]
+    st1 = sim.mazars(thr, bd, k0)
+    assert int((thr > k0).sum()) == int(m[f"{tag}_updated1"])
+    assert np.abs(st1 - m[f"{tag}_st1"]).max() < MZ_TOL
+    sim.u[:] = m["u2"]
+    st2 = sim.mazars(thr, bd, k0)
+    assert np.abs(st2 - m[f"{tag}_st2"]).max() < MZ_TOL
+    assert np.abs(thr - m[f"{tag}_thr2"]).max() < MZ_TOL * np.abs(m[f"{tag}_thr2"]).max()
+    assert np.abs(bd - m[f"{tag}_bd2"]).max() < MZ_TOL
+    # the fixture exercises both branches at the second call: loading and unloading bonds
+    assert 0 < int((m[f"{tag}_thr2"] > k0).sum()) < nnz and 0.2 < m[f"{tag}_st2"].mean() < 0.9
