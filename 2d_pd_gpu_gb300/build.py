@@ -33,6 +33,7 @@ CUDA_UNITS = [
     ("pd_bondassoc.cu", ["--fmad=false"]),
     ("pd_mixed.cu", []),
     ("pd_noalloc.cu", ["--fmad=false"]),
+    ("pd_mazars.cu", ["--fmad=false"]),
     ("pd_probe.cu", []),
     ("pd_api.cu", []),
 ]

@@ -56,6 +56,9 @@ struct pd_ctx {
   double2* tb = nullptr;
   int64_t* rslot = nullptr;
   int32_t max_family = 0;
+  // Mazars damage history (pd_mazars_*)
+  double *mz_thr = nullptr, *mz_bd = nullptr, *mz_status = nullptr;
+  pd_mazars_params mz{};
   // counters (device) + host mirror of steps
   unsigned long long* counters = nullptr;
   int64_t steps = 0;
@@ -136,6 +139,9 @@ void free_families(pd_ctx* c) {
   dfree(c->sell.chunk_w);
   dfree(c->sell.nbr);
   dfree(c->sell.chunk_order);
+  dfree(c->mz_thr);
+  dfree(c->mz_bd);
+  dfree(c->mz_status);
   dfree(c->halo.visit);
   dfree(c->halo.loc);
   dfree(c->halo.loc0);
@@ -911,6 +917,113 @@ int pd_step(pd_ctx* c, int32_t nsteps) {
   return check_after_step(c);
 }
 
+// ---- Mazars damage
+namespace {
+
+pd::MazarsArgs mazars_args(pd_ctx* c) {
+  pd::MazarsArgs m{};
+  m.kappa0 = c->mz.kappa0;
+  m.a_t = c->mz.a_t;
+  m.b_t = c->mz.b_t;
+  m.a_c = c->mz.a_c;
+  m.b_c = c->mz.b_c;
+  m.thr = c->mz_thr;
+  m.bd = c->mz_bd;
+  m.status = c->mz_status;
+  return m;
+}
+
+bool bond_associated(const pd_ctx* c) { return c->p.n1 != 0.0 || c->p.n2 != 0.0; }
+
+}  // namespace
+
+void pd_mazars_default_params(pd_mazars_params* p) {
+  if (!p) return;
+  p->kappa0 = 3.0 / 3.5e4;
+  p->a_t = 0.87;
+  p->b_t = 20000.0;
+  p->a_c = 0.65;
+  p->b_c = 2150.0;
+}
+
+int pd_mazars_init(pd_ctx* c, const pd_mazars_params* p) {
+  if (!c || !p) return PD_ERR_ARG;
+  if (!c->has_families) return fail(c, PD_ERR_ORDER, "families first");
+  if (mixed(c)) return fail(c, PD_ERR_ARG, "Mazars damage needs PD_FP64");
+  if (!(p->kappa0 >= 0.0) || !std::isfinite(p->kappa0) || !std::isfinite(p->a_t) || !std::isfinite(p->b_t) ||
+      !std::isfinite(p->a_c) || !std::isfinite(p->b_c))
+    return fail(c, PD_ERR_ARG, "invalid Mazars parameters");
+  if (bond_associated(c) && c->max_family > 64)
+    return fail(c, PD_ERR_CAPACITY, "bond-associated Mazars damage: families are limited to 64 bonds");
+  PD_CK(c, cudaSetDevice(c->p.device));
+  PD_CK(c, cudaStreamSynchronize(c->stream));
+  const size_t ns = (size_t)(c->sell.nslots > 0 ? c->sell.nslots : 1), nn = (size_t)(c->n > 0 ? c->n : 1);
+  if (!c->mz_thr) PD_CK(c, cudaMalloc(&c->mz_thr, ns * sizeof(double)));
+  if (!c->mz_bd) PD_CK(c, cudaMalloc(&c->mz_bd, ns * sizeof(double)));
+  if (!c->mz_status) PD_CK(c, cudaMalloc(&c->mz_status, nn * sizeof(double)));
+  c->mz = *p;
+  pd::launch_mazars_reset(c->sell.nslots, c->n, mazars_args(c), c->stream);
+  PD_CK(c, cudaGetLastError());
+  PD_CK(c, cudaStreamSynchronize(c->stream));
+  return PD_OK;
+}
+
+int pd_mazars_update(pd_ctx* c) {
+  if (!c) return PD_ERR_ARG;
+  if (!c->mz_thr) return fail(c, PD_ERR_ORDER, "pd_mazars_init first");
+  PD_CK(c, cudaSetDevice(c->p.device));
+  const pd::BondAssoc ba = ba_args(c);
+  pd::launch_mazars_update(fp64_args(c), bond_associated(c) ? &ba : nullptr, mazars_args(c), c->stream);
+  PD_CK(c, cudaGetLastError());
+  return PD_OK;
+}
+
+int pd_mazars_get(pd_ctx* c, double* thr, double* bd, double* status) {
+  if (!c) return PD_ERR_ARG;
+  if (!c->mz_thr) return fail(c, PD_ERR_ORDER, "pd_mazars_init first");
+  PD_CK(c, cudaSetDevice(c->p.device));
+  cudaStream_t s = c->stream;
+  if ((thr || bd) && c->nnz > 0) {
+    double *dt = nullptr, *db = nullptr;
+    if (thr) PD_CK(c, cudaMallocAsync(&dt, (size_t)c->nnz * sizeof(double), s));
+    if (bd) PD_CK(c, cudaMallocAsync(&db, (size_t)c->nnz * sizeof(double), s));
+    pd::launch_mazars_to_csr(fp64_args(c), c->row_ptr, mazars_args(c), dt, db, s);
+    PD_CK(c, cudaGetLastError());
+    if (thr) PD_CK(c, cudaMemcpyAsync(thr, dt, (size_t)c->nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (bd) PD_CK(c, cudaMemcpyAsync(bd, db, (size_t)c->nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (dt) PD_CK(c, cudaFreeAsync(dt, s));
+    if (db) PD_CK(c, cudaFreeAsync(db, s));
+  }
+  if (status && c->n > 0)
+    PD_CK(c, cudaMemcpyAsync(status, c->mz_status, (size_t)c->n * sizeof(double), cudaMemcpyDeviceToHost, s));
+  PD_CK(c, cudaStreamSynchronize(s));
+  return PD_OK;
+}
+
+int pd_mazars_set(pd_ctx* c, const double* thr, const double* bd) {
+  if (!c) return PD_ERR_ARG;
+  if (!c->mz_thr) return fail(c, PD_ERR_ORDER, "pd_mazars_init first");
+  PD_CK(c, cudaSetDevice(c->p.device));
+  cudaStream_t s = c->stream;
+  if (c->nnz > 0) {
+    double *dt = nullptr, *db = nullptr;
+    if (thr) {
+      PD_CK(c, cudaMallocAsync(&dt, (size_t)c->nnz * sizeof(double), s));
+      PD_CK(c, cudaMemcpyAsync(dt, thr, (size_t)c->nnz * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    if (bd) {
+      PD_CK(c, cudaMallocAsync(&db, (size_t)c->nnz * sizeof(double), s));
+      PD_CK(c, cudaMemcpyAsync(db, bd, (size_t)c->nnz * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    pd::launch_mazars_from_csr(fp64_args(c), c->row_ptr, mazars_args(c), dt, db, s);
+    PD_CK(c, cudaGetLastError());
+    if (dt) PD_CK(c, cudaFreeAsync(dt, s));
+    if (db) PD_CK(c, cudaFreeAsync(db, s));
+  }
+  PD_CK(c, cudaStreamSynchronize(s));
+  return PD_OK;
+}
+
 // ---- checkpoint / restore
 namespace {
 
@@ -920,6 +1033,8 @@ struct CkptHeader {
   int64_t n, nslots, nnz, steps;
   uint64_t problem;  // FNV-1a of the reference positions, volumes, families layout and parameters
   unsigned long long counters[pd::CNT_N];
+  int32_t mazars, pad;   // 1: the Mazars history follows the state arrays
+  pd_mazars_params mz;
 };
 
 uint64_t fnv1a(uint64_t h, const void* p, size_t bytes) {
@@ -959,6 +1074,11 @@ std::vector<std::pair<void*, size_t>> ckpt_arrays(pd_ctx* c) {
   a.push_back({c->broken, n * sizeof(int32_t)});
   a.push_back({c->damage, n * sizeof(double)});
   a.push_back({c->sell.nbr, ns * sizeof(int32_t)});
+  if (c->mz_thr) {
+    a.push_back({c->mz_thr, ns * sizeof(double)});
+    a.push_back({c->mz_bd, ns * sizeof(double)});
+    a.push_back({c->mz_status, n * sizeof(double)});
+  }
   return a;
 }
 
@@ -994,6 +1114,8 @@ int pd_checkpoint_save(pd_ctx* c, void* buf, int64_t bytes) {
   h.nnz = c->nnz;
   h.steps = c->steps;
   h.problem = problem_hash(c);
+  h.mazars = c->mz_thr ? 1 : 0;
+  h.mz = c->mz;
   PD_CK(c, cudaMemcpy(h.counters, c->counters, sizeof(h.counters), cudaMemcpyDeviceToHost));
   unsigned char* o = static_cast<unsigned char*>(buf);
   std::memcpy(o, &h, sizeof(h));
@@ -1008,8 +1130,6 @@ int pd_checkpoint_save(pd_ctx* c, void* buf, int64_t bytes) {
 int pd_checkpoint_load(pd_ctx* c, const void* buf, int64_t bytes) {
   if (!c || !buf) return PD_ERR_ARG;
   if (!c->has_families) return fail(c, PD_ERR_ORDER, "families first");
-  int64_t need = 0;
-  ckpt_bytes(c, &need);
   CkptHeader h;
   if (bytes < (int64_t)sizeof(h)) return fail(c, PD_ERR_ARG, "not a checkpoint (too short)");
   std::memcpy(&h, buf, sizeof(h));
@@ -1018,9 +1138,21 @@ int pd_checkpoint_load(pd_ctx* c, const void* buf, int64_t bytes) {
   if (h.precision != c->p.precision) return fail(c, PD_ERR_ARG, "checkpoint precision differs from the context's");
   if (h.n != c->n || h.nslots != c->sell.nslots || h.nnz != c->nnz || h.problem != problem_hash(c))
     return fail(c, PD_ERR_ARG, "checkpoint of another problem (particles, families or parameters differ)");
-  if (bytes < need) return fail(c, PD_ERR_ARG, "checkpoint truncated");
   PD_CK(c, cudaSetDevice(c->p.device));
   PD_CK(c, cudaStreamSynchronize(c->stream));
+  // the Mazars history follows the blob: allocated if it has one, dropped if not
+  if (h.mazars && !c->mz_thr) {
+    const int rc = pd_mazars_init(c, &h.mz);
+    if (rc != PD_OK) return rc;
+  } else if (!h.mazars && c->mz_thr) {
+    dfree(c->mz_thr);
+    dfree(c->mz_bd);
+    dfree(c->mz_status);
+  }
+  c->mz = h.mz;
+  int64_t need = 0;
+  ckpt_bytes(c, &need);
+  if (bytes < need) return fail(c, PD_ERR_ARG, "checkpoint truncated");
   const unsigned char* p = static_cast<const unsigned char*>(buf) + sizeof(h);
   for (const auto& x : ckpt_arrays(c)) {
     if (x.second) PD_CK(c, cudaMemcpy(x.first, p, x.second, cudaMemcpyHostToDevice));

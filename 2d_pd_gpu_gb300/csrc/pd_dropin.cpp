@@ -469,6 +469,54 @@ void compute_velocity_GPU_host(int, double n1, double n2, double horizon, double
                true);
 }
 
+void computeDamageStatus(int, double n1, double n2, double dx, double horizon,
+                         vector<vector<double>>& bondDamageThreshold, vector<Particle>& localParticles,
+                         const vector<vector<Particle*>>& Neighborslist, vector<vector<double>>& bondDamage,
+                         const unordered_map<int, int>&) {
+  vector<Particle>& P = localParticles;
+  const size_t n = P.size();
+  // the particle vector's context (computeVelocity's, or a new one whose
+  // material parameters computeVelocity replaces later: Mazars needs none)
+  auto it = cache().find(&P);
+  const bool have = it != cache().end() && it->second && it->second->data == P.data() && it->second->n == n;
+  matrix C = have ? matrix() : getStiffnessTensor(2, 1.0, 0.0);
+  if (have) {
+    C = matrix(3, vector<long double>(9, 0.0));
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) C.elements[r][c] = it->second->C[3 * r + c];
+  }
+  Cached& k = context_for(P, const_cast<vector<vector<Particle*>>&>(Neighborslist),
+                          have ? it->second->rho : 1.0L, have ? it->second->dt : 1.0L, C, n1, n2, horizon * dx);
+  for (size_t i = 0; i < n; ++i)
+    for (int m = 0; m < 2; ++m) k.u[2 * i + m] = (double)(P[i].currentPositions[m] - P[i].initialPositions[m]);
+  check(pd_set_state(k.ctx, k.u, nullptr, nullptr), k.ctx, "pd_set_state");
+  vector<double> thr, bd;
+  for (size_t i = 0; i < n; ++i) {
+    const size_t deg = Neighborslist.at(i).size();
+    if (bondDamageThreshold.at(i).size() < deg || bondDamage.at(i).size() < deg)
+      throw std::runtime_error("computeDamageStatus: bondDamageThreshold / bondDamage rows shorter than the families");
+    thr.insert(thr.end(), bondDamageThreshold[i].begin(), bondDamageThreshold[i].begin() + deg);
+    bd.insert(bd.end(), bondDamage[i].begin(), bondDamage[i].begin() + deg);
+  }
+  pd_mazars_params mp;
+  pd_mazars_default_params(&mp);
+  if (!thr.empty()) mp.kappa0 = thr[0];
+  check(pd_mazars_init(k.ctx, &mp), k.ctx, "pd_mazars_init");
+  check(pd_mazars_set(k.ctx, thr.data(), bd.data()), k.ctx, "pd_mazars_set");
+  check(pd_mazars_update(k.ctx), k.ctx, "pd_mazars_update");
+  vector<double> status(n);
+  check(pd_mazars_get(k.ctx, thr.data(), bd.data(), status.data()), k.ctx, "pd_mazars_get");
+  size_t o = 0;
+  for (size_t i = 0; i < n; ++i) {
+    const size_t deg = Neighborslist[i].size();
+    std::copy(thr.begin() + o, thr.begin() + o + deg, bondDamageThreshold[i].begin());
+    std::copy(bd.begin() + o, bd.begin() + o + deg, bondDamage[i].begin());
+    o += deg;
+    P[i].damageStatus = status[i];
+  }
+  if (bondDamage.size() > n) bondDamage[n].resize(30, 0.0);  // the reference's ghost row (src/main_seq.cpp:596)
+}
+
 void pd_dropin_set_critical_stretch(double s_c) { g_s_c = s_c; }
 
 void pd_dropin_damage(const vector<Particle>& P, vector<double>& damage) {

@@ -82,6 +82,14 @@ struct BondAssoc {
   int64_t* rslot;  // slot of the reverse bond (j, i)
 };
 
+// Mazars damage (pd_mazars.cu): law constants and per-slot history.
+struct MazarsArgs {
+  double kappa0, a_t, b_t, a_c, b_c;
+  double* thr;     // per SELL slot: history threshold
+  double* bd;      // per SELL slot: bond damage
+  double* status;  // per particle: sum of bond damage / family size
+};
+
 // Chunk a warp runs in the mixed single-plate passes, in visiting order.
 struct alignas(16) VisitRec {
   int32_t chunk, w;  // chunk id, width (slot rows)
@@ -173,6 +181,14 @@ int batch_occupancy_fp64(const BatchLaunch& cfg);  // resident persistent blocks
 void launch_ba_reverse(const Fp64Args& a, const BondAssoc& b, cudaStream_t s);
 void launch_ba_pass_a(const Fp64Args& a, const BondAssoc& b, cudaStream_t s);
 void launch_ba_pass_b(const Fp64Args& a, const BondAssoc& b, int mode, cudaStream_t s);
+
+// ---- Mazars damage (pd_mazars.cu), FP64 contexts; ba != nullptr: bond-associated weights
+void launch_mazars_reset(int64_t nslots, int64_t n, const MazarsArgs& m, cudaStream_t s);
+void launch_mazars_update(const Fp64Args& a, const BondAssoc* ba, const MazarsArgs& m, cudaStream_t s);
+void launch_mazars_to_csr(const Fp64Args& a, const int64_t* row_ptr, const MazarsArgs& m, double* thr_csr,
+                          double* bd_csr, cudaStream_t s);
+void launch_mazars_from_csr(const Fp64Args& a, const int64_t* row_ptr, const MazarsArgs& m, const double* thr_csr,
+                            const double* bd_csr, cudaStream_t s);
 
 // ---- mixed step (pd_mixed.cu)
 void launch_init_geometry_mixed(const MixedArgs& a, cudaStream_t s);

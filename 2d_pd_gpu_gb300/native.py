@@ -28,6 +28,20 @@ class PdError(RuntimeError):
         self.code = code
 
 
+class MazarsParams(ctypes.Structure):
+    """pd_mazars_params (include/pd_gb300.h)."""
+    _fields_ = [("kappa0", ctypes.c_double), ("a_t", ctypes.c_double), ("b_t", ctypes.c_double),
+                ("a_c", ctypes.c_double), ("b_c", ctypes.c_double)]
+
+
+def mazars_default_params(**kw):
+    p = MazarsParams()
+    lib().pd_mazars_default_params(ctypes.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
 class Params(ctypes.Structure):
     _fields_ = [
         ("precision", ctypes.c_int32),
@@ -92,6 +106,11 @@ _SIGS = {
     "pd_get_damage": [_vp, _vp],
     "pd_get_bond_mask": [_vp, _vp],
     "pd_get_counters": [_vp, ctypes.POINTER(Counters)],
+    "pd_mazars_default_params": [_vp],
+    "pd_mazars_init": [_vp, _vp],
+    "pd_mazars_update": [_vp],
+    "pd_mazars_get": [_vp, _vp, _vp, _vp],
+    "pd_mazars_set": [_vp, _vp, _vp],
     "pd_checkpoint_size": [_vp, ctypes.POINTER(ctypes.c_int64)],
     "pd_checkpoint_save": [_vp, _vp, ctypes.c_int64],
     "pd_checkpoint_load": [_vp, _vp, ctypes.c_int64],
@@ -119,7 +138,8 @@ _SIGS = {
     "pd_host_alloc": [ctypes.c_int64, ctypes.POINTER(_vp)],
     "pd_host_free": [_vp],
 }
-_RESTYPES = {"pd_default_params": None, "pd_last_error": ctypes.c_char_p, "pd_batch_last_error": ctypes.c_char_p}
+_RESTYPES = {"pd_default_params": None, "pd_mazars_default_params": None, "pd_last_error": ctypes.c_char_p,
+             "pd_batch_last_error": ctypes.c_char_p}
 
 EXPORTED = tuple(_SIGS)
 
@@ -297,6 +317,25 @@ class Context:
         self._ck(lib().pd_get_counters(self._h, ctypes.byref(c)))
         return {"bonds_broken": c.bonds_broken, "singular_events": c.singular_events, "steps": c.steps,
                 "device_error": c.device_error}
+
+    # -- Mazars damage (pd_mazars_*)
+    def mazars_init(self, params=None, **kw):
+        p = params if params is not None else mazars_default_params(**kw)
+        self._ck(lib().pd_mazars_init(self._h, ctypes.byref(p)))
+
+    def mazars_update(self):
+        self._ck(lib().pd_mazars_update(self._h))
+
+    def mazars(self):
+        """(threshold[nnz], bond_damage[nnz]) in family order and status[n]."""
+        thr, bd, st = np.empty(self.nnz), np.empty(self.nnz), np.empty(self.n)
+        self._ck(lib().pd_mazars_get(self._h, ptr(thr), ptr(bd), ptr(st)))
+        return thr, bd, st
+
+    def mazars_set(self, threshold=None, bond_damage=None):
+        t = None if threshold is None else np.ascontiguousarray(threshold, dtype=np.float64)
+        b = None if bond_damage is None else np.ascontiguousarray(bond_damage, dtype=np.float64)
+        self._ck(lib().pd_mazars_set(self._h, ptr(t) if t is not None else None, ptr(b) if b is not None else None))
 
     # -- checkpoint / restore (pd_checkpoint_*)
     def checkpoint(self) -> bytes:

@@ -104,6 +104,16 @@ void compute_velocity_GPU_host(int ndim, double n1, double n2, double horizon, d
                                vector<vector<long double>>& netF, vector<Particle>& allParticles,
                                const unordered_map<int, int>& globalLocalIDmap, vector<vector<double>>& bondDamage);
 
+// The reference's Mazars damage (src/main_seq.cpp:473-598) on the GPU
+// (pd_mazars_*): from the particles' current positions, updates the per-bond
+// thresholds and damage in place and sets each Particle::damageStatus.  The
+// tensile / compressive strain parts start at zero (the reference leaves
+// them uninitialised).
+void computeDamageStatus(int ndim, double n1, double n2, double dx, double horizon,
+                         vector<vector<double>>& bondDamageThreshold, vector<Particle>& localParticles,
+                         const vector<vector<Particle*>>& Neighborslist, vector<vector<double>>& bondDamage,
+                         const unordered_map<int, int>& globalLocalIDmap);
+
 // ---- drop-in controls (no reference counterpart)
 // Critical stretch for the GPU contexts the drop-in creates (default 0: no
 // bond breaking, as the reference).  Broken bonds then persist across calls,

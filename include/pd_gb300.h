@@ -182,6 +182,28 @@ int pd_checkpoint_size(pd_ctx* ctx, int64_t* bytes);
 int pd_checkpoint_save(pd_ctx* ctx, void* buf, int64_t bytes);
 int pd_checkpoint_load(pd_ctx* ctx, const void* buf, int64_t bytes);
 
+/* ---------------------------------------------------------- Mazars damage
+ * The reference's damage law (computeDamageStatus, src/main_seq.cpp:473-598,
+ * called at the start of each step of its main, :683; it does not feed the
+ * forces).  Per bond: history threshold and damage; per particle: damage
+ * status = sum of its bonds' damage / family size.  FP64 contexts, classic
+ * or bond-associated weights (the context's n1, n2).  The tensile and
+ * compressive strain parts start at zero (the reference leaves them
+ * uninitialised, :509-515). */
+typedef struct pd_mazars_params {
+  double kappa0;              /* initial threshold: tensile strength / E (reference main: 3 / 3.5e4) */
+  double a_t, b_t, a_c, b_c;  /* 0.87, 20000, 0.65, 2150 (src/main_seq.cpp:481) */
+} pd_mazars_params;
+void pd_mazars_default_params(pd_mazars_params* p);
+/* Allocates the history (thresholds = kappa0, damage = 0).  Families first. */
+int pd_mazars_init(pd_ctx* ctx, const pd_mazars_params* p);
+/* One computeDamageStatus from the context's current displacements
+ * (asynchronous on the context's stream). */
+int pd_mazars_update(pd_ctx* ctx);
+/* Per-bond history in family (CSR) order and per-particle status; any NULL. */
+int pd_mazars_get(pd_ctx* ctx, double* threshold, double* bond_damage, double* status);
+int pd_mazars_set(pd_ctx* ctx, const double* threshold, const double* bond_damage);
+
 /* ------------------------------------------------------------------ step */
 
 /* nsteps full steps on the device (one CUDA graph per distinct nsteps).

@@ -7,15 +7,62 @@
 //   output/LocalParticlesPositions_rank_0step_0.txt
 //   dropin_state.bin: per step int32 step, then u, v, netF as n x 2 doubles
 // Usage: dropin_main <nsteps> <gpu-wrapper 0/1> [n1 n2]
+//        dropin_main mazars <n1>: the reference's Mazars damage
+//        (computeDamageStatus) at the two imposed displacement fields of the
+//        reference fixture (same field as oracle/ref_harness.cpp), writing
+//        dropin_mazars.bin: per level thresholds, bond damage (family order)
+//        and damageStatus as doubles.
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <iostream>
 #include <sys/stat.h>
 
 #include "pd_dropin.h"
 
+static int mazars_main(double n1) {
+  vector<Particle> P;
+  long double dx = 1.0, horizon = 3.0;
+  vector<long double> boxlimit(4);
+  P = readMeshFile(boxlimit, dx);
+  findNeighbor(P, dx, horizon, 2);
+  for (auto& p : P) p.partitionID = 0;
+  const int n = (int)P.size();
+  unordered_map<int, int> g2l;
+  defineParticleIDmap(P, g2l);
+  vector<vector<Particle*>> NL;
+  buildLocalNeighborlist(2, (double)dx, (double)horizon, P, g2l, NL);
+  const long double E = 3.5e4, tensileStrength = 3.0;
+  const long double damageThreshold = tensileStrength / E;
+  vector<vector<double>> bondDamage(n + 1), thr(n);
+  for (int i = 0; i < n; ++i) {
+    thr[i].resize(NL[i].size(), damageThreshold);
+    bondDamage[i].resize(NL[i].size(), 0.0);
+  }
+  bondDamage[n].resize(30, 0.0);
+  FILE* fo = fopen("dropin_mazars.bin", "wb");
+  for (int level = 1; level <= 2; ++level) {
+    const long double e = level == 1 ? 1.0e-4L : 1.4e-4L, a = 4.0e-4L, ph = level == 1 ? 0.0L : 1.3L;
+    for (auto& p : P) {
+      const long double X = p.initialPositions[0], Y = p.initialPositions[1];
+      p.currentPositions[0] = X + e * (X + 0.3L * Y) + a * sinl(0.23L * X + 0.11L * Y + ph);
+      p.currentPositions[1] = Y + (-0.4L * e * Y + a * cosl(0.19L * Y - 0.07L * X + ph));
+    }
+    computeDamageStatus(2, n1, n1, (double)dx, (double)horizon, thr, P, NL, bondDamage, g2l);
+    for (int i = 0; i < n; ++i) fwrite(thr[i].data(), sizeof(double), thr[i].size(), fo);
+    for (int i = 0; i < n; ++i) fwrite(bondDamage[i].data(), sizeof(double), NL[i].size(), fo);
+    for (const auto& p : P) fwrite(&p.damageStatus, sizeof(double), 1, fo);
+  }
+  fclose(fo);
+  pd_dropin_release();
+  std::cout << "dropin mazars ok " << n << " particles" << std::endl;
+  return 0;
+}
+
 int main(int argc, char** argv) {
+  if (argc > 2 && std::strcmp(argv[1], "mazars") == 0) return mazars_main(atof(argv[2]));
   const int nsteps = argc > 1 ? atoi(argv[1]) : 1;
   const bool gpu_wrapper = argc > 2 && atoi(argv[2]) != 0;
   vector<Particle> allParticles;

@@ -14,7 +14,7 @@ import pytest
 from conftest import GOLDEN, ROOT, normwise
 from test_oracle_golden import F_TOL, V_TOL, u_tol
 
-REFERENCE_NAMES = ["computeInitialPositions", "readMeshFile", "findNeighbor", "defineParticleIDmap",
+REFERENCE_NAMES = ["computeInitialPositions", "readMeshFile", "findNeighbor", "defineParticleIDmap", "computeDamageStatus",
                    "defineBoundarySet", "outputLocalParticlesPositions", "storeVelocity", "applyDispBC",
                    "applyVelocityBC", "applyFixedBC", "buildLocalNeighborlist", "getStiffnessTensor",
                    "updatePositions", "computeVelocity", "compute_velocity_GPU_host"]
@@ -103,3 +103,25 @@ def test_dropin_reference_main_matches_reference(pdg, hassa, tmp_path, gpu_wrapp
     assert len(txt) == n
     vals = np.array([[float(t) for t in l.split()] for l in txt])
     assert normwise(vals, hassa["c_v1"]) < 1e-5  # 6 significant digits
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tag,w", [("c", 0), ("b", 10)])
+def test_dropin_compute_damage_status_matches_reference(pdg, hassa, tmp_path, tag, w):
+    """computeDamageStatus through the drop-in (GPU) against the reference's
+    own run at the same two imposed displacement fields."""
+    from test_oracle_golden import MZ_TOL
+
+    mz = dict(np.load(os.path.join(GOLDEN, "mazars_ref.npz")))
+    tmp = str(tmp_path)
+    exe = _build_driver(pdg, tmp)
+    _hassa_mesh(os.path.join(tmp, "2D_Hassa_test_mesh.dat"))
+    subprocess.run([exe, "mazars", str(w)], cwd=tmp, check=True, capture_output=True, timeout=300)
+    n, nnz = hassa["x"].shape[0], int(hassa["row_ptr"][-1])
+    a = np.fromfile(os.path.join(tmp, "dropin_mazars.bin"), "<f8")
+    assert a.size == 2 * (2 * nnz + n)
+    lv1, lv2 = a[: 2 * nnz + n], a[2 * nnz + n:]
+    assert np.abs(lv1[2 * nnz:] - mz[f"{tag}_st1"]).max() < MZ_TOL
+    assert np.abs(lv2[:nnz] - mz[f"{tag}_thr2"]).max() < MZ_TOL * np.abs(mz[f"{tag}_thr2"]).max()
+    assert np.abs(lv2[nnz:2 * nnz] - mz[f"{tag}_bd2"]).max() < MZ_TOL
+    assert np.abs(lv2[2 * nnz:] - mz[f"{tag}_st2"]).max() < MZ_TOL
