@@ -758,19 +758,18 @@ int pd_set_state(pd_ctx* c, const double* u, const double* v, const double* f) {
   PD_CK(c, cudaStreamSynchronize(c->stream));
   const size_t b = (size_t)c->n * sizeof(double2);
   if (b == 0) return PD_OK;
-  if (u) PD_CK(c, cudaMemcpy(c->u, u, b, cudaMemcpyHostToDevice));
-  if (v) PD_CK(c, cudaMemcpy(c->v, v, b, cudaMemcpyHostToDevice));
-  if (f) PD_CK(c, cudaMemcpy(c->f, f, b, cudaMemcpyHostToDevice));
-  if (mixed(c)) {
-    if (!c->has_families) return fail(c, PD_ERR_ORDER, "mixed form: families first (they fix the scales)");
-    pd::launch_to_mixed(mixed_args(c), u ? c->u : nullptr, v ? c->v : nullptr, f ? c->f : nullptr, c->stream);
-    PD_CK(c, cudaGetLastError());
-    PD_CK(c, cudaStreamSynchronize(c->stream));
-  } else if (u && c->has_families) {
-    pd::launch_shadow_fp64(fp64_args(c), c->stream);
-    PD_CK(c, cudaGetLastError());
-    PD_CK(c, cudaStreamSynchronize(c->stream));
-  }
+  if (mixed(c) && !c->has_families) return fail(c, PD_ERR_ORDER, "mixed form: families first (they fix the scales)");
+  // one stream, one wait: copies from page-locked buffers run at full link speed
+  cudaStream_t s = c->stream;
+  if (u) PD_CK(c, cudaMemcpyAsync(c->u, u, b, cudaMemcpyHostToDevice, s));
+  if (v) PD_CK(c, cudaMemcpyAsync(c->v, v, b, cudaMemcpyHostToDevice, s));
+  if (f) PD_CK(c, cudaMemcpyAsync(c->f, f, b, cudaMemcpyHostToDevice, s));
+  if (mixed(c))
+    pd::launch_to_mixed(mixed_args(c), u ? c->u : nullptr, v ? c->v : nullptr, f ? c->f : nullptr, s);
+  else if (u && c->has_families)
+    pd::launch_shadow_fp64(fp64_args(c), s);
+  PD_CK(c, cudaGetLastError());
+  PD_CK(c, cudaStreamSynchronize(s));
   return PD_OK;
 }
 
@@ -781,15 +780,16 @@ int pd_get_state(pd_ctx* c, double* u, double* v, double* f) {
   PD_CK(c, cudaStreamSynchronize(c->stream));
   const size_t b = (size_t)c->n * sizeof(double2);
   if (b == 0) return PD_OK;
+  if (mixed(c) && !c->has_families) return fail(c, PD_ERR_ORDER, "mixed form: families first (they fix the scales)");
+  cudaStream_t s = c->stream;
   if (mixed(c)) {
-    if (!c->has_families) return fail(c, PD_ERR_ORDER, "mixed form: families first (they fix the scales)");
-    pd::launch_from_mixed(mixed_args(c), u ? c->u : nullptr, v ? c->v : nullptr, f ? c->f : nullptr, c->stream);
+    pd::launch_from_mixed(mixed_args(c), u ? c->u : nullptr, v ? c->v : nullptr, f ? c->f : nullptr, s);
     PD_CK(c, cudaGetLastError());
-    PD_CK(c, cudaStreamSynchronize(c->stream));
   }
-  if (u) PD_CK(c, cudaMemcpy(u, c->u, b, cudaMemcpyDeviceToHost));
-  if (v) PD_CK(c, cudaMemcpy(v, c->v, b, cudaMemcpyDeviceToHost));
-  if (f) PD_CK(c, cudaMemcpy(f, c->f, b, cudaMemcpyDeviceToHost));
+  if (u) PD_CK(c, cudaMemcpyAsync(u, c->u, b, cudaMemcpyDeviceToHost, s));
+  if (v) PD_CK(c, cudaMemcpyAsync(v, c->v, b, cudaMemcpyDeviceToHost, s));
+  if (f) PD_CK(c, cudaMemcpyAsync(f, c->f, b, cudaMemcpyDeviceToHost, s));
+  PD_CK(c, cudaStreamSynchronize(s));
   return PD_OK;
 }
 

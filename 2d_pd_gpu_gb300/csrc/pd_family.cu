@@ -35,10 +35,33 @@ __device__ __forceinline__ bool crosses(double px, double py, double qx, double 
   return ((o1 > 0.0 && o2 < 0.0) || (o1 < 0.0 && o2 > 0.0)) && ((o3 > 0.0 && o4 < 0.0) || (o3 < 0.0 && o4 > 0.0));
 }
 
+// Bounding boxes of the crack segments (FP32, widened by a margin): a bond
+// whose box misses a crack's box cannot properly cross it, so the exact FP64
+// test runs only near cracks.
+__constant__ float c_crack_box[PD_MAX_CRACKS * 4];
+
 struct Grid {
   double x0, y0, inv_cs;
   int64_t gx, gy;
+  float c2_lo, c2_hi;  // cutoff^2 (1 -+ 4e-6): FP32 accept / reject bounds of the pair test
 };
+
+// The pair test sqrt(d2) < cutoff of the oracle, decided in FP32 when the
+// FP32 squared distance is clearly inside or outside.  rx, ry are the exact
+// FP64 differences; rounding them to FP32 and the FP32 squares and sum move
+// d2 by < 2.5e-7 relative, far inside the 4e-6 band, so only pairs within the
+// band (none on a jittered lattice) take the exact FP64 path.
+__device__ __forceinline__ bool within_cutoff(double rx, double ry, double cutoff, const Grid& G) {
+  const float fx = (float)rx, fy = (float)ry;
+  const float q = fmaf(fx, fx, fy * fy);
+  if (q < G.c2_lo) return true;
+  if (q > G.c2_hi) return false;
+  return sqrt(rx * rx + ry * ry) < cutoff;
+}
+
+__device__ __forceinline__ bool near_crack(float ax, float ay, float bx, float by, const float* box) {
+  return fmaxf(ax, bx) >= box[0] && fminf(ax, bx) <= box[2] && fmaxf(ay, by) >= box[1] && fminf(ay, by) <= box[3];
+}
 
 __device__ __forceinline__ int64_t cell_coord(double v, double v0, double inv_cs, int64_t g) {
   int64_t c = (int64_t)floor((v - v0) * inv_cs);
@@ -87,11 +110,11 @@ __global__ void k_family(int64_t n, const double2* __restrict__ x, Grid G, const
         const int32_t j = items[k];
         if ((int64_t)j == i) continue;
         const double2 pj = x[j];
-        const double rx = pj.x - pi.x, ry = pj.y - pi.y;
-        const double d2 = rx * rx + ry * ry;
-        if (!(sqrt(d2) < cutoff)) continue;
+        if (!within_cutoff(pj.x - pi.x, pj.y - pi.y, cutoff, G)) continue;
         bool cut = false;
-        for (int q = 0; q < n_cracks && !cut; ++q) cut = crosses(pi.x, pi.y, pj.x, pj.y, c_cracks + 4 * q);
+        for (int q = 0; q < n_cracks && !cut; ++q)
+          cut = near_crack((float)pi.x, (float)pi.y, (float)pj.x, (float)pj.y, c_crack_box + 4 * q) &&
+                crosses(pi.x, pi.y, pj.x, pj.y, c_cracks + 4 * q);
         if (cut) continue;
         if (FILL) {
           if (cnt < PD_MAX_FAMILY) {
@@ -340,9 +363,32 @@ int build_families_gpu(int64_t n, const double2* d_x, const double* h_x, double 
   G.x0 = xmin;
   G.y0 = ymin;
   G.inv_cs = 1.0 / cs;
+  const double c2 = cutoff * cutoff;
+  if (c2 > 1e-30 && c2 < 1e30) {  // FP32 pre-filter only where FP32 holds c^2 with full precision
+    G.c2_lo = (float)(c2 * (1.0 - 4e-6));
+    G.c2_hi = (float)(c2 * (1.0 + 4e-6));
+  } else {
+    G.c2_lo = -1.0f;
+    G.c2_hi = INFINITY;
+  }
   const int64_t nc = G.gx * G.gy;
-  if (n_cracks > 0)
+  if (n_cracks > 0) {
     cudaMemcpyToSymbolAsync(c_cracks, h_cracks, sizeof(double) * 4 * n_cracks, 0, cudaMemcpyHostToDevice, s);
+    // crack boxes widened by far more than the FP32 rounding of any coordinate
+    double big = fmax(fmax(fabs(xmin), fabs(xmax)), fmax(fabs(ymin), fabs(ymax)));
+    for (int q = 0; q < 4 * n_cracks; ++q) big = fmax(big, fabs(h_cracks[q]));
+    const double m = 1e-5 * big + 1e-300;
+    float box[PD_MAX_CRACKS * 4];
+    for (int q = 0; q < n_cracks; ++q) {
+      const double* c = h_cracks + 4 * q;
+      box[4 * q + 0] = (float)(fmin(c[0], c[2]) - m);
+      box[4 * q + 1] = (float)(fmin(c[1], c[3]) - m);
+      box[4 * q + 2] = (float)(fmax(c[0], c[2]) + m);
+      box[4 * q + 3] = (float)(fmax(c[1], c[3]) + m);
+    }
+    cudaMemcpyToSymbolAsync(c_crack_box, box, sizeof(float) * 4 * n_cracks, 0, cudaMemcpyHostToDevice, s);
+    cudaStreamSynchronize(s);  // box lives on this stack frame
+  }
 
   int64_t *cell_of = nullptr, *cell_start = nullptr, *deg = nullptr;
   unsigned long long *cnt = nullptr, *counters = nullptr;

@@ -40,7 +40,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-MEASURED_FP64_DFMA_PER_S = 5.98e11  # DFMA warp-lane issue rate measured on this GB300 (profiles/fp64_alu_peak.md)
+MEASURED_FP64_DFMA_PER_S = 6.27e11  # FP64 FMA rate of this GB300 (profiles/fp64_fma_rate_probe.txt), if the live probe fails
 
 
 def load_peaks():
@@ -369,7 +369,7 @@ def run_ours(args, comm):
         peak64, peak32 = nat.probe_fma_rates(device)
         src = "pd_probe_fma_rates on this GPU, measured in this run"
     except Exception:
-        peak64, peak32, src = MEASURED_FP64_DFMA_PER_S, None, "recorded DFMA rate (profiles/fp64_alu_peak.md)"
+        peak64, peak32, src = MEASURED_FP64_DFMA_PER_S, None, "recorded DFMA rate (profiles/fp64_fma_rate_probe.txt)"
     result["fp64_alu"] = {"ops_per_s": ops, "peak_ops_per_s": peak64, "frac": ops / peak64,
                           "ops_per_step": fp64_ops(n, nb), "peak_source": src, "fp32_fma_per_s": peak32}
     # end to end through the public API with pinned host buffers, every step
