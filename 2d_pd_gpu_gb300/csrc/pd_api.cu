@@ -194,6 +194,17 @@ int check_params(pd_ctx* c, const pd_params* p) {
 
 bool bond_assoc(const pd_ctx* c) { return c->p.n1 != 0.0 || c->p.n2 != 0.0; }
 
+// Device-side address of a page-locked host buffer (nullptr if it is not one).
+void* mapped_host(const void* p) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
+  return at.devicePointer;
+}
+
 void stiffness(const pd_ctx* c, double* c11, double* c12, double* c33);
 
 Fp64Args fp64_args(pd_ctx* c) {
@@ -1173,6 +1184,45 @@ int pd_checkpoint_load(pd_ctx* c, const void* buf, int64_t bytes) {
   PD_CK(c, cudaStreamSynchronize(s));
   c->steps = h.steps;
   return PD_OK;
+}
+
+
+int pd_step_host(pd_ctx* c, int32_t nsteps, const double* u_in, const double* v_in, const double* f_in, double* u_out,
+                 double* v_out, double* f_out) {
+  if (!c) return PD_ERR_ARG;
+  if (!c->has_families) return fail(c, PD_ERR_ORDER, "families first");
+  if (mixed(c)) return fail(c, PD_ERR_ARG, "pd_step_host: PD_FP64 contexts (use pd_set_state / pd_get_state)");
+  if (nsteps < 1) return fail(c, PD_ERR_ARG, "pd_step_host: nsteps >= 1");
+  if (!u_in || !v_in || !f_in || !u_out || !v_out || !f_out) return fail(c, PD_ERR_ARG, "pd_step_host: NULL buffer");
+  if (c->n == 0) return PD_OK;
+  PD_CK(c, cudaSetDevice(c->p.device));
+  Fp64Args in = fp64_args(c), out = fp64_args(c);
+  in.in_u = static_cast<const double2*>(mapped_host(u_in));
+  in.in_v = static_cast<const double2*>(mapped_host(v_in));
+  in.in_f = static_cast<const double2*>(mapped_host(f_in));
+  out.out_u = static_cast<double2*>(mapped_host(u_out));
+  out.out_v = static_cast<double2*>(mapped_host(v_out));
+  out.out_f = static_cast<double2*>(mapped_host(f_out));
+  if (!in.in_u || !in.in_v || !in.in_f || !out.out_u || !out.out_v || !out.out_f)
+    return fail(c, PD_ERR_ARG, "pd_step_host: buffers must be page-locked host memory (pd_host_alloc)");
+  cudaStream_t s = c->stream;
+  const Fp64Args plain = fp64_args(c);
+  const bool brk = c->p.s_c > 0.0;
+  pd::launch_drift_fp64(in, s);  // reads the state over the CPU-GPU link
+  for (int32_t k = 0; k < nsteps; ++k) {
+    const bool last = k + 1 == nsteps;
+    if (bond_assoc(c)) {
+      pd::launch_ba_pass_a(plain, ba_args(c), s);
+      pd::launch_ba_pass_b(last ? out : plain, ba_args(c), last ? 0 : 1, s);
+    } else {
+      pd::launch_pass_a_fp64(plain, brk, s);
+      pd::launch_pass_b_fp64(last ? out : plain, last ? 0 : 1, s);  // the last writes the state back
+    }
+  }
+  PD_CK(c, cudaGetLastError());
+  PD_CK(c, cudaStreamSynchronize(s));
+  c->steps += nsteps;
+  return check_after_step(c);
 }
 
 int pd_synchronize(pd_ctx* c) {

@@ -156,6 +156,11 @@ __global__ void __launch_bounds__(kBlock) k_ba_pass_b(Fp64Args a, BondAssoc b) {
     a.u[i] = u;
   }
   a.v[i] = v;
+  if (a.out_v) {  // pd_step_host's last pass
+    a.out_u[i] = a.u[i];
+    a.out_v[i] = v;
+    a.out_f[i] = make_double2(fx, fy);
+  }
 }
 
 // rslot[s] = slot of (j, i) in j's SELL rows, for every slot s = (i, j).

@@ -87,8 +87,9 @@ __device__ __forceinline__ void drift_one(const Fp64Args& a, int64_t i, double2&
 }
 
 __device__ __forceinline__ void drift_particle(const Fp64Args& a, int64_t i) {
-  double2 v = a.v[i], u = a.u[i];
-  const double2 f = a.f[i];
+  double2 v = a.in_v ? a.in_v[i] : a.v[i], u = a.in_u ? a.in_u[i] : a.u[i];
+  const double2 f = a.in_f ? a.in_f[i] : a.f[i];
+  if (a.in_f) a.f[i] = f;
   drift_one(a, i, v, u, f.x * a.inv_rho, f.y * a.inv_rho);
   a.v[i] = v;
   a.u[i] = u;
@@ -249,6 +250,11 @@ __device__ __forceinline__ void pass_b_particle(const Fp64Args& a, int64_t i) {
     a.u32[i] = make_float2((float)u.x, (float)u.y);
   }
   a.v[i] = v;
+  if (a.out_v) {  // pd_step_host's last pass: the state straight to host memory
+    a.out_u[i] = a.u[i];
+    a.out_v[i] = v;
+    a.out_f[i] = make_double2(fx, fy);
+  }
 }
 
 template <int MODE, bool HG>

@@ -68,6 +68,15 @@ struct Fp64Args {
   const float* __restrict__ br2;  // (s_c |xi|)^2 (1 - 1e-5), rounded toward 0: FP32 stretch certificate
   float2* u32;                    // u rounded to FP32 (shadow for the certificate)
   double2* hg;  // 2 k_hg sum_j V_j (u_j - u_i), pass A -> pass B
+  // pd_step_host: the drift takes the state from page-locked host memory
+  // (read over the CPU-GPU link by the kernel itself) and the last pass B
+  // writes it back there; null otherwise
+  const double2* in_u;
+  const double2* in_v;
+  const double2* in_f;
+  double2* out_u;
+  double2* out_v;
+  double2* out_f;
   double c11, c12, c33;
   double dt, dt2, inv_rho, det_guard, k_hg, damage_fail;
   unsigned long long* counters;

@@ -115,6 +115,7 @@ _SIGS = {
     "pd_checkpoint_save": [_vp, _vp, ctypes.c_int64],
     "pd_checkpoint_load": [_vp, _vp, ctypes.c_int64],
     "pd_step": [_vp, ctypes.c_int32],
+    "pd_step_host": [_vp, ctypes.c_int32, _vp, _vp, _vp, _vp, _vp, _vp],
     "pd_synchronize": [_vp],
     "pd_compute_velocity": [_vp, _vp, _vp, _vp, _vp],
     "pd_step_timed": [_vp, ctypes.c_int32, ctypes.POINTER(ctypes.c_float)],
@@ -351,6 +352,15 @@ class Context:
         self._ck(lib().pd_checkpoint_load(self._h, buf, len(blob)))
 
     # -- stepping
+    def step_host(self, nsteps, u, v, f, u_out=None, v_out=None, f_out=None):
+        """pd_step_host: u, v, f ([n][2], page-locked: PinnedArray.array) in,
+        the new state written to the *_out buffers (default: in place)."""
+        u_out = u if u_out is None else u_out
+        v_out = v if v_out is None else v_out
+        f_out = f if f_out is None else f_out
+        self._ck(lib().pd_step_host(self._h, int(nsteps), ptr(u), ptr(v), ptr(f), ptr(u_out), ptr(v_out),
+                                    ptr(f_out)))
+
     def step(self, nsteps=1):
         self._ck(lib().pd_step(self._h, int(nsteps)))
 

@@ -189,3 +189,29 @@ def test_gpu_singular_policy(pdg):
             ctx.step(2)
             u, v, f = ctx.state()
             assert np.all(f == 0.0) and ctx.counters()["singular_events"] == 3
+
+
+def test_gpu_step_host_equals_staged_copies(pdg):
+    """pd_step_host (state read / written by the kernels over the CPU-GPU
+    link) is pd_set_state + pd_step + pd_get_state, bit for bit."""
+    p = pdg.plates.make_plate(90, seed=4, crack="centre-half")
+    p.material.s_c = 2e-4
+    a = p.context()
+    b = p.context()
+    a.step(7)
+    b.step(7)
+    u, v, f = a.state()
+    bufs = [pdg.native.PinnedArray((p.n, 2)) for _ in range(3)]
+    hu, hv, hf = (x.array for x in bufs)
+    hu[:], hv[:], hf[:] = u, v, f
+    for nsteps in (1, 3):
+        a.set_state(u=hu, v=hv, f=hf)
+        a.step(nsteps)
+        ua, va, fa = a.state()
+        b.step_host(nsteps, hu, hv, hf)
+        assert np.array_equal(ua, hu) and np.array_equal(va, hv) and np.array_equal(fa, hf)
+        assert np.array_equal(a.bond_mask(), b.bond_mask())
+    with pytest.raises(pdg.PdError):  # pageable numpy memory is refused
+        b.step_host(1, u.copy(), v.copy(), f.copy())
+    for x in bufs:
+        x.free()
