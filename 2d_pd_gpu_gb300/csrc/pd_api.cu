@@ -907,7 +907,10 @@ int pd_step(pd_ctx* c, int32_t nsteps) {
   if (!c) return PD_ERR_ARG;
   if (!c->has_families) return fail(c, PD_ERR_ORDER, "families first");
   if (nsteps < 0) return fail(c, PD_ERR_ARG, "nsteps < 0");
-  if (nsteps == 0 || c->n == 0) return PD_OK;
+  if (nsteps == 0 || c->n == 0) {
+    c->steps += nsteps;
+    return PD_OK;
+  }
   PD_CK(c, cudaSetDevice(c->p.device));
   auto it = c->graphs.find(nsteps);
   if (it == c->graphs.end()) {

@@ -1,0 +1,101 @@
+"""Edge cases of the device path against the oracle: empty and tiny
+problems, partial SELL chunks and blocks, ragged families (holes), the
+largest families the layout takes, and family overflow."""
+import dataclasses
+
+import numpy as np
+import pytest
+
+from conftest import normwise, plate_oracle
+from test_gpu_fp64_parity import _assert_same
+
+pytestmark = pytest.mark.gpu
+
+
+def _subset(p, keep):
+    keep = np.asarray(keep)
+    return dataclasses.replace(p, x=np.ascontiguousarray(p.x[keep]), vol=np.ascontiguousarray(p.vol[keep]),
+                               group_of=np.ascontiguousarray(p.group_of[keep]))
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_empty_problem(pdg, precision):
+    ctx = pdg.native.Context(pdg.default_params(precision=precision))
+    ctx.set_particles(np.zeros((0, 2)), np.zeros(0))
+    ctx.build_families(1.0)
+    ctx.step(3)
+    u, v, f = ctx.state()
+    assert u.shape == (0, 2) and ctx.nnz == 0 and ctx.counters()["steps"] == 3
+
+
+@pytest.mark.parametrize("n", [1, 2, 31, 33, 35, 257])
+def test_tiny_and_partial_chunks_bit_exact(pdg, po, n):
+    """n not a multiple of the 32-particle chunk or the 256-particle block."""
+    p = _subset(pdg.plates.make_plate(20, seed=6, crack="centre-half"), np.arange(n))
+    p.material.s_c = 2e-4
+    ctx = p.context()
+    sim = plate_oracle(po, p)
+    ctx.step(15)
+    sim.step(15)
+    _assert_same(ctx, sim)
+    m = p.context(precision=pdg.native.PD_MIXED)
+    m.step(15)
+    u = ctx.state()[0]
+    if np.abs(u).max() > 0:
+        assert normwise(m.state()[0], u) < 1e-6
+
+
+def test_ragged_families_with_holes(pdg, po):
+    """Two circular holes and a slot: families from 0 to 28 bonds, particles
+    with no neighbours (singular), SELL chunks of very different widths."""
+    p = pdg.plates.make_plate(64, seed=8, crack="centre-half")
+    p.material.s_c = 3e-4
+    c = p.x / p.dx
+    hole = (((c[:, 0] - 10) ** 2 + (c[:, 1] - 8) ** 2) < 81) | (((c[:, 0] + 12) ** 2 + (c[:, 1] + 5) ** 2) < 20)
+    slot = (np.abs(c[:, 1] - 20) < 1.2) & (c[:, 0] > -5)
+    lone = np.zeros_like(hole)
+    for cx, cy in ((10, 8), (-12, -5)):  # one isolated particle left at each hole's centre
+        lone[np.argmin((c[:, 0] - cx) ** 2 + (c[:, 1] - cy) ** 2)] = True
+    q = _subset(p, np.nonzero(~(hole | slot) | lone)[0])
+    ctx = q.context()
+    sim = plate_oracle(po, q)
+    fam = np.diff(sim.row_ptr)
+    assert fam.min() == 0 and fam.max() >= 26
+    for chunk in (5, 20):
+        ctx.step(chunk)
+        sim.step(chunk)
+        _assert_same(ctx, sim)
+    m = q.context(precision=pdg.native.PD_MIXED)
+    m.step(25)
+    assert normwise(m.state()[0], ctx.state()[0]) < 1e-6
+    assert np.array_equal(m.bond_mask(), ctx.bond_mask())
+
+
+def test_largest_families(pdg, po):
+    """Horizon 5.9 dx: ~109 bonds per particle, close to PD_MAX_FAMILY = 128."""
+    p = pdg.plates.make_plate(40, seed=2, horizon=5.9, crack="centre-half")
+    ctx = p.context(s_c=0.0)
+    sim = plate_oracle(po, p, s_c=0.0)
+    assert 100 <= np.diff(sim.row_ptr).max() <= 128
+    ctx.step(6)
+    sim.step(6)
+    _assert_same(ctx, sim)
+    m = p.context(precision=pdg.native.PD_MIXED, s_c=0.0)
+    m.step(6)
+    assert normwise(m.state()[0], ctx.state()[0]) < 1e-6
+
+
+def test_family_overflow_is_an_error(pdg):
+    p = pdg.plates.make_plate(30, seed=2, horizon=7.0)  # ~154 bonds > PD_MAX_FAMILY
+    with pytest.raises(pdg.PdError):
+        p.context()
+
+
+def test_bad_particles_rejected(pdg):
+    ctx = pdg.native.Context(pdg.default_params())
+    with pytest.raises(pdg.PdError):
+        ctx.set_particles(np.array([[0.0, 0.0], [np.nan, 1.0]]), np.ones(2))
+    with pytest.raises(pdg.PdError):
+        ctx.set_particles(np.array([[0.0, 0.0], [1.0, 1.0]]), np.array([1.0, 0.0]))
+    with pytest.raises(pdg.PdError):
+        ctx.step(1)  # no families yet
