@@ -182,6 +182,12 @@ def cpu_step_rate(plate, steps, nthreads, s_c=None):
     return int(rp[-1]), dt
 
 
+def replica_plate(pdg, side, seed, rank):
+    """The plate rank `rank` steps: the same size on every rank (weak scaling),
+    its own seed (jitter and crack), so replicas are independent solves."""
+    return pdg.plates.config_plate_scale(side=side, seed=seed + rank)
+
+
 def run_reference(args, comm):
     """Reference arm: the oracle's C restatement of the reference step, all host cores."""
     if comm.rank != 0:
@@ -345,7 +351,7 @@ def run_serve(args, pdg, device, capacity, configs):
 def run_ours(args, comm):
     pdg = importlib.import_module("2d_pd_gpu_gb300")
     nat = pdg.native
-    plate = pdg.plates.config_plate_scale(side=args.side, seed=args.seed + comm.rank)
+    plate = replica_plate(pdg, args.side, args.seed, comm.rank)
     device = comm.local
     sampler = ClockSampler(device)
     sampler.start()
