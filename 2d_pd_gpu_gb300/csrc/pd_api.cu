@@ -145,6 +145,7 @@ void free_families(pd_ctx* c) {
   dfree(c->halo.visit);
   dfree(c->halo.loc);
   dfree(c->halo.loc0);
+  dfree(c->halo.self_loc);
   dfree(c->halo.halo);
   dfree(c->halo.halo_n);
   c->halo = pd::HaloLayout{};
@@ -279,6 +280,7 @@ pd::MixedArgs mixed_args(pd_ctx* c) {
   a.chunk_order = c->sell.chunk_order;
   a.visit = c->halo.visit;
   a.loc = c->halo.loc;
+  a.self_loc = c->halo.self_loc;
   a.halo = c->halo.halo;
   a.halo_n = c->halo.halo_n;
   a.halo_cap = pd::kHaloCap;
@@ -741,7 +743,7 @@ int pd_reset(pd_ctx* c) {
   PD_CK(c, cudaMemsetAsync(c->counters, 0, pd::CNT_N * sizeof(unsigned long long), s));
   pd::launch_sell_reset(c->n, c->row_ptr, c->col, c->sell, s);
   if (mixed(c)) {
-    pd::launch_halo_relink(c->sell.nslots, c->sell.nbr, c->halo, s);
+    pd::launch_halo_relink(mixed_args(c), c->halo, s);
     PD_CK(c, cudaMemsetAsync(c->us, 0, nn * sizeof(float4), s));
     PD_CK(c, cudaMemsetAsync(c->vsm, 0, nn * sizeof(float4), s));
     PD_CK(c, cudaMemsetAsync(c->ws, 0, nn * sizeof(float4), s));
@@ -1176,7 +1178,7 @@ int pd_checkpoint_load(pd_ctx* c, const void* buf, int64_t bytes) {
   // the FP32 shadows (FP64 form) or the live halo indices (mixed form)
   cudaStream_t s = c->stream;
   if (mixed(c)) {
-    pd::launch_halo_relink(c->sell.nslots, c->sell.nbr, c->halo, s);
+    pd::launch_halo_relink(mixed_args(c), c->halo, s);
     pd::launch_init_geometry_mixed(mixed_args(c), s);
   } else {
     pd::launch_init_geometry_fp64(fp64_args(c), s);

@@ -131,7 +131,9 @@ struct MixedArgs {
   int32_t* nbr;
   const int32_t* __restrict__ chunk_order;  // warp w of a pass runs chunk chunk_order[w]
   const VisitRec* __restrict__ visit;       // the same, with the chunk's width and first slot
-  uint16_t* loc;                            // per slot: position in the block's halo (0xFFFF: padding / broken)
+  uint16_t* loc;                            // per slot: position in the block's halo (padding / broken: the
+                                            // particle's own position, whose data adds exact zeros)
+  const uint16_t* __restrict__ self_loc;    // per particle: its own position in its block's halo
   const int32_t* __restrict__ halo;         // per block: halo particle ids (halo_cap entries per block)
   const int32_t* __restrict__ halo_n;       // per block: halo size, -1 = not staged
   int32_t halo_cap, halo_max;               // halo_max: largest halo (multiple of 8), sizes shared memory
@@ -207,12 +209,13 @@ struct HaloLayout {
   VisitRec* visit = nullptr;
   uint16_t* loc = nullptr;   // live 16-bit indices
   uint16_t* loc0 = nullptr;  // pristine (all bonds intact)
+  uint16_t* self_loc = nullptr;
   int32_t* halo = nullptr;
   int32_t* halo_n = nullptr;
   int32_t halo_max = 0;
 };
 int build_halo_mixed(const MixedArgs& a, int64_t nslots, cudaStream_t s, HaloLayout* out, std::string* msg);
-void launch_halo_relink(int64_t nslots, const int32_t* nbr, const HaloLayout& h, cudaStream_t s);
+void launch_halo_relink(const MixedArgs& a, const HaloLayout& h, cudaStream_t s);
 void launch_drift_mixed(const MixedArgs& a, cudaStream_t s);
 void launch_pass_a_mixed(const MixedArgs& a, bool breaking, cudaStream_t s);
 void launch_pass_b_mixed(const MixedArgs& a, bool drift, cudaStream_t s);

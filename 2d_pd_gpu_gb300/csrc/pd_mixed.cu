@@ -53,7 +53,8 @@ __device__ __forceinline__ void tf_add2(float& hi, float& lo, float dh, float dl
 // (x, y) work, so one instruction does both components.
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+// a - b as one FFMA2: b * -1 is exact, so the single rounding is that of a - b
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 // (hi_j + lo_j) - (hi_i + lo_i) for two-float 2-vectors {hi.x, hi.y, lo.x, lo.y}
@@ -176,10 +177,11 @@ struct NbB {
 struct PreA {
   float4 ui, xi, geo;
   int singular;
+  int self_l;  // own halo position (staged blocks)
 };
 
 __device__ __forceinline__ PreA load_a(const MixedArgs& a, int64_t i) {
-  return PreA{a.us[i], a.xs[i], a.geo[i], a.singular[i]};
+  return PreA{a.us[i], a.xs[i], a.geo[i], a.singular[i], a.self_loc ? (int)a.self_loc[i] : 0};
 }
 
 // Pass A of particle i: slots s0 + 32 k, k < w; idx(k) gives a slot's
@@ -201,7 +203,7 @@ __device__ __forceinline__ void pass_a_core(const MixedArgs& a, int64_t i, const
       if (q.x + q.y > a.s2 * (ee.x + ee.y)) {
         const int64_t s = s0 + (int64_t)k * kChunk;
         a.nbr[s] = -2 - a.nbr[s];  // the particle id of slot s (j may be a halo position)
-        if (a.loc) a.loc[s] = 0xFFFF;
+        if (a.loc) a.loc[s] = (uint16_t)pre.self_l;  // the slot now adds exact zeros
         ++newly;
         return;
       }
@@ -546,7 +548,7 @@ inline size_t pass_smem_bytes(const MixedArgs& a, bool pass_a) {
 __device__ __forceinline__ int decode_nbr(int v) { return v >= 0 ? v : (v <= -2 ? -2 - v : -1); }
 
 __global__ void __launch_bounds__(kBlock) k_halo_build(MixedArgs a, int32_t* halo, int32_t* halo_n, uint16_t* loc,
-                                                       uint16_t* loc0) {
+                                                       uint16_t* loc0, uint16_t* self_loc) {
   __shared__ uint32_t bits[kHaloSpanWords];
   __shared__ int32_t pre[kHaloSpanWords];
   __shared__ int32_t wsum[kBlock / 32];
@@ -630,23 +632,26 @@ __global__ void __launch_bounds__(kBlock) k_halo_build(MixedArgs a, int32_t* hal
           m &= m - 1u;
         }
       }
+      auto pos = [&](int j) {
+        const int d = j - L;
+        return (uint16_t)(pre[d >> 5] + __popc(bits[d >> 5] & ((1u << (d & 31)) - 1u)));
+      };
+      const uint16_t self = i >= 0 ? pos((int)i) : (uint16_t)0;
+      if (i >= 0) self_loc[i] = self;
       for (int k = 0; k < w; ++k) {
         const int64_t s = s0 + (int64_t)k * kChunk;
         const int v = a.nbr[s];
         const int j = decode_nbr(v);
-        uint16_t l = 0xFFFF;
-        if (j >= 0) {
-          const int d = j - L;
-          l = (uint16_t)(pre[d >> 5] + __popc(bits[d >> 5] & ((1u << (d & 31)) - 1u)));
-        }
+        const uint16_t l = j >= 0 ? pos(j) : self;  // padding: the particle itself (adds exact zeros)
         loc0[s] = l;
-        loc[s] = v >= 0 ? l : (uint16_t)0xFFFF;
+        loc[s] = v >= 0 ? l : self;
       }
       return;
     }
   }
-  // too wide or too many: the block reads neighbour data from HBM
+  // too wide or too many: the block reads neighbour data from HBM (loc unused)
   if (tid == 0) halo_n[blockIdx.x] = -1;
+  if (i >= 0) self_loc[i] = 0;
   for (int k = 0; k < w; ++k) {
     const int64_t s = s0 + (int64_t)k * kChunk;
     loc0[s] = 0xFFFF;
@@ -663,11 +668,20 @@ __global__ void k_visit_build(int64_t nchunks, const int32_t* __restrict__ order
   visit[k] = VisitRec{c, chunk_w[c], chunk_base[c]};
 }
 
-// live 16-bit indices from the pristine ones and the int32 mask (after a reset)
-__global__ void k_halo_relink(int64_t nslots, const int32_t* __restrict__ nbr, const uint16_t* __restrict__ loc0,
+// live 16-bit indices from the pristine ones and the int32 mask (after a
+// reset or a restore): broken slots point at the particle itself
+__global__ void k_halo_relink(MixedArgs a, const uint16_t* __restrict__ loc0, const uint16_t* __restrict__ self_loc,
                               uint16_t* loc) {
-  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (s < nslots) loc[s] = nbr[s] >= 0 ? loc0[s] : (uint16_t)0xFFFF;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const int64_t c = i >> 5;
+  const int w = a.chunk_w[c];
+  const int64_t s0 = a.chunk_base[c] + (i & 31);
+  const uint16_t self = self_loc[i];
+  for (int k = 0; k < w; ++k) {
+    const int64_t s = s0 + (int64_t)k * kChunk;
+    loc[s] = a.nbr[s] >= 0 ? loc0[s] : self;
+  }
 }
 
 // ---- batched plates (see pd_batch.cuh): phase 0 drift, 1 pass A, 2 pass B +
@@ -889,13 +903,14 @@ int build_halo_mixed(const MixedArgs& a, int64_t nslots, cudaStream_t s, HaloLay
   if (cudaMalloc(&h->visit, (size_t)nch * sizeof(VisitRec)) != cudaSuccess ||
       cudaMalloc(&h->loc, ns * sizeof(uint16_t)) != cudaSuccess ||
       cudaMalloc(&h->loc0, ns * sizeof(uint16_t)) != cudaSuccess ||
+      cudaMalloc(&h->self_loc, (size_t)a.n * sizeof(uint16_t)) != cudaSuccess ||
       cudaMalloc(&h->halo, (size_t)nb * kHaloCap * sizeof(int32_t)) != cudaSuccess ||
       cudaMalloc(&h->halo_n, (size_t)nb * sizeof(int32_t)) != cudaSuccess) {
     *msg = "halo staging: out of device memory";
     return PD_ERR_CUDA;
   }
   k_visit_build<<<(unsigned)blocks_for(nch), kBlock, 0, s>>>(nch, a.chunk_order, a.chunk_w, a.chunk_base, h->visit);
-  k_halo_build<<<(unsigned)nb, kBlock, 0, s>>>(a, h->halo, h->halo_n, h->loc, h->loc0);
+  k_halo_build<<<(unsigned)nb, kBlock, 0, s>>>(a, h->halo, h->halo_n, h->loc, h->loc0, h->self_loc);
   std::vector<int32_t> cnt((size_t)nb);
   cudaError_t e = cudaMemcpyAsync(cnt.data(), h->halo_n, (size_t)nb * sizeof(int32_t), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -913,8 +928,8 @@ int build_halo_mixed(const MixedArgs& a, int64_t nslots, cudaStream_t s, HaloLay
   return PD_OK;
 }
 
-void launch_halo_relink(int64_t nslots, const int32_t* nbr, const HaloLayout& h, cudaStream_t s) {
-  if (nslots > 0 && h.loc) k_halo_relink<<<(unsigned)blocks_for(nslots), kBlock, 0, s>>>(nslots, nbr, h.loc0, h.loc);
+void launch_halo_relink(const MixedArgs& a, const HaloLayout& h, cudaStream_t s) {
+  if (a.n > 0 && h.loc) k_halo_relink<<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a, h.loc0, h.self_loc, h.loc);
 }
 
 }  // namespace pd

@@ -74,20 +74,19 @@ __device__ __forceinline__ bool stage_chunk(int32_t* dst, const int32_t* src, in
 
 // Index of slot k of lane `lane` in a staged int32 chunk.
 struct SharedIdx {
+  static constexpr bool kDense = false;
   const int32_t* base;
   int lane;
   __device__ __forceinline__ int operator()(int k) const { return base[k * 32 + lane]; }
 };
 
-// Halo index of slot k of lane `lane` in a staged 16-bit chunk (0xFFFF:
-// padding or broken -> -1).
+// Halo position of slot k of lane `lane` in a staged 16-bit chunk; padding
+// and broken slots hold the particle's own position (dense: never negative).
 struct SharedHaloIdx {
+  static constexpr bool kDense = true;
   const uint16_t* base;
   int lane;
-  __device__ __forceinline__ int operator()(int k) const {
-    const int v = base[k * 32 + lane];
-    return v == 0xFFFF ? -1 : v;
-  }
+  __device__ __forceinline__ int operator()(int k) const { return base[k * 32 + lane]; }
 };
 
 }  // namespace pd

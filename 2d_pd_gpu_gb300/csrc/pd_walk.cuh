@@ -11,7 +11,9 @@
 //
 // idx(k) returns the neighbour index of the particle's slot k (from global
 // memory or from a staged shared-memory copy); body(k, j, g) gets the slot
-// number k, the index j >= 0 and the gathered data.
+// number k, the index j >= 0 and the gathered data.  An index source with
+// kDense = true never yields a negative index (padding and broken slots
+// point at data that contributes exact zeros), so the bodies run unguarded.
 #pragma once
 #include <cstdint>
 
@@ -26,20 +28,28 @@ __device__ __forceinline__ void walk_bonds(int w, int64_t self, Idx idx, Gather 
 #pragma unroll
     for (int q = 0; q < U; ++q) j[q] = idx(k + q);
     G g[U];
+    if constexpr (Idx::kDense) {
 #pragma unroll
-    for (int q = 0; q < U; ++q) g[q] = gather(j[q] < 0 ? self : (int64_t)j[q]);
+      for (int q = 0; q < U; ++q) g[q] = gather((int64_t)j[q]);
 #pragma unroll
-    for (int q = 0; q < U; ++q)
-      if (j[q] >= 0) body(k + q, j[q], g[q]);
+      for (int q = 0; q < U; ++q) body(k + q, j[q], g[q]);
+    } else {
+#pragma unroll
+      for (int q = 0; q < U; ++q) g[q] = gather(j[q] < 0 ? self : (int64_t)j[q]);
+#pragma unroll
+      for (int q = 0; q < U; ++q)
+        if (j[q] >= 0) body(k + q, j[q], g[q]);
+    }
   }
   for (; k < w; ++k) {
     const int jj = idx(k);
-    if (jj >= 0) body(k, jj, gather((int64_t)jj));
+    if (Idx::kDense || jj >= 0) body(k, jj, gather((int64_t)jj));
   }
 }
 
 // Streaming (evict-first) load of global slot s0 + 32 k of a SELL-32 row.
 struct GlobalIdx {
+  static constexpr bool kDense = false;
   const int32_t* nbr;
   int64_t s0;
   __device__ __forceinline__ int operator()(int k) const { return __ldcs(&nbr[s0 + (int64_t)k * 32]); }

@@ -34,7 +34,7 @@ from . import native, plates
 # geometry, staging, CSR, SELL and per-bond data; the mixed form adds its
 # halo lists (2048 ids per 256 particles) and two 16-bit halo indices per
 # slot.  Used for admission.
-FOOTPRINT = {native.PD_FP64: (215.0, 4.0 + 48.0 + 4.0), native.PD_MIXED: (230.0 + 32.0, 4.0 + 4.0 + 4.0 + 4.0)}
+FOOTPRINT = {native.PD_FP64: (215.0, 4.0 + 48.0 + 4.0), native.PD_MIXED: (230.0 + 34.0, 4.0 + 4.0 + 4.0 + 4.0)}
 
 
 @dataclass
