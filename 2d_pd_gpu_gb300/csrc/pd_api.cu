@@ -332,12 +332,12 @@ __global__ void k_fam_from_rowptr(int64_t n, const int64_t* rp, int32_t* fam) {
 // 32 consecutive particles; for the usual row-major numbering it is a short
 // row segment (long axis along x).  Chunks are ordered by (band, column,
 // row) on a grid whose cells are the median chunk extent along the long axis
-// and along the short axis, with bands of 8 cells across: the 8 warps of a
-// 256-thread block then run 8 chunks stacked across their long axis (32
-// columns x 8 rows of a row-major plate), so the block's neighbour gathers
-// touch about half as many distinct particles as 8 consecutive chunks would
-// and mostly hit L1.  The particle order, and with it every array the API
-// exposes, is unchanged.
+// and along the short axis, with bands of kHaloBlock / 32 cells across: the
+// warps of a visiting block then run chunks stacked across their long axis
+// (32 columns x 8 rows of a row-major plate), so the block's bonds reach
+// about half as many distinct particles (its halo) as 8 consecutive chunks
+// would.  The particle order, and with it every array the API exposes, is
+// unchanged.
 std::vector<int32_t> chunk_visit_order(const std::vector<double>& x, int64_t n, double min_cell) {
   const int64_t nch = (n + 31) / 32;
   std::vector<int32_t> order((size_t)nch);
@@ -388,7 +388,7 @@ std::vector<int32_t> chunk_visit_order(const std::vector<double>& x, int64_t n, 
     const double l = ((long_x ? cx[(size_t)ch] : cy[(size_t)ch]) - lo_l) / ql;
     const double t = ((long_x ? cy[(size_t)ch] : cx[(size_t)ch]) - lo_s) / qs;
     const int64_t row = (int64_t)std::floor(t);
-    key[(size_t)ch] = {row >> 3, (int64_t)std::floor(l), row, (int32_t)ch};
+    key[(size_t)ch] = {row / (pd::kHaloBlock / 32), (int64_t)std::floor(l), row, (int32_t)ch};
   }
   std::sort(key.begin(), key.end());
   for (int64_t k = 0; k < nch; ++k) order[(size_t)k] = key[(size_t)k].ch;
@@ -1382,10 +1382,10 @@ int batch_refresh(pd_batch* b) {
       const pd::MixedArgs m = mixed_args(c);
       std::memcpy(plates.data() + k * asz, &m, asz);
       b->smem = std::max(b->smem, pd::mixed_pass_smem(m));
-      // one tile per visiting block (256 particles) of the plate
-      for (int64_t blk = 0; blk * pd::kBlock < c->n; ++blk)
+      // one tile per visiting block (kHaloBlock particles) of the plate
+      for (int64_t blk = 0; blk * pd::kHaloBlock < c->n; ++blk)
         tiles.push_back(
-            pd::BatchTile{(int32_t)k, (int32_t)std::min<int64_t>(pd::kBlock, c->n - blk * pd::kBlock), blk});
+            pd::BatchTile{(int32_t)k, (int32_t)std::min<int64_t>(pd::kHaloBlock, c->n - blk * pd::kHaloBlock), blk});
     } else {
       const Fp64Args f = fp64_args(c);
       std::memcpy(plates.data() + k * asz, &f, asz);

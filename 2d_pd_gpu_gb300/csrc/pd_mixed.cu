@@ -323,7 +323,7 @@ struct GatherB {
 struct HaloSmem {  // dynamic shared memory carve-up of a halo block
   float4* q0;      // pass A: u^, pass B: x^
   float4* q1;      // pass A: x^, pass B: W^
-  uint16_t* li;    // 8 warps x wmax x 32 halo indices
+  uint16_t* li;    // kHaloBlock / 32 warps x wmax x 32 halo indices
   float* vh;       // pass A: V^
 };
 
@@ -333,7 +333,7 @@ __device__ __forceinline__ HaloSmem halo_smem(const MixedArgs& a, unsigned char*
   h.q0 = reinterpret_cast<float4*>(sm);
   h.q1 = h.q0 + hm;
   h.li = reinterpret_cast<uint16_t*>(h.q1 + hm);
-  h.vh = reinterpret_cast<float*>(h.li + (kBlock / 32) * a.wmax * 32);
+  h.vh = reinterpret_cast<float*>(h.li + (kHaloBlock / 32) * a.wmax * 32);
   return h;
 }
 
@@ -353,7 +353,7 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 
 // The calling warp's chunk (one 16 B visit record); false if the warp has none.
 __device__ __forceinline__ bool warp_chunk(const MixedArgs& a, int64_t blk, int64_t* chunk, int* w, int64_t* base) {
-  const int64_t gw = blk * (kBlock / 32) + (threadIdx.x >> 5);
+  const int64_t gw = blk * (kHaloBlock / 32) + (threadIdx.x >> 5);
   if ((gw << 5) >= a.n) return false;  // warp-uniform
   if (a.visit) {
     const VisitRec r = a.visit[gw];
@@ -400,8 +400,9 @@ __device__ __forceinline__ bool warp_stage_done(const MixedArgs& a, uint64_t* ba
   return true;
 }
 
-// Pass A of visiting block blk (8 chunks) of plate a.  Every thread of the
-// 256-thread block calls it; sm = the pass's dynamic shared memory.  False if
+// Pass A of visiting block blk (kHaloBlock / 32 chunks) of plate a.  Every
+// thread of the kHaloBlock-thread block calls it; sm = the pass's dynamic
+// shared memory.  False if
 // a staged copy timed out.
 template <bool BREAK>
 __device__ __forceinline__ bool pass_a_block(const MixedArgs& a, int64_t blk, unsigned char* sm, uint64_t* bars) {
@@ -426,17 +427,17 @@ __device__ __forceinline__ bool pass_a_block(const MixedArgs& a, int64_t blk, un
   const HaloSmem h = halo_smem(a, sm);
   halo_begin(a, h, bars, has, w, base);
   const int32_t* H = a.halo + blk * a.halo_cap;
-  for (int k0 = 0; k0 < hn; k0 += kHaloBatch * kBlock) {
+  for (int k0 = 0; k0 < hn; k0 += kHaloBatch * kHaloBlock) {
     int g[kHaloBatch];
 #pragma unroll
     for (int q = 0; q < kHaloBatch; ++q) {
-      const int k = k0 + q * kBlock + threadIdx.x;
+      const int k = k0 + q * kHaloBlock + threadIdx.x;
       g[q] = k < hn ? H[k] : -1;
     }
 #pragma unroll
     for (int q = 0; q < kHaloBatch; ++q)
       if (g[q] >= 0) {
-        const int k = k0 + q * kBlock + threadIdx.x;
+        const int k = k0 + q * kHaloBlock + threadIdx.x;
         cp_async16(&h.q0[k], &a.us[g[q]]);
         cp_async16(&h.q1[k], &a.xs[g[q]]);
         cp_async4(&h.vh[k], &a.vh[g[q]]);
@@ -480,17 +481,17 @@ __device__ __forceinline__ bool pass_b_block(const MixedArgs& a, int64_t blk, un
   const HaloSmem h = halo_smem(a, sm);
   halo_begin(a, h, bars, has, w, base);
   const int32_t* H = a.halo + blk * a.halo_cap;
-  for (int k0 = 0; k0 < hn; k0 += kHaloBatch * kBlock) {
+  for (int k0 = 0; k0 < hn; k0 += kHaloBatch * kHaloBlock) {
     int g[kHaloBatch];
 #pragma unroll
     for (int q = 0; q < kHaloBatch; ++q) {
-      const int k = k0 + q * kBlock + threadIdx.x;
+      const int k = k0 + q * kHaloBlock + threadIdx.x;
       g[q] = k < hn ? H[k] : -1;
     }
 #pragma unroll
     for (int q = 0; q < kHaloBatch; ++q)
       if (g[q] >= 0) {
-        const int k = k0 + q * kBlock + threadIdx.x;
+        const int k = k0 + q * kHaloBlock + threadIdx.x;
         cp_async16(&h.q0[k], &a.xs[g[q]]);
         cp_async16(&h.q1[k], &a.ws[g[q]]);
       }
@@ -519,26 +520,26 @@ __device__ __forceinline__ void drift_block(const MixedArgs& a, int64_t blk) {
 }
 
 template <bool BREAK>
-__global__ void __launch_bounds__(kBlock) k_pass_a_mixed(MixedArgs a) {
+__global__ void __launch_bounds__(kHaloBlock) k_pass_a_mixed(MixedArgs a) {
   extern __shared__ __align__(128) unsigned char sm[];
-  __shared__ uint64_t bars[kBlock / 32];
+  __shared__ uint64_t bars[kHaloBlock / 32];
   pass_a_block<BREAK>(a, blockIdx.x, sm, bars);
 }
 
 template <bool DRIFT>
-__global__ void __launch_bounds__(kBlock, 4) k_pass_b_mixed(MixedArgs a) {
+__global__ void __launch_bounds__(kHaloBlock, 1024 / kHaloBlock) k_pass_b_mixed(MixedArgs a) {  // <= 64 registers
   extern __shared__ __align__(128) unsigned char sm[];
-  __shared__ uint64_t bars[kBlock / 32];
+  __shared__ uint64_t bars[kHaloBlock / 32];
   pass_b_block<DRIFT>(a, blockIdx.x, sm, bars);
 }
 
 // Dynamic shared memory of the single-plate passes: the larger of the int32
-// index staging (8 warps x wmax rows x 128 B) and the halo carve-up.
+// index staging (one wmax x 128 B chunk per warp) and the halo carve-up.
 inline size_t pass_smem_bytes(const MixedArgs& a, bool pass_a) {
-  const size_t idx32 = (size_t)(kBlock / 32) * (size_t)a.wmax * 128u;
+  const size_t idx32 = (size_t)(kHaloBlock / 32) * (size_t)a.wmax * 128u;
   if (!a.halo_n) return idx32;
   const size_t hm = (size_t)a.halo_max;
-  const size_t halo = hm * 32u + (size_t)(kBlock / 32) * (size_t)a.wmax * 64u + (pass_a ? hm * 4u : 0u);
+  const size_t halo = hm * 32u + (size_t)(kHaloBlock / 32) * (size_t)a.wmax * 64u + (pass_a ? hm * 4u : 0u);
   return halo > idx32 ? halo : idx32;
 }
 
@@ -547,11 +548,11 @@ inline size_t pass_smem_bytes(const MixedArgs& a, bool pass_a) {
 // the block's id span, and every slot's position in that list.
 __device__ __forceinline__ int decode_nbr(int v) { return v >= 0 ? v : (v <= -2 ? -2 - v : -1); }
 
-__global__ void __launch_bounds__(kBlock) k_halo_build(MixedArgs a, int32_t* halo, int32_t* halo_n, uint16_t* loc,
+__global__ void __launch_bounds__(kHaloBlock) k_halo_build(MixedArgs a, int32_t* halo, int32_t* halo_n, uint16_t* loc,
                                                        uint16_t* loc0, uint16_t* self_loc) {
   __shared__ uint32_t bits[kHaloSpanWords];
   __shared__ int32_t pre[kHaloSpanWords];
-  __shared__ int32_t wsum[kBlock / 32];
+  __shared__ int32_t wsum[kHaloBlock / 32];
   __shared__ int32_t s_lo, s_hi;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   int64_t chunk = 0, base = 0;
@@ -585,7 +586,7 @@ __global__ void __launch_bounds__(kBlock) k_halo_build(MixedArgs a, int32_t* hal
   const int L = s_lo, Hi = s_hi;
   bool fits = Hi >= L && (int64_t)Hi - L < 32LL * kHaloSpanWords;
   if (fits) {
-    for (int k = tid; k < kHaloSpanWords; k += kBlock) bits[k] = 0u;
+    for (int k = tid; k < kHaloSpanWords; k += kHaloBlock) bits[k] = 0u;
     __syncthreads();
     if (i >= 0) atomicOr(&bits[(i - L) >> 5], 1u << ((i - L) & 31));
     for (int k = 0; k < w; ++k) {
@@ -593,7 +594,7 @@ __global__ void __launch_bounds__(kBlock) k_halo_build(MixedArgs a, int32_t* hal
       if (j >= 0) atomicOr(&bits[(j - L) >> 5], 1u << ((j - L) & 31));
     }
     __syncthreads();
-    constexpr int kPer = kHaloSpanWords / kBlock;
+    constexpr int kPer = kHaloSpanWords / kHaloBlock;
     int c8[kPer], cnt = 0;
 #pragma unroll
     for (int q = 0; q < kPer; ++q) {
@@ -608,7 +609,7 @@ __global__ void __launch_bounds__(kBlock) k_halo_build(MixedArgs a, int32_t* hal
     if (lane == 31) wsum[warp] = incl;
     __syncthreads();
     int wpre = 0, tot = 0;
-    for (int q = 0; q < kBlock / 32; ++q) {
+    for (int q = 0; q < kHaloBlock / 32; ++q) {
       if (q < warp) wpre += wsum[q];
       tot += wsum[q];
     }
@@ -623,7 +624,7 @@ __global__ void __launch_bounds__(kBlock) k_halo_build(MixedArgs a, int32_t* hal
     if (fits) {
       if (tid == 0) halo_n[blockIdx.x] = tot;
       int32_t* H = halo + (int64_t)blockIdx.x * kHaloCap;
-      for (int word = tid; word < kHaloSpanWords; word += kBlock) {
+      for (int word = tid; word < kHaloSpanWords; word += kHaloBlock) {
         uint32_t m = bits[word];
         int r = pre[word];
         while (m) {
@@ -712,11 +713,11 @@ __device__ __forceinline__ bool batch_phase_mixed(const MixedArgs* __restrict__ 
   return ok;
 }
 
-__global__ void __launch_bounds__(kBlock) k_batch_persistent_mixed(const MixedArgs* __restrict__ plates,
+__global__ void __launch_bounds__(kHaloBlock) k_batch_persistent_mixed(const MixedArgs* __restrict__ plates,
                                                                    const BatchTile* __restrict__ tiles, int ntiles,
                                                                    int nsteps, GridBarrier* bar) {
   extern __shared__ __align__(128) unsigned char sm[];
-  __shared__ uint64_t bars[kBlock / 32];
+  __shared__ uint64_t bars[kHaloBlock / 32];
   const unsigned nb = gridDim.x;
   bool ok = batch_phase_mixed<-1>(plates, tiles, ntiles, 0, sm, bars);
   for (int s = 0; s < nsteps && ok; ++s) {
@@ -730,10 +731,10 @@ __global__ void __launch_bounds__(kBlock) k_batch_persistent_mixed(const MixedAr
 }
 
 template <int PHASE>
-__global__ void __launch_bounds__(kBlock) k_batch_phase_mixed(const MixedArgs* __restrict__ plates,
+__global__ void __launch_bounds__(kHaloBlock) k_batch_phase_mixed(const MixedArgs* __restrict__ plates,
                                                               const BatchTile* __restrict__ tiles, int ntiles) {
   extern __shared__ __align__(128) unsigned char sm[];
-  __shared__ uint64_t bars[kBlock / 32];
+  __shared__ uint64_t bars[kHaloBlock / 32];
   batch_phase_mixed<PHASE>(plates, tiles, ntiles, PHASE, sm, bars);
 }
 
@@ -803,25 +804,25 @@ size_t mixed_pass_smem(const MixedArgs& a) {
 int batch_occupancy_mixed(const BatchLaunch& cfg, size_t smem) {
   (void)cfg;
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch_persistent_mixed, kBlock, smem) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch_persistent_mixed, kHaloBlock, smem) != cudaSuccess)
     return 0;
   return nb;
 }
 
-// Mixed batches run 256-thread blocks over visiting-block tiles; cfg.block is
+// Mixed batches run kHaloBlock-thread blocks over visiting-block tiles; cfg.block is
 // not used.
 cudaError_t launch_batch_mixed(const MixedArgs* d_plates, const BatchTile* d_tiles, int ntiles, int nsteps,
                                const BatchLaunch& cfg, size_t smem, GridBarrier* d_bar, int nsm, cudaStream_t s) {
   if (ntiles <= 0 || nsteps <= 0) return cudaSuccess;
   if (!cfg.persistent) {
     const unsigned g = (unsigned)ntiles;
-    k_batch_phase_mixed<0><<<g, kBlock, smem, s>>>(d_plates, d_tiles, ntiles);
+    k_batch_phase_mixed<0><<<g, kHaloBlock, smem, s>>>(d_plates, d_tiles, ntiles);
     for (int k = 0; k < nsteps; ++k) {
-      k_batch_phase_mixed<1><<<g, kBlock, smem, s>>>(d_plates, d_tiles, ntiles);
+      k_batch_phase_mixed<1><<<g, kHaloBlock, smem, s>>>(d_plates, d_tiles, ntiles);
       if (k + 1 < nsteps)
-        k_batch_phase_mixed<2><<<g, kBlock, smem, s>>>(d_plates, d_tiles, ntiles);
+        k_batch_phase_mixed<2><<<g, kHaloBlock, smem, s>>>(d_plates, d_tiles, ntiles);
       else
-        k_batch_phase_mixed<3><<<g, kBlock, smem, s>>>(d_plates, d_tiles, ntiles);
+        k_batch_phase_mixed<3><<<g, kHaloBlock, smem, s>>>(d_plates, d_tiles, ntiles);
     }
     return cudaGetLastError();
   }
@@ -834,7 +835,7 @@ cudaError_t launch_batch_mixed(const MixedArgs* d_plates, const BatchTile* d_til
   if (e != cudaSuccess) return e;
   cudaLaunchConfig_t lc = {};
   lc.gridDim = dim3((unsigned)grid);
-  lc.blockDim = dim3((unsigned)kBlock);
+  lc.blockDim = dim3((unsigned)kHaloBlock);
   lc.dynamicSmemBytes = smem;
   lc.stream = s;
   cudaLaunchAttribute at[1];
@@ -847,8 +848,8 @@ cudaError_t launch_batch_mixed(const MixedArgs* d_plates, const BatchTile* d_til
 
 void launch_init_geometry_mixed(const MixedArgs& a, cudaStream_t s) {
   if (a.n <= 0) return;
-  // the passes may take up to kHaloCap x 36 B + 8 warps x PD_MAX_FAMILY rows x 64 B of dynamic shared memory
-  const int mx = kHaloCap * 36 + (kBlock / 32) * PD_MAX_FAMILY * 64;
+  // the passes may take up to kHaloCap x 36 B + one PD_MAX_FAMILY x 64 B index chunk per warp of shared memory
+  const int mx = kHaloCap * 36 + (kHaloBlock / 32) * PD_MAX_FAMILY * 64;
   cudaFuncSetAttribute(k_pass_a_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   cudaFuncSetAttribute(k_pass_a_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   cudaFuncSetAttribute(k_pass_b_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
@@ -870,18 +871,18 @@ void launch_pass_a_mixed(const MixedArgs& a, bool breaking, cudaStream_t s) {
   if (a.n <= 0) return;
   const size_t sm = pass_smem_bytes(a, true);
   if (breaking)
-    k_pass_a_mixed<true><<<(unsigned)blocks_for(a.n), kBlock, sm, s>>>(a);
+    k_pass_a_mixed<true><<<(unsigned)blocks_for(a.n, kHaloBlock), kHaloBlock, sm, s>>>(a);
   else
-    k_pass_a_mixed<false><<<(unsigned)blocks_for(a.n), kBlock, sm, s>>>(a);
+    k_pass_a_mixed<false><<<(unsigned)blocks_for(a.n, kHaloBlock), kHaloBlock, sm, s>>>(a);
 }
 
 void launch_pass_b_mixed(const MixedArgs& a, bool drift, cudaStream_t s) {
   if (a.n <= 0) return;
   const size_t sm = pass_smem_bytes(a, false);
   if (drift)
-    k_pass_b_mixed<true><<<(unsigned)blocks_for(a.n), kBlock, sm, s>>>(a);
+    k_pass_b_mixed<true><<<(unsigned)blocks_for(a.n, kHaloBlock), kHaloBlock, sm, s>>>(a);
   else
-    k_pass_b_mixed<false><<<(unsigned)blocks_for(a.n), kBlock, sm, s>>>(a);
+    k_pass_b_mixed<false><<<(unsigned)blocks_for(a.n, kHaloBlock), kHaloBlock, sm, s>>>(a);
 }
 
 void launch_to_mixed(const MixedArgs& a, const double2* u, const double2* v, const double2* f, cudaStream_t s) {
@@ -893,7 +894,7 @@ void launch_from_mixed(const MixedArgs& a, double2* u, double2* v, double2* f, c
 }
 
 int build_halo_mixed(const MixedArgs& a, int64_t nslots, cudaStream_t s, HaloLayout* h, std::string* msg) {
-  const int64_t nb = blocks_for(a.n);
+  const int64_t nb = blocks_for(a.n, kHaloBlock);
   h->nblocks = nb;
   h->staged = 0;
   h->halo_max = 0;
@@ -910,7 +911,7 @@ int build_halo_mixed(const MixedArgs& a, int64_t nslots, cudaStream_t s, HaloLay
     return PD_ERR_CUDA;
   }
   k_visit_build<<<(unsigned)blocks_for(nch), kBlock, 0, s>>>(nch, a.chunk_order, a.chunk_w, a.chunk_base, h->visit);
-  k_halo_build<<<(unsigned)nb, kBlock, 0, s>>>(a, h->halo, h->halo_n, h->loc, h->loc0, h->self_loc);
+  k_halo_build<<<(unsigned)nb, kHaloBlock, 0, s>>>(a, h->halo, h->halo_n, h->loc, h->loc0, h->self_loc);
   std::vector<int32_t> cnt((size_t)nb);
   cudaError_t e = cudaMemcpyAsync(cnt.data(), h->halo_n, (size_t)nb * sizeof(int32_t), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
