@@ -89,7 +89,7 @@ struct pd_batch {
   int64_t particles = 0, bonds = 0;
   std::map<int32_t, cudaGraphExec_t> graphs;
   bool direct = false;  // persistent kernel launched directly (its capture was refused)
-  size_t smem = 0;      // mixed: dynamic shared memory of the batched passes
+  size_t smem_a = 0, smem_b = 0;  // mixed: dynamic shared memory of the batched passes A and B
 };
 
 namespace {
@@ -1374,14 +1374,15 @@ int batch_refresh(pd_batch* b) {
   plates.resize(asz * (b->members.empty() ? 1 : b->members.size()));
   b->particles = 0;
   b->bonds = 0;
-  b->smem = 0;
+  b->smem_a = b->smem_b = 0;
   for (size_t k = 0; k < b->members.size(); ++k) {
     pd_ctx* c = b->members[k];
     if (!c->has_families) return bfail(b, PD_ERR_ORDER, "a member has no families");
     if (b->precision == PD_MIXED) {
       const pd::MixedArgs m = mixed_args(c);
       std::memcpy(plates.data() + k * asz, &m, asz);
-      b->smem = std::max(b->smem, pd::mixed_pass_smem(m));
+      b->smem_a = std::max(b->smem_a, pd::mixed_pass_smem(m, true));
+      b->smem_b = std::max(b->smem_b, pd::mixed_pass_smem(m, false));
       // one tile per visiting block (kHaloBlock particles) of the plate
       for (int64_t blk = 0; blk * pd::kHaloBlock < c->n; ++blk)
         tiles.push_back(
@@ -1422,7 +1423,7 @@ int batch_refresh(pd_batch* b) {
 cudaError_t batch_enqueue(pd_batch* b, int32_t nsteps) {
   if (b->precision == PD_MIXED)
     return pd::launch_batch_mixed(static_cast<const pd::MixedArgs*>(b->d_plates), b->d_tiles, b->ntiles, nsteps,
-                                  b->cfg, b->smem, b->d_bar, b->nsm, b->stream);
+                                  b->cfg, b->smem_a, b->smem_b, b->d_bar, b->nsm, b->stream);
   return pd::launch_batch_fp64(static_cast<const Fp64Args*>(b->d_plates), b->d_tiles, b->ntiles, nsteps, b->cfg,
                                b->d_bar, b->nsm, b->stream);
 }

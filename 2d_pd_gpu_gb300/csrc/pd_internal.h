@@ -226,11 +226,12 @@ void launch_pass_b_mixed(const MixedArgs& a, bool drift, cudaStream_t s);
 void launch_to_mixed(const MixedArgs& a, const double2* u, const double2* v, const double2* f, cudaStream_t s);
 void launch_from_mixed(const MixedArgs& a, double2* u, double2* v, double2* f, cudaStream_t s);
 // mixed tiles: {plate, particles <= 256, first = visiting block}; smem = the
-// largest mixed_pass_smem of the batch's plates
+// largest mixed_pass_smem of the batch's plates for pass A (smem_a) and pass B (smem_b)
 cudaError_t launch_batch_mixed(const MixedArgs* d_plates, const BatchTile* d_tiles, int ntiles, int nsteps,
-                               const BatchLaunch& cfg, size_t smem, GridBarrier* d_bar, int nsm, cudaStream_t s);
+                               const BatchLaunch& cfg, size_t smem_a, size_t smem_b, GridBarrier* d_bar, int nsm,
+                               cudaStream_t s);
 int batch_occupancy_mixed(const BatchLaunch& cfg, size_t smem);
-size_t mixed_pass_smem(const MixedArgs& a);  // dynamic shared memory of the mixed passes
+size_t mixed_pass_smem(const MixedArgs& a, bool pass_a);  // dynamic shared memory of a mixed pass
 
 inline int64_t blocks_for(int64_t n, int64_t per = kBlock) { return (n + per - 1) / per; }
 

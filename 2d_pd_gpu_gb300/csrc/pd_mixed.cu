@@ -702,8 +702,8 @@ __device__ __forceinline__ bool batch_phase_mixed(const MixedArgs* __restrict__ 
     __syncthreads();  // the previous tile's shared memory is no longer read
     if (phase == 0)
       drift_block(p, T.first);
-    else if (phase == 1)
-      ok = p.brk ? pass_a_block<true>(p, T.first, sm, bars) : pass_a_block<false>(p, T.first, sm, bars);
+    else if (phase == 1)  // the breaking pass also serves plates without breaking (their s2 is +inf)
+      ok = pass_a_block<true>(p, T.first, sm, bars);
     else if (phase == 2)
       ok = pass_b_block<true>(p, T.first, sm, bars);
     else
@@ -730,8 +730,10 @@ __global__ void __launch_bounds__(kHaloBlock) k_batch_persistent_mixed(const Mix
   if (!ok && threadIdx.x == 0) atomicExch(&bar->err, 1);  // releases the other blocks' barrier waits
 }
 
+// registers as the single-plate passes: pass A 80 (3 blocks / SM), pass B 64 (4)
 template <int PHASE>
-__global__ void __launch_bounds__(kHaloBlock) k_batch_phase_mixed(const MixedArgs* __restrict__ plates,
+__global__ void __launch_bounds__(kHaloBlock, PHASE == 1 ? 768 / kHaloBlock : 1024 / kHaloBlock)
+    k_batch_phase_mixed(const MixedArgs* __restrict__ plates,
                                                               const BatchTile* __restrict__ tiles, int ntiles) {
   extern __shared__ __align__(128) unsigned char sm[];
   __shared__ uint64_t bars[kHaloBlock / 32];
@@ -796,10 +798,7 @@ __global__ void k_positions_mixed(MixedArgs a) {
 
 }  // namespace
 
-size_t mixed_pass_smem(const MixedArgs& a) {
-  const size_t pa = pass_smem_bytes(a, true), pb = pass_smem_bytes(a, false);
-  return pa > pb ? pa : pb;
-}
+size_t mixed_pass_smem(const MixedArgs& a, bool pass_a) { return pass_smem_bytes(a, pass_a); }
 
 int batch_occupancy_mixed(const BatchLaunch& cfg, size_t smem) {
   (void)cfg;
@@ -812,17 +811,19 @@ int batch_occupancy_mixed(const BatchLaunch& cfg, size_t smem) {
 // Mixed batches run kHaloBlock-thread blocks over visiting-block tiles; cfg.block is
 // not used.
 cudaError_t launch_batch_mixed(const MixedArgs* d_plates, const BatchTile* d_tiles, int ntiles, int nsteps,
-                               const BatchLaunch& cfg, size_t smem, GridBarrier* d_bar, int nsm, cudaStream_t s) {
+                               const BatchLaunch& cfg, size_t smem_a, size_t smem_b, GridBarrier* d_bar, int nsm,
+                               cudaStream_t s) {
   if (ntiles <= 0 || nsteps <= 0) return cudaSuccess;
+  const size_t smem = smem_a > smem_b ? smem_a : smem_b;
   if (!cfg.persistent) {
     const unsigned g = (unsigned)ntiles;
-    k_batch_phase_mixed<0><<<g, kHaloBlock, smem, s>>>(d_plates, d_tiles, ntiles);
+    k_batch_phase_mixed<0><<<g, kHaloBlock, 0, s>>>(d_plates, d_tiles, ntiles);
     for (int k = 0; k < nsteps; ++k) {
-      k_batch_phase_mixed<1><<<g, kHaloBlock, smem, s>>>(d_plates, d_tiles, ntiles);
+      k_batch_phase_mixed<1><<<g, kHaloBlock, smem_a, s>>>(d_plates, d_tiles, ntiles);
       if (k + 1 < nsteps)
-        k_batch_phase_mixed<2><<<g, kHaloBlock, smem, s>>>(d_plates, d_tiles, ntiles);
+        k_batch_phase_mixed<2><<<g, kHaloBlock, smem_b, s>>>(d_plates, d_tiles, ntiles);
       else
-        k_batch_phase_mixed<3><<<g, kHaloBlock, smem, s>>>(d_plates, d_tiles, ntiles);
+        k_batch_phase_mixed<3><<<g, kHaloBlock, smem_b, s>>>(d_plates, d_tiles, ntiles);
     }
     return cudaGetLastError();
   }
