@@ -3,7 +3,7 @@
 The FP64 kernels perform the oracle's IEEE operations in the oracle's order
 (--fmad=false + the same explicit fma() calls), so the bar here is bit
 equality for displacements, velocities, forces, the bond mask and damage;
-against the reference's own outputs the bar is the benchmark spec's 1e-10
+against the reference's own outputs the bar is 1e-10
 (normwise) on velocities/displacements, see test_oracle_golden.py for the
 reference's long-double floor on the Hassa mesh.
 """
@@ -102,7 +102,7 @@ def test_gpu_fp64_bit_exact_vs_oracle(pdg, po, side, seed, s_c, steps):
 
 
 def test_gpu_config1_plate_100_steps_bit_exact(pdg, po):
-    """Config 1 (100x100, centred half-width crack, s_c = 5e-4, 100 steps)."""
+    """The CPU-runnable plate: 100x100, centred half-width crack, s_c = 5e-4, 100 steps."""
     p = pdg.plates.config_plate_100(seed=0)
     ctx = p.context()
     sim = plate_oracle(po, p)

@@ -2,7 +2,7 @@
 
 The FP64 GPU path is bit-identical to the oracle (test_gpu_fp64_parity.py),
 so it serves as the FP64 oracle at sizes the CPU restatement would take long
-on.  Bars (the benchmark spec): <= 1e-6 normwise relative displacement error and an
+on.  Bars: <= 1e-6 normwise relative displacement error and an
 identical damage mask; the velocity error and mask mismatches are reported.
 """
 import numpy as np

@@ -6,7 +6,7 @@ build reproduced the reference's shipped golden files byte for byte
 (tests/golden/make_golden.py, manifest.json).
 
 Tolerances (normwise max|d|/max|ref|): velocities and displacements 1e-10
-(the spec bar); net force 1e-8 -- the reference keeps absolute
+(the parity bar); net force 1e-8 -- the reference keeps absolute
 positions (~30 mm) in 80-bit long double while displacements are ~5e-9 mm,
 so its own force carries ~2e-10 relative rounding, which is what we measure.
 """
