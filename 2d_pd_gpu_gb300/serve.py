@@ -69,6 +69,7 @@ class Result:
     steps: int
     digest: str
     broken: int
+    state: tuple | None = None  # (u, bond mask) when the request id is in Server.keep
 
     @property
     def latency(self):
@@ -149,6 +150,7 @@ class Server:
     workers: int = 4
     preempt: bool = True
     preempt_ratio: float = 4.0
+    keep: set = field(default_factory=set)  # request ids whose final (u, mask) the results keep
     results: list = field(default_factory=list)
     preemptions: int = 0
 
@@ -217,7 +219,9 @@ class Server:
                     q, ctx = a[0], a[1]
                     batch.remove(ctx)
                     dig, broken = state_digest(ctx)
-                    self.results.append(Result(q.rid, q.arrival, a[3], fin, q.particles, ctx.nnz, q.steps, dig, broken))
+                    kept = (ctx.state()[0], ctx.bond_mask()) if q.rid in self.keep else None
+                    self.results.append(Result(q.rid, q.arrival, a[3], fin, q.particles, ctx.nnz, q.steps, dig, broken,
+                                               kept))
                     ctx.close()
                     used -= a[4]
                     del active[rid]

@@ -339,11 +339,28 @@ def run_serve(args, pdg, device, capacity, configs):
         work = float(np.mean([27.9 * q.particles * q.steps for q in probe]))
         rate = 0.8 * capacity[name] / work
         reqs = serve.make_requests(count, seed=args.seed + 17, rate=rate)
+        # the mixed results' error against the FP64 form, on the three smallest requests
+        sample = sorted(reqs, key=lambda q: q.particles * q.steps)[:3] if prec == nat.PD_MIXED else []
         srv = serve.Server(precision=prec, device=device, budget_bytes=150e9, chunk=args.serve_chunk,
-                           batch_config=configs.get(name))
+                           batch_config=configs.get(name), keep={q.rid for q in sample})
         m = srv.run(reqs)
         m.update({"arrival_rate_per_s": rate, "offered_load": 0.8, "capacity_bond_updates_per_s": capacity[name],
                   "particles_range": [min(q.particles for q in reqs), max(q.particles for q in reqs)]})
+        if sample:
+            by = {r.rid: r for r in srv.results}
+            acc = []
+            for q in sample:
+                ref = q.plate().context(precision=nat.PD_FP64, device=device)
+                ref.step(q.steps)
+                u64, m64 = ref.state()[0], ref.bond_mask()
+                ref.close()
+                u32, m32 = by[q.rid].state
+                du = np.abs(u32 - u64)
+                acc.append({"rid": q.rid, "particles": q.particles, "steps": q.steps,
+                            "u_max_rel": float(du.max() / np.abs(u64).max()),
+                            "u_rms_rel": float(np.sqrt((du ** 2).mean() / (u64 ** 2).mean())),
+                            "mask_mismatch": int((m32 != m64).sum()), "bonds_broken_fp64": int((m64 == 0).sum())})
+            m["accuracy_vs_fp64"] = acc
         out[name] = m
     return out
 
