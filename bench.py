@@ -471,7 +471,7 @@ def main():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--scale-side", type=int, default=4000, help="mixed form on this plate too (0: skip)")
     ap.add_argument("--batch-plates", type=int, default=256)
-    ap.add_argument("--batch-steps", type=int, default=20)
+    ap.add_argument("--batch-steps", type=int, default=500)
     ap.add_argument("--serve-requests", type=int, default=64)
     ap.add_argument("--serve-chunk", type=int, default=50)
     args = ap.parse_args()

@@ -215,3 +215,19 @@ def test_gpu_step_host_equals_staged_copies(pdg):
         b.step_host(1, u.copy(), v.copy(), f.copy())
     for x in bufs:
         x.free()
+
+
+def test_gpu_scale_plate_200_cut_1000_steps_bit_exact(pdg, po):
+    """The 1000 x 1000 workload's generator at 200 x 200 (same seed rule,
+    seeded crack), 1000 steps with bond breaking: bit-exact damage mask,
+    damage and state against the CPU restatement at steps 100, 500, 1000."""
+    p = pdg.plates.config_plate_scale(side=200, seed=0)
+    ctx = p.context()
+    sim = plate_oracle(po, p)
+    done = 0
+    for target in (100, 500, 1000):
+        ctx.step(target - done)
+        sim.step(target - done)
+        done = target
+        _assert_same(ctx, sim)
+    assert int((sim.mask == 0).sum()) > 0, "the crack is meant to run"
