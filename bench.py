@@ -395,6 +395,10 @@ def run_ours(args, comm):
         peak64, peak32, src = MEASURED_FP64_DFMA_PER_S, None, "recorded DFMA rate (profiles/fp64_fma_rate_probe.txt)"
     result["fp64_alu"] = {"ops_per_s": ops, "peak_ops_per_s": peak64, "frac": ops / peak64,
                           "ops_per_step": fp64_ops(n, nb), "peak_source": src, "fp32_fma_per_s": peak32}
+    # the FP64 step's binding limit is the FP64 pipe, not HBM (ncu: FP64 pipe 83-87 % busy)
+    result["roofline"]["binding"] = {"limit": "fp64_pipe", "frac": ops / peak64,
+                                     "why": "GB300 executes FP64 at 1/58 of its FP32 rate; 12 FP64 operations "
+                                            "per bond take ~8x longer than the step's algorithmic HBM bytes"}
     # end to end through the public API with pinned host buffers, every step
     if not args.no_e2e:
         esteps = min(args.steps, args.e2e_steps)
