@@ -185,8 +185,9 @@ __device__ __forceinline__ PreA load_a(const MixedArgs& a, int64_t i) {
 }
 
 // Pass A of particle i: slots s0 + 32 k, k < w; idx(k) gives a slot's
-// neighbour (-1: padding or broken; a particle id, or a halo position when
-// the data is staged) and gather(j) its data.
+// neighbour (a particle id, -1 for padding or broken; or, when the data is
+// staged, a halo position, the particle's own for padding or broken) and
+// gather(j) its data.
 template <bool BREAK, typename Idx, typename Gather>
 __device__ __forceinline__ void pass_a_core(const MixedArgs& a, int64_t i, const PreA& pre, int w, int64_t s0, Idx idx,
                                             Gather gather) {
@@ -312,13 +313,13 @@ struct GatherB {
 };
 
 
-// ---- single-plate passes.  Block b runs the chunks chunk_order[8b .. 8b+8)
-// (spatially compact, see the chunk order in pd_api.cu).  Blocks whose halo
-// -- the distinct particles their bonds reach -- was staged at setup
-// (halo_n[b] >= 0) first copy the halo's data into shared memory with
-// coalesced loads and then walk their bonds entirely out of shared memory
-// (16-bit halo indices, TMA-staged per warp); other blocks stage their int32
-// indices and gather neighbour data from L1/L2.
+// ---- single-plate and batched passes.  Visiting block b runs the chunks
+// visit[8b .. 8b+8) (spatially compact, see the chunk order in pd_api.cu).
+// Blocks whose halo -- the distinct particles their bonds reach -- was
+// staged at setup (halo_n[b] >= 0) gather the halo's data into shared memory
+// (cp.async) and walk their bonds entirely out of shared memory (16-bit halo
+// indices, TMA-staged per warp); other blocks stage their int32 indices and
+// gather neighbour data from L1/L2.
 
 struct HaloSmem {  // dynamic shared memory carve-up of a halo block
   float4* q0;      // pass A: u^, pass B: x^
@@ -373,7 +374,7 @@ __device__ __forceinline__ void stage_timeout(const MixedArgs& a) {
 }
 
 // Halo blocks: lane 0 of each warp issues the TMA copy of its 16-bit index
-// chunk, then the whole block loads the halo; returns after __syncthreads.
+// chunk (waited on after the halo gather).
 __device__ __forceinline__ void halo_begin(const MixedArgs& a, const HaloSmem& h, uint64_t* bars, bool has, int w,
                                            int64_t base) {
   const int warp = threadIdx.x >> 5;
