@@ -132,13 +132,24 @@ void clear_graphs(pd_ctx* c) {
   }
 }
 
+// A copy ordered on stream s (the contexts' and batches' streams are
+// non-blocking, so a plain cudaMemcpy is not ordered with their kernels, and
+// one from pageable memory may return before its data has landed), waited for.
+cudaError_t copy_sync(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, cudaStream_t s) {
+  cudaError_t e = cudaMemcpyAsync(dst, src, bytes, kind, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return e;
+}
+
 void free_families(pd_ctx* c) {
   dfree(c->row_ptr);
   dfree(c->col);
   dfree(c->sell.chunk_base);
   dfree(c->sell.chunk_w);
   dfree(c->sell.nbr);
-  dfree(c->sell.chunk_order);
+  dfree(c->sell.member);
+  dfree(c->sell.rank);
+  dfree(c->sell.pos_of);
   dfree(c->mz_thr);
   dfree(c->mz_bd);
   dfree(c->mz_status);
@@ -216,6 +227,7 @@ Fp64Args fp64_args(pd_ctx* c) {
   a.bc = c->bc; a.gkind = c->gkind; a.gval = c->gval;
   a.broken = c->broken; a.damage = c->damage; a.singular = c->singular; a.fam = c->fam;
   a.chunk_base = c->sell.chunk_base; a.chunk_w = c->sell.chunk_w; a.nbr = c->sell.nbr;
+  a.member = c->sell.member; a.pos_of = c->sell.pos_of;
   a.bxi = c->bxi; a.bgeo = c->bgeo; a.blim = c->blim; a.br2 = c->br2; a.u32 = c->u32;
   stiffness(c, &a.c11, &a.c12, &a.c33);  // getStiffnessTensor, src/main_seq.cpp:185-187
   a.dt = c->p.dt;
@@ -277,8 +289,9 @@ pd::MixedArgs mixed_args(pd_ctx* c) {
   a.bc = c->bc; a.gkind = c->gkind; a.gvel = c->gvel;
   a.broken = c->broken; a.damage = c->damage; a.singular = c->singular; a.fam = c->fam;
   a.chunk_base = c->sell.chunk_base; a.chunk_w = c->sell.chunk_w; a.nbr = c->sell.nbr;
-  a.chunk_order = c->sell.chunk_order;
+  a.member = c->sell.member; a.pos_of = c->sell.pos_of;
   a.visit = c->halo.visit;
+  a.nblocks = c->halo.nblocks;
   a.loc = c->halo.loc;
   a.self_loc = c->halo.self_loc;
   a.halo = c->halo.halo;
@@ -318,7 +331,7 @@ int upload_gvel(pd_ctx* c) {
       g[4 * k + m] = hi;
       g[4 * k + 2 + m] = (float)(v - (double)hi);
     }
-  PD_CK(c, cudaMemcpy(c->gvel, g.data(), g.size() * sizeof(float), cudaMemcpyHostToDevice));
+  PD_CK(c, copy_sync(c->gvel, g.data(), g.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
   return PD_OK;
 }
 
@@ -327,82 +340,139 @@ __global__ void k_fam_from_rowptr(int64_t n, const int64_t* rp, int32_t* fam) {
   if (i < n) fam[i] = (int32_t)(rp[i + 1] - rp[i]);
 }
 
-// After row_ptr/col exist: SELL layout, bond geometry, per-particle geometry, reset.
-// Visiting order of the SELL-32 chunks for the mixed passes.  A chunk is
-// 32 consecutive particles; for the usual row-major numbering it is a short
-// row segment (long axis along x).  Chunks are ordered by (band, column,
-// row) on a grid whose cells are the median chunk extent along the long axis
-// and along the short axis, with bands of kHaloBlock / 32 cells across: the
-// warps of a visiting block then run chunks stacked across their long axis
-// (32 columns x 8 rows of a row-major plate), so the block's bonds reach
-// about half as many distinct particles (its halo) as 8 consecutive chunks
-// would.  The particle order, and with it every array the API exposes, is
-// unchanged.
-std::vector<int32_t> chunk_visit_order(const std::vector<double>& x, int64_t n, double min_cell) {
-  const int64_t nch = (n + 31) / 32;
-  std::vector<int32_t> order((size_t)nch);
-  for (int64_t k = 0; k < nch; ++k) order[(size_t)k] = (int32_t)k;
-  if (nch <= 1) return order;
-  std::vector<double> cx((size_t)nch), cy((size_t)nch), ex((size_t)nch), ey((size_t)nch);
-  for (int64_t ch = 0; ch < nch; ++ch) {
-    const int64_t a = ch * 32, b = std::min(n, a + 32);
-    double sx = 0.0, sy = 0.0, x0 = INFINITY, x1 = -INFINITY, y0 = INFINITY, y1 = -INFINITY;
-    for (int64_t i = a; i < b; ++i) {
-      const double px = x[2 * i], py = x[2 * i + 1];
-      sx += px;
-      sy += py;
-      x0 = std::min(x0, px);
-      x1 = std::max(x1, px);
-      y0 = std::min(y0, py);
-      y1 = std::max(y1, py);
+// Stable LSD radix sort of the indices 0..n-1 by 64-bit keys (16-bit digits;
+// equal keys keep index order).
+std::vector<int32_t> sort_by_key(std::vector<uint64_t> key) {
+  const size_t n = key.size();
+  std::vector<int32_t> idx(n), tmp(n);
+  std::vector<uint64_t> key2(n);
+  for (size_t i = 0; i < n; ++i) idx[i] = (int32_t)i;
+  if (n <= 1) return idx;
+  std::vector<int64_t> cnt(65537);
+  for (int shift = 0; shift < 64; shift += 16) {
+    std::fill(cnt.begin(), cnt.end(), 0);
+    for (size_t i = 0; i < n; ++i) ++cnt[((key[i] >> shift) & 0xFFFF) + 1];
+    if (cnt[((key[0] >> shift) & 0xFFFF) + 1] == (int64_t)n) continue;  // one digit value: identity pass
+    for (int d = 0; d < 65536; ++d) cnt[d + 1] += cnt[d];
+    for (size_t i = 0; i < n; ++i) {
+      const int64_t o = cnt[(key[i] >> shift) & 0xFFFF]++;
+      key2[(size_t)o] = key[i];
+      tmp[(size_t)o] = idx[i];
     }
-    cx[(size_t)ch] = sx / (double)(b - a);
-    cy[(size_t)ch] = sy / (double)(b - a);
-    ex[(size_t)ch] = x1 - x0;
-    ey[(size_t)ch] = y1 - y0;
+    key.swap(key2);
+    idx.swap(tmp);
   }
-  auto median = [](std::vector<double> v) {
-    std::nth_element(v.begin(), v.begin() + v.size() / 2, v.end());
-    return v[v.size() / 2];
-  };
-  const double mx = std::max(median(ex), min_cell), my = std::max(median(ey), min_cell);
-  const bool long_x = mx >= my;  // chunks are stacked across their long axis
-  const double ql = long_x ? mx : my, qs = long_x ? my : mx;
-  double lo_l = INFINITY, lo_s = INFINITY;
-  for (int64_t ch = 0; ch < nch; ++ch) {
-    lo_l = std::min(lo_l, long_x ? cx[(size_t)ch] : cy[(size_t)ch]);
-    lo_s = std::min(lo_s, long_x ? cy[(size_t)ch] : cx[(size_t)ch]);
-  }
-  struct Key {
-    int64_t band, col, row;
-    int32_t ch;
-    bool operator<(const Key& o) const {
-      if (band != o.band) return band < o.band;
-      if (col != o.col) return col < o.col;
-      if (row != o.row) return row < o.row;
-      return ch < o.ch;
-    }
-  };
-  std::vector<Key> key((size_t)nch);
-  for (int64_t ch = 0; ch < nch; ++ch) {
-    const double l = ((long_x ? cx[(size_t)ch] : cy[(size_t)ch]) - lo_l) / ql;
-    const double t = ((long_x ? cy[(size_t)ch] : cx[(size_t)ch]) - lo_s) / qs;
-    const int64_t row = (int64_t)std::floor(t);
-    key[(size_t)ch] = {row / (pd::kHaloBlock / 32), (int64_t)std::floor(l), row, (int32_t)ch};
-  }
-  std::sort(key.begin(), key.end());
-  for (int64_t k = 0; k < nch; ++k) order[(size_t)k] = key[(size_t)k].ch;
-  return order;
+  return idx;
 }
 
+// Spatial orders of the mixed form, from the reference positions binned into
+// square cells of side sqrt(bbox area / n) (about one particle per cell; a
+// lattice's cells are its sites).  Particle numbering, and with it every array
+// the API exposes, is unchanged.
+//   member:  SELL positions in tiles of 32 cells x 8 rows (tiles row-major,
+//            bands of 8 rows), cells row-major inside a tile, every tile
+//            starting a new chunk (the tail of its last chunk is a hole,
+//            member -1).  A chunk (32 positions) is then a row segment with
+//            its lanes in x order, and a visiting block (blocks: up to
+//            kHaloBlock / 32 chunks, -1 = none) is one tile, whose bonds reach
+//            few distinct particles (its halo); a tile of more than
+//            kHaloBlock particles is split into several blocks.
+//   by_rank: particles in global row-major cell order.  Halos are sorted by
+//            this rank and every family is walked in ascending rank of its
+//            neighbours (for a row-major numbering that is the family order),
+//            so the 32 lanes of a row segment read the same neighbour offset
+//            at the same slot, from consecutive halo entries (no shared-memory
+//            bank conflicts), and the step is bit-identical whatever the
+//            numbering.
+// Equal cells keep particle order.
+struct SpatialOrder {
+  std::vector<int32_t> member, blocks, by_rank;
+};
+
+SpatialOrder spatial_order(const std::vector<double>& x, int64_t n) {
+  static_assert(pd::kHaloBlock == 32 * 8, "a visiting block is one 32 x 8 tile");
+  SpatialOrder o;
+  double x0 = INFINITY, x1 = -INFINITY, y0 = INFINITY, y1 = -INFINITY;
+  for (int64_t i = 0; i < n; ++i) {
+    const double px = x[2 * i], py = x[2 * i + 1];
+    if (!std::isfinite(px) || !std::isfinite(py)) continue;
+    x0 = std::min(x0, px);
+    x1 = std::max(x1, px);
+    y0 = std::min(y0, py);
+    y1 = std::max(y1, py);
+  }
+  const double ex = x1 - x0, ey = y1 - y0;
+  double q = std::sqrt(ex * ey / (double)n);
+  if (!(q > 0.0) || !std::isfinite(q)) q = std::max(ex, ey) / (double)n;
+  std::vector<uint64_t> cx((size_t)n, 0), cy((size_t)n, 0);
+  if (q > 0.0 && std::isfinite(q)) {
+    auto cell = [&](double v, double lo) {
+      const double t = std::floor((v - lo) / q);
+      return (uint64_t)(t > 0.0 ? std::min(t, 4294967295.0) : 0.0);
+    };
+    for (int64_t i = 0; i < n; ++i) {
+      const double px = x[2 * i], py = x[2 * i + 1];
+      if (std::isfinite(px) && std::isfinite(py)) {
+        cx[(size_t)i] = cell(px, x0);
+        cy[(size_t)i] = cell(py, y0);
+      }
+    }
+  }
+  uint64_t gx = 1;
+  for (int64_t i = 0; i < n; ++i) gx = std::max(gx, cx[(size_t)i] + 1);
+  const uint64_t tiles_x = (gx + 31) / 32;
+  std::vector<uint64_t> key((size_t)n);
+  for (int64_t i = 0; i < n; ++i) {
+    const uint64_t u = cx[(size_t)i], v = cy[(size_t)i];
+    key[(size_t)i] = (((v >> 3) * tiles_x + (u >> 5)) * 8 + (v & 7)) * 32 + (u & 31);
+  }
+  const std::vector<int32_t> sorted = sort_by_key(key);
+  constexpr int kWarps = pd::kHaloBlock / 32;
+  for (int64_t a = 0; a < n;) {  // one tile: sorted[a .. b)
+    const uint64_t tile = key[(size_t)sorted[(size_t)a]] >> 8;
+    int64_t b = a + 1;
+    while (b < n && (key[(size_t)sorted[(size_t)b]] >> 8) == tile) ++b;
+    const int64_t first_chunk = (int64_t)o.member.size() / 32, nch = (b - a + 31) / 32;
+    for (int64_t k = a; k < b; ++k) o.member.push_back(sorted[(size_t)k]);
+    o.member.resize((size_t)(first_chunk + nch) * 32, -1);
+    for (int64_t c = 0; c < nch; c += kWarps)
+      for (int w = 0; w < kWarps; ++w) o.blocks.push_back(c + w < nch ? (int32_t)(first_chunk + c + w) : -1);
+    a = b;
+  }
+  for (int64_t i = 0; i < n; ++i) key[(size_t)i] = cy[(size_t)i] * gx + cx[(size_t)i];
+  o.by_rank = sort_by_key(std::move(key));
+  return o;
+}
+
+int upload_i32(pd_ctx* c, int32_t** d, const std::vector<int32_t>& h) {
+  PD_CK(c, cudaMalloc(d, (h.empty() ? 1 : h.size()) * sizeof(int32_t)));
+  if (!h.empty()) PD_CK(c, copy_sync(*d, h.data(), h.size() * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
+  return PD_OK;
+}
+
+// After row_ptr/col exist: SELL layout, bond geometry, per-particle geometry, reset.
 int finish_families(pd_ctx* c) {
   cudaStream_t s = c->stream;
   std::string msg;
   PD_CK(c, cudaMemsetAsync(c->counters, 0, pd::CNT_N * sizeof(unsigned long long), s));
+  SpatialOrder order;  // mixed form: SELL chunks and visiting blocks are spatial tiles
+  if (mixed(c)) {
+    order = spatial_order(c->h_x, c->n);
+    std::vector<int32_t> pos((size_t)c->n);
+    for (size_t p = 0; p < order.member.size(); ++p)
+      if (order.member[p] >= 0) pos[(size_t)order.member[p]] = (int32_t)p;
+    std::vector<int32_t> rank((size_t)c->n);
+    for (size_t r = 0; r < rank.size(); ++r) rank[(size_t)order.by_rank[r]] = (int32_t)r;
+    c->sell.npos = (int64_t)order.member.size();
+    int ru = upload_i32(c, &c->sell.member, order.member);
+    if (ru == PD_OK) ru = upload_i32(c, &c->sell.pos_of, pos);
+    if (ru == PD_OK) ru = upload_i32(c, &c->sell.rank, rank);
+    if (ru != PD_OK) return ru;
+  }
   int rc = pd::build_sell(c->n, c->row_ptr, c->col, s, &c->sell, c->counters, &msg);
   if (rc != PD_OK) return fail(c, rc, msg);
   unsigned long long h[pd::CNT_N];
-  PD_CK(c, cudaMemcpy(h, c->counters, sizeof(h), cudaMemcpyDeviceToHost));
+  PD_CK(c, copy_sync(h, c->counters, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
   if (h[pd::CNT_ERROR])
     return fail(c, PD_ERR_ARG, "invalid family: neighbour id out of range or a self bond (error word " +
                                    std::to_string(h[pd::CNT_ERROR]) + ")");
@@ -420,9 +490,9 @@ int finish_families(pd_ctx* c) {
     if (!(ls > 0.0)) {
       std::vector<int64_t> rp(c->n + 1);
       std::vector<int32_t> col((size_t)(c->nnz > 0 ? c->nnz : 1));
-      PD_CK(c, cudaMemcpy(rp.data(), c->row_ptr, rp.size() * sizeof(int64_t), cudaMemcpyDeviceToHost));
+      PD_CK(c, copy_sync(rp.data(), c->row_ptr, rp.size() * sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
       if (c->nnz > 0)
-        PD_CK(c, cudaMemcpy(col.data(), c->col, (size_t)c->nnz * sizeof(int32_t), cudaMemcpyDeviceToHost));
+        PD_CK(c, copy_sync(col.data(), c->col, (size_t)c->nnz * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
       double m2 = 0.0;
       for (int64_t i = 0; i < c->n; ++i)
         for (int64_t k = rp[i]; k < rp[i + 1]; ++k) {
@@ -435,11 +505,16 @@ int finish_families(pd_ctx* c) {
     for (double v : c->h_vol) vsum += v;
     c->ls = ls;
     c->vs_scale = c->n > 0 ? vsum / (double)c->n : 1.0;
-    const std::vector<int32_t> order = chunk_visit_order(c->h_x, c->n, ls / 3.0);
-    PD_CK(c, cudaMalloc(&c->sell.chunk_order, (order.empty() ? 1 : order.size()) * sizeof(int32_t)));
-    if (!order.empty())
-      PD_CK(c, cudaMemcpy(c->sell.chunk_order, order.data(), order.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
-    const int rch = pd::build_halo_mixed(mixed_args(c), c->sell.nslots, s, &c->halo, &msg);
+    int32_t *d_by_rank = nullptr, *d_blocks = nullptr;
+    int ru = upload_i32(c, &d_by_rank, order.by_rank);
+    if (ru == PD_OK) ru = upload_i32(c, &d_blocks, order.blocks);
+    const int64_t nblocks = (int64_t)order.blocks.size() / (pd::kHaloBlock / 32);
+    const int rch = ru != PD_OK ? ru
+                                : pd::build_halo_mixed(mixed_args(c), c->sell.nslots, nblocks, d_blocks,
+                                                       c->sell.rank, d_by_rank, s, &c->halo, &msg);
+    dfree(d_by_rank);
+    dfree(d_blocks);
+    if (ru != PD_OK) return ru;
     if (rch != PD_OK) return fail(c, rch, msg);
     int rc2 = upload_gvel(c);
     if (rc2 != PD_OK) return rc2;
@@ -448,7 +523,7 @@ int finish_families(pd_ctx* c) {
   PD_CK(c, cudaGetLastError());
   {
     std::vector<int64_t> rp((size_t)c->n + 1);
-    PD_CK(c, cudaMemcpy(rp.data(), c->row_ptr, rp.size() * sizeof(int64_t), cudaMemcpyDeviceToHost));
+    PD_CK(c, copy_sync(rp.data(), c->row_ptr, rp.size() * sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
     int64_t m = 0;
     for (int64_t i = 0; i < c->n; ++i) m = std::max(m, rp[i + 1] - rp[i]);
     c->max_family = (int32_t)m;
@@ -504,12 +579,12 @@ int pd_create(const pd_params* p, pd_ctx** out) {
   cudaError_t e = cudaSetDevice(p->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMalloc(&c->counters, pd::CNT_N * sizeof(unsigned long long));
-  if (e == cudaSuccess) e = cudaMemset(c->counters, 0, pd::CNT_N * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->counters, 0, pd::CNT_N * sizeof(unsigned long long), c->stream);
   if (e == cudaSuccess) e = cudaMalloc(&c->gkind, PD_MAX_BC_GROUPS * sizeof(int32_t));
   if (e == cudaSuccess) e = cudaMalloc(&c->gval, PD_MAX_BC_GROUPS * sizeof(double2));
-  if (e == cudaSuccess) e = cudaMemset(c->gkind, 0, PD_MAX_BC_GROUPS * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->gkind, 0, PD_MAX_BC_GROUPS * sizeof(int32_t), c->stream);
   if (e == cudaSuccess && p->precision == PD_MIXED) e = cudaMalloc(&c->gvel, PD_MAX_BC_GROUPS * sizeof(float4));
-  if (e == cudaSuccess && c->gvel) e = cudaMemset(c->gvel, 0, PD_MAX_BC_GROUPS * sizeof(float4));
+  if (e == cudaSuccess && c->gvel) e = cudaMemsetAsync(c->gvel, 0, PD_MAX_BC_GROUPS * sizeof(float4), c->stream);
   if (e != cudaSuccess) {
     g_create_err = std::string("pd_create: ") + cudaGetErrorString(e);
     pd_destroy(c.release());
@@ -625,10 +700,10 @@ int pd_set_particles(pd_ctx* c, int64_t n, const double* x, const double* vol) {
   PD_CK(c, cudaMalloc(&c->singular, nn));
   PD_CK(c, cudaMalloc(&c->broken, nn * sizeof(int32_t)));
   PD_CK(c, cudaMalloc(&c->fam, nn * sizeof(int32_t)));
-  PD_CK(c, cudaMemset(c->bc, 0, nn));
+  PD_CK(c, cudaMemsetAsync(c->bc, 0, nn, c->stream));
   if (n > 0) {
-    PD_CK(c, cudaMemcpy(c->x, x, (size_t)n * sizeof(double2), cudaMemcpyHostToDevice));
-    PD_CK(c, cudaMemcpy(c->vol, vol, (size_t)n * sizeof(double), cudaMemcpyHostToDevice));
+    PD_CK(c, copy_sync(c->x, x, (size_t)n * sizeof(double2), cudaMemcpyHostToDevice, c->stream));
+    PD_CK(c, copy_sync(c->vol, vol, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   }
   c->h_x.assign(x, x + 2 * n);
   c->h_vol.assign(vol, vol + n);
@@ -672,8 +747,8 @@ int pd_set_families(pd_ctx* c, const int64_t* row_ptr, const int32_t* col) {
   c->nnz = nnz;
   PD_CK(c, cudaMalloc(&c->row_ptr, (size_t)(n + 1) * sizeof(int64_t)));
   PD_CK(c, cudaMalloc(&c->col, (size_t)(nnz > 0 ? nnz : 1) * sizeof(int32_t)));
-  PD_CK(c, cudaMemcpy(c->row_ptr, row_ptr, (size_t)(n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
-  if (nnz > 0) PD_CK(c, cudaMemcpy(c->col, col, (size_t)nnz * sizeof(int32_t), cudaMemcpyHostToDevice));
+  PD_CK(c, copy_sync(c->row_ptr, row_ptr, (size_t)(n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, c->stream));
+  if (nnz > 0) PD_CK(c, copy_sync(c->col, col, (size_t)nnz * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
   return finish_families(c);
 }
 
@@ -688,8 +763,10 @@ int pd_get_families(pd_ctx* c, int64_t* row_ptr, int32_t* col) {
   if (!c->has_families) return fail(c, PD_ERR_ORDER, "no families");
   PD_CK(c, cudaSetDevice(c->p.device));
   PD_CK(c, cudaStreamSynchronize(c->stream));
-  if (row_ptr) PD_CK(c, cudaMemcpy(row_ptr, c->row_ptr, (size_t)(c->n + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost));
-  if (col && c->nnz > 0) PD_CK(c, cudaMemcpy(col, c->col, (size_t)c->nnz * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  if (row_ptr)
+    PD_CK(c, copy_sync(row_ptr, c->row_ptr, (size_t)(c->n + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
+  if (col && c->nnz > 0)
+    PD_CK(c, copy_sync(col, c->col, (size_t)c->nnz * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
   return PD_OK;
 }
 
@@ -713,8 +790,8 @@ int pd_set_bc(pd_ctx* c, int32_t n_groups, const int32_t* kind, const double* va
     val[2 * g] = value[2 * g];
     val[2 * g + 1] = value[2 * g + 1];
   }
-  PD_CK(c, cudaMemcpy(c->gkind, k.data(), k.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
-  PD_CK(c, cudaMemcpy(c->gval, val.data(), val.size() * sizeof(double), cudaMemcpyHostToDevice));
+  PD_CK(c, copy_sync(c->gkind, k.data(), k.size() * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
+  PD_CK(c, copy_sync(c->gval, val.data(), val.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   c->h_gval = val;
   if (c->has_families) {
     int rc = upload_gvel(c);
@@ -722,9 +799,9 @@ int pd_set_bc(pd_ctx* c, int32_t n_groups, const int32_t* kind, const double* va
   }
   if (c->n > 0) {
     if (group_of)
-      PD_CK(c, cudaMemcpy(c->bc, group_of, (size_t)c->n, cudaMemcpyHostToDevice));
+      PD_CK(c, copy_sync(c->bc, group_of, (size_t)c->n, cudaMemcpyHostToDevice, c->stream));
     else
-      PD_CK(c, cudaMemset(c->bc, 0, (size_t)c->n));
+      PD_CK(c, cudaMemsetAsync(c->bc, 0, (size_t)c->n, c->stream));
   }
   return PD_OK;
 }
@@ -811,7 +888,8 @@ int pd_get_damage(pd_ctx* c, double* damage) {
   if (!c->has_families) return fail(c, PD_ERR_ORDER, "families first");
   PD_CK(c, cudaSetDevice(c->p.device));
   PD_CK(c, cudaStreamSynchronize(c->stream));
-  if (c->n > 0) PD_CK(c, cudaMemcpy(damage, c->damage, (size_t)c->n * sizeof(double), cudaMemcpyDeviceToHost));
+  if (c->n > 0)
+    PD_CK(c, copy_sync(damage, c->damage, (size_t)c->n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   return PD_OK;
 }
 
@@ -822,7 +900,7 @@ int pd_get_bond_mask(pd_ctx* c, uint8_t* alive) {
   if (c->nnz == 0) return PD_OK;
   uint8_t* d = nullptr;
   PD_CK(c, cudaMallocAsync(&d, (size_t)c->nnz, c->stream));
-  pd::launch_mask_out(c->n, c->row_ptr, c->sell, d, c->stream);
+  pd::launch_mask_out(c->n, c->row_ptr, c->col, c->sell, d, c->stream);
   PD_CK(c, cudaGetLastError());
   PD_CK(c, cudaMemcpyAsync(alive, d, (size_t)c->nnz, cudaMemcpyDeviceToHost, c->stream));
   PD_CK(c, cudaFreeAsync(d, c->stream));
@@ -835,7 +913,7 @@ int pd_get_counters(pd_ctx* c, pd_counters* out) {
   PD_CK(c, cudaSetDevice(c->p.device));
   PD_CK(c, cudaStreamSynchronize(c->stream));
   unsigned long long h[pd::CNT_N];
-  PD_CK(c, cudaMemcpy(h, c->counters, sizeof(h), cudaMemcpyDeviceToHost));
+  PD_CK(c, copy_sync(h, c->counters, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
   out->bonds_broken = (int64_t)h[pd::CNT_BROKEN];
   out->singular_events = (int64_t)h[pd::CNT_SINGULAR];
   out->steps = c->steps;
@@ -1132,12 +1210,12 @@ int pd_checkpoint_save(pd_ctx* c, void* buf, int64_t bytes) {
   h.problem = problem_hash(c);
   h.mazars = c->mz_thr ? 1 : 0;
   h.mz = c->mz;
-  PD_CK(c, cudaMemcpy(h.counters, c->counters, sizeof(h.counters), cudaMemcpyDeviceToHost));
+  PD_CK(c, copy_sync(h.counters, c->counters, sizeof(h.counters), cudaMemcpyDeviceToHost, c->stream));
   unsigned char* o = static_cast<unsigned char*>(buf);
   std::memcpy(o, &h, sizeof(h));
   o += sizeof(h);
   for (const auto& x : ckpt_arrays(c)) {
-    if (x.second) PD_CK(c, cudaMemcpy(o, x.first, x.second, cudaMemcpyDeviceToHost));
+    if (x.second) PD_CK(c, copy_sync(o, x.first, x.second, cudaMemcpyDeviceToHost, c->stream));
     o += x.second;
   }
   return PD_OK;
@@ -1171,7 +1249,7 @@ int pd_checkpoint_load(pd_ctx* c, const void* buf, int64_t bytes) {
   if (bytes < need) return fail(c, PD_ERR_ARG, "checkpoint truncated");
   const unsigned char* p = static_cast<const unsigned char*>(buf) + sizeof(h);
   for (const auto& x : ckpt_arrays(c)) {
-    if (x.second) PD_CK(c, cudaMemcpy(x.first, p, x.second, cudaMemcpyHostToDevice));
+    if (x.second) PD_CK(c, copy_sync(x.first, p, x.second, cudaMemcpyHostToDevice, c->stream));
     p += x.second;
   }
   // derived data: K^-1 / m / singular flags from the restored mask and broken counts,
@@ -1236,7 +1314,7 @@ int pd_synchronize(pd_ctx* c) {
   PD_CK(c, cudaStreamSynchronize(c->stream));
   if (!c->counters) return PD_OK;
   unsigned long long err = 0;
-  PD_CK(c, cudaMemcpy(&err, c->counters + pd::CNT_ERROR, sizeof(err), cudaMemcpyDeviceToHost));
+  PD_CK(c, copy_sync(&err, c->counters + pd::CNT_ERROR, sizeof(err), cudaMemcpyDeviceToHost, c->stream));
   if (err & pd::ERR_STAGE_TIMEOUT) return fail(c, PD_ERR_TIMEOUT, "a bounded wait for a staged bond-index copy gave up");
   return PD_OK;
 }
@@ -1383,10 +1461,9 @@ int batch_refresh(pd_batch* b) {
       std::memcpy(plates.data() + k * asz, &m, asz);
       b->smem_a = std::max(b->smem_a, pd::mixed_pass_smem(m, true));
       b->smem_b = std::max(b->smem_b, pd::mixed_pass_smem(m, false));
-      // one tile per visiting block (kHaloBlock particles) of the plate
-      for (int64_t blk = 0; blk * pd::kHaloBlock < c->n; ++blk)
-        tiles.push_back(
-            pd::BatchTile{(int32_t)k, (int32_t)std::min<int64_t>(pd::kHaloBlock, c->n - blk * pd::kHaloBlock), blk});
+      // one tile per visiting block (one spatial tile of up to kHaloBlock particles) of the plate
+      for (int64_t blk = 0; blk < c->halo.nblocks; ++blk)
+        tiles.push_back(pd::BatchTile{(int32_t)k, pd::kHaloBlock, blk});
     } else {
       const Fp64Args f = fp64_args(c);
       std::memcpy(plates.data() + k * asz, &f, asz);
@@ -1447,7 +1524,7 @@ int pd_batch_create(int32_t device, int32_t precision, pd_batch** out) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMalloc(&b->d_bar, sizeof(pd::GridBarrier));
-  if (e == cudaSuccess) e = cudaMemset(b->d_bar, 0, sizeof(pd::GridBarrier));
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->d_bar, 0, sizeof(pd::GridBarrier), b->stream);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->nsm, cudaDevAttrMultiProcessorCount, device);
   if (e != cudaSuccess) {
     g_create_err = std::string("pd_batch_create: ") + cudaGetErrorString(e);
@@ -1594,7 +1671,7 @@ int pd_batch_synchronize(pd_batch* b) {
   PD_BCK(b, cudaSetDevice(b->device));
   PD_BCK(b, cudaStreamSynchronize(b->stream));
   pd::GridBarrier h;
-  PD_BCK(b, cudaMemcpy(&h, b->d_bar, sizeof(h), cudaMemcpyDeviceToHost));
+  PD_BCK(b, copy_sync(&h, b->d_bar, sizeof(h), cudaMemcpyDeviceToHost, b->stream));
   if (h.err) return bfail(b, PD_ERR_TIMEOUT, "a grid-barrier wait of the persistent batch kernel gave up");
   return PD_OK;
 }

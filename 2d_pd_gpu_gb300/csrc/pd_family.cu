@@ -204,14 +204,16 @@ __global__ void k_scan_add(int64_t* out, int64_t n, const int64_t* tile_off) {
 }
 
 // ---- SELL-32
-__global__ void k_chunk_width(int64_t n, const int64_t* __restrict__ row_ptr, int64_t nchunks, int32_t* chunk_w,
-                              int64_t* chunk_slots) {
+__global__ void k_chunk_width(int64_t npos, const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ member,
+                              int64_t nchunks, int32_t* chunk_w, int64_t* chunk_slots) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nchunks) return;
   int64_t w = 0;
   for (int l = 0; l < kChunk; ++l) {
-    const int64_t i = c * kChunk + l;
-    if (i < n) {
+    const int64_t p = c * kChunk + l;
+    if (p < npos) {
+      const int64_t i = sell_member(member, p);
+      if (i < 0) continue;  // a hole
       const int64_t d = row_ptr[i + 1] - row_ptr[i];
       w = d > w ? d : w;
     }
@@ -220,29 +222,44 @@ __global__ void k_chunk_width(int64_t n, const int64_t* __restrict__ row_ptr, in
   chunk_slots[c] = w * kChunk;
 }
 
+// Slot (0 .. deg) of family entry k of a particle whose family is
+// col[r0 .. r0 + deg): k itself (family order), or with a rank array the
+// entry's place in ascending (rank of the neighbour, k) order; entries that
+// are not valid neighbour ids sort last.
+__device__ __forceinline__ int64_t family_slot(const int32_t* __restrict__ col, int64_t r0, int64_t deg, int64_t k,
+                                               const int32_t* __restrict__ rank, int64_t n) {
+  if (!rank) return k;
+  auto key = [&](int64_t q) {
+    const int32_t j = col[r0 + q];
+    return j >= 0 && (int64_t)j < n ? (int64_t)rank[j] : n + q;
+  };
+  const int64_t kk = key(k);
+  int64_t slot = 0;
+  for (int64_t q = 0; q < deg; ++q) {
+    const int64_t kq = key(q);
+    slot += kq < kk || (kq == kk && q < k);
+  }
+  return slot;
+}
+
+// nbr: every slot is padding (-1) before the fill.
 __global__ void k_sell_fill(int64_t n, const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
-                            const int64_t* __restrict__ chunk_base, const int32_t* __restrict__ chunk_w,
-                            int32_t* nbr, unsigned long long* counters) {
+                            const int64_t* __restrict__ chunk_base, const int32_t* __restrict__ pos_of,
+                            const int32_t* __restrict__ rank, int32_t* nbr, unsigned long long* counters) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const int64_t c = i / kChunk;
-  const int lane = (int)(i % kChunk);
-  const int w = chunk_w[c];
+  const int64_t s0 = sell_slot0(chunk_base, sell_pos(pos_of, i));
   const int64_t r0 = row_ptr[i], deg = row_ptr[i + 1] - r0;
-  for (int k = 0; k < w; ++k) {
-    const int64_t s = chunk_base[c] + (int64_t)k * kChunk + lane;
-    int32_t j = -1;
-    if (k < deg) {
-      j = col[r0 + k];
-      if (j < 0 || (int64_t)j >= n) {
-        atomicOr(counters + CNT_ERROR, (unsigned long long)ERR_BAD_NEIGHBOR);
-        j = -1;
-      } else if ((int64_t)j == i) {
-        atomicOr(counters + CNT_ERROR, (unsigned long long)ERR_SELF_BOND);
-        j = -1;
-      }
+  for (int64_t k = 0; k < deg; ++k) {
+    int32_t j = col[r0 + k];
+    if (j < 0 || (int64_t)j >= n) {
+      atomicOr(counters + CNT_ERROR, (unsigned long long)ERR_BAD_NEIGHBOR);
+      j = -1;
+    } else if ((int64_t)j == i) {
+      atomicOr(counters + CNT_ERROR, (unsigned long long)ERR_SELF_BOND);
+      j = -1;
     }
-    nbr[s] = j;
+    nbr[s0 + family_slot(col, r0, deg, k, rank, n) * kChunk] = j;
   }
 }
 
@@ -257,16 +274,16 @@ __device__ __forceinline__ void bond_limits(double ex, double ey, double s_c, do
 
 __global__ void k_bond_geometry(int64_t n, const double2* __restrict__ x, const double* __restrict__ vol,
                                 const int64_t* __restrict__ chunk_base, const int32_t* __restrict__ chunk_w,
-                                const int32_t* __restrict__ nbr, double s_c, double2* bxi, double2* bgeo,
-                                double* blim, float* br2) {
+                                const int32_t* __restrict__ pos_of, const int32_t* __restrict__ nbr, double s_c,
+                                double2* bxi, double2* bgeo, double* blim, float* br2) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const int64_t c = i / kChunk;
-  const int lane = (int)(i % kChunk);
-  const int w = chunk_w[c];
+  const int64_t p = sell_pos(pos_of, i);
+  const int w = chunk_w[p >> 5];
+  const int64_t s0 = sell_slot0(chunk_base, p);
   const double2 pi = x[i];
   for (int k = 0; k < w; ++k) {
-    const int64_t s = chunk_base[c] + (int64_t)k * kChunk + lane;
+    const int64_t s = s0 + (int64_t)k * kChunk;
     int32_t j = nbr[s];
     if (j < -1) j = -2 - j;  // broken bonds keep their geometry
     if (j < 0) {
@@ -298,26 +315,27 @@ __global__ void k_bond_limit(int64_t nslots, const double2* __restrict__ bxi, do
   }
 }
 
-__global__ void k_mask_out(int64_t n, const int64_t* __restrict__ row_ptr, const int64_t* __restrict__ chunk_base,
-                           const int32_t* __restrict__ nbr, uint8_t* alive) {
+__global__ void k_mask_out(int64_t n, const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
+                           const int64_t* __restrict__ chunk_base, const int32_t* __restrict__ pos_of,
+                           const int32_t* __restrict__ rank, const int32_t* __restrict__ nbr, uint8_t* alive) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const int64_t c = i / kChunk;
-  const int lane = (int)(i % kChunk);
+  const int64_t s0 = sell_slot0(chunk_base, sell_pos(pos_of, i));
   const int64_t r0 = row_ptr[i], deg = row_ptr[i + 1] - r0;
-  for (int64_t k = 0; k < deg; ++k) alive[r0 + k] = nbr[chunk_base[c] + k * kChunk + lane] >= 0 ? 1 : 0;
+  for (int64_t k = 0; k < deg; ++k)
+    alive[r0 + k] = nbr[s0 + family_slot(col, r0, deg, k, rank, n) * kChunk] >= 0 ? 1 : 0;
 }
 
 // Restore every family bond to intact (pd_reset).
 __global__ void k_sell_reset(int64_t n, const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
-                             const int64_t* __restrict__ chunk_base, int32_t* nbr) {
+                             const int64_t* __restrict__ chunk_base, const int32_t* __restrict__ pos_of,
+                             const int32_t* __restrict__ rank, int32_t* nbr) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const int64_t c = i / kChunk;
-  const int lane = (int)(i % kChunk);
+  const int64_t s0 = sell_slot0(chunk_base, sell_pos(pos_of, i));
   const int64_t r0 = row_ptr[i], deg = row_ptr[i + 1] - r0;
   for (int64_t k = 0; k < deg; ++k) {
-    const int64_t s = chunk_base[c] + k * kChunk + lane;
+    const int64_t s = s0 + family_slot(col, r0, deg, k, rank, n) * kChunk;
     if (nbr[s] < -1) nbr[s] = col[r0 + k];
   }
 }
@@ -447,14 +465,16 @@ int build_families_gpu(int64_t n, const double2* d_x, const double* h_x, double 
 
 int build_sell(int64_t n, const int64_t* d_row_ptr, const int32_t* d_col, cudaStream_t s, SellLayout* L,
                unsigned long long* d_counters, std::string* msg) {
-  L->nchunks = (n + kChunk - 1) / kChunk;
+  if (!L->member) L->npos = n;
+  L->nchunks = (L->npos + kChunk - 1) / kChunk;
   int64_t* slots = nullptr;
   const size_t nch = (size_t)(L->nchunks > 0 ? L->nchunks : 1);
   cudaMallocAsync(&L->chunk_w, nch * sizeof(int32_t), s);
   cudaMallocAsync(&L->chunk_base, (nch + 1) * sizeof(int64_t), s);
   cudaMallocAsync(&slots, nch * sizeof(int64_t), s);
   if (L->nchunks > 0)
-    k_chunk_width<<<(unsigned)blocks_for(L->nchunks), kBlock, 0, s>>>(n, d_row_ptr, L->nchunks, L->chunk_w, slots);
+    k_chunk_width<<<(unsigned)blocks_for(L->nchunks), kBlock, 0, s>>>(L->npos, d_row_ptr, L->member, L->nchunks,
+                                                                      L->chunk_w, slots);
   scan_exclusive_i64(slots, L->chunk_base, L->nchunks, s);
   cudaMemcpyAsync(&L->nslots, L->chunk_base + L->nchunks, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
   cudaFreeAsync(slots, s);
@@ -467,9 +487,11 @@ int build_sell(int64_t n, const int64_t* d_row_ptr, const int32_t* d_col, cudaSt
     *msg = "out of device memory (bond slots)";
     return PD_ERR_CAPACITY;
   }
+  // every slot starts as padding: the lanes past n of the last chunk own slots no particle fills
+  if (L->nslots > 0) cudaMemsetAsync(L->nbr, 0xFF, (size_t)L->nslots * sizeof(int32_t), s);
   if (n > 0)
-    k_sell_fill<<<(unsigned)blocks_for(n), kBlock, 0, s>>>(n, d_row_ptr, d_col, L->chunk_base, L->chunk_w, L->nbr,
-                                                          d_counters);
+    k_sell_fill<<<(unsigned)blocks_for(n), kBlock, 0, s>>>(n, d_row_ptr, d_col, L->chunk_base, L->pos_of, L->rank,
+                                                          L->nbr, d_counters);
   e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) {
     *msg = std::string("sell fill: ") + cudaGetErrorString(e);
@@ -482,8 +504,8 @@ void launch_bond_geometry_fp64(int64_t n, const double2* x, const double* vol, c
                                const int64_t* /*row_ptr*/, double s_c, double2* bxi, double2* bgeo, double* blim,
                                float* br2, cudaStream_t s) {
   if (n > 0)
-    k_bond_geometry<<<(unsigned)blocks_for(n), kBlock, 0, s>>>(n, x, vol, L.chunk_base, L.chunk_w, L.nbr, s_c, bxi,
-                                                              bgeo, blim, br2);
+    k_bond_geometry<<<(unsigned)blocks_for(n), kBlock, 0, s>>>(n, x, vol, L.chunk_base, L.chunk_w, L.pos_of, L.nbr,
+                                                              s_c, bxi, bgeo, blim, br2);
 }
 
 void launch_bond_limit_fp64(int64_t nslots, const double2* bxi, double s_c, const int32_t* nbr, double* blim,
@@ -491,12 +513,16 @@ void launch_bond_limit_fp64(int64_t nslots, const double2* bxi, double s_c, cons
   if (nslots > 0) k_bond_limit<<<(unsigned)blocks_for(nslots), kBlock, 0, s>>>(nslots, bxi, s_c, nbr, blim, br2);
 }
 
-void launch_mask_out(int64_t n, const int64_t* row_ptr, const SellLayout& L, uint8_t* alive, cudaStream_t s) {
-  if (n > 0) k_mask_out<<<(unsigned)blocks_for(n), kBlock, 0, s>>>(n, row_ptr, L.chunk_base, L.nbr, alive);
+void launch_mask_out(int64_t n, const int64_t* row_ptr, const int32_t* col, const SellLayout& L, uint8_t* alive,
+                     cudaStream_t s) {
+  if (n > 0)
+    k_mask_out<<<(unsigned)blocks_for(n), kBlock, 0, s>>>(n, row_ptr, col, L.chunk_base, L.pos_of, L.rank, L.nbr,
+                                                         alive);
 }
 
 void launch_sell_reset(int64_t n, const int64_t* row_ptr, const int32_t* col, const SellLayout& L, cudaStream_t s) {
-  if (n > 0) k_sell_reset<<<(unsigned)blocks_for(n), kBlock, 0, s>>>(n, row_ptr, col, L.chunk_base, L.nbr);
+  if (n > 0)
+    k_sell_reset<<<(unsigned)blocks_for(n), kBlock, 0, s>>>(n, row_ptr, col, L.chunk_base, L.pos_of, L.rank, L.nbr);
 }
 
 }  // namespace pd

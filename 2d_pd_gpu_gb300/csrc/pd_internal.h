@@ -5,11 +5,14 @@
 //                      w01/w23 double2 (W = V sigma K^-1, rows), kinv01 double2
 //                      + kinv22 double (K^-1), mt double2 (m / V), bc uint8,
 //                      broken int32, damage double, singular uint8, fam int32.
-//   per bond:          SELL-32 ("sliced ELL", chunk = 32 consecutive particles
-//                      = one warp, column-major inside a chunk): slot k of
-//                      particle i lives at chunk_base[i/32] + 32*k + (i%32),
-//                      so each bond slot of a warp is one coalesced 128 B (int)
-//                      or 512 B (double2) line.  nbr int32 (j, -1 padding,
+//   per bond:          SELL-32 ("sliced ELL", chunk = 32 particles = one
+//                      warp, column-major inside a chunk): particle i sits at
+//                      SELL position p = pos_of[i] (member[p] = i; the FP64
+//                      form uses p = i, the mixed form a tiled spatial order
+//                      of the reference positions), and its slot k at
+//                      chunk_base[p/32] + 32*k + (p%32), so each bond slot of
+//                      a warp is one coalesced 128 B (int) or 512 B (double2)
+//                      line.  nbr int32 (j, -1 padding,
 //                      -2-j broken), bxi double2 (xi = x_j - x_i), bgeo double2
 //                      (V_j xi), blim double (((1+s_c)^2-1) |xi|^2).
 //   Precomputing the bond geometry trades HBM bytes for FP64 operations: on
@@ -29,14 +32,25 @@ namespace pd {
 
 constexpr int kChunk = 32;
 constexpr int kBlock = 256;
+
+// SELL position of particle i and particle at position p (null maps: identity).
+__host__ __device__ __forceinline__ int64_t sell_pos(const int32_t* pos_of, int64_t i) {
+  return pos_of ? (int64_t)pos_of[i] : i;
+}
+__host__ __device__ __forceinline__ int64_t sell_member(const int32_t* member, int64_t p) {
+  return member ? (int64_t)member[p] : p;
+}
+// First slot (k = 0) of the particle at SELL position p.
+__host__ __device__ __forceinline__ int64_t sell_slot0(const int64_t* chunk_base, int64_t p) {
+  return chunk_base[p >> 5] + (p & 31);
+}
 // Threads (= particles) of one visiting block of the mixed single-plate and
-// batched passes: kHaloBlock / 32 chunks stacked across rows share a halo.
-// (128 measured 4 % slower on the 1000 x 1000 plate: more halo per particle.)
+// batched passes: kHaloBlock consecutive SELL positions (a 32 x 8 tile of
+// the reference positions) share a halo.
 constexpr int kHaloBlock = 256;
 // Halo staging of the mixed passes: a block stages at most kHaloCap
-// particles whose ids span at most 32 * kHaloSpanWords.
+// distinct particles (a power of two).
 constexpr int kHaloCap = 2048;
-constexpr int kHaloSpanWords = 2048;
 
 // Counters word layout (device int64 array).
 enum { CNT_BROKEN = 0, CNT_SINGULAR = 1, CNT_ERROR = 2, CNT_N = 4 };
@@ -66,6 +80,8 @@ struct Fp64Args {
   const int64_t* __restrict__ chunk_base;
   const int32_t* __restrict__ chunk_w;
   int32_t* nbr;
+  const int32_t* __restrict__ member;  // SELL position -> particle
+  const int32_t* __restrict__ pos_of;  // particle -> SELL position
   const double2* __restrict__ bxi;
   const double2* __restrict__ bgeo;
   const double* __restrict__ blim;
@@ -103,9 +119,10 @@ struct MazarsArgs {
   double* status;  // per particle: sum of bond damage / family size
 };
 
-// Chunk a warp runs in the mixed single-plate passes, in visiting order.
+// Chunk a warp runs in the mixed passes: warp w of visiting block b runs
+// visit[b * kHaloBlock / 32 + w].
 struct alignas(16) VisitRec {
-  int32_t chunk, w;  // chunk id, width (slot rows)
+  int32_t chunk, w;  // chunk id (-1: the warp has none), width (slot rows)
   int64_t base;      // first slot
 };
 
@@ -133,8 +150,10 @@ struct MixedArgs {
   const int64_t* __restrict__ chunk_base;
   const int32_t* __restrict__ chunk_w;
   int32_t* nbr;
-  const int32_t* __restrict__ chunk_order;  // warp w of a pass runs chunk chunk_order[w]
-  const VisitRec* __restrict__ visit;       // the same, with the chunk's width and first slot
+  const int32_t* __restrict__ member;       // SELL position -> particle (-1: a hole)
+  const int32_t* __restrict__ pos_of;       // particle -> SELL position
+  const VisitRec* __restrict__ visit;       // per warp of each visiting block: its chunk
+  int64_t nblocks;                          // visiting blocks (kHaloBlock threads, one tile each)
   uint16_t* loc;                            // per slot: position in the block's halo (padding / broken: the
                                             // particle's own position, whose data adds exact zeros)
   const uint16_t* __restrict__ self_loc;    // per particle: its own position in its block's halo
@@ -161,11 +180,16 @@ int build_families_gpu(int64_t n, const double2* d_x, const double* h_x, double 
                        const double* h_cracks, cudaStream_t s, FamilyBuild* out, std::string* msg);
 // SELL-32 layout of a CSR family (+ FP64 bond geometry).  d_* are device pointers.
 struct SellLayout {
+  int64_t npos = 0;  // SELL positions: n, or more when member leaves holes (-1 entries)
   int64_t nchunks = 0, nslots = 0;
   int64_t* chunk_base = nullptr;
   int32_t* chunk_w = nullptr;
   int32_t* nbr = nullptr;
-  int32_t* chunk_order = nullptr;  // mixed form: chunks in visiting order (spatially compact blocks)
+  int32_t* member = nullptr;  // SELL position -> particle, -1 = hole (set with npos before build_sell)
+  int32_t* pos_of = nullptr;  // particle -> SELL position
+  // null: a particle's slots follow its family order (the reference's summation
+  // order); else in ascending rank[j] of the neighbours (set before build_sell)
+  int32_t* rank = nullptr;
 };
 int build_sell(int64_t n, const int64_t* d_row_ptr, const int32_t* d_col, cudaStream_t s, SellLayout* out,
                unsigned long long* d_counters, std::string* msg);
@@ -174,7 +198,8 @@ void launch_bond_geometry_fp64(int64_t n, const double2* x, const double* vol, c
                                float* br2, cudaStream_t s);
 void launch_bond_limit_fp64(int64_t nslots, const double2* bxi, double s_c, const int32_t* nbr, double* blim,
                             float* br2, cudaStream_t s);
-void launch_mask_out(int64_t n, const int64_t* row_ptr, const SellLayout& L, uint8_t* alive, cudaStream_t s);
+void launch_mask_out(int64_t n, const int64_t* row_ptr, const int32_t* col, const SellLayout& L, uint8_t* alive,
+                     cudaStream_t s);
 void launch_sell_reset(int64_t n, const int64_t* row_ptr, const int32_t* col, const SellLayout& L, cudaStream_t s);
 // exclusive scan of int64 in[0..n) -> out[0..n], out[n] = total (device)
 void scan_exclusive_i64(const int64_t* in, int64_t* out, int64_t n, cudaStream_t s);
@@ -207,7 +232,7 @@ void launch_mazars_from_csr(const Fp64Args& a, const int64_t* row_ptr, const Maz
 
 // ---- mixed step (pd_mixed.cu)
 void launch_init_geometry_mixed(const MixedArgs& a, cudaStream_t s);
-// per-block halos of the single-plate passes (needs chunk_order, SELL)
+// per-block halos of the single-plate passes (needs the SELL layout)
 struct HaloLayout {
   int64_t nblocks = 0, staged = 0;
   VisitRec* visit = nullptr;
@@ -218,7 +243,12 @@ struct HaloLayout {
   int32_t* halo_n = nullptr;
   int32_t halo_max = 0;
 };
-int build_halo_mixed(const MixedArgs& a, int64_t nslots, cudaStream_t s, HaloLayout* out, std::string* msg);
+// block_chunks: nblocks x (kHaloBlock / 32) chunk ids (-1: none) of the
+// visiting blocks; rank: particle -> spatial rank, by_rank: its inverse
+// (halos are sorted by rank)
+int build_halo_mixed(const MixedArgs& a, int64_t nslots, int64_t nblocks, const int32_t* block_chunks,
+                     const int32_t* rank, const int32_t* by_rank, cudaStream_t s, HaloLayout* out,
+                     std::string* msg);
 void launch_halo_relink(const MixedArgs& a, const HaloLayout& h, cudaStream_t s);
 void launch_drift_mixed(const MixedArgs& a, cudaStream_t s);
 void launch_pass_a_mixed(const MixedArgs& a, bool breaking, cudaStream_t s);

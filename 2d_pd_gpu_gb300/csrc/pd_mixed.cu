@@ -62,16 +62,9 @@ __device__ __forceinline__ float2 tf_diff2(float4 j, float2 nhi, float2 nlo) {
   return add2(add2(f2(j.x, j.y), nhi), add2(f2(j.z, j.w), nlo));
 }
 
-__device__ __forceinline__ int64_t slot0(const MixedArgs& a, int64_t i, int* w) {
-  const int64_t c = i >> 5;
-  *w = a.chunk_w[c];
-  return a.chunk_base[c] + (i & 31);
-}
-
-// K^-1 (FP64 inversion + guard) and m^ from the FP64 reference positions.
-__device__ void kinv_update_mixed(const MixedArgs& a, int64_t i) {
-  int w;
-  const int64_t s0 = slot0(a, i, &w);
+// K^-1 (FP64 inversion + guard) and m^ from the FP64 reference positions;
+// particle i's slots are s0 + 32 k, k < w.
+__device__ void kinv_update_mixed(const MixedArgs& a, int64_t i, int64_t s0, int w) {
   const double2 xi = a.x[i];
   double k11 = 0.0, k12 = 0.0, k22 = 0.0, mx = 0.0, my = 0.0;
   int nal = 0;
@@ -109,7 +102,9 @@ __device__ void kinv_update_mixed(const MixedArgs& a, int64_t i) {
 
 __global__ void __launch_bounds__(kBlock) k_init_geometry_mixed(MixedArgs a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < a.n) kinv_update_mixed(a, i);
+  if (i >= a.n) return;
+  const int64_t p = sell_pos(a.pos_of, i);
+  kinv_update_mixed(a, i, sell_slot0(a.chunk_base, p), a.chunk_w[p >> 5]);
 }
 
 // BC + drift of particle i in scaled per-step units; an = a^ of the new force.
@@ -224,7 +219,7 @@ __device__ __forceinline__ void pass_a_core(const MixedArgs& a, int64_t i, const
     const int32_t b = a.broken[i] + newly;
     a.broken[i] = b;
     a.damage[i] = (double)b / (double)a.fam[i];
-    kinv_update_mixed(a, i);
+    kinv_update_mixed(a, i, s0, w);
     g = a.geo[i];
     singular = a.singular[i];
   }
@@ -314,7 +309,8 @@ struct GatherB {
 
 
 // ---- single-plate and batched passes.  Visiting block b runs the chunks
-// visit[8b .. 8b+8) (spatially compact, see the chunk order in pd_api.cu).
+// visit[8b .. 8b+8): SELL positions 256 b .. 256 b + 256, one 32 x 8 tile
+// of the reference positions (8 row segments of 32).
 // Blocks whose halo -- the distinct particles their bonds reach -- was
 // staged at setup (halo_n[b] >= 0) gather the halo's data into shared memory
 // (cp.async) and walk their bonds entirely out of shared memory (16-bit halo
@@ -354,19 +350,17 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 
 // The calling warp's chunk (one 16 B visit record); false if the warp has none.
 __device__ __forceinline__ bool warp_chunk(const MixedArgs& a, int64_t blk, int64_t* chunk, int* w, int64_t* base) {
-  const int64_t gw = blk * (kHaloBlock / 32) + (threadIdx.x >> 5);
-  if ((gw << 5) >= a.n) return false;  // warp-uniform
-  if (a.visit) {
-    const VisitRec r = a.visit[gw];
-    *chunk = r.chunk;
-    *w = r.w;
-    *base = r.base;
-  } else {
-    *chunk = a.chunk_order[gw];
-    *w = a.chunk_w[*chunk];
-    *base = a.chunk_base[*chunk];
-  }
+  const VisitRec r = a.visit[blk * (kHaloBlock / 32) + (threadIdx.x >> 5)];
+  if (r.chunk < 0) return false;  // warp-uniform
+  *chunk = r.chunk;
+  *w = r.w;
+  *base = r.base;
   return true;
+}
+
+// Particle of lane `lane` of SELL chunk `chunk`, -1 for a hole.
+__device__ __forceinline__ int64_t lane_particle(const MixedArgs& a, int64_t chunk, int lane) {
+  return a.member[chunk * 32 + lane];
 }
 
 __device__ __forceinline__ void stage_timeout(const MixedArgs& a) {
@@ -411,9 +405,9 @@ __device__ __forceinline__ bool pass_a_block(const MixedArgs& a, int64_t blk, un
   int w = 0;
   const bool has = warp_chunk(a, blk, &chunk, &w, &base);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t i = chunk * 32 + lane;
   const int hn = a.halo_n ? a.halo_n[blk] : -1;
-  const bool live = has && i < a.n;
+  const int64_t i = has ? lane_particle(a, chunk, lane) : -1;
+  const bool live = i >= 0;
   PreA pre{};
   if (live) pre = load_a(a, i);  // in flight during the staging below
   if (hn < 0) {  // int32 indices staged per warp, neighbour data from L1/L2
@@ -464,9 +458,9 @@ __device__ __forceinline__ bool pass_b_block(const MixedArgs& a, int64_t blk, un
   int w = 0;
   const bool has = warp_chunk(a, blk, &chunk, &w, &base);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t i = chunk * 32 + lane;
   const int hn = a.halo_n ? a.halo_n[blk] : -1;
-  const bool live = has && i < a.n;
+  const int64_t i = has ? lane_particle(a, chunk, lane) : -1;
+  const bool live = i >= 0;
   PreB pre{};
   if (live) pre = load_b<DRIFT>(a, i);  // in flight during the staging below
   if (hn < 0) {
@@ -516,8 +510,8 @@ __device__ __forceinline__ void drift_block(const MixedArgs& a, int64_t blk) {
   int64_t chunk = 0, base = 0;
   int w = 0;
   if (!warp_chunk(a, blk, &chunk, &w, &base)) return;
-  const int64_t i = chunk * 32 + (threadIdx.x & 31);
-  if (i < a.n) drift_particle_mixed(a, i);
+  const int64_t i = lane_particle(a, chunk, threadIdx.x & 31);
+  if (i >= 0) drift_particle_mixed(a, i);
 }
 
 template <bool BREAK>
@@ -544,114 +538,114 @@ inline size_t pass_smem_bytes(const MixedArgs& a, bool pass_a) {
   return halo > idx32 ? halo : idx32;
 }
 
-// ---- halo build (setup): per block, the sorted distinct particles its
-// chunks' bonds reach (own particles included), found with a bitmap over
-// the block's id span, and every slot's position in that list.
+// ---- halo build (setup): per block, the distinct particles its chunks'
+// bonds reach (own particles included) in spatial-rank order, and every
+// slot's position in that list.  The ranks are collected in a shared-memory
+// hash set (open addressing, linear probing), compacted, sorted (bitonic)
+// and looked up by binary search; a block with more than kHaloCap distinct
+// particles is not staged.
 __device__ __forceinline__ int decode_nbr(int v) { return v >= 0 ? v : (v <= -2 ? -2 - v : -1); }
 
-__global__ void __launch_bounds__(kHaloBlock) k_halo_build(MixedArgs a, int32_t* halo, int32_t* halo_n, uint16_t* loc,
-                                                       uint16_t* loc0, uint16_t* self_loc) {
-  __shared__ uint32_t bits[kHaloSpanWords];
-  __shared__ int32_t pre[kHaloSpanWords];
-  __shared__ int32_t wsum[kHaloBlock / 32];
-  __shared__ int32_t s_lo, s_hi;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+constexpr int kHaloHashBits = 12;
+constexpr int kHaloHash = 1 << kHaloHashBits;
+static_assert(kHaloHash >= 2 * kHaloCap && kHaloHash > kHaloCap + kHaloBlock, "halo hash table too small");
+static_assert((kHaloCap & (kHaloCap - 1)) == 0, "kHaloCap is a power of two (bitonic sort)");
+
+__global__ void __launch_bounds__(kHaloBlock) k_halo_build(MixedArgs a, const int32_t* __restrict__ rank,
+                                                       const int32_t* __restrict__ by_rank, int32_t* halo,
+                                                       int32_t* halo_n, uint16_t* loc, uint16_t* loc0,
+                                                       uint16_t* self_loc) {
+  __shared__ int32_t tab[kHaloHash];
+  __shared__ int32_t list[kHaloCap];
+  __shared__ int32_t s_cnt, s_put;
+  const int tid = threadIdx.x, lane = tid & 31;
   int64_t chunk = 0, base = 0;
   int w = 0;
   const bool has = warp_chunk(a, blockIdx.x, &chunk, &w, &base);
   if (!has) w = 0;
   const int64_t s0 = base + lane;
-  const int64_t i = has && chunk * 32 + lane < a.n ? chunk * 32 + lane : -1;
+  const int64_t i = has ? lane_particle(a, chunk, lane) : -1;
+  for (int k = tid; k < kHaloHash; k += kHaloBlock) tab[k] = -1;
   if (tid == 0) {
-    s_lo = INT_MAX;
-    s_hi = -1;
+    s_cnt = 0;
+    s_put = 0;
   }
   __syncthreads();
-  int lo = i >= 0 ? (int)i : INT_MAX, hi = (int)i;
-  for (int k = 0; k < w; ++k) {
+  // A thread inserts only while the count is <= kHaloCap, so at most
+  // kHaloCap + kHaloBlock ids enter the table: it never fills, and every
+  // probe sequence ends at a free or matching entry within kHaloHash steps.
+  auto insert = [&](int j) {
+    if (*reinterpret_cast<volatile int32_t*>(&s_cnt) > kHaloCap) return;
+    uint32_t h = ((uint32_t)j * 2654435761u) >> (32 - kHaloHashBits);
+    for (int probe = 0; probe < kHaloHash; ++probe) {
+      const int prev = atomicCAS(&tab[h], -1, j);
+      if (prev == -1) {
+        atomicAdd(&s_cnt, 1);
+        return;
+      }
+      if (prev == j) return;
+      h = (h + 1u) & (uint32_t)(kHaloHash - 1);
+    }
+  };
+  const int wl = i >= 0 ? w : 0;  // lanes past n own padding slots only
+  if (i >= 0) insert(rank[i]);
+  for (int k = 0; k < wl; ++k) {
     const int j = decode_nbr(a.nbr[s0 + (int64_t)k * kChunk]);
-    if (j >= 0) {
-      lo = min(lo, j);
-      hi = max(hi, j);
-    }
-  }
-  for (int o = 16; o; o >>= 1) {
-    lo = min(lo, __shfl_xor_sync(~0u, lo, o));
-    hi = max(hi, __shfl_xor_sync(~0u, hi, o));
-  }
-  if (lane == 0) {
-    atomicMin(&s_lo, lo);
-    atomicMax(&s_hi, hi);
+    if (j >= 0) insert(rank[j]);
   }
   __syncthreads();
-  const int L = s_lo, Hi = s_hi;
-  bool fits = Hi >= L && (int64_t)Hi - L < 32LL * kHaloSpanWords;
-  if (fits) {
-    for (int k = tid; k < kHaloSpanWords; k += kHaloBlock) bits[k] = 0u;
+  const int tot = s_cnt;  // block-uniform
+  if (tot <= kHaloCap) {
+    int P = 1;
+    while (P < tot) P <<= 1;
+    for (int k = tid; k < kHaloHash; k += kHaloBlock) {
+      const int v = tab[k];
+      if (v >= 0) list[atomicAdd(&s_put, 1)] = v;
+    }
+    for (int k = tot + tid; k < P; k += kHaloBlock) list[k] = INT_MAX;
     __syncthreads();
-    if (i >= 0) atomicOr(&bits[(i - L) >> 5], 1u << ((i - L) & 31));
-    for (int k = 0; k < w; ++k) {
-      const int j = decode_nbr(a.nbr[s0 + (int64_t)k * kChunk]);
-      if (j >= 0) atomicOr(&bits[(j - L) >> 5], 1u << ((j - L) & 31));
-    }
-    __syncthreads();
-    constexpr int kPer = kHaloSpanWords / kHaloBlock;
-    int c8[kPer], cnt = 0;
-#pragma unroll
-    for (int q = 0; q < kPer; ++q) {
-      c8[q] = __popc(bits[tid * kPer + q]);
-      cnt += c8[q];
-    }
-    int incl = cnt;
-    for (int o = 1; o < 32; o <<= 1) {
-      const int t = __shfl_up_sync(~0u, incl, o);
-      if (lane >= o) incl += t;
-    }
-    if (lane == 31) wsum[warp] = incl;
-    __syncthreads();
-    int wpre = 0, tot = 0;
-    for (int q = 0; q < kHaloBlock / 32; ++q) {
-      if (q < warp) wpre += wsum[q];
-      tot += wsum[q];
-    }
-    int run = wpre + incl - cnt;
-#pragma unroll
-    for (int q = 0; q < kPer; ++q) {
-      pre[tid * kPer + q] = run;
-      run += c8[q];
-    }
-    __syncthreads();
-    fits = tot <= kHaloCap;
-    if (fits) {
-      if (tid == 0) halo_n[blockIdx.x] = tot;
-      int32_t* H = halo + (int64_t)blockIdx.x * kHaloCap;
-      for (int word = tid; word < kHaloSpanWords; word += kHaloBlock) {
-        uint32_t m = bits[word];
-        int r = pre[word];
-        while (m) {
-          const int bpos = __ffs(m) - 1;
-          H[r++] = L + 32 * word + bpos;
-          m &= m - 1u;
+    for (int kk = 2; kk <= P; kk <<= 1)
+      for (int jj = kk >> 1; jj > 0; jj >>= 1) {
+        for (int t = tid; t < P; t += kHaloBlock) {
+          const int o = t ^ jj;
+          if (o > t) {
+            const int x = list[t], y = list[o];
+            if ((x > y) == ((t & kk) == 0)) {
+              list[t] = y;
+              list[o] = x;
+            }
+          }
         }
+        __syncthreads();
       }
-      auto pos = [&](int j) {
-        const int d = j - L;
-        return (uint16_t)(pre[d >> 5] + __popc(bits[d >> 5] & ((1u << (d & 31)) - 1u)));
-      };
-      const uint16_t self = i >= 0 ? pos((int)i) : (uint16_t)0;
-      if (i >= 0) self_loc[i] = self;
-      for (int k = 0; k < w; ++k) {
-        const int64_t s = s0 + (int64_t)k * kChunk;
-        const int v = a.nbr[s];
-        const int j = decode_nbr(v);
-        const uint16_t l = j >= 0 ? pos(j) : self;  // padding: the particle itself (adds exact zeros)
-        loc0[s] = l;
-        loc[s] = v >= 0 ? l : self;
+    if (tid == 0) halo_n[blockIdx.x] = tot;
+    int32_t* H = halo + (int64_t)blockIdx.x * kHaloCap;
+    for (int k = tid; k < tot; k += kHaloBlock) H[k] = by_rank[list[k]];
+    auto pos = [&](int j) {  // the entry of particle j (its rank is in the list)
+      const int r = rank[j];
+      int lo = 0, hi = tot;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (list[mid] < r)
+          lo = mid + 1;
+        else
+          hi = mid;
       }
-      return;
+      return (uint16_t)lo;
+    };
+    const uint16_t self = i >= 0 ? pos((int)i) : (uint16_t)0;
+    if (i >= 0) self_loc[i] = self;
+    for (int k = 0; k < w; ++k) {
+      const int64_t s = s0 + (int64_t)k * kChunk;
+      const int v = k < wl ? a.nbr[s] : -1;
+      const int j = decode_nbr(v);
+      const uint16_t l = j >= 0 ? pos(j) : self;  // padding: the particle itself (adds exact zeros)
+      loc0[s] = l;
+      loc[s] = v >= 0 ? l : self;
     }
+    return;
   }
-  // too wide or too many: the block reads neighbour data from HBM (loc unused)
+  // too many: the block reads neighbour data from HBM (loc unused)
   if (tid == 0) halo_n[blockIdx.x] = -1;
   if (i >= 0) self_loc[i] = 0;
   for (int k = 0; k < w; ++k) {
@@ -661,13 +655,14 @@ __global__ void __launch_bounds__(kHaloBlock) k_halo_build(MixedArgs a, int32_t*
   }
 }
 
-// visit record of every warp position: {chunk, width, first slot}
-__global__ void k_visit_build(int64_t nchunks, const int32_t* __restrict__ order, const int32_t* __restrict__ chunk_w,
-                              const int64_t* __restrict__ chunk_base, VisitRec* visit) {
+// visit record of every warp of every visiting block: {chunk, width, first slot}
+__global__ void k_visit_build(int64_t nwarps, const int32_t* __restrict__ block_chunks,
+                              const int32_t* __restrict__ chunk_w, const int64_t* __restrict__ chunk_base,
+                              VisitRec* visit) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= nchunks) return;
-  const int32_t c = order[k];
-  visit[k] = VisitRec{c, chunk_w[c], chunk_base[c]};
+  if (k >= nwarps) return;
+  const int32_t c = block_chunks[k];
+  visit[k] = c >= 0 ? VisitRec{c, chunk_w[c], chunk_base[c]} : VisitRec{-1, 0, 0};
 }
 
 // live 16-bit indices from the pristine ones and the int32 mask (after a
@@ -676,9 +671,9 @@ __global__ void k_halo_relink(MixedArgs a, const uint16_t* __restrict__ loc0, co
                               uint16_t* loc) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
-  const int64_t c = i >> 5;
-  const int w = a.chunk_w[c];
-  const int64_t s0 = a.chunk_base[c] + (i & 31);
+  const int64_t p = sell_pos(a.pos_of, i);
+  const int w = a.chunk_w[p >> 5];
+  const int64_t s0 = sell_slot0(a.chunk_base, p);
   const uint16_t self = self_loc[i];
   for (int k = 0; k < w; ++k) {
     const int64_t s = s0 + (int64_t)k * kChunk;
@@ -873,18 +868,18 @@ void launch_pass_a_mixed(const MixedArgs& a, bool breaking, cudaStream_t s) {
   if (a.n <= 0) return;
   const size_t sm = pass_smem_bytes(a, true);
   if (breaking)
-    k_pass_a_mixed<true><<<(unsigned)blocks_for(a.n, kHaloBlock), kHaloBlock, sm, s>>>(a);
+    k_pass_a_mixed<true><<<(unsigned)a.nblocks, kHaloBlock, sm, s>>>(a);
   else
-    k_pass_a_mixed<false><<<(unsigned)blocks_for(a.n, kHaloBlock), kHaloBlock, sm, s>>>(a);
+    k_pass_a_mixed<false><<<(unsigned)a.nblocks, kHaloBlock, sm, s>>>(a);
 }
 
 void launch_pass_b_mixed(const MixedArgs& a, bool drift, cudaStream_t s) {
   if (a.n <= 0) return;
   const size_t sm = pass_smem_bytes(a, false);
   if (drift)
-    k_pass_b_mixed<true><<<(unsigned)blocks_for(a.n, kHaloBlock), kHaloBlock, sm, s>>>(a);
+    k_pass_b_mixed<true><<<(unsigned)a.nblocks, kHaloBlock, sm, s>>>(a);
   else
-    k_pass_b_mixed<false><<<(unsigned)blocks_for(a.n, kHaloBlock), kHaloBlock, sm, s>>>(a);
+    k_pass_b_mixed<false><<<(unsigned)a.nblocks, kHaloBlock, sm, s>>>(a);
 }
 
 void launch_to_mixed(const MixedArgs& a, const double2* u, const double2* v, const double2* f, cudaStream_t s) {
@@ -895,15 +890,17 @@ void launch_from_mixed(const MixedArgs& a, double2* u, double2* v, double2* f, c
   if (a.n > 0) k_from_mixed<<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a, u, v, f);
 }
 
-int build_halo_mixed(const MixedArgs& a, int64_t nslots, cudaStream_t s, HaloLayout* h, std::string* msg) {
-  const int64_t nb = blocks_for(a.n, kHaloBlock);
+int build_halo_mixed(const MixedArgs& a0, int64_t nslots, int64_t nblocks, const int32_t* block_chunks,
+                     const int32_t* rank, const int32_t* by_rank, cudaStream_t s, HaloLayout* h, std::string* msg) {
+  const int64_t nb = nblocks;
   h->nblocks = nb;
   h->staged = 0;
   h->halo_max = 0;
-  if (a.n <= 0) return PD_OK;
+  if (a0.n <= 0 || nb <= 0) return PD_OK;
   const size_t ns = (size_t)(nslots > 0 ? nslots : 1);
-  const int64_t nch = (a.n + kChunk - 1) / kChunk;
-  if (cudaMalloc(&h->visit, (size_t)nch * sizeof(VisitRec)) != cudaSuccess ||
+  const int64_t nw = nb * (kHaloBlock / 32);
+  MixedArgs a = a0;
+  if (cudaMalloc(&h->visit, (size_t)nw * sizeof(VisitRec)) != cudaSuccess ||
       cudaMalloc(&h->loc, ns * sizeof(uint16_t)) != cudaSuccess ||
       cudaMalloc(&h->loc0, ns * sizeof(uint16_t)) != cudaSuccess ||
       cudaMalloc(&h->self_loc, (size_t)a.n * sizeof(uint16_t)) != cudaSuccess ||
@@ -912,8 +909,11 @@ int build_halo_mixed(const MixedArgs& a, int64_t nslots, cudaStream_t s, HaloLay
     *msg = "halo staging: out of device memory";
     return PD_ERR_CUDA;
   }
-  k_visit_build<<<(unsigned)blocks_for(nch), kBlock, 0, s>>>(nch, a.chunk_order, a.chunk_w, a.chunk_base, h->visit);
-  k_halo_build<<<(unsigned)nb, kHaloBlock, 0, s>>>(a, h->halo, h->halo_n, h->loc, h->loc0, h->self_loc);
+  k_visit_build<<<(unsigned)blocks_for(nw), kBlock, 0, s>>>(nw, block_chunks, a.chunk_w, a.chunk_base, h->visit);
+  a.visit = h->visit;
+  a.nblocks = nb;
+  k_halo_build<<<(unsigned)nb, kHaloBlock, 0, s>>>(a, rank, by_rank, h->halo, h->halo_n, h->loc, h->loc0,
+                                                   h->self_loc);
   std::vector<int32_t> cnt((size_t)nb);
   cudaError_t e = cudaMemcpyAsync(cnt.data(), h->halo_n, (size_t)nb * sizeof(int32_t), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
