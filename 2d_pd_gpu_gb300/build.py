@@ -34,6 +34,7 @@ CUDA_UNITS = [
     ("pd_mixed.cu", []),
     ("pd_noalloc.cu", ["--fmad=false"]),
     ("pd_mazars.cu", ["--fmad=false"]),
+    ("pd_order.cu", []),
     ("pd_probe.cu", []),
     ("pd_api.cu", []),
 ]

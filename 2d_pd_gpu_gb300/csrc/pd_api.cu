@@ -148,7 +148,7 @@ void free_families(pd_ctx* c) {
   dfree(c->sell.chunk_w);
   dfree(c->sell.nbr);
   dfree(c->sell.member);
-  dfree(c->sell.rank);
+  dfree(c->sell.rk);
   dfree(c->sell.pos_of);
   dfree(c->mz_thr);
   dfree(c->mz_bd);
@@ -340,134 +340,19 @@ __global__ void k_fam_from_rowptr(int64_t n, const int64_t* rp, int32_t* fam) {
   if (i < n) fam[i] = (int32_t)(rp[i + 1] - rp[i]);
 }
 
-// Stable LSD radix sort of the indices 0..n-1 by 64-bit keys (16-bit digits;
-// equal keys keep index order).
-std::vector<int32_t> sort_by_key(std::vector<uint64_t> key) {
-  const size_t n = key.size();
-  std::vector<int32_t> idx(n), tmp(n);
-  std::vector<uint64_t> key2(n);
-  for (size_t i = 0; i < n; ++i) idx[i] = (int32_t)i;
-  if (n <= 1) return idx;
-  std::vector<int64_t> cnt(65537);
-  for (int shift = 0; shift < 64; shift += 16) {
-    std::fill(cnt.begin(), cnt.end(), 0);
-    for (size_t i = 0; i < n; ++i) ++cnt[((key[i] >> shift) & 0xFFFF) + 1];
-    if (cnt[((key[0] >> shift) & 0xFFFF) + 1] == (int64_t)n) continue;  // one digit value: identity pass
-    for (int d = 0; d < 65536; ++d) cnt[d + 1] += cnt[d];
-    for (size_t i = 0; i < n; ++i) {
-      const int64_t o = cnt[(key[i] >> shift) & 0xFFFF]++;
-      key2[(size_t)o] = key[i];
-      tmp[(size_t)o] = idx[i];
-    }
-    key.swap(key2);
-    idx.swap(tmp);
-  }
-  return idx;
-}
-
-// Spatial orders of the mixed form, from the reference positions binned into
-// square cells of side sqrt(bbox area / n) (about one particle per cell; a
-// lattice's cells are its sites).  Particle numbering, and with it every array
-// the API exposes, is unchanged.
-//   member:  SELL positions in tiles of 32 cells x 8 rows (tiles row-major,
-//            bands of 8 rows), cells row-major inside a tile, every tile
-//            starting a new chunk (the tail of its last chunk is a hole,
-//            member -1).  A chunk (32 positions) is then a row segment with
-//            its lanes in x order, and a visiting block (blocks: up to
-//            kHaloBlock / 32 chunks, -1 = none) is one tile, whose bonds reach
-//            few distinct particles (its halo); a tile of more than
-//            kHaloBlock particles is split into several blocks.
-//   by_rank: particles in global row-major cell order.  Halos are sorted by
-//            this rank and every family is walked in ascending rank of its
-//            neighbours (for a row-major numbering that is the family order),
-//            so the 32 lanes of a row segment read the same neighbour offset
-//            at the same slot, from consecutive halo entries (no shared-memory
-//            bank conflicts), and the step is bit-identical whatever the
-//            numbering.
-// Equal cells keep particle order.
-struct SpatialOrder {
-  std::vector<int32_t> member, blocks, by_rank;
-};
-
-SpatialOrder spatial_order(const std::vector<double>& x, int64_t n) {
-  static_assert(pd::kHaloBlock == 32 * 8, "a visiting block is one 32 x 8 tile");
-  SpatialOrder o;
-  double x0 = INFINITY, x1 = -INFINITY, y0 = INFINITY, y1 = -INFINITY;
-  for (int64_t i = 0; i < n; ++i) {
-    const double px = x[2 * i], py = x[2 * i + 1];
-    if (!std::isfinite(px) || !std::isfinite(py)) continue;
-    x0 = std::min(x0, px);
-    x1 = std::max(x1, px);
-    y0 = std::min(y0, py);
-    y1 = std::max(y1, py);
-  }
-  const double ex = x1 - x0, ey = y1 - y0;
-  double q = std::sqrt(ex * ey / (double)n);
-  if (!(q > 0.0) || !std::isfinite(q)) q = std::max(ex, ey) / (double)n;
-  std::vector<uint64_t> cx((size_t)n, 0), cy((size_t)n, 0);
-  if (q > 0.0 && std::isfinite(q)) {
-    auto cell = [&](double v, double lo) {
-      const double t = std::floor((v - lo) / q);
-      return (uint64_t)(t > 0.0 ? std::min(t, 4294967295.0) : 0.0);
-    };
-    for (int64_t i = 0; i < n; ++i) {
-      const double px = x[2 * i], py = x[2 * i + 1];
-      if (std::isfinite(px) && std::isfinite(py)) {
-        cx[(size_t)i] = cell(px, x0);
-        cy[(size_t)i] = cell(py, y0);
-      }
-    }
-  }
-  uint64_t gx = 1;
-  for (int64_t i = 0; i < n; ++i) gx = std::max(gx, cx[(size_t)i] + 1);
-  const uint64_t tiles_x = (gx + 31) / 32;
-  std::vector<uint64_t> key((size_t)n);
-  for (int64_t i = 0; i < n; ++i) {
-    const uint64_t u = cx[(size_t)i], v = cy[(size_t)i];
-    key[(size_t)i] = (((v >> 3) * tiles_x + (u >> 5)) * 8 + (v & 7)) * 32 + (u & 31);
-  }
-  const std::vector<int32_t> sorted = sort_by_key(key);
-  constexpr int kWarps = pd::kHaloBlock / 32;
-  for (int64_t a = 0; a < n;) {  // one tile: sorted[a .. b)
-    const uint64_t tile = key[(size_t)sorted[(size_t)a]] >> 8;
-    int64_t b = a + 1;
-    while (b < n && (key[(size_t)sorted[(size_t)b]] >> 8) == tile) ++b;
-    const int64_t first_chunk = (int64_t)o.member.size() / 32, nch = (b - a + 31) / 32;
-    for (int64_t k = a; k < b; ++k) o.member.push_back(sorted[(size_t)k]);
-    o.member.resize((size_t)(first_chunk + nch) * 32, -1);
-    for (int64_t c = 0; c < nch; c += kWarps)
-      for (int w = 0; w < kWarps; ++w) o.blocks.push_back(c + w < nch ? (int32_t)(first_chunk + c + w) : -1);
-    a = b;
-  }
-  for (int64_t i = 0; i < n; ++i) key[(size_t)i] = cy[(size_t)i] * gx + cx[(size_t)i];
-  o.by_rank = sort_by_key(std::move(key));
-  return o;
-}
-
-int upload_i32(pd_ctx* c, int32_t** d, const std::vector<int32_t>& h) {
-  PD_CK(c, cudaMalloc(d, (h.empty() ? 1 : h.size()) * sizeof(int32_t)));
-  if (!h.empty()) PD_CK(c, copy_sync(*d, h.data(), h.size() * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
-  return PD_OK;
-}
-
 // After row_ptr/col exist: SELL layout, bond geometry, per-particle geometry, reset.
 int finish_families(pd_ctx* c) {
   cudaStream_t s = c->stream;
   std::string msg;
   PD_CK(c, cudaMemsetAsync(c->counters, 0, pd::CNT_N * sizeof(unsigned long long), s));
-  SpatialOrder order;  // mixed form: SELL chunks and visiting blocks are spatial tiles
-  if (mixed(c)) {
-    order = spatial_order(c->h_x, c->n);
-    std::vector<int32_t> pos((size_t)c->n);
-    for (size_t p = 0; p < order.member.size(); ++p)
-      if (order.member[p] >= 0) pos[(size_t)order.member[p]] = (int32_t)p;
-    std::vector<int32_t> rank((size_t)c->n);
-    for (size_t r = 0; r < rank.size(); ++r) rank[(size_t)order.by_rank[r]] = (int32_t)r;
-    c->sell.npos = (int64_t)order.member.size();
-    int ru = upload_i32(c, &c->sell.member, order.member);
-    if (ru == PD_OK) ru = upload_i32(c, &c->sell.pos_of, pos);
-    if (ru == PD_OK) ru = upload_i32(c, &c->sell.rank, rank);
-    if (ru != PD_OK) return ru;
+  struct Blocks {  // visiting blocks of the mixed form, freed on every return
+    int32_t* p = nullptr;
+    ~Blocks() { dfree(p); }
+  } blocks;
+  int64_t nblocks = 0;
+  if (mixed(c)) {  // SELL chunks and visiting blocks are spatial tiles
+    const int ro = pd::build_spatial_order(c->n, c->x, c->h_x.data(), s, &c->sell, &blocks.p, &nblocks, &msg);
+    if (ro != PD_OK) return fail(c, ro, msg);
   }
   int rc = pd::build_sell(c->n, c->row_ptr, c->col, s, &c->sell, c->counters, &msg);
   if (rc != PD_OK) return fail(c, rc, msg);
@@ -505,16 +390,8 @@ int finish_families(pd_ctx* c) {
     for (double v : c->h_vol) vsum += v;
     c->ls = ls;
     c->vs_scale = c->n > 0 ? vsum / (double)c->n : 1.0;
-    int32_t *d_by_rank = nullptr, *d_blocks = nullptr;
-    int ru = upload_i32(c, &d_by_rank, order.by_rank);
-    if (ru == PD_OK) ru = upload_i32(c, &d_blocks, order.blocks);
-    const int64_t nblocks = (int64_t)order.blocks.size() / (pd::kHaloBlock / 32);
-    const int rch = ru != PD_OK ? ru
-                                : pd::build_halo_mixed(mixed_args(c), c->sell.nslots, nblocks, d_blocks,
-                                                       c->sell.rank, d_by_rank, s, &c->halo, &msg);
-    dfree(d_by_rank);
-    dfree(d_blocks);
-    if (ru != PD_OK) return ru;
+    const int rch = pd::build_halo_mixed(mixed_args(c), c->sell.nslots, nblocks, blocks.p, c->sell.rk, s, &c->halo,
+                                         &msg);
     if (rch != PD_OK) return fail(c, rch, msg);
     int rc2 = upload_gvel(c);
     if (rc2 != PD_OK) return rc2;

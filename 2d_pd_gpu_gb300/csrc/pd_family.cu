@@ -223,20 +223,20 @@ __global__ void k_chunk_width(int64_t npos, const int64_t* __restrict__ row_ptr,
 }
 
 // Slot (0 .. deg) of family entry k of a particle whose family is
-// col[r0 .. r0 + deg): k itself (family order), or with a rank array the
-// entry's place in ascending (rank of the neighbour, k) order; entries that
+// col[r0 .. r0 + deg): k itself (family order), or with a spatial key array
+// the entry's place in ascending (rk of the neighbour, k) order; entries that
 // are not valid neighbour ids sort last.
 __device__ __forceinline__ int64_t family_slot(const int32_t* __restrict__ col, int64_t r0, int64_t deg, int64_t k,
-                                               const int32_t* __restrict__ rank, int64_t n) {
-  if (!rank) return k;
+                                               const uint64_t* __restrict__ rk, int64_t n) {
+  if (!rk) return k;
   auto key = [&](int64_t q) {
     const int32_t j = col[r0 + q];
-    return j >= 0 && (int64_t)j < n ? (int64_t)rank[j] : n + q;
+    return j >= 0 && (int64_t)j < n ? rk[j] : ~0ull;
   };
-  const int64_t kk = key(k);
+  const uint64_t kk = key(k);
   int64_t slot = 0;
   for (int64_t q = 0; q < deg; ++q) {
-    const int64_t kq = key(q);
+    const uint64_t kq = key(q);
     slot += kq < kk || (kq == kk && q < k);
   }
   return slot;
@@ -245,7 +245,7 @@ __device__ __forceinline__ int64_t family_slot(const int32_t* __restrict__ col, 
 // nbr: every slot is padding (-1) before the fill.
 __global__ void k_sell_fill(int64_t n, const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
                             const int64_t* __restrict__ chunk_base, const int32_t* __restrict__ pos_of,
-                            const int32_t* __restrict__ rank, int32_t* nbr, unsigned long long* counters) {
+                            const uint64_t* __restrict__ rk, int32_t* nbr, unsigned long long* counters) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int64_t s0 = sell_slot0(chunk_base, sell_pos(pos_of, i));
@@ -259,7 +259,7 @@ __global__ void k_sell_fill(int64_t n, const int64_t* __restrict__ row_ptr, cons
       atomicOr(counters + CNT_ERROR, (unsigned long long)ERR_SELF_BOND);
       j = -1;
     }
-    nbr[s0 + family_slot(col, r0, deg, k, rank, n) * kChunk] = j;
+    nbr[s0 + family_slot(col, r0, deg, k, rk, n) * kChunk] = j;
   }
 }
 
@@ -317,25 +317,25 @@ __global__ void k_bond_limit(int64_t nslots, const double2* __restrict__ bxi, do
 
 __global__ void k_mask_out(int64_t n, const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
                            const int64_t* __restrict__ chunk_base, const int32_t* __restrict__ pos_of,
-                           const int32_t* __restrict__ rank, const int32_t* __restrict__ nbr, uint8_t* alive) {
+                           const uint64_t* __restrict__ rk, const int32_t* __restrict__ nbr, uint8_t* alive) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int64_t s0 = sell_slot0(chunk_base, sell_pos(pos_of, i));
   const int64_t r0 = row_ptr[i], deg = row_ptr[i + 1] - r0;
   for (int64_t k = 0; k < deg; ++k)
-    alive[r0 + k] = nbr[s0 + family_slot(col, r0, deg, k, rank, n) * kChunk] >= 0 ? 1 : 0;
+    alive[r0 + k] = nbr[s0 + family_slot(col, r0, deg, k, rk, n) * kChunk] >= 0 ? 1 : 0;
 }
 
 // Restore every family bond to intact (pd_reset).
 __global__ void k_sell_reset(int64_t n, const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
                              const int64_t* __restrict__ chunk_base, const int32_t* __restrict__ pos_of,
-                             const int32_t* __restrict__ rank, int32_t* nbr) {
+                             const uint64_t* __restrict__ rk, int32_t* nbr) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int64_t s0 = sell_slot0(chunk_base, sell_pos(pos_of, i));
   const int64_t r0 = row_ptr[i], deg = row_ptr[i + 1] - r0;
   for (int64_t k = 0; k < deg; ++k) {
-    const int64_t s = s0 + family_slot(col, r0, deg, k, rank, n) * kChunk;
+    const int64_t s = s0 + family_slot(col, r0, deg, k, rk, n) * kChunk;
     if (nbr[s] < -1) nbr[s] = col[r0 + k];
   }
 }
@@ -490,7 +490,7 @@ int build_sell(int64_t n, const int64_t* d_row_ptr, const int32_t* d_col, cudaSt
   // every slot starts as padding: the lanes past n of the last chunk own slots no particle fills
   if (L->nslots > 0) cudaMemsetAsync(L->nbr, 0xFF, (size_t)L->nslots * sizeof(int32_t), s);
   if (n > 0)
-    k_sell_fill<<<(unsigned)blocks_for(n), kBlock, 0, s>>>(n, d_row_ptr, d_col, L->chunk_base, L->pos_of, L->rank,
+    k_sell_fill<<<(unsigned)blocks_for(n), kBlock, 0, s>>>(n, d_row_ptr, d_col, L->chunk_base, L->pos_of, L->rk,
                                                           L->nbr, d_counters);
   e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) {
@@ -516,13 +516,13 @@ void launch_bond_limit_fp64(int64_t nslots, const double2* bxi, double s_c, cons
 void launch_mask_out(int64_t n, const int64_t* row_ptr, const int32_t* col, const SellLayout& L, uint8_t* alive,
                      cudaStream_t s) {
   if (n > 0)
-    k_mask_out<<<(unsigned)blocks_for(n), kBlock, 0, s>>>(n, row_ptr, col, L.chunk_base, L.pos_of, L.rank, L.nbr,
+    k_mask_out<<<(unsigned)blocks_for(n), kBlock, 0, s>>>(n, row_ptr, col, L.chunk_base, L.pos_of, L.rk, L.nbr,
                                                          alive);
 }
 
 void launch_sell_reset(int64_t n, const int64_t* row_ptr, const int32_t* col, const SellLayout& L, cudaStream_t s) {
   if (n > 0)
-    k_sell_reset<<<(unsigned)blocks_for(n), kBlock, 0, s>>>(n, row_ptr, col, L.chunk_base, L.pos_of, L.rank, L.nbr);
+    k_sell_reset<<<(unsigned)blocks_for(n), kBlock, 0, s>>>(n, row_ptr, col, L.chunk_base, L.pos_of, L.rk, L.nbr);
 }
 
 }  // namespace pd

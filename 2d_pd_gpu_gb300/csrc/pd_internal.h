@@ -188,9 +188,14 @@ struct SellLayout {
   int32_t* member = nullptr;  // SELL position -> particle, -1 = hole (set with npos before build_sell)
   int32_t* pos_of = nullptr;  // particle -> SELL position
   // null: a particle's slots follow its family order (the reference's summation
-  // order); else in ascending rank[j] of the neighbours (set before build_sell)
-  int32_t* rank = nullptr;
+  // order); else in ascending rk[j] of the neighbours (set before build_sell)
+  uint64_t* rk = nullptr;
 };
+// Spatial layout of the mixed form (pd_order.cu): sets L->member, pos_of, rk
+// and npos; *d_blocks (device, caller frees) = *nblocks x (kHaloBlock / 32)
+// chunk ids (-1: none) of the visiting blocks.  h_x: the positions on the host.
+int build_spatial_order(int64_t n, const double2* d_x, const double* h_x, cudaStream_t s, SellLayout* L,
+                        int32_t** d_blocks, int64_t* nblocks, std::string* msg);
 int build_sell(int64_t n, const int64_t* d_row_ptr, const int32_t* d_col, cudaStream_t s, SellLayout* out,
                unsigned long long* d_counters, std::string* msg);
 void launch_bond_geometry_fp64(int64_t n, const double2* x, const double* vol, const SellLayout& L,
@@ -244,11 +249,9 @@ struct HaloLayout {
   int32_t halo_max = 0;
 };
 // block_chunks: nblocks x (kHaloBlock / 32) chunk ids (-1: none) of the
-// visiting blocks; rank: particle -> spatial rank, by_rank: its inverse
-// (halos are sorted by rank)
+// visiting blocks; halos are sorted by the spatial key rk
 int build_halo_mixed(const MixedArgs& a, int64_t nslots, int64_t nblocks, const int32_t* block_chunks,
-                     const int32_t* rank, const int32_t* by_rank, cudaStream_t s, HaloLayout* out,
-                     std::string* msg);
+                     const uint64_t* rk, cudaStream_t s, HaloLayout* out, std::string* msg);
 void launch_halo_relink(const MixedArgs& a, const HaloLayout& h, cudaStream_t s);
 void launch_drift_mixed(const MixedArgs& a, cudaStream_t s);
 void launch_pass_a_mixed(const MixedArgs& a, bool breaking, cudaStream_t s);

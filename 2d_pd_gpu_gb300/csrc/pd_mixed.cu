@@ -539,11 +539,11 @@ inline size_t pass_smem_bytes(const MixedArgs& a, bool pass_a) {
 }
 
 // ---- halo build (setup): per block, the distinct particles its chunks'
-// bonds reach (own particles included) in spatial-rank order, and every
-// slot's position in that list.  The ranks are collected in a shared-memory
-// hash set (open addressing, linear probing), compacted, sorted (bitonic)
-// and looked up by binary search; a block with more than kHaloCap distinct
-// particles is not staged.
+// bonds reach (own particles included) in ascending spatial key rk, and
+// every slot's position in that list.  The ids are collected in a
+// shared-memory hash set (open addressing, linear probing), their keys
+// compacted, sorted (bitonic) and looked up by binary search; a block with
+// more than kHaloCap distinct particles is not staged.
 __device__ __forceinline__ int decode_nbr(int v) { return v >= 0 ? v : (v <= -2 ? -2 - v : -1); }
 
 constexpr int kHaloHashBits = 12;
@@ -551,12 +551,11 @@ constexpr int kHaloHash = 1 << kHaloHashBits;
 static_assert(kHaloHash >= 2 * kHaloCap && kHaloHash > kHaloCap + kHaloBlock, "halo hash table too small");
 static_assert((kHaloCap & (kHaloCap - 1)) == 0, "kHaloCap is a power of two (bitonic sort)");
 
-__global__ void __launch_bounds__(kHaloBlock) k_halo_build(MixedArgs a, const int32_t* __restrict__ rank,
-                                                       const int32_t* __restrict__ by_rank, int32_t* halo,
+__global__ void __launch_bounds__(kHaloBlock) k_halo_build(MixedArgs a, const uint64_t* __restrict__ rk, int32_t* halo,
                                                        int32_t* halo_n, uint16_t* loc, uint16_t* loc0,
                                                        uint16_t* self_loc) {
   __shared__ int32_t tab[kHaloHash];
-  __shared__ int32_t list[kHaloCap];
+  __shared__ uint64_t list[kHaloCap];
   __shared__ int32_t s_cnt, s_put;
   const int tid = threadIdx.x, lane = tid & 31;
   int64_t chunk = 0, base = 0;
@@ -588,10 +587,10 @@ __global__ void __launch_bounds__(kHaloBlock) k_halo_build(MixedArgs a, const in
     }
   };
   const int wl = i >= 0 ? w : 0;  // lanes past n own padding slots only
-  if (i >= 0) insert(rank[i]);
+  if (i >= 0) insert((int)i);
   for (int k = 0; k < wl; ++k) {
     const int j = decode_nbr(a.nbr[s0 + (int64_t)k * kChunk]);
-    if (j >= 0) insert(rank[j]);
+    if (j >= 0) insert(j);
   }
   __syncthreads();
   const int tot = s_cnt;  // block-uniform
@@ -600,16 +599,16 @@ __global__ void __launch_bounds__(kHaloBlock) k_halo_build(MixedArgs a, const in
     while (P < tot) P <<= 1;
     for (int k = tid; k < kHaloHash; k += kHaloBlock) {
       const int v = tab[k];
-      if (v >= 0) list[atomicAdd(&s_put, 1)] = v;
+      if (v >= 0) list[atomicAdd(&s_put, 1)] = rk[v];
     }
-    for (int k = tot + tid; k < P; k += kHaloBlock) list[k] = INT_MAX;
+    for (int k = tot + tid; k < P; k += kHaloBlock) list[k] = ~0ull;
     __syncthreads();
     for (int kk = 2; kk <= P; kk <<= 1)
       for (int jj = kk >> 1; jj > 0; jj >>= 1) {
         for (int t = tid; t < P; t += kHaloBlock) {
           const int o = t ^ jj;
           if (o > t) {
-            const int x = list[t], y = list[o];
+            const uint64_t x = list[t], y = list[o];
             if ((x > y) == ((t & kk) == 0)) {
               list[t] = y;
               list[o] = x;
@@ -620,9 +619,9 @@ __global__ void __launch_bounds__(kHaloBlock) k_halo_build(MixedArgs a, const in
       }
     if (tid == 0) halo_n[blockIdx.x] = tot;
     int32_t* H = halo + (int64_t)blockIdx.x * kHaloCap;
-    for (int k = tid; k < tot; k += kHaloBlock) H[k] = by_rank[list[k]];
-    auto pos = [&](int j) {  // the entry of particle j (its rank is in the list)
-      const int r = rank[j];
+    for (int k = tid; k < tot; k += kHaloBlock) H[k] = (int32_t)(list[k] & 0x7FFFFFFFull);  // rk's low bits: the id
+    auto pos = [&](int j) {  // the entry of particle j (its key is in the list)
+      const uint64_t r = rk[j];
       int lo = 0, hi = tot;
       while (lo < hi) {
         const int mid = (lo + hi) >> 1;
@@ -891,7 +890,7 @@ void launch_from_mixed(const MixedArgs& a, double2* u, double2* v, double2* f, c
 }
 
 int build_halo_mixed(const MixedArgs& a0, int64_t nslots, int64_t nblocks, const int32_t* block_chunks,
-                     const int32_t* rank, const int32_t* by_rank, cudaStream_t s, HaloLayout* h, std::string* msg) {
+                     const uint64_t* rk, cudaStream_t s, HaloLayout* h, std::string* msg) {
   const int64_t nb = nblocks;
   h->nblocks = nb;
   h->staged = 0;
@@ -912,8 +911,7 @@ int build_halo_mixed(const MixedArgs& a0, int64_t nslots, int64_t nblocks, const
   k_visit_build<<<(unsigned)blocks_for(nw), kBlock, 0, s>>>(nw, block_chunks, a.chunk_w, a.chunk_base, h->visit);
   a.visit = h->visit;
   a.nblocks = nb;
-  k_halo_build<<<(unsigned)nb, kHaloBlock, 0, s>>>(a, rank, by_rank, h->halo, h->halo_n, h->loc, h->loc0,
-                                                   h->self_loc);
+  k_halo_build<<<(unsigned)nb, kHaloBlock, 0, s>>>(a, rk, h->halo, h->halo_n, h->loc, h->loc0, h->self_loc);
   std::vector<int32_t> cnt((size_t)nb);
   cudaError_t e = cudaMemcpyAsync(cnt.data(), h->halo_n, (size_t)nb * sizeof(int32_t), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
