@@ -227,7 +227,6 @@ Fp64Args fp64_args(pd_ctx* c) {
   a.bc = c->bc; a.gkind = c->gkind; a.gval = c->gval;
   a.broken = c->broken; a.damage = c->damage; a.singular = c->singular; a.fam = c->fam;
   a.chunk_base = c->sell.chunk_base; a.chunk_w = c->sell.chunk_w; a.nbr = c->sell.nbr;
-  a.member = c->sell.member; a.pos_of = c->sell.pos_of;
   a.bxi = c->bxi; a.bgeo = c->bgeo; a.blim = c->blim; a.br2 = c->br2; a.u32 = c->u32;
   stiffness(c, &a.c11, &a.c12, &a.c33);  // getStiffnessTensor, src/main_seq.cpp:185-187
   a.dt = c->p.dt;

@@ -35,11 +35,11 @@ __device__ __forceinline__ double ba_weight(double n1, double n2, double inv_wle
 }
 
 __global__ void __launch_bounds__(128) k_ba_pass_a(Fp64Args a, BondAssoc b) {
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // SELL position
-  if (p >= a.n) return;
-  const int64_t i = sell_member(a.member, p);
-  const int w = a.chunk_w[p >> 5];
-  const int64_t s0 = sell_slot0(a.chunk_base, p);
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const int64_t c0 = i >> 5;
+  const int w = a.chunk_w[c0];
+  const int64_t s0 = a.chunk_base[c0] + (i & 31);
   double ex[kBaMax], ey[kBaMax], el[kBaMax], vv[kBaMax], dx[kBaMax], dy[kBaMax], P[kBaMax][4];
   int64_t slot[kBaMax];
   const double2 ui = a.u[i];
@@ -119,11 +119,11 @@ __device__ __forceinline__ void ba_drift(const Fp64Args& a, int64_t i, double2& 
 
 template <int MODE>
 __global__ void __launch_bounds__(kBlock) k_ba_pass_b(Fp64Args a, BondAssoc b) {
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // SELL position
-  if (p >= a.n) return;
-  const int64_t i = sell_member(a.member, p);
-  const int w = a.chunk_w[p >> 5];
-  const int64_t s0 = sell_slot0(a.chunk_base, p);
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const int64_t c0 = i >> 5;
+  const int w = a.chunk_w[c0];
+  const int64_t s0 = a.chunk_base[c0] + (i & 31);
   double fx = 0.0, fy = 0.0;
   for (int k = 0; k < w; ++k) {
     const int64_t s = s0 + (int64_t)k * kChunk;
@@ -165,18 +165,18 @@ __global__ void __launch_bounds__(kBlock) k_ba_pass_b(Fp64Args a, BondAssoc b) {
 
 // rslot[s] = slot of (j, i) in j's SELL rows, for every slot s = (i, j).
 __global__ void k_ba_reverse(Fp64Args a, BondAssoc b, unsigned long long* counters) {
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // SELL position
-  if (p >= a.n) return;
-  const int64_t i = sell_member(a.member, p);
-  const int w = a.chunk_w[p >> 5];
-  const int64_t s0 = sell_slot0(a.chunk_base, p);
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const int64_t c0 = i >> 5;
+  const int w = a.chunk_w[c0];
+  const int64_t s0 = a.chunk_base[c0] + (i & 31);
   for (int k = 0; k < w; ++k) {
     const int64_t s = s0 + (int64_t)k * kChunk;
     const int j = a.nbr[s];
     if (j < 0) continue;
-    const int64_t pj = sell_pos(a.pos_of, j);
-    const int wj = a.chunk_w[pj >> 5];
-    const int64_t sj0 = sell_slot0(a.chunk_base, pj);
+    const int64_t cj = (int64_t)j >> 5;
+    const int wj = a.chunk_w[cj];
+    const int64_t sj0 = a.chunk_base[cj] + (j & 31);
     int64_t found = -1;
     for (int q = 0; q < wj; ++q)
       if (a.nbr[sj0 + (int64_t)q * kChunk] == (int)i) {

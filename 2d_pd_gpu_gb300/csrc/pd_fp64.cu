@@ -3,8 +3,7 @@
 // places as the oracle's restatement, so results are bit-identical to it.
 //
 // One thread per particle, bonds walked in family order through the SELL-32
-// layout (every slot load of a warp is one coalesced line): thread t of a
-// bond pass runs SELL position p = t, particle i = member[p].  Per-particle sums
+// layout (every slot load of a warp is one coalesced line).  Per-particle sums
 // are sequential in family order, with no atomics, so results are
 // deterministic and independent of the launch shape.
 //
@@ -27,16 +26,16 @@ namespace pd {
 
 namespace {
 
-// First slot and chunk width of SELL position p.
-__device__ __forceinline__ int64_t slot0(const Fp64Args& a, int64_t p, int* w) {
-  *w = a.chunk_w[p >> 5];
-  return sell_slot0(a.chunk_base, p);
+__device__ __forceinline__ int64_t slot0(const Fp64Args& a, int64_t i, int* w) {
+  const int64_t c = i >> 5;
+  *w = a.chunk_w[c];
+  return a.chunk_base[c] + (i & 31);
 }
 
-// K^-1 and m/V of particle i (SELL position p) over its intact bonds (oracle: kinv_of).
-__device__ void kinv_update(const Fp64Args& a, int64_t i, int64_t p) {
+// K^-1 and m/V of particle i over its intact bonds (oracle: kinv_of).
+__device__ void kinv_update(const Fp64Args& a, int64_t i) {
   int w;
-  const int64_t s0 = slot0(a, p, &w);
+  const int64_t s0 = slot0(a, i, &w);
   double k11 = 0.0, k12 = 0.0, k22 = 0.0, mx = 0.0, my = 0.0;
   int nal = 0;
   for (int k = 0; k < w; ++k) {
@@ -71,9 +70,9 @@ __device__ void kinv_update(const Fp64Args& a, int64_t i, int64_t p) {
 }
 
 __global__ void __launch_bounds__(kBlock) k_init_geometry(Fp64Args a) {
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= a.n) return;
-  kinv_update(a, sell_member(a.member, p), p);
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  kinv_update(a, i);
 }
 
 // Velocity BC, drift, fixed BC of particle i; an = f_i / rho.
@@ -125,9 +124,9 @@ __device__ __forceinline__ bool surely_intact(float2 ui, float2 uj, float r2) {
 
 // Pass A of particle i (stretch tests, D, penalty sum, stress, W).
 template <bool BREAK, bool HG>
-__device__ __forceinline__ void pass_a_particle(const Fp64Args& a, int64_t i, int64_t p) {
+__device__ __forceinline__ void pass_a_particle(const Fp64Args& a, int64_t i) {
   int w;
-  const int64_t s0 = slot0(a, p, &w);
+  const int64_t s0 = slot0(a, i, &w);
   const double2 ui = a.u[i];
   const float2 ui32 = a.u32[i];
   double d11 = 0.0, d12 = 0.0, d21 = 0.0, d22 = 0.0, ax = 0.0, ay = 0.0;
@@ -167,7 +166,7 @@ __device__ __forceinline__ void pass_a_particle(const Fp64Args& a, int64_t i, in
     const int32_t b = a.broken[i] + newly;
     a.broken[i] = b;
     a.damage[i] = (double)b / (double)a.fam[i];
-    kinv_update(a, i, p);
+    kinv_update(a, i);
   }
   if (a.singular[i]) {
     a.w01[i] = make_double2(0.0, 0.0);
@@ -196,16 +195,16 @@ __device__ __forceinline__ void pass_a_particle(const Fp64Args& a, int64_t i, in
 
 template <bool BREAK, bool HG>
 __global__ void __launch_bounds__(kBlock) k_pass_a(Fp64Args a) {
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p < a.n) pass_a_particle<BREAK, HG>(a, sell_member(a.member, p), p);
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < a.n) pass_a_particle<BREAK, HG>(a, i);
 }
 
 // Pass B of particle i (force gather, kick; MODE 1 adds the next drift,
 // MODE 2 is the drop-in kick with acce in/out).
 template <int MODE, bool HG>
-__device__ __forceinline__ void pass_b_particle(const Fp64Args& a, int64_t i, int64_t p) {
+__device__ __forceinline__ void pass_b_particle(const Fp64Args& a, int64_t i) {
   int w;
-  const int64_t s0 = slot0(a, p, &w);
+  const int64_t s0 = slot0(a, i, &w);
   const double2 wa = a.w01[i], wb = a.w23[i], m = a.mt[i];
   double fx, fy;
   if (HG) {
@@ -260,26 +259,24 @@ __device__ __forceinline__ void pass_b_particle(const Fp64Args& a, int64_t i, in
 
 template <int MODE, bool HG>
 __global__ void __launch_bounds__(kBlock) k_pass_b(Fp64Args a) {
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p < a.n) pass_b_particle<MODE, HG>(a, sell_member(a.member, p), p);
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < a.n) pass_b_particle<MODE, HG>(a, i);
 }
 
 // ---- batched plates: phase 0 drift, 1 pass A, 2 pass B + next drift, 3 pass B
-// (tiles run SELL positions; pos is one of plate pl)
-__device__ __forceinline__ void batch_particle(const Fp64Args& pl, int64_t pos, int phase) {
-  const bool hg = pl.k_hg != 0.0;
-  const int64_t i = sell_member(pl.member, pos);
+__device__ __forceinline__ void batch_particle(const Fp64Args& p, int64_t i, int phase) {
+  const bool hg = p.k_hg != 0.0;
   if (phase == 0) {
-    drift_particle(pl, i);
+    drift_particle(p, i);
   } else if (phase == 1) {
-    if (pl.brk)
-      hg ? pass_a_particle<true, true>(pl, i, pos) : pass_a_particle<true, false>(pl, i, pos);
+    if (p.brk)
+      hg ? pass_a_particle<true, true>(p, i) : pass_a_particle<true, false>(p, i);
     else
-      hg ? pass_a_particle<false, true>(pl, i, pos) : pass_a_particle<false, false>(pl, i, pos);
+      hg ? pass_a_particle<false, true>(p, i) : pass_a_particle<false, false>(p, i);
   } else if (phase == 2) {
-    hg ? pass_b_particle<1, true>(pl, i, pos) : pass_b_particle<1, false>(pl, i, pos);
+    hg ? pass_b_particle<1, true>(p, i) : pass_b_particle<1, false>(p, i);
   } else {
-    hg ? pass_b_particle<0, true>(pl, i, pos) : pass_b_particle<0, false>(pl, i, pos);
+    hg ? pass_b_particle<0, true>(p, i) : pass_b_particle<0, false>(p, i);
   }
 }
 

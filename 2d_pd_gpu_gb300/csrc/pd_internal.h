@@ -79,9 +79,7 @@ struct Fp64Args {
   const int32_t* __restrict__ fam;
   const int64_t* __restrict__ chunk_base;
   const int32_t* __restrict__ chunk_w;
-  int32_t* nbr;
-  const int32_t* __restrict__ member;  // SELL position -> particle
-  const int32_t* __restrict__ pos_of;  // particle -> SELL position
+  int32_t* nbr;  // the FP64 form's SELL position of particle i is i
   const double2* __restrict__ bxi;
   const double2* __restrict__ bgeo;
   const double* __restrict__ blim;

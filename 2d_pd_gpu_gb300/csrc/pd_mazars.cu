@@ -95,10 +95,9 @@ __device__ __forceinline__ void family_status(const Fp64Args& a, const MazarsArg
 
 // Classic weights: one strain per particle, from the same D sum as pass A.
 __global__ void __launch_bounds__(kBlock) k_mazars_classic(Fp64Args a, MazarsArgs m) {
-  const int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // SELL position
-  if (pos >= a.n) return;
-  const int64_t i = sell_member(a.member, pos);
-  const int64_t s0 = sell_slot0(a.chunk_base, pos);
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const int64_t s0 = a.chunk_base[i >> 5] + (i & 31);
   const int fam = a.fam[i];
   const double2 ui = a.u[i];
   double d11 = 0.0, d12 = 0.0, d21 = 0.0, d22 = 0.0;
@@ -142,10 +141,9 @@ __device__ __forceinline__ double mz_weight(const BondAssoc& b, double bx, doubl
 }
 
 __global__ void __launch_bounds__(128) k_mazars_ba(Fp64Args a, BondAssoc ba, MazarsArgs m) {
-  const int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // SELL position
-  if (pos >= a.n) return;
-  const int64_t i = sell_member(a.member, pos);
-  const int64_t s0 = sell_slot0(a.chunk_base, pos);
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const int64_t s0 = a.chunk_base[i >> 5] + (i & 31);
   const int fam = a.fam[i] < kMzMax ? a.fam[i] : kMzMax;
   double ex[kMzMax], ey[kMzMax], el[kMzMax], vv[kMzMax], dx[kMzMax], dy[kMzMax];
   const double2 ui = a.u[i];
@@ -192,11 +190,11 @@ __global__ void __launch_bounds__(128) k_mazars_ba(Fp64Args a, BondAssoc ba, Maz
 
 // Per-bond history <-> family (CSR) order, and statuses from the bond damage.
 __global__ void k_mz_to_csr(int64_t n, const int64_t* __restrict__ row_ptr, const int64_t* __restrict__ chunk_base,
-                            const int32_t* __restrict__ pos_of, const double* __restrict__ thr,
-                            const double* __restrict__ bd, double* thr_csr, double* bd_csr) {
+                            const double* __restrict__ thr, const double* __restrict__ bd, double* thr_csr,
+                            double* bd_csr) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const int64_t s0 = sell_slot0(chunk_base, sell_pos(pos_of, i)), r0 = row_ptr[i], deg = row_ptr[i + 1] - r0;
+  const int64_t s0 = chunk_base[i >> 5] + (i & 31), r0 = row_ptr[i], deg = row_ptr[i + 1] - r0;
   for (int64_t k = 0; k < deg; ++k) {
     if (thr_csr) thr_csr[r0 + k] = thr[s0 + k * kChunk];
     if (bd_csr) bd_csr[r0 + k] = bd[s0 + k * kChunk];
@@ -207,7 +205,7 @@ __global__ void k_mz_from_csr(Fp64Args a, MazarsArgs m, const int64_t* __restric
                               const double* __restrict__ thr_csr, const double* __restrict__ bd_csr) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
-  const int64_t s0 = sell_slot0(a.chunk_base, sell_pos(a.pos_of, i)), r0 = row_ptr[i], deg = row_ptr[i + 1] - r0;
+  const int64_t s0 = a.chunk_base[i >> 5] + (i & 31), r0 = row_ptr[i], deg = row_ptr[i + 1] - r0;
   for (int64_t k = 0; k < deg; ++k) {
     if (thr_csr) m.thr[s0 + k * kChunk] = thr_csr[r0 + k];
     if (bd_csr) m.bd[s0 + k * kChunk] = bd_csr[r0 + k];
@@ -240,8 +238,7 @@ void launch_mazars_update(const Fp64Args& a, const BondAssoc* ba, const MazarsAr
 void launch_mazars_to_csr(const Fp64Args& a, const int64_t* row_ptr, const MazarsArgs& m, double* thr_csr,
                           double* bd_csr, cudaStream_t s) {
   if (a.n > 0)
-    k_mz_to_csr<<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a.n, row_ptr, a.chunk_base, a.pos_of, m.thr, m.bd,
-                                                                   thr_csr, bd_csr);
+    k_mz_to_csr<<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a.n, row_ptr, a.chunk_base, m.thr, m.bd, thr_csr, bd_csr);
 }
 
 void launch_mazars_from_csr(const Fp64Args& a, const int64_t* row_ptr, const MazarsArgs& m, const double* thr_csr,
