@@ -33,10 +33,11 @@ struct pd_ctx {
   double2 *w01 = nullptr, *w23 = nullptr, *kinv01 = nullptr, *mt = nullptr, *hg = nullptr;
   uint8_t *bc = nullptr, *singular = nullptr;
   int32_t *broken = nullptr, *fam = nullptr;
-  // mixed form (PD_MIXED)
+  // mixed form (PD_MIXED): by SELL position (sell.npos entries), with the families
   float4 *xs = nullptr, *us = nullptr, *vsm = nullptr, *ws = nullptr, *geo = nullptr;
   float2 *fs = nullptr, *mh = nullptr, *hgs = nullptr;
   float* vh = nullptr;
+  uint8_t *bcp = nullptr, *sgp = nullptr;  // BC group, singular flag
   // BC groups
   int32_t* gkind = nullptr;
   double2* gval = nullptr;
@@ -150,6 +151,8 @@ void free_families(pd_ctx* c) {
   dfree(c->sell.member);
   dfree(c->sell.rk);
   dfree(c->sell.pos_of);
+  dfree(c->xs); dfree(c->us); dfree(c->vsm); dfree(c->ws); dfree(c->geo);
+  dfree(c->fs); dfree(c->mh); dfree(c->hgs); dfree(c->vh); dfree(c->bcp); dfree(c->sgp);
   dfree(c->mz_thr);
   dfree(c->mz_bd);
   dfree(c->mz_status);
@@ -176,11 +179,9 @@ void free_particles(pd_ctx* c) {
   free_families(c);
   dfree(c->x); dfree(c->u); dfree(c->v); dfree(c->f); dfree(c->acc);
   dfree(c->vol); dfree(c->kinv22); dfree(c->damage);
-  dfree(c->w01); dfree(c->w23); dfree(c->kinv01); dfree(c->mt); dfree(c->hg); dfree(c->hgs);
+  dfree(c->w01); dfree(c->w23); dfree(c->kinv01); dfree(c->mt); dfree(c->hg);
   dfree(c->bc); dfree(c->singular); dfree(c->broken); dfree(c->fam);
   dfree(c->u32);
-  dfree(c->xs); dfree(c->us); dfree(c->vsm); dfree(c->ws); dfree(c->geo);
-  dfree(c->fs); dfree(c->mh); dfree(c->vh);
   c->n = 0;
   c->has_particles = false;
 }
@@ -282,11 +283,12 @@ void stiffness(const pd_ctx* c, double* c11, double* c12, double* c33) {
 pd::MixedArgs mixed_args(pd_ctx* c) {
   pd::MixedArgs a{};
   a.n = c->n;
+  a.npos = c->sell.npos;
   a.x = c->x; a.vol = c->vol;
   a.xs = c->xs; a.vh = c->vh; a.us = c->us; a.vs = c->vsm; a.fs = c->fs; a.ws = c->ws; a.geo = c->geo; a.mh = c->mh;
   a.hgs = c->hgs;
-  a.bc = c->bc; a.gkind = c->gkind; a.gvel = c->gvel;
-  a.broken = c->broken; a.damage = c->damage; a.singular = c->singular; a.fam = c->fam;
+  a.bc = c->bcp; a.gkind = c->gkind; a.gvel = c->gvel;
+  a.broken = c->broken; a.damage = c->damage; a.singular = c->sgp; a.fam = c->fam;
   a.chunk_base = c->sell.chunk_base; a.chunk_w = c->sell.chunk_w; a.nbr = c->sell.nbr;
   a.member = c->sell.member; a.pos_of = c->sell.pos_of;
   a.visit = c->halo.visit;
@@ -349,9 +351,25 @@ int finish_families(pd_ctx* c) {
     ~Blocks() { dfree(p); }
   } blocks;
   int64_t nblocks = 0;
-  if (mixed(c)) {  // SELL chunks and visiting blocks are spatial tiles
+  if (mixed(c)) {  // SELL chunks and visiting blocks are spatial tiles; the state follows them
     const int ro = pd::build_spatial_order(c->n, c->x, c->h_x.data(), s, &c->sell, &blocks.p, &nblocks, &msg);
     if (ro != PD_OK) return fail(c, ro, msg);
+    const size_t np = (size_t)(c->sell.npos > 0 ? c->sell.npos : 1);
+    PD_CK(c, cudaMalloc(&c->xs, np * sizeof(float4)));
+    PD_CK(c, cudaMalloc(&c->us, np * sizeof(float4)));
+    PD_CK(c, cudaMalloc(&c->vsm, np * sizeof(float4)));
+    PD_CK(c, cudaMalloc(&c->ws, np * sizeof(float4)));
+    PD_CK(c, cudaMalloc(&c->geo, np * sizeof(float4)));
+    PD_CK(c, cudaMalloc(&c->fs, np * sizeof(float2)));
+    PD_CK(c, cudaMalloc(&c->mh, np * sizeof(float2)));
+    PD_CK(c, cudaMalloc(&c->hgs, np * sizeof(float2)));
+    PD_CK(c, cudaMalloc(&c->vh, np * sizeof(float)));
+    PD_CK(c, cudaMalloc(&c->bcp, np));
+    PD_CK(c, cudaMalloc(&c->sgp, np));
+    PD_CK(c, cudaMemsetAsync(c->geo, 0, np * sizeof(float4), s));  // holes stay zero
+    PD_CK(c, cudaMemsetAsync(c->mh, 0, np * sizeof(float2), s));
+    PD_CK(c, cudaMemsetAsync(c->sgp, 0, np, s));
+    pd::launch_bc_by_position(c->sell.npos, c->sell.member, c->bc, c->bcp, s);
   }
   int rc = pd::build_sell(c->n, c->row_ptr, c->col, s, &c->sell, c->counters, &msg);
   if (rc != PD_OK) return fail(c, rc, msg);
@@ -551,17 +569,7 @@ int pd_set_particles(pd_ctx* c, int64_t n, const double* x, const double* vol) {
   PD_CK(c, cudaMalloc(&c->v, nn * sizeof(double2)));
   PD_CK(c, cudaMalloc(&c->f, nn * sizeof(double2)));
   PD_CK(c, cudaMalloc(&c->vol, nn * sizeof(double)));
-  if (mixed(c)) {
-    PD_CK(c, cudaMalloc(&c->xs, nn * sizeof(float4)));
-    PD_CK(c, cudaMalloc(&c->us, nn * sizeof(float4)));
-    PD_CK(c, cudaMalloc(&c->vsm, nn * sizeof(float4)));
-    PD_CK(c, cudaMalloc(&c->ws, nn * sizeof(float4)));
-    PD_CK(c, cudaMalloc(&c->geo, nn * sizeof(float4)));
-    PD_CK(c, cudaMalloc(&c->fs, nn * sizeof(float2)));
-    PD_CK(c, cudaMalloc(&c->mh, nn * sizeof(float2)));
-    PD_CK(c, cudaMalloc(&c->hgs, nn * sizeof(float2)));
-    PD_CK(c, cudaMalloc(&c->vh, nn * sizeof(float)));
-  } else {
+  if (!mixed(c)) {  // (the mixed form's state is allocated with its families: finish_families)
     PD_CK(c, cudaMalloc(&c->acc, nn * sizeof(double2)));
     PD_CK(c, cudaMalloc(&c->w01, nn * sizeof(double2)));
     PD_CK(c, cudaMalloc(&c->w23, nn * sizeof(double2)));
@@ -679,6 +687,11 @@ int pd_set_bc(pd_ctx* c, int32_t n_groups, const int32_t* kind, const double* va
     else
       PD_CK(c, cudaMemsetAsync(c->bc, 0, (size_t)c->n, c->stream));
   }
+  if (mixed(c) && c->has_families) {
+    pd::launch_bc_by_position(c->sell.npos, c->sell.member, c->bc, c->bcp, c->stream);
+    PD_CK(c, cudaGetLastError());
+    PD_CK(c, cudaStreamSynchronize(c->stream));
+  }
   return PD_OK;
 }
 
@@ -697,11 +710,12 @@ int pd_reset(pd_ctx* c) {
   pd::launch_sell_reset(c->n, c->row_ptr, c->col, c->sell, s);
   if (mixed(c)) {
     pd::launch_halo_relink(mixed_args(c), c->halo, s);
-    PD_CK(c, cudaMemsetAsync(c->us, 0, nn * sizeof(float4), s));
-    PD_CK(c, cudaMemsetAsync(c->vsm, 0, nn * sizeof(float4), s));
-    PD_CK(c, cudaMemsetAsync(c->ws, 0, nn * sizeof(float4), s));
-    PD_CK(c, cudaMemsetAsync(c->fs, 0, nn * sizeof(float2), s));
-    PD_CK(c, cudaMemsetAsync(c->hgs, 0, nn * sizeof(float2), s));
+    const size_t np = (size_t)(c->sell.npos > 0 ? c->sell.npos : 1);
+    PD_CK(c, cudaMemsetAsync(c->us, 0, np * sizeof(float4), s));
+    PD_CK(c, cudaMemsetAsync(c->vsm, 0, np * sizeof(float4), s));
+    PD_CK(c, cudaMemsetAsync(c->ws, 0, np * sizeof(float4), s));
+    PD_CK(c, cudaMemsetAsync(c->fs, 0, np * sizeof(float2), s));
+    PD_CK(c, cudaMemsetAsync(c->hgs, 0, np * sizeof(float2), s));
     pd::launch_init_geometry_mixed(mixed_args(c), s);
   } else {
     PD_CK(c, cudaMemsetAsync(c->acc, 0, nn * sizeof(double2), s));
@@ -1031,10 +1045,11 @@ uint64_t problem_hash(const pd_ctx* c) {
 std::vector<std::pair<void*, size_t>> ckpt_arrays(pd_ctx* c) {
   const size_t n = (size_t)c->n, ns = (size_t)c->sell.nslots;
   std::vector<std::pair<void*, size_t>> a;
-  if (mixed(c)) {
-    a.push_back({c->us, n * sizeof(float4)});
-    a.push_back({c->vsm, n * sizeof(float4)});
-    a.push_back({c->fs, n * sizeof(float2)});
+  if (mixed(c)) {  // by SELL position
+    const size_t np = (size_t)c->sell.npos;
+    a.push_back({c->us, np * sizeof(float4)});
+    a.push_back({c->vsm, np * sizeof(float4)});
+    a.push_back({c->fs, np * sizeof(float2)});
   } else {
     a.push_back({c->u, n * sizeof(double2)});
     a.push_back({c->v, n * sizeof(double2)});

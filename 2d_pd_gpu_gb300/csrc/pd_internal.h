@@ -120,13 +120,18 @@ struct MazarsArgs {
 // Chunk a warp runs in the mixed passes: warp w of visiting block b runs
 // visit[b * kHaloBlock / 32 + w].
 struct alignas(16) VisitRec {
-  int32_t chunk, w;  // chunk id (-1: the warp has none), width (slot rows)
-  int64_t base;      // first slot
+  int32_t chunk;    // chunk id (-1: the warp has none)
+  int16_t w, live;  // width (slot rows); lanes 0 .. live-1 hold particles (the rest are holes)
+  int64_t base;     // first slot
 };
 
 // Mixed form (pd_mixed.cu): scaled two-float state, FP32 bond arithmetic.
+// The scaled state (xs .. hgs), bc, singular and self_loc are stored in SELL
+// position order (npos entries; holes hold zeros): a warp's per-particle
+// loads are coalesced and halo gathers follow space whatever the particle
+// numbering.  x, vol, broken, damage and fam are per particle (i = member[p]).
 struct MixedArgs {
-  int64_t n;
+  int64_t n, npos;
   const double2* __restrict__ x;    // FP64 reference positions (K^-1 recompute)
   const double* __restrict__ vol;   // FP64 volumes
   float4* xs;                       // x^ two-float {hi.x, hi.y, lo.x, lo.y}
@@ -138,24 +143,24 @@ struct MixedArgs {
   float4* geo;                      // {K^-1 11, 12, 22, V^_i}
   float2* mh;                       // m^ / V^_i
   float2* hgs;                      // 2 k^ sum_j V^_j du^ (pass A -> pass B)
-  const uint8_t* __restrict__ bc;
+  const uint8_t* __restrict__ bc;   // BC group by position
   const int32_t* __restrict__ gkind;
   const float4* __restrict__ gvel;  // prescribed v^ per group, two-float
   int32_t* broken;
   double* damage;
-  uint8_t* singular;
+  uint8_t* singular;                // by position
   const int32_t* __restrict__ fam;
   const int64_t* __restrict__ chunk_base;
   const int32_t* __restrict__ chunk_w;
-  int32_t* nbr;
+  int32_t* nbr;                             // particle ids (the FP64 form's encoding)
   const int32_t* __restrict__ member;       // SELL position -> particle (-1: a hole)
   const int32_t* __restrict__ pos_of;       // particle -> SELL position
   const VisitRec* __restrict__ visit;       // per warp of each visiting block: its chunk
   int64_t nblocks;                          // visiting blocks (kHaloBlock threads, one tile each)
   uint16_t* loc;                            // per slot: position in the block's halo (padding / broken: the
                                             // particle's own position, whose data adds exact zeros)
-  const uint16_t* __restrict__ self_loc;    // per particle: its own position in its block's halo
-  const int32_t* __restrict__ halo;         // per block: halo particle ids (halo_cap entries per block)
+  const uint16_t* __restrict__ self_loc;    // per position: the particle's own entry in its block's halo
+  const int32_t* __restrict__ halo;         // per block: SELL positions of its halo (halo_cap entries per block)
   const int32_t* __restrict__ halo_n;       // per block: halo size, -1 = not staged
   int32_t halo_cap, halo_max;               // halo_max: largest halo (multiple of 8), sizes shared memory
   float c11, c12, c33;  // C / Es
@@ -251,6 +256,8 @@ struct HaloLayout {
 int build_halo_mixed(const MixedArgs& a, int64_t nslots, int64_t nblocks, const int32_t* block_chunks,
                      const uint64_t* rk, cudaStream_t s, HaloLayout* out, std::string* msg);
 void launch_halo_relink(const MixedArgs& a, const HaloLayout& h, cudaStream_t s);
+// bcp[p] = bc[member[p]] (0 for holes): the mixed form's BC groups by SELL position
+void launch_bc_by_position(int64_t npos, const int32_t* member, const uint8_t* bc, uint8_t* bcp, cudaStream_t s);
 void launch_drift_mixed(const MixedArgs& a, cudaStream_t s);
 void launch_pass_a_mixed(const MixedArgs& a, bool breaking, cudaStream_t s);
 void launch_pass_b_mixed(const MixedArgs& a, bool drift, cudaStream_t s);

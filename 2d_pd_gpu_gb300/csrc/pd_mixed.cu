@@ -62,9 +62,9 @@ __device__ __forceinline__ float2 tf_diff2(float4 j, float2 nhi, float2 nlo) {
   return add2(add2(f2(j.x, j.y), nhi), add2(f2(j.z, j.w), nlo));
 }
 
-// K^-1 (FP64 inversion + guard) and m^ from the FP64 reference positions;
-// particle i's slots are s0 + 32 k, k < w.
-__device__ void kinv_update_mixed(const MixedArgs& a, int64_t i, int64_t s0, int w) {
+// K^-1 (FP64 inversion + guard) and m^ from the FP64 reference positions of
+// particle i at SELL position p, whose slots are s0 + 32 k, k < w.
+__device__ void kinv_update_mixed(const MixedArgs& a, int64_t i, int64_t p, int64_t s0, int w) {
   const double2 xi = a.x[i];
   double k11 = 0.0, k12 = 0.0, k22 = 0.0, mx = 0.0, my = 0.0;
   int nal = 0;
@@ -88,23 +88,23 @@ __device__ void kinv_update_mixed(const MixedArgs& a, int64_t i, int64_t s0, int
   const int32_t fam = a.fam[i];
   const bool failed = fam > 0 && (double)a.broken[i] / (double)fam > a.damage_fail;
   if (nal == 0 || failed || !(det > a.det_guard * (k11 * k22))) {
-    a.geo[i] = make_float4(0.f, 0.f, 0.f, (float)vi);
-    a.mh[i] = make_float2(0.f, 0.f);
-    a.singular[i] = 1;
+    a.geo[p] = make_float4(0.f, 0.f, 0.f, (float)vi);
+    a.mh[p] = make_float2(0.f, 0.f);
+    a.singular[p] = 1;
     atomicAdd(a.counters + CNT_SINGULAR, 1ull);
     return;
   }
   const double r = 1.0 / det;
-  a.geo[i] = make_float4((float)(k22 * r), (float)(-k12 * r), (float)(k11 * r), (float)vi);
-  a.mh[i] = make_float2((float)(mx / vi), (float)(my / vi));
-  a.singular[i] = 0;
+  a.geo[p] = make_float4((float)(k22 * r), (float)(-k12 * r), (float)(k11 * r), (float)vi);
+  a.mh[p] = make_float2((float)(mx / vi), (float)(my / vi));
+  a.singular[p] = 0;
 }
 
 __global__ void __launch_bounds__(kBlock) k_init_geometry_mixed(MixedArgs a) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   const int64_t p = sell_pos(a.pos_of, i);
-  kinv_update_mixed(a, i, sell_slot0(a.chunk_base, p), a.chunk_w[p >> 5]);
+  kinv_update_mixed(a, i, p, sell_slot0(a.chunk_base, p), a.chunk_w[p >> 5]);
 }
 
 // BC + drift of particle i in scaled per-step units; an = a^ of the new force.
@@ -133,9 +133,9 @@ __device__ __forceinline__ void drift_bc(const BcOf& b, float4& v, float4& u, fl
   if (b.kind == PD_BC_FIXED) u = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
-__device__ __forceinline__ void drift_mixed(const MixedArgs& a, int64_t i, float4& v, float4& u, float anx,
+__device__ __forceinline__ void drift_mixed(const MixedArgs& a, int64_t p, float4& v, float4& u, float anx,
                                             float any) {
-  const int g = a.bc[i];
+  const int g = a.bc[p];
   const int kind = g ? a.gkind[g - 1] : PD_BC_NONE;
   if (kind == PD_BC_VELOCITY) v = a.gvel[g - 1];
   // u += v + a/2   (v two-float, a/2 FP32)
@@ -146,17 +146,18 @@ __device__ __forceinline__ void drift_mixed(const MixedArgs& a, int64_t i, float
   if (kind == PD_BC_FIXED) u = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
-__device__ __forceinline__ void drift_particle_mixed(const MixedArgs& a, int64_t i) {
-  float4 v = a.vs[i], u = a.us[i];
-  const float2 f = a.fs[i];
-  drift_mixed(a, i, v, u, a.tau2 * f.x, a.tau2 * f.y);
-  a.vs[i] = v;
-  a.us[i] = u;
+// Drift of SELL position p (a hole holds zeros and stays zero).
+__device__ __forceinline__ void drift_particle_mixed(const MixedArgs& a, int64_t p) {
+  float4 v = a.vs[p], u = a.us[p];
+  const float2 f = a.fs[p];
+  drift_mixed(a, p, v, u, a.tau2 * f.x, a.tau2 * f.y);
+  a.vs[p] = v;
+  a.us[p] = u;
 }
 
 __global__ void __launch_bounds__(kBlock) k_drift_mixed(MixedArgs a) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < a.n) drift_particle_mixed(a, i);
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < a.npos) drift_particle_mixed(a, p);
 }
 
 // Neighbour data gathered by the two passes.
@@ -175,16 +176,16 @@ struct PreA {
   int self_l;  // own halo position (staged blocks)
 };
 
-__device__ __forceinline__ PreA load_a(const MixedArgs& a, int64_t i) {
-  return PreA{a.us[i], a.xs[i], a.geo[i], a.singular[i], a.self_loc ? (int)a.self_loc[i] : 0};
+__device__ __forceinline__ PreA load_a(const MixedArgs& a, int64_t p) {
+  return PreA{a.us[p], a.xs[p], a.geo[p], a.singular[p], a.self_loc ? (int)a.self_loc[p] : 0};
 }
 
-// Pass A of particle i: slots s0 + 32 k, k < w; idx(k) gives a slot's
-// neighbour (a particle id, -1 for padding or broken; or, when the data is
-// staged, a halo position, the particle's own for padding or broken) and
-// gather(j) its data.
+// Pass A of the particle at SELL position p: slots s0 + 32 k, k < w; idx(k)
+// gives a slot's neighbour (a particle id, -1 for padding or broken; or, when
+// the data is staged, a halo entry, the particle's own for padding or
+// broken) and gather(j) its data.
 template <bool BREAK, typename Idx, typename Gather>
-__device__ __forceinline__ void pass_a_core(const MixedArgs& a, int64_t i, const PreA& pre, int w, int64_t s0, Idx idx,
+__device__ __forceinline__ void pass_a_core(const MixedArgs& a, int64_t p, const PreA& pre, int w, int64_t s0, Idx idx,
                                             Gather gather) {
   const float4 ui = pre.ui, xi = pre.xi;
   int newly = 0;
@@ -211,20 +212,21 @@ __device__ __forceinline__ void pass_a_core(const MixedArgs& a, int64_t i, const
     A = fma2(vv, d, A);
   });
   const float d11 = D1.x, d12 = D1.y, d21 = D2.x, d22 = D2.y;
-  a.hgs[i] = make_float2(2.f * a.k_hg * A.x, 2.f * a.k_hg * A.y);
+  a.hgs[p] = make_float2(2.f * a.k_hg * A.x, 2.f * a.k_hg * A.y);
   float4 g = pre.geo;
   int singular = pre.singular;
   if (BREAK && newly) {
     atomicAdd(a.counters + CNT_BROKEN, (unsigned long long)newly);
+    const int64_t i = a.member[p];
     const int32_t b = a.broken[i] + newly;
     a.broken[i] = b;
     a.damage[i] = (double)b / (double)a.fam[i];
-    kinv_update_mixed(a, i, s0, w);
-    g = a.geo[i];
-    singular = a.singular[i];
+    kinv_update_mixed(a, i, p, s0, w);
+    g = a.geo[p];
+    singular = a.singular[p];
   }
   if (singular) {
-    a.ws[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    a.ws[p] = make_float4(0.f, 0.f, 0.f, 0.f);
     return;
   }
   const float k11 = g.x, k12 = g.y, k22 = g.z, vi = g.w;
@@ -235,13 +237,16 @@ __device__ __forceinline__ void pass_a_core(const MixedArgs& a, int64_t i, const
   const float s22 = fmaf(a.c12, e11, a.c11 * e22);
   const float s12 = a.c33 * e12;
   const float kh = -a.k_hg;  // W^ = V^ (sigma^ K^-1 - k^ G), stored by columns {W11, W21, W12, W22}
-  a.ws[i] = make_float4(vi * fmaf(kh, g11, fmaf(s11, k11, s12 * k12)), vi * fmaf(kh, g21, fmaf(s12, k11, s22 * k12)),
+  a.ws[p] = make_float4(vi * fmaf(kh, g11, fmaf(s11, k11, s12 * k12)), vi * fmaf(kh, g21, fmaf(s12, k11, s22 * k12)),
                         vi * fmaf(kh, g12, fmaf(s11, k12, s12 * k22)), vi * fmaf(kh, g22, fmaf(s12, k12, s22 * k22)));
 }
 
-struct GatherA {
+struct GatherA {  // neighbour data of particle j (unstaged blocks)
   const MixedArgs* a;
-  __device__ __forceinline__ NbA operator()(int64_t j) const { return NbA{a->us[j], a->xs[j], a->vh[j]}; }
+  __device__ __forceinline__ NbA operator()(int64_t j) const {
+    const int64_t q = a->pos_of[j];
+    return NbA{a->us[q], a->xs[q], a->vh[q]};
+  }
 };
 
 // Per-particle inputs of pass B, loaded ahead of the bond walk (the BC
@@ -253,24 +258,25 @@ struct PreB {
 };
 
 template <bool DRIFT>
-__device__ __forceinline__ PreB load_b(const MixedArgs& a, int64_t i) {
+__device__ __forceinline__ PreB load_b(const MixedArgs& a, int64_t q) {
   PreB p;
-  p.wi = a.ws[i];
-  p.xi = a.xs[i];
-  p.m = a.mh[i];
-  p.h = a.hgs[i];
-  p.fo = a.fs[i];
-  p.v = a.vs[i];
+  p.wi = a.ws[q];
+  p.xi = a.xs[q];
+  p.m = a.mh[q];
+  p.h = a.hgs[q];
+  p.fo = a.fs[q];
+  p.v = a.vs[q];
   if (DRIFT) {
-    p.u = a.us[i];
-    p.g = a.bc[i];
+    p.u = a.us[q];
+    p.g = a.bc[q];
   }
   return p;
 }
 
-// Pass B of particle i (force gather, kick, optional next drift).
+// Pass B of the particle at SELL position p (force gather, kick, optional
+// next drift).
 template <bool DRIFT, typename Idx, typename Gather>
-__device__ __forceinline__ void pass_b_core(const MixedArgs& a, int64_t i, const PreB& pre, const BcOf& bc, int w,
+__device__ __forceinline__ void pass_b_core(const MixedArgs& a, int64_t p, const PreB& pre, const BcOf& bc, int w,
                                             Idx idx, Gather gather) {
   const float4 wi = pre.wi, xi = pre.xi;
   const float2 m = pre.m, h = pre.h;
@@ -293,18 +299,21 @@ __device__ __forceinline__ void pass_b_core(const MixedArgs& a, int64_t i, const
   float4 v = pre.v;
   tf_add(v.x, v.z, 0.5f * (aox + anx));
   tf_add(v.y, v.w, 0.5f * (aoy + any));
-  a.fs[i] = make_float2(fx, fy);
+  a.fs[p] = make_float2(fx, fy);
   if (DRIFT) {
     float4 u = pre.u;
     drift_bc(bc, v, u, anx, any);
-    a.us[i] = u;
+    a.us[p] = u;
   }
-  a.vs[i] = v;
+  a.vs[p] = v;
 }
 
-struct GatherB {
+struct GatherB {  // neighbour data of particle j (unstaged blocks)
   const MixedArgs* a;
-  __device__ __forceinline__ NbB operator()(int64_t j) const { return NbB{a->xs[j], a->ws[j]}; }
+  __device__ __forceinline__ NbB operator()(int64_t j) const {
+    const int64_t q = a->pos_of[j];
+    return NbB{a->xs[q], a->ws[q]};
+  }
 };
 
 
@@ -348,19 +357,17 @@ __device__ __forceinline__ void cp_async4(void* dst, const void* src) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-// The calling warp's chunk (one 16 B visit record); false if the warp has none.
-__device__ __forceinline__ bool warp_chunk(const MixedArgs& a, int64_t blk, int64_t* chunk, int* w, int64_t* base) {
+// The calling warp's chunk (one 16 B visit record): false if the warp has
+// none; *live = its lanes that hold a particle (the first ones).
+__device__ __forceinline__ bool warp_chunk(const MixedArgs& a, int64_t blk, int64_t* chunk, int* w, int64_t* base,
+                                           int* live) {
   const VisitRec r = a.visit[blk * (kHaloBlock / 32) + (threadIdx.x >> 5)];
   if (r.chunk < 0) return false;  // warp-uniform
   *chunk = r.chunk;
   *w = r.w;
+  *live = r.live;
   *base = r.base;
   return true;
-}
-
-// Particle of lane `lane` of SELL chunk `chunk`, -1 for a hole.
-__device__ __forceinline__ int64_t lane_particle(const MixedArgs& a, int64_t chunk, int lane) {
-  return a.member[chunk * 32 + lane];
 }
 
 __device__ __forceinline__ void stage_timeout(const MixedArgs& a) {
@@ -402,21 +409,21 @@ __device__ __forceinline__ bool warp_stage_done(const MixedArgs& a, uint64_t* ba
 template <bool BREAK>
 __device__ __forceinline__ bool pass_a_block(const MixedArgs& a, int64_t blk, unsigned char* sm, uint64_t* bars) {
   int64_t chunk = 0, base = 0;
-  int w = 0;
-  const bool has = warp_chunk(a, blk, &chunk, &w, &base);
+  int w = 0, nlive = 0;
+  const bool has = warp_chunk(a, blk, &chunk, &w, &base, &nlive);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int hn = a.halo_n ? a.halo_n[blk] : -1;
-  const int64_t i = has ? lane_particle(a, chunk, lane) : -1;
-  const bool live = i >= 0;
+  const int64_t p = chunk * 32 + lane;  // SELL position
+  const bool live = has && lane < nlive;
   PreA pre{};
-  if (live) pre = load_a(a, i);  // in flight during the staging below
+  if (live) pre = load_a(a, p);  // in flight during the staging below
   if (hn < 0) {  // int32 indices staged per warp, neighbour data from L1/L2
     if (!has) return true;
     int32_t* mine = reinterpret_cast<int32_t*>(sm) + warp * a.wmax * 32;
     if (w > 0 && lane == 0) stage_issue(mine, a.nbr + base, (uint32_t)w * 128u, &bars[warp]);
     __syncwarp();
     if (!warp_stage_done(a, &bars[warp], w)) return false;
-    if (live) pass_a_core<BREAK>(a, i, pre, w, base + lane, SharedIdx{mine, lane}, GatherA{&a});
+    if (live) pass_a_core<BREAK>(a, p, pre, w, base + lane, SharedIdx{mine, lane}, GatherA{&a});
     return true;
   }
   const HaloSmem h = halo_smem(a, sm);
@@ -446,7 +453,7 @@ __device__ __forceinline__ bool pass_a_block(const MixedArgs& a, int64_t blk, un
   const float4* q0 = h.q0;
   const float4* q1 = h.q1;
   const float* vh = h.vh;
-  pass_a_core<BREAK>(a, i, pre, w, base + lane, SharedHaloIdx{h.li + warp * a.wmax * 32, lane},
+  pass_a_core<BREAK>(a, p, pre, w, base + lane, SharedHaloIdx{h.li + warp * a.wmax * 32, lane},
                      [=](int64_t l) { return NbA{q0[l], q1[l], vh[l]}; });
   return true;
 }
@@ -455,14 +462,14 @@ __device__ __forceinline__ bool pass_a_block(const MixedArgs& a, int64_t blk, un
 template <bool DRIFT>
 __device__ __forceinline__ bool pass_b_block(const MixedArgs& a, int64_t blk, unsigned char* sm, uint64_t* bars) {
   int64_t chunk = 0, base = 0;
-  int w = 0;
-  const bool has = warp_chunk(a, blk, &chunk, &w, &base);
+  int w = 0, nlive = 0;
+  const bool has = warp_chunk(a, blk, &chunk, &w, &base, &nlive);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int hn = a.halo_n ? a.halo_n[blk] : -1;
-  const int64_t i = has ? lane_particle(a, chunk, lane) : -1;
-  const bool live = i >= 0;
+  const int64_t p = chunk * 32 + lane;  // SELL position
+  const bool live = has && lane < nlive;
   PreB pre{};
-  if (live) pre = load_b<DRIFT>(a, i);  // in flight during the staging below
+  if (live) pre = load_b<DRIFT>(a, p);  // in flight during the staging below
   if (hn < 0) {
     if (!has) return true;
     int32_t* mine = reinterpret_cast<int32_t*>(sm) + warp * a.wmax * 32;
@@ -470,7 +477,7 @@ __device__ __forceinline__ bool pass_b_block(const MixedArgs& a, int64_t blk, un
     __syncwarp();
     if (!warp_stage_done(a, &bars[warp], w)) return false;
     if (live)
-      pass_b_core<DRIFT>(a, i, pre, DRIFT ? resolve_bc(a, pre.g) : BcOf{}, w, SharedIdx{mine, lane}, GatherB{&a});
+      pass_b_core<DRIFT>(a, p, pre, DRIFT ? resolve_bc(a, pre.g) : BcOf{}, w, SharedIdx{mine, lane}, GatherB{&a});
     return true;
   }
   const HaloSmem h = halo_smem(a, sm);
@@ -500,7 +507,7 @@ __device__ __forceinline__ bool pass_b_block(const MixedArgs& a, int64_t blk, un
   if (!live) return true;
   const float4* q0 = h.q0;
   const float4* q1 = h.q1;
-  pass_b_core<DRIFT>(a, i, pre, bc, w, SharedHaloIdx{h.li + warp * a.wmax * 32, lane},
+  pass_b_core<DRIFT>(a, p, pre, bc, w, SharedHaloIdx{h.li + warp * a.wmax * 32, lane},
                      [=](int64_t l) { return NbB{q0[l], q1[l]}; });
   return true;
 }
@@ -508,10 +515,10 @@ __device__ __forceinline__ bool pass_b_block(const MixedArgs& a, int64_t blk, un
 // Drift of visiting block blk of plate a (the first drift of a batched call).
 __device__ __forceinline__ void drift_block(const MixedArgs& a, int64_t blk) {
   int64_t chunk = 0, base = 0;
-  int w = 0;
-  if (!warp_chunk(a, blk, &chunk, &w, &base)) return;
-  const int64_t i = lane_particle(a, chunk, threadIdx.x & 31);
-  if (i >= 0) drift_particle_mixed(a, i);
+  int w = 0, nlive = 0;
+  if (!warp_chunk(a, blk, &chunk, &w, &base, &nlive)) return;
+  const int lane = threadIdx.x & 31;
+  if (lane < nlive) drift_particle_mixed(a, chunk * 32 + lane);
 }
 
 template <bool BREAK>
@@ -559,11 +566,12 @@ __global__ void __launch_bounds__(kHaloBlock) k_halo_build(MixedArgs a, const ui
   __shared__ int32_t s_cnt, s_put;
   const int tid = threadIdx.x, lane = tid & 31;
   int64_t chunk = 0, base = 0;
-  int w = 0;
-  const bool has = warp_chunk(a, blockIdx.x, &chunk, &w, &base);
+  int w = 0, nlive = 0;
+  const bool has = warp_chunk(a, blockIdx.x, &chunk, &w, &base, &nlive);
   if (!has) w = 0;
   const int64_t s0 = base + lane;
-  const int64_t i = has ? lane_particle(a, chunk, lane) : -1;
+  const int64_t p = chunk * 32 + lane;  // SELL position
+  const int64_t i = has && lane < nlive ? (int64_t)a.member[p] : -1;
   for (int k = tid; k < kHaloHash; k += kHaloBlock) tab[k] = -1;
   if (tid == 0) {
     s_cnt = 0;
@@ -619,7 +627,7 @@ __global__ void __launch_bounds__(kHaloBlock) k_halo_build(MixedArgs a, const ui
       }
     if (tid == 0) halo_n[blockIdx.x] = tot;
     int32_t* H = halo + (int64_t)blockIdx.x * kHaloCap;
-    for (int k = tid; k < tot; k += kHaloBlock) H[k] = (int32_t)(list[k] & 0x7FFFFFFFull);  // rk's low bits: the id
+    for (int k = tid; k < tot; k += kHaloBlock) H[k] = a.pos_of[list[k] & 0x7FFFFFFFull];  // rk's low bits: the id
     auto pos = [&](int j) {  // the entry of particle j (its key is in the list)
       const uint64_t r = rk[j];
       int lo = 0, hi = tot;
@@ -633,7 +641,7 @@ __global__ void __launch_bounds__(kHaloBlock) k_halo_build(MixedArgs a, const ui
       return (uint16_t)lo;
     };
     const uint16_t self = i >= 0 ? pos((int)i) : (uint16_t)0;
-    if (i >= 0) self_loc[i] = self;
+    if (i >= 0) self_loc[p] = self;
     for (int k = 0; k < w; ++k) {
       const int64_t s = s0 + (int64_t)k * kChunk;
       const int v = k < wl ? a.nbr[s] : -1;
@@ -646,7 +654,7 @@ __global__ void __launch_bounds__(kHaloBlock) k_halo_build(MixedArgs a, const ui
   }
   // too many: the block reads neighbour data from HBM (loc unused)
   if (tid == 0) halo_n[blockIdx.x] = -1;
-  if (i >= 0) self_loc[i] = 0;
+  if (i >= 0) self_loc[p] = 0;
   for (int k = 0; k < w; ++k) {
     const int64_t s = s0 + (int64_t)k * kChunk;
     loc0[s] = 0xFFFF;
@@ -654,14 +662,21 @@ __global__ void __launch_bounds__(kHaloBlock) k_halo_build(MixedArgs a, const ui
   }
 }
 
-// visit record of every warp of every visiting block: {chunk, width, first slot}
+// visit record of every warp of every visiting block: {chunk, width, live
+// lanes, first slot} (a chunk's holes are its last lanes)
 __global__ void k_visit_build(int64_t nwarps, const int32_t* __restrict__ block_chunks,
                               const int32_t* __restrict__ chunk_w, const int64_t* __restrict__ chunk_base,
-                              VisitRec* visit) {
+                              const int32_t* __restrict__ member, VisitRec* visit) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= nwarps) return;
   const int32_t c = block_chunks[k];
-  visit[k] = c >= 0 ? VisitRec{c, chunk_w[c], chunk_base[c]} : VisitRec{-1, 0, 0};
+  VisitRec r{-1, 0, 0, 0};
+  if (c >= 0) {
+    int live = 0;
+    for (int l = 0; l < 32; ++l) live += member[(int64_t)c * 32 + l] >= 0;
+    r = VisitRec{c, (int16_t)chunk_w[c], (int16_t)live, chunk_base[c]};
+  }
+  visit[k] = r;
 }
 
 // live 16-bit indices from the pristine ones and the int32 mask (after a
@@ -673,7 +688,7 @@ __global__ void k_halo_relink(MixedArgs a, const uint16_t* __restrict__ loc0, co
   const int64_t p = sell_pos(a.pos_of, i);
   const int w = a.chunk_w[p >> 5];
   const int64_t s0 = sell_slot0(a.chunk_base, p);
-  const uint16_t self = self_loc[i];
+  const uint16_t self = self_loc[p];
   for (int k = 0; k < w; ++k) {
     const int64_t s = s0 + (int64_t)k * kChunk;
     loc[s] = a.nbr[s] >= 0 ? loc0[s] : self;
@@ -741,54 +756,73 @@ __device__ __forceinline__ void split2(double v, float& hi, float& lo) {
   lo = (float)(v - (double)hi);
 }
 
+// (per particle i; the scaled state of i sits at SELL position pos_of[i])
 __global__ void k_to_mixed(MixedArgs a, const double2* u, const double2* v, const double2* f) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
+  const int64_t p = a.pos_of[i];
   float4 o;
   if (u) {
     const double2 q = u[i];
     split2(q.x * a.inv_ls, o.x, o.z);
     split2(q.y * a.inv_ls, o.y, o.w);
-    a.us[i] = o;
+    a.us[p] = o;
   }
   if (v) {
     const double2 q = v[i];
     split2(q.x * a.v_scale, o.x, o.z);
     split2(q.y * a.v_scale, o.y, o.w);
-    a.vs[i] = o;
+    a.vs[p] = o;
   }
   if (f) {
     const double2 q = f[i];
-    a.fs[i] = make_float2((float)(q.x * a.f_scale), (float)(q.y * a.f_scale));
+    a.fs[p] = make_float2((float)(q.x * a.f_scale), (float)(q.y * a.f_scale));
   }
 }
 
 __global__ void k_from_mixed(MixedArgs a, double2* u, double2* v, double2* f) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
+  const int64_t p = a.pos_of[i];
   if (u) {
-    const float4 q = a.us[i];
+    const float4 q = a.us[p];
     u[i] = make_double2(((double)q.x + (double)q.z) / a.inv_ls, ((double)q.y + (double)q.w) / a.inv_ls);
   }
   if (v) {
-    const float4 q = a.vs[i];
+    const float4 q = a.vs[p];
     v[i] = make_double2(((double)q.x + (double)q.z) / a.v_scale, ((double)q.y + (double)q.w) / a.v_scale);
   }
   if (f) {
-    const float2 q = a.fs[i];
+    const float2 q = a.fs[p];
     f[i] = make_double2((double)q.x / a.f_scale, (double)q.y / a.f_scale);
   }
 }
 
+// x^, V^ by SELL position (holes: zeros)
 __global__ void k_positions_mixed(MixedArgs a) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= a.npos) return;
+  const int64_t i = a.member[p];
+  if (i < 0) {
+    a.xs[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+    a.vh[p] = 0.f;
+    return;
+  }
   const double2 q = a.x[i];
   float4 o;
   split2(q.x * a.inv_ls, o.x, o.z);
   split2(q.y * a.inv_ls, o.y, o.w);
-  a.xs[i] = o;
-  a.vh[i] = (float)(a.vol[i] * a.inv_vs);
+  a.xs[p] = o;
+  a.vh[p] = (float)(a.vol[i] * a.inv_vs);
+}
+
+// BC group by SELL position (holes: none)
+__global__ void k_bc_by_position(int64_t npos, const int32_t* __restrict__ member, const uint8_t* __restrict__ bc,
+                                 uint8_t* bcp) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npos) return;
+  const int32_t i = member[p];
+  bcp[p] = i >= 0 ? bc[i] : 0;
 }
 
 }  // namespace
@@ -855,12 +889,12 @@ void launch_init_geometry_mixed(const MixedArgs& a, cudaStream_t s) {
   cudaFuncSetAttribute(k_batch_phase_mixed<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   cudaFuncSetAttribute(k_batch_phase_mixed<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   cudaFuncSetAttribute(k_batch_phase_mixed<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  k_positions_mixed<<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
+  k_positions_mixed<<<(unsigned)blocks_for(a.npos), kBlock, 0, s>>>(a);
   k_init_geometry_mixed<<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
 }
 
 void launch_drift_mixed(const MixedArgs& a, cudaStream_t s) {
-  if (a.n > 0) k_drift_mixed<<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
+  if (a.n > 0) k_drift_mixed<<<(unsigned)blocks_for(a.npos), kBlock, 0, s>>>(a);
 }
 
 void launch_pass_a_mixed(const MixedArgs& a, bool breaking, cudaStream_t s) {
@@ -902,13 +936,14 @@ int build_halo_mixed(const MixedArgs& a0, int64_t nslots, int64_t nblocks, const
   if (cudaMalloc(&h->visit, (size_t)nw * sizeof(VisitRec)) != cudaSuccess ||
       cudaMalloc(&h->loc, ns * sizeof(uint16_t)) != cudaSuccess ||
       cudaMalloc(&h->loc0, ns * sizeof(uint16_t)) != cudaSuccess ||
-      cudaMalloc(&h->self_loc, (size_t)a.n * sizeof(uint16_t)) != cudaSuccess ||
+      cudaMalloc(&h->self_loc, (size_t)a.npos * sizeof(uint16_t)) != cudaSuccess ||
       cudaMalloc(&h->halo, (size_t)nb * kHaloCap * sizeof(int32_t)) != cudaSuccess ||
       cudaMalloc(&h->halo_n, (size_t)nb * sizeof(int32_t)) != cudaSuccess) {
     *msg = "halo staging: out of device memory";
     return PD_ERR_CUDA;
   }
-  k_visit_build<<<(unsigned)blocks_for(nw), kBlock, 0, s>>>(nw, block_chunks, a.chunk_w, a.chunk_base, h->visit);
+  k_visit_build<<<(unsigned)blocks_for(nw), kBlock, 0, s>>>(nw, block_chunks, a.chunk_w, a.chunk_base, a.member,
+                                                            h->visit);
   a.visit = h->visit;
   a.nblocks = nb;
   k_halo_build<<<(unsigned)nb, kHaloBlock, 0, s>>>(a, rk, h->halo, h->halo_n, h->loc, h->loc0, h->self_loc);
@@ -927,6 +962,10 @@ int build_halo_mixed(const MixedArgs& a0, int64_t nslots, int64_t nblocks, const
     }
   h->halo_max = (mx + 7) & ~7;
   return PD_OK;
+}
+
+void launch_bc_by_position(int64_t npos, const int32_t* member, const uint8_t* bc, uint8_t* bcp, cudaStream_t s) {
+  if (npos > 0) k_bc_by_position<<<(unsigned)blocks_for(npos), kBlock, 0, s>>>(npos, member, bc, bcp);
 }
 
 void launch_halo_relink(const MixedArgs& a, const HaloLayout& h, cudaStream_t s) {
