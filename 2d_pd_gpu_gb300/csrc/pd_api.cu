@@ -808,7 +808,7 @@ int pd_get_counters(pd_ctx* c, pd_counters* out) {
   out->singular_events = (int64_t)h[pd::CNT_SINGULAR];
   out->steps = c->steps;
   out->device_error = (int32_t)h[pd::CNT_ERROR];
-  out->reserved = 0;
+  out->unstaged_blocks = (int32_t)(c->halo.nblocks - c->halo.staged);
   return PD_OK;
 }
 

@@ -68,7 +68,7 @@ class Counters(ctypes.Structure):
         ("singular_events", ctypes.c_int64),
         ("steps", ctypes.c_int64),
         ("device_error", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("unstaged_blocks", ctypes.c_int32),
     ]
 
 
@@ -317,7 +317,7 @@ class Context:
         c = Counters()
         self._ck(lib().pd_get_counters(self._h, ctypes.byref(c)))
         return {"bonds_broken": c.bonds_broken, "singular_events": c.singular_events, "steps": c.steps,
-                "device_error": c.device_error}
+                "device_error": c.device_error, "unstaged_blocks": c.unstaged_blocks}
 
     # -- Mazars damage (pd_mazars_*)
     def mazars_init(self, params=None, **kw):

@@ -98,7 +98,8 @@ typedef struct pd_counters {
   int64_t singular_events; /* det-guard trips since pd_reset */
   int64_t steps;           /* steps taken since pd_reset */
   int32_t device_error;    /* device error word (0 = none) */
-  int32_t reserved;
+  int32_t unstaged_blocks; /* mixed form: visiting blocks whose halo exceeds the shared-memory
+                              cap and whose passes gather neighbour data from HBM (0: FP64) */
 } pd_counters;
 
 /* ---------------------------------------------------------------- context */

@@ -97,6 +97,7 @@ def test_mixed_shuffled_numbering_matches(pdg):
     a = q.context(precision=pdg.native.PD_FP64)
     b = q.context(precision=pdg.native.PD_MIXED)
     r = p.context(precision=pdg.native.PD_MIXED)
+    assert b.counters()["unstaged_blocks"] == 0 and r.counters()["unstaged_blocks"] == 0
     for c in (a, b, r):
         c.step(200)
     e = _errors(a, b)
@@ -106,6 +107,33 @@ def test_mixed_shuffled_numbering_matches(pdg):
     for got, want in zip(b.state(), r.state()):
         assert np.array_equal(got, want[perm])
     assert np.array_equal(b.damage(), r.damage()[perm])
+
+
+def test_mixed_dense_cluster_unstaged_blocks(pdg):
+    """A 120 x 120 plate with scrambled numbering and two lone particles 10 m
+    apart: the layout's cells follow the bounding box, so each holds thousands
+    of plate particles, its tile (more than 2,048 particles) is ordered on the
+    host, and a block's 256 particles are scattered over a cell, reaching more
+    particles than a block can stage.  Those blocks gather neighbour data from
+    HBM; the result agrees with the FP64 form within the mixed-form bar."""
+    import dataclasses
+    p = pdg.plates.make_plate(120, seed=5, crack="centre-half")
+    perm = np.random.default_rng(11).permutation(p.n)
+    far = np.array([[-5.0, -5.0], [5.0, 5.0]])
+    q = dataclasses.replace(p, x=np.ascontiguousarray(np.vstack([p.x[perm], far])),
+                            vol=np.ascontiguousarray(np.concatenate([p.vol[perm], p.vol[:2]])),
+                            group_of=np.ascontiguousarray(np.concatenate([p.group_of[perm],
+                                                                          np.zeros(2, p.group_of.dtype)])))
+    a = q.context(precision=pdg.native.PD_FP64)
+    b = q.context(precision=pdg.native.PD_MIXED)
+    assert b.counters()["unstaged_blocks"] > 0
+    assert a.counters()["unstaged_blocks"] == 0
+    for c in (a, b):
+        c.step(200)
+    e = _errors(a, b)
+    print("dense cluster, mixed vs fp64:", e, "unstaged blocks:", b.counters()["unstaged_blocks"])
+    assert e["u_max"] < DISP_TOL
+    assert e["broken"] > 0 and e["mask_mismatch"] <= max(2, e["broken"] // 1000)
 
 
 @pytest.mark.parametrize("precision", [0, 1])
