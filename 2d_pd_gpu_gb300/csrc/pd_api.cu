@@ -57,6 +57,11 @@ struct pd_ctx {
   double2* tb = nullptr;
   int64_t* rslot = nullptr;
   int32_t max_family = 0;
+  // pd_step_host's copy / compute pipeline (streams and events, see plan_slabs)
+  cudaStream_t io[3] = {nullptr, nullptr, nullptr};
+  std::vector<cudaEvent_t> slab_ev;
+  int64_t slab = 0;                 // particles per slab (a multiple of 32); 0: not planned
+  std::vector<int32_t> slab_need;   // slab k's pass A needs slabs 0 .. slab_need[k] imported
   // Mazars damage history (pd_mazars_*)
   double *mz_thr = nullptr, *mz_bd = nullptr, *mz_status = nullptr;
   pd_mazars_params mz{};
@@ -170,6 +175,8 @@ void free_families(pd_ctx* c) {
   dfree(c->tb);
   dfree(c->rslot);
   c->sell = pd::SellLayout{};
+  c->slab = 0;
+  c->slab_need.clear();
   c->nnz = 0;
   c->has_families = false;
   clear_graphs(c);
@@ -499,6 +506,9 @@ int pd_destroy(pd_ctx* c) {
   dfree(c->gval);
   dfree(c->gvel);
   for (void* q : c->scratch) cudaFreeHost(q);
+  for (cudaEvent_t e : c->slab_ev) cudaEventDestroy(e);
+  for (cudaStream_t q : c->io)
+    if (q) cudaStreamDestroy(q);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return PD_OK;
@@ -1161,6 +1171,104 @@ int pd_checkpoint_load(pd_ctx* c, const void* buf, int64_t bytes) {
 }
 
 
+// pd_step_host pipeline (FP64 form).  The particles are cut into kSlabs index
+// ranges (multiples of 32); slab_need[k] = the last slab holding slab k's
+// particles or any of their neighbours.  Streams (io[0], io[1] at high
+// priority): io[1] copies u, v, f in slab by slab (host-to-device copies
+// share one path, ~200 GB/s, so slab order is what matters), io[0] runs each
+// slab's drift as its copy lands, and pass A of slab k starts, on the main
+// stream or io[2] alternately, as soon as slabs 0 .. slab_need[k] are in.
+// The last pass B writes the state back to the host buffers itself, which
+// hides the export under the pass (separate copies measured slower).
+constexpr int kSlabs = 8;
+enum { kEvImport = 0, kEvCopy = kSlabs, kEvStart = 2 * kSlabs, kEvJoin = 2 * kSlabs + 1, kEvCount = 2 * kSlabs + 2 };
+
+static int plan_slabs(pd_ctx* c) {
+  if (c->slab > 0) return PD_OK;
+  if (!c->io[0]) {
+    int lo = 0, hi = 0;
+    PD_CK(c, cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    for (int q = 0; q < 2; ++q) PD_CK(c, cudaStreamCreateWithPriority(&c->io[q], cudaStreamNonBlocking, hi));
+    PD_CK(c, cudaStreamCreateWithFlags(&c->io[2], cudaStreamNonBlocking));
+  }
+  while ((int)c->slab_ev.size() < kEvCount) {
+    cudaEvent_t e;
+    PD_CK(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    c->slab_ev.push_back(e);
+  }
+  const int64_t slab = ((c->n + kSlabs - 1) / kSlabs + 31) / 32 * 32;
+  int32_t* reach = nullptr;
+  PD_CK(c, cudaMalloc(&reach, kSlabs * sizeof(int32_t)));
+  std::vector<int32_t> h(kSlabs, 0);
+  cudaError_t e = cudaMemsetAsync(reach, 0, kSlabs * sizeof(int32_t), c->stream);
+  if (e == cudaSuccess) {
+    pd::launch_slab_reach(c->n, c->row_ptr, c->col, slab, reach, c->stream);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = copy_sync(h.data(), reach, kSlabs * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
+  cudaFree(reach);
+  PD_CK(c, e);
+  c->slab_need.assign(kSlabs, 0);
+  for (int k = 0; k < kSlabs; ++k) {
+    const int64_t last = std::min<int64_t>(kSlabs - 1, (int64_t)h[k] / slab);
+    c->slab_need[k] = (int32_t)std::max<int64_t>(k, last);
+  }
+  c->slab = slab;
+  return PD_OK;
+}
+
+// Fp64Args restricted to slab k.
+static Fp64Args slab_args(const pd_ctx* c, const Fp64Args& a, int k) {
+  Fp64Args r = a;
+  r.i0 = std::min<int64_t>(c->n, k * c->slab);
+  r.n = std::min<int64_t>(c->n, (k + 1) * c->slab);
+  return r;
+}
+
+// Enqueues pd_step_host's pipeline (slabs planned) on the main stream.  (A
+// CUDA graph of it measured the same: the GPU, not the enqueue, sets the pace.)
+static cudaError_t enqueue_host_step(pd_ctx* c, int32_t nsteps, const double* u_in, const double* v_in,
+                                     const double* f_in, const Fp64Args& plain, const Fp64Args& out, bool brk) {
+  cudaError_t e = cudaSuccess;
+  auto ck = [&](cudaError_t r) {
+    if (e == cudaSuccess) e = r;
+  };
+  cudaStream_t s = c->stream;
+  cudaEvent_t* ev = c->slab_ev.data();
+  cudaStream_t* io = c->io;
+  const size_t b16 = sizeof(double2);
+  ck(cudaEventRecord(ev[kEvStart], s));
+  for (int q = 0; q < 3; ++q) ck(cudaStreamWaitEvent(io[q], ev[kEvStart], 0));
+  for (int k = 0; k < kSlabs; ++k) {  // import
+    const Fp64Args a = slab_args(c, plain, k);
+    const size_t off = (size_t)a.i0, cnt = (size_t)(a.n - a.i0);
+    if (cnt > 0) {
+      ck(cudaMemcpyAsync(c->u + off, u_in + 2 * off, cnt * b16, cudaMemcpyHostToDevice, io[1]));
+      ck(cudaMemcpyAsync(c->v + off, v_in + 2 * off, cnt * b16, cudaMemcpyHostToDevice, io[1]));
+      ck(cudaMemcpyAsync(c->f + off, f_in + 2 * off, cnt * b16, cudaMemcpyHostToDevice, io[1]));
+    }
+    ck(cudaEventRecord(ev[kEvCopy + k], io[1]));
+    ck(cudaStreamWaitEvent(io[0], ev[kEvCopy + k], 0));
+    pd::launch_drift_fp64(a, io[0]);  // in place, on the device copy
+    ck(cudaEventRecord(ev[kEvImport + k], io[0]));
+  }
+  for (int k = 0; k < kSlabs; ++k) {  // pass A of slab k once its neighbours are in
+    cudaStream_t sk = k % 2 ? io[2] : s;
+    ck(cudaStreamWaitEvent(sk, ev[kEvImport + c->slab_need[k]], 0));
+    pd::launch_pass_a_fp64(slab_args(c, plain, k), brk, sk);
+  }
+  ck(cudaEventRecord(ev[kEvJoin], io[2]));
+  ck(cudaStreamWaitEvent(s, ev[kEvJoin], 0));
+  ck(cudaStreamWaitEvent(s, ev[kEvImport + kSlabs - 1], 0));
+  for (int32_t k = 0; k < nsteps; ++k) {
+    const bool last = k + 1 == nsteps;
+    if (k > 0) pd::launch_pass_a_fp64(plain, brk, s);
+    pd::launch_pass_b_fp64(last ? out : plain, last ? 0 : 1, s);  // the last writes the state back
+  }
+  ck(cudaGetLastError());
+  return e;
+}
+
 int pd_step_host(pd_ctx* c, int32_t nsteps, const double* u_in, const double* v_in, const double* f_in, double* u_out,
                  double* v_out, double* f_out) {
   if (!c) return PD_ERR_ARG;
@@ -1182,16 +1290,17 @@ int pd_step_host(pd_ctx* c, int32_t nsteps, const double* u_in, const double* v_
   cudaStream_t s = c->stream;
   const Fp64Args plain = fp64_args(c);
   const bool brk = c->p.s_c > 0.0;
-  pd::launch_drift_fp64(in, s);  // reads the state over the CPU-GPU link
-  for (int32_t k = 0; k < nsteps; ++k) {
-    const bool last = k + 1 == nsteps;
-    if (bond_assoc(c)) {
+  if (bond_assoc(c)) {  // one stream: the state is read and written by the kernels over the CPU-GPU link
+    pd::launch_drift_fp64(in, s);
+    for (int32_t k = 0; k < nsteps; ++k) {
+      const bool last = k + 1 == nsteps;
       pd::launch_ba_pass_a(plain, ba_args(c), s);
       pd::launch_ba_pass_b(last ? out : plain, ba_args(c), last ? 0 : 1, s);
-    } else {
-      pd::launch_pass_a_fp64(plain, brk, s);
-      pd::launch_pass_b_fp64(last ? out : plain, last ? 0 : 1, s);  // the last writes the state back
     }
+  } else {
+    const int rp = plan_slabs(c);
+    if (rp != PD_OK) return rp;
+    PD_CK(c, enqueue_host_step(c, nsteps, u_in, v_in, f_in, plain, out, brk));
   }
   PD_CK(c, cudaGetLastError());
   PD_CK(c, cudaStreamSynchronize(s));

@@ -97,7 +97,7 @@ __device__ __forceinline__ void drift_particle(const Fp64Args& a, int64_t i) {
 }
 
 __global__ void __launch_bounds__(kBlock) k_drift(Fp64Args a) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t i = a.i0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < a.n) drift_particle(a, i);
 }
 
@@ -195,7 +195,7 @@ __device__ __forceinline__ void pass_a_particle(const Fp64Args& a, int64_t i) {
 
 template <bool BREAK, bool HG>
 __global__ void __launch_bounds__(kBlock) k_pass_a(Fp64Args a) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t i = a.i0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < a.n) pass_a_particle<BREAK, HG>(a, i);
 }
 
@@ -259,7 +259,7 @@ __device__ __forceinline__ void pass_b_particle(const Fp64Args& a, int64_t i) {
 
 template <int MODE, bool HG>
 __global__ void __launch_bounds__(kBlock) k_pass_b(Fp64Args a) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t i = a.i0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < a.n) pass_b_particle<MODE, HG>(a, i);
 }
 
@@ -349,12 +349,29 @@ cudaError_t launch_batch_fp64(const Fp64Args* d_plates, const BatchTile* d_tiles
 namespace {
 }  // namespace
 
+namespace {
+// reach[k] = the largest neighbour id of slab k (particles k*slab .. k*slab + slab - 1)
+__global__ void k_slab_reach(int64_t n, const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
+                             int64_t slab, int32_t* reach) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int32_t m = (int32_t)i;
+  for (int64_t k = row_ptr[i]; k < row_ptr[i + 1]; ++k) m = col[k] > m ? col[k] : m;
+  atomicMax(&reach[i / slab], m);
+}
+}  // namespace
+
+void launch_slab_reach(int64_t n, const int64_t* row_ptr, const int32_t* col, int64_t slab, int32_t* reach,
+                       cudaStream_t s) {
+  if (n > 0) k_slab_reach<<<(unsigned)blocks_for(n), kBlock, 0, s>>>(n, row_ptr, col, slab, reach);
+}
+
 void launch_init_geometry_fp64(const Fp64Args& a, cudaStream_t s) {
   if (a.n > 0) k_init_geometry<<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
 }
 
 void launch_drift_fp64(const Fp64Args& a, cudaStream_t s) {
-  if (a.n > 0) k_drift<<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
+  if (a.n > a.i0) k_drift<<<(unsigned)blocks_for(a.n - a.i0), kBlock, 0, s>>>(a);
 }
 
 void launch_shadow_fp64(const Fp64Args& a, cudaStream_t s) {
@@ -362,8 +379,8 @@ void launch_shadow_fp64(const Fp64Args& a, cudaStream_t s) {
 }
 
 void launch_pass_a_fp64(const Fp64Args& a, bool breaking, cudaStream_t s) {
-  if (a.n <= 0) return;
-  const unsigned nb = (unsigned)blocks_for(a.n);
+  if (a.n <= a.i0) return;
+  const unsigned nb = (unsigned)blocks_for(a.n - a.i0);
   const bool hg = a.k_hg != 0.0;
   if (breaking)
     hg ? k_pass_a<true, true><<<nb, kBlock, 0, s>>>(a) : k_pass_a<true, false><<<nb, kBlock, 0, s>>>(a);
@@ -380,8 +397,8 @@ void launch_b(const Fp64Args& a, unsigned nb, cudaStream_t s) {
 }
 
 void launch_pass_b_fp64(const Fp64Args& a, int mode, cudaStream_t s) {
-  if (a.n <= 0) return;
-  const unsigned nb = (unsigned)blocks_for(a.n);
+  if (a.n <= a.i0) return;
+  const unsigned nb = (unsigned)blocks_for(a.n - a.i0);
   if (mode == 0)
     launch_b<0>(a, nb, s);
   else if (mode == 1)

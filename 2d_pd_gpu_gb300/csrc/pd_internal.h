@@ -59,6 +59,7 @@ enum { ERR_FAMILY_OVERFLOW = 1, ERR_BAD_NEIGHBOR = 2, ERR_SELF_BOND = 4, ERR_ASY
 
 struct Fp64Args {
   int64_t n;
+  int64_t i0;  // drift and the passes run particles i0 <= i < n (a slab; 0 for the whole plate)
   const double2* __restrict__ x;
   const double* __restrict__ vol;
   double2* u;
@@ -216,6 +217,9 @@ void scan_exclusive_i64(const int64_t* in, int64_t* out, int64_t n, cudaStream_t
 void launch_init_geometry_fp64(const Fp64Args& a, cudaStream_t s);
 void launch_drift_fp64(const Fp64Args& a, cudaStream_t s);
 void launch_shadow_fp64(const Fp64Args& a, cudaStream_t s);  // u32 := (float)u
+// reach[k] := max(reach[k], largest neighbour id of slab k); reach zeroed by the caller
+void launch_slab_reach(int64_t n, const int64_t* row_ptr, const int32_t* col, int64_t slab, int32_t* reach,
+                       cudaStream_t s);
 void launch_pass_a_fp64(const Fp64Args& a, bool breaking, cudaStream_t s);  // hourglass term if a.k_hg != 0
 // mode 0: kick; 1: kick + next step's drift; 2: drop-in kick (acc array in/out)
 void launch_pass_b_fp64(const Fp64Args& a, int mode, cudaStream_t s);

@@ -214,12 +214,13 @@ int pd_mazars_set(pd_ctx* ctx, const double* threshold, const double* bond_damag
 int pd_step(pd_ctx* ctx, int32_t nsteps);
 /* nsteps steps from a host state to a host state, FP64 contexts (no
  * reference counterpart; the end-to-end form of the reference's per-call
- * host-buffer contract, include/mechanics.cuh:867-881): the first kernel
- * reads u_in, v_in, f_in ([n][2] doubles) directly from page-locked host
- * memory (pd_host_alloc) over the CPU-GPU link, and the last one writes the
- * new state to u_out, v_out, f_out the same way, so no separate copies run.
- * In and out may be the same buffers.  Synchronous; the device state is
- * updated as by pd_set_state + pd_step + pd_get_state. */
+ * host-buffer contract, include/mechanics.cuh:867-881).  u_in, v_in, f_in
+ * ([n][2] doubles, page-locked: pd_host_alloc) are copied in by slabs of
+ * particles while the first pass runs on the slabs already in; the last
+ * kernel writes the new state to u_out, v_out, f_out directly over the
+ * CPU-GPU link.  In and out may be the same buffers.  Synchronous; the
+ * device state is updated as by pd_set_state + pd_step + pd_get_state, bit
+ * for bit. */
 int pd_step_host(pd_ctx* ctx, int32_t nsteps, const double* u_in, const double* v_in, const double* f_in,
                  double* u_out, double* v_out, double* f_out);
 /* Waits for the context's stream.  PD_ERR_TIMEOUT if a bounded device wait
