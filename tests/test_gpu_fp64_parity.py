@@ -192,8 +192,9 @@ def test_gpu_singular_policy(pdg):
 
 
 def test_gpu_step_host_equals_staged_copies(pdg):
-    """pd_step_host (state read / written by the kernels over the CPU-GPU
-    link) is pd_set_state + pd_step + pd_get_state, bit for bit."""
+    """pd_step_host (the state copied in by slabs while the first pass runs,
+    written back by the last kernel over the CPU-GPU link) is pd_set_state +
+    pd_step + pd_get_state, bit for bit, call after call while bonds break."""
     p = pdg.plates.make_plate(90, seed=4, crack="centre-half")
     p.material.s_c = 2e-4
     a = p.context()
@@ -204,7 +205,7 @@ def test_gpu_step_host_equals_staged_copies(pdg):
     bufs = [pdg.native.PinnedArray((p.n, 2)) for _ in range(3)]
     hu, hv, hf = (x.array for x in bufs)
     hu[:], hv[:], hf[:] = u, v, f
-    for nsteps in (1, 3):
+    for nsteps in (1, 1, 3, 1, 2, 1):
         a.set_state(u=hu, v=hv, f=hf)
         a.step(nsteps)
         ua, va, fa = a.state()
