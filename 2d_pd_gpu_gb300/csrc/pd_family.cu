@@ -19,8 +19,6 @@ namespace pd {
 
 namespace {
 
-__constant__ double c_cracks[PD_MAX_CRACKS * 4];
-
 __device__ __forceinline__ double orient(double ax, double ay, double bx, double by, double px, double py) {
   const double d1 = (bx - ax) * (py - ay);
   const double d2 = (by - ay) * (px - ax);
@@ -35,10 +33,16 @@ __device__ __forceinline__ bool crosses(double px, double py, double qx, double 
   return ((o1 > 0.0 && o2 < 0.0) || (o1 < 0.0 && o2 > 0.0)) && ((o3 > 0.0 && o4 < 0.0) || (o3 < 0.0 && o4 > 0.0));
 }
 
-// Bounding boxes of the crack segments (FP32, widened by a margin): a bond
-// whose box misses a crack's box cannot properly cross it, so the exact FP64
-// test runs only near cracks.
-__constant__ float c_crack_box[PD_MAX_CRACKS * 4];
+// The pre-crack segments of one family build, passed by value (a kernel
+// parameter, read in place through __grid_constant__), so builds of several
+// contexts can run at once.  box: each segment's bounding box in FP32,
+// widened by a margin: a bond whose box misses a crack's box cannot properly
+// cross it, so the exact FP64 test runs only near cracks.
+struct CrackSet {
+  int32_t n;
+  double seg[PD_MAX_CRACKS * 4];
+  float box[PD_MAX_CRACKS * 4];
+};
 
 struct Grid {
   double x0, y0, inv_cs;
@@ -90,7 +94,8 @@ __global__ void k_cell_fill(int64_t n, const int64_t* cell_of, const int64_t* ce
 // Count (FILL = false) or write the family of each particle.
 template <bool FILL>
 __global__ void k_family(int64_t n, const double2* __restrict__ x, Grid G, const int64_t* __restrict__ cell_start,
-                         const int32_t* __restrict__ items, double cutoff, int n_cracks, int64_t* deg,
+                         const int32_t* __restrict__ items, double cutoff, const __grid_constant__ CrackSet cr,
+                         int64_t* deg,
                          const int64_t* __restrict__ row_ptr, int32_t* col, unsigned long long* counters) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -112,9 +117,9 @@ __global__ void k_family(int64_t n, const double2* __restrict__ x, Grid G, const
         const double2 pj = x[j];
         if (!within_cutoff(pj.x - pi.x, pj.y - pi.y, cutoff, G)) continue;
         bool cut = false;
-        for (int q = 0; q < n_cracks && !cut; ++q)
-          cut = near_crack((float)pi.x, (float)pi.y, (float)pj.x, (float)pj.y, c_crack_box + 4 * q) &&
-                crosses(pi.x, pi.y, pj.x, pj.y, c_cracks + 4 * q);
+        for (int q = 0; q < cr.n && !cut; ++q)
+          cut = near_crack((float)pi.x, (float)pi.y, (float)pj.x, (float)pj.y, cr.box + 4 * q) &&
+                crosses(pi.x, pi.y, pj.x, pj.y, cr.seg + 4 * q);
         if (cut) continue;
         if (FILL) {
           if (cnt < PD_MAX_FAMILY) {
@@ -390,22 +395,21 @@ int build_families_gpu(int64_t n, const double2* d_x, const double* h_x, double 
     G.c2_hi = INFINITY;
   }
   const int64_t nc = G.gx * G.gy;
+  CrackSet cr{};
+  cr.n = n_cracks;
   if (n_cracks > 0) {
-    cudaMemcpyToSymbolAsync(c_cracks, h_cracks, sizeof(double) * 4 * n_cracks, 0, cudaMemcpyHostToDevice, s);
+    for (int q = 0; q < 4 * n_cracks; ++q) cr.seg[q] = h_cracks[q];
     // crack boxes widened by far more than the FP32 rounding of any coordinate
     double big = fmax(fmax(fabs(xmin), fabs(xmax)), fmax(fabs(ymin), fabs(ymax)));
     for (int q = 0; q < 4 * n_cracks; ++q) big = fmax(big, fabs(h_cracks[q]));
     const double m = 1e-5 * big + 1e-300;
-    float box[PD_MAX_CRACKS * 4];
     for (int q = 0; q < n_cracks; ++q) {
       const double* c = h_cracks + 4 * q;
-      box[4 * q + 0] = (float)(fmin(c[0], c[2]) - m);
-      box[4 * q + 1] = (float)(fmin(c[1], c[3]) - m);
-      box[4 * q + 2] = (float)(fmax(c[0], c[2]) + m);
-      box[4 * q + 3] = (float)(fmax(c[1], c[3]) + m);
+      cr.box[4 * q + 0] = (float)(fmin(c[0], c[2]) - m);
+      cr.box[4 * q + 1] = (float)(fmin(c[1], c[3]) - m);
+      cr.box[4 * q + 2] = (float)(fmax(c[0], c[2]) + m);
+      cr.box[4 * q + 3] = (float)(fmax(c[1], c[3]) + m);
     }
-    cudaMemcpyToSymbolAsync(c_crack_box, box, sizeof(float) * 4 * n_cracks, 0, cudaMemcpyHostToDevice, s);
-    cudaStreamSynchronize(s);  // box lives on this stack frame
   }
 
   int64_t *cell_of = nullptr, *cell_start = nullptr, *deg = nullptr;
@@ -427,7 +431,7 @@ int build_families_gpu(int64_t n, const double2* d_x, const double* h_x, double 
   cudaMemsetAsync(cnt, 0, (size_t)nc * sizeof(unsigned long long), s);
   if (n > 0) {
     k_cell_fill<<<nb, kBlock, 0, s>>>(n, cell_of, cell_start, cnt, items);
-    k_family<false><<<nb, kBlock, 0, s>>>(n, d_x, G, cell_start, items, cutoff, n_cracks, deg, nullptr, nullptr,
+    k_family<false><<<nb, kBlock, 0, s>>>(n, d_x, G, cell_start, items, cutoff, cr, deg, nullptr, nullptr,
                                           counters);
   }
   scan_exclusive_i64(deg, out->row_ptr, n, s);
@@ -446,7 +450,7 @@ int build_families_gpu(int64_t n, const double2* d_x, const double* h_x, double 
   } else {
     cudaMallocAsync(&out->col, (size_t)(out->nnz > 0 ? out->nnz : 1) * sizeof(int32_t), s);
     if (n > 0)
-      k_family<true><<<nb, kBlock, 0, s>>>(n, d_x, G, cell_start, items, cutoff, n_cracks, nullptr, out->row_ptr,
+      k_family<true><<<nb, kBlock, 0, s>>>(n, d_x, G, cell_start, items, cutoff, cr, nullptr, out->row_ptr,
                                            out->col, counters);
   }
   cudaFreeAsync(cell_of, s);

@@ -3,8 +3,9 @@
 Requests (plate size, crack, material, load, step count) arrive over time.
 A request is admitted when its estimated HBM footprint fits under the budget
 and a batch slot is free; its plate is then built on the GPU (families by
-the cell list), kept resident, and joins the running pd_batch, so its steps
-overlap with everyone else's.  The loop advances all active requests
+the cell list, spatial layout) on a builder thread while the GPU steps the
+batch, kept resident, and joins the running pd_batch, so its steps overlap
+with everyone else's.  The loop advances all active requests
 together in chunks (never past any request's remaining step count), retires
 finished requests between chunks (reads their result, frees their memory)
 and admits waiting ones as memory and slots free up.  Host-side plate
@@ -161,30 +162,53 @@ class Server:
             batch.set_config(**self.batch_config)
         pending = deque(sorted(requests, key=lambda q: q.arrival))
         queue, active, used = deque(), {}, 0.0
-        pool = ThreadPoolExecutor(max_workers=self.workers)
-        futs = {}
+        pool = ThreadPoolExecutor(max_workers=self.workers)  # host plates
+        builders = ThreadPoolExecutor(max_workers=2)  # device contexts, built while the GPU steps the batch
+        futs, building, reserved = {}, {}, 0.0
         t0 = time.perf_counter()
         busy = 0.0
         bond_steps = 0
         done = 0
+
+        def build(q, plate_future):
+            p = plate_future.result()
+            return p, p.context(precision=self.precision, device=self.device)
+
+        def start_build(q, need):
+            nonlocal reserved
+            building[q.rid] = (builders.submit(build, q, futs.pop(q.rid)), need)
+            reserved += need
+
         while pending or queue or active:
             now = time.perf_counter() - t0
             while pending and pending[0].arrival <= now:
                 q = pending.popleft()
                 queue.append(q)
-                futs[q.rid] = pool.submit(q.plate)
-            # prefetch the next arrivals' plates too
+                if q.rid not in futs:
+                    futs[q.rid] = pool.submit(q.plate)
+            # prefetch the next arrivals' host plates too
             for q in list(pending)[: self.workers]:
                 if q.rid not in futs:
                     futs[q.rid] = pool.submit(q.plate)
+            # build the device contexts of arrived requests ahead of admission, in FIFO order,
+            # while their footprint fits next to the active and building ones
+            for q in list(queue)[: self.workers]:
+                if isinstance(q, _Parked) or q.rid in building:
+                    continue
+                need = footprint(q.particles, self.precision)
+                if used + reserved + need > self.budget_bytes or len(active) + len(building) >= self.max_plates:
+                    break
+                start_build(q, need)
             # admission: FIFO, by footprint and slots (preempting long requests if enabled)
             while queue and len(active) < self.max_plates:
                 q = queue[0]
                 need = footprint(q.particles, self.precision)
-                if used + need > self.budget_bytes and active and self.preempt and not isinstance(q, _Parked):
-                    used -= self._preempt_for(q, need, used, active, batch, queue)
-                if used + need > self.budget_bytes and active:
-                    break
+                if q.rid not in building:
+                    if used + reserved + need > self.budget_bytes and active and self.preempt and \
+                            not isinstance(q, _Parked):
+                        used -= self._preempt_for(q, need, used + reserved, active, batch, queue)
+                    if used + reserved + need > self.budget_bytes and (active or building):
+                        break
                 if isinstance(q, _Parked):
                     queue.popleft()
                     ctx = q.plate.context(precision=self.precision, device=self.device)
@@ -193,11 +217,15 @@ class Server:
                     used += need
                     active[q.rid] = [q.request, ctx, q.remaining, q.admitted, need, q.plate]
                     continue
-                if not futs[q.rid].done() and active:
-                    break  # keep the GPU busy; admit when its plate is ready
-                p = futs.pop(q.rid).result()
+                if q.rid not in building:
+                    start_build(q, need)
+                fut, need = building[q.rid]
+                if not fut.done() and active:
+                    break  # keep the GPU busy; admit when its context is built
+                p, ctx = fut.result()
+                del building[q.rid]
+                reserved -= need
                 queue.popleft()
-                ctx = p.context(precision=self.precision, device=self.device)
                 batch.add(ctx)
                 used += need
                 active[q.rid] = [q, ctx, q.steps, time.perf_counter() - t0, need, p]
@@ -230,6 +258,9 @@ class Server:
                 break
         makespan = time.perf_counter() - t0
         pool.shutdown()
+        for fut, _ in building.values():  # stopped early: contexts built ahead of admission
+            fut.result()[1].close()
+        builders.shutdown()
         batch.close()
         lat = np.array([r.latency for r in self.results])
         wait = np.array([r.admitted - r.arrival for r in self.results])
