@@ -232,3 +232,25 @@ def test_gpu_scale_plate_200_cut_1000_steps_bit_exact(pdg, po):
         done = target
         _assert_same(ctx, sim)
     assert int((sim.mask == 0).sum()) > 0, "the crack is meant to run"
+
+
+def test_gpu_concurrent_family_builds_match_sequential(pdg):
+    """Contexts built on several threads at once, as the serving loop builds
+    them, get the families of a build on its own: each family build carries
+    its own crack segments."""
+    import math
+    from concurrent.futures import ThreadPoolExecutor
+    plates = [pdg.plates.make_plate(150, seed=s, crack=(0.0, 0.004 * (s - 3), 0.02 + 0.015 * s,
+                                                        math.radians(-30.0 + 12.0 * s))) for s in range(6)]
+    want = []
+    for p in plates:
+        c = p.context()
+        want.append(c.families())
+        c.close()
+    for _ in range(2):
+        with ThreadPoolExecutor(max_workers=6) as ex:
+            ctxs = list(ex.map(lambda p: p.context(), plates))
+        for c, (rp, col) in zip(ctxs, want):
+            grp, gcol = c.families()
+            assert np.array_equal(grp, rp) and np.array_equal(gcol, col)
+            c.close()
