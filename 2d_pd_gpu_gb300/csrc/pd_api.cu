@@ -80,6 +80,7 @@ struct pd_batch {
   int32_t device = 0, precision = PD_FP64;
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;  // around the last pd_batch_step's GPU work
   std::string err;
   std::vector<pd_ctx*> members;
   pd::BatchLaunch cfg;
@@ -1523,6 +1524,8 @@ int pd_batch_create(int32_t device, int32_t precision, pd_batch** out) {
   cudaError_t e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreate(&b->t0);
+  if (e == cudaSuccess) e = cudaEventCreate(&b->t1);
   if (e == cudaSuccess) e = cudaMalloc(&b->d_bar, sizeof(pd::GridBarrier));
   if (e == cudaSuccess) e = cudaMemsetAsync(b->d_bar, 0, sizeof(pd::GridBarrier), b->stream);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->nsm, cudaDevAttrMultiProcessorCount, device);
@@ -1545,6 +1548,8 @@ int pd_batch_destroy(pd_batch* b) {
   if (b->d_tiles) cudaFree(b->d_tiles);
   if (b->d_bar) cudaFree(b->d_bar);
   if (b->done) cudaEventDestroy(b->done);
+  if (b->t0) cudaEventDestroy(b->t0);
+  if (b->t1) cudaEventDestroy(b->t1);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
   return PD_OK;
@@ -1631,6 +1636,7 @@ int pd_batch_step(pd_batch* b, int32_t nsteps) {
     PD_BCK(b, cudaEventRecord(b->done, c->stream));
     PD_BCK(b, cudaStreamWaitEvent(b->stream, b->done, 0));
   }
+  PD_BCK(b, cudaEventRecord(b->t0, b->stream));
   if (b->cfg.persistent && b->direct) {
     PD_BCK(b, batch_enqueue(b, nsteps));
   } else {
@@ -1658,11 +1664,21 @@ int pd_batch_step(pd_batch* b, int32_t nsteps) {
     }
     if (!(b->cfg.persistent && b->direct)) PD_BCK(b, cudaGraphLaunch(it->second, b->stream));
   }
+  PD_BCK(b, cudaEventRecord(b->t1, b->stream));
   PD_BCK(b, cudaEventRecord(b->done, b->stream));
   for (pd_ctx* c : b->members) {
     PD_BCK(b, cudaStreamWaitEvent(c->stream, b->done, 0));
     c->steps += nsteps;
   }
+  return PD_OK;
+}
+
+int pd_batch_last_step_ms(pd_batch* b, float* ms) {
+  if (!b || !ms) return PD_ERR_ARG;
+  *ms = 0.f;
+  PD_BCK(b, cudaSetDevice(b->device));
+  PD_BCK(b, cudaEventSynchronize(b->t1));
+  PD_BCK(b, cudaEventElapsedTime(ms, b->t0, b->t1));
   return PD_OK;
 }
 

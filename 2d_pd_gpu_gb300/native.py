@@ -135,6 +135,7 @@ _SIGS = {
     "pd_batch_step": [_vp, ctypes.c_int32],
     "pd_batch_synchronize": [_vp],
     "pd_batch_step_timed": [_vp, ctypes.c_int32, ctypes.POINTER(ctypes.c_float)],
+    "pd_batch_last_step_ms": [_vp, ctypes.POINTER(ctypes.c_float)],
     "pd_probe_fma_rates": [ctypes.c_int32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
     "pd_host_alloc": [ctypes.c_int64, ctypes.POINTER(_vp)],
     "pd_host_free": [_vp],
@@ -443,6 +444,12 @@ class Batch:
     def step_timed(self, nsteps):
         ms = ctypes.c_float(0.0)
         self._ck(lib().pd_batch_step_timed(self._h, int(nsteps), ctypes.byref(ms)))
+        return ms.value
+
+    def last_step_ms(self):
+        """GPU time of the last step() call's kernels."""
+        ms = ctypes.c_float(0.0)
+        self._ck(lib().pd_batch_last_step_ms(self._h, ctypes.byref(ms)))
         return ms.value
 
     def close(self):

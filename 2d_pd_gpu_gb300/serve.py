@@ -7,9 +7,10 @@ the cell list, spatial layout) on a builder thread while the GPU steps the
 batch, kept resident, and joins the running pd_batch, so its steps overlap
 with everyone else's.  The loop advances all active requests
 together in chunks (never past any request's remaining step count), retires
-finished requests between chunks (reads their result, frees their memory)
-and admits waiting ones as memory and slots free up.  Host-side plate
-generation runs on worker threads ahead of admission.
+finished requests from the batch between chunks and reads their results
+(and frees their memory) while the next chunk runs, and admits waiting ones
+as memory and slots free up.  Host-side plate generation runs on worker
+threads ahead of admission.
 
 Because every plate's arithmetic is independent of the batch it runs in, a
 request's result is the same alone and in the mix (bit for bit, FP64 and
@@ -179,6 +180,20 @@ class Server:
             building[q.rid] = (builders.submit(build, q, futs.pop(q.rid)), need)
             reserved += need
 
+        # finished requests whose results are read (and memory freed) while the next chunk runs
+        retired = []
+
+        def finish():
+            nonlocal used
+            for q, ctx, admitted, fin, need in retired:
+                dig, broken = state_digest(ctx)
+                kept = (ctx.state()[0], ctx.bond_mask()) if q.rid in self.keep else None
+                self.results.append(Result(q.rid, q.arrival, admitted, fin, q.particles, ctx.nnz, q.steps, dig,
+                                           broken, kept))
+                ctx.close()
+                used -= need
+            retired.clear()
+
         while pending or queue or active:
             now = time.perf_counter() - t0
             while pending and pending[0].arrival <= now:
@@ -230,32 +245,28 @@ class Server:
                 used += need
                 active[q.rid] = [q, ctx, q.steps, time.perf_counter() - t0, need, p]
             if not active:
+                finish()
                 if pending:
                     time.sleep(max(0.0, min(0.01, pending[0].arrival - (time.perf_counter() - t0))))
                 continue
             k = min(self.chunk, min(a[2] for a in active.values()))
-            ts = time.perf_counter()
             batch.step(k)
+            finish()  # the previous chunk's finished requests, while this chunk runs
             batch.synchronize()
-            busy += time.perf_counter() - ts
+            busy += batch.last_step_ms() / 1e3
             fin = time.perf_counter() - t0
             for rid in list(active):
                 a = active[rid]
                 a[2] -= k
                 bond_steps += a[1].nnz * k
                 if a[2] == 0:
-                    q, ctx = a[0], a[1]
-                    batch.remove(ctx)
-                    dig, broken = state_digest(ctx)
-                    kept = (ctx.state()[0], ctx.bond_mask()) if q.rid in self.keep else None
-                    self.results.append(Result(q.rid, q.arrival, a[3], fin, q.particles, ctx.nnz, q.steps, dig, broken,
-                                               kept))
-                    ctx.close()
-                    used -= a[4]
+                    batch.remove(a[1])
+                    retired.append((a[0], a[1], a[3], fin, a[4]))
                     del active[rid]
                     done += 1
             if stop_after and done >= stop_after:
                 break
+        finish()
         makespan = time.perf_counter() - t0
         pool.shutdown()
         for fut, _ in building.values():  # stopped early: contexts built ahead of admission

@@ -289,6 +289,9 @@ int pd_batch_get_config(const pd_batch* b, pd_batch_config* cfg);
 int pd_batch_step(pd_batch* b, int32_t nsteps);
 int pd_batch_synchronize(pd_batch* b);
 int pd_batch_step_timed(pd_batch* b, int32_t nsteps, float* ms);
+/* GPU time of the last pd_batch_step call's kernels (CUDA events on the
+ * batch stream, from its first kernel to its last; waits for them). */
+int pd_batch_last_step_ms(pd_batch* b, float* ms);
 
 /* Page-locked host buffers for pd_set_state / pd_get_state /
  * pd_compute_velocity (full-bandwidth host<->device copies).  No reference
