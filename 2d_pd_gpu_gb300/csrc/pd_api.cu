@@ -60,7 +60,7 @@ struct pd_ctx {
   // pd_step_host's copy / compute pipeline (streams and events, see plan_slabs)
   cudaStream_t io[3] = {nullptr, nullptr, nullptr};
   std::vector<cudaEvent_t> slab_ev;
-  int64_t slab = 0;                 // particles per slab (a multiple of 32); 0: not planned
+  std::vector<int64_t> slab_bnd;    // slab k = particles slab_bnd[k] .. slab_bnd[k+1]; empty: not planned
   std::vector<int32_t> slab_need;   // slab k's pass A needs slabs 0 .. slab_need[k] imported
   // Mazars damage history (pd_mazars_*)
   double *mz_thr = nullptr, *mz_bd = nullptr, *mz_status = nullptr;
@@ -176,7 +176,7 @@ void free_families(pd_ctx* c) {
   dfree(c->tb);
   dfree(c->rslot);
   c->sell = pd::SellLayout{};
-  c->slab = 0;
+  c->slab_bnd.clear();
   c->slab_need.clear();
   c->nnz = 0;
   c->has_families = false;
@@ -1173,7 +1173,8 @@ int pd_checkpoint_load(pd_ctx* c, const void* buf, int64_t bytes) {
 
 
 // pd_step_host pipeline (FP64 form).  The particles are cut into kSlabs index
-// ranges (multiples of 32); slab_need[k] = the last slab holding slab k's
+// ranges (multiples of 32; the first two small, so the first pass A starts
+// early, the rest even); slab_need[k] = the last slab holding slab k's
 // particles or any of their neighbours.  Streams (io[0], io[1] at high
 // priority): io[1] copies u, v, f in slab by slab (host-to-device copies
 // share one path, ~200 GB/s, so slab order is what matters), io[0] runs each
@@ -1185,7 +1186,7 @@ constexpr int kSlabs = 8;
 enum { kEvImport = 0, kEvCopy = kSlabs, kEvStart = 2 * kSlabs, kEvJoin = 2 * kSlabs + 1, kEvCount = 2 * kSlabs + 2 };
 
 static int plan_slabs(pd_ctx* c) {
-  if (c->slab > 0) return PD_OK;
+  if (!c->slab_bnd.empty()) return PD_OK;
   if (!c->io[0]) {
     int lo = 0, hi = 0;
     PD_CK(c, cudaDeviceGetStreamPriorityRange(&lo, &hi));
@@ -1197,32 +1198,44 @@ static int plan_slabs(pd_ctx* c) {
     PD_CK(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     c->slab_ev.push_back(e);
   }
-  const int64_t slab = ((c->n + kSlabs - 1) / kSlabs + 31) / 32 * 32;
+  // the largest neighbour id of every 32-particle chunk
+  const int64_t nch = (c->n + 31) / 32;
+  std::vector<int32_t> h((size_t)nch, 0);
   int32_t* reach = nullptr;
-  PD_CK(c, cudaMalloc(&reach, kSlabs * sizeof(int32_t)));
-  std::vector<int32_t> h(kSlabs, 0);
-  cudaError_t e = cudaMemsetAsync(reach, 0, kSlabs * sizeof(int32_t), c->stream);
+  PD_CK(c, cudaMalloc(&reach, h.size() * sizeof(int32_t)));
+  cudaError_t e = cudaMemsetAsync(reach, 0, h.size() * sizeof(int32_t), c->stream);
   if (e == cudaSuccess) {
-    pd::launch_slab_reach(c->n, c->row_ptr, c->col, slab, reach, c->stream);
+    pd::launch_slab_reach(c->n, c->row_ptr, c->col, 32, reach, c->stream);
     e = cudaGetLastError();
   }
-  if (e == cudaSuccess) e = copy_sync(h.data(), reach, kSlabs * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = copy_sync(h.data(), reach, h.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
   cudaFree(reach);
   PD_CK(c, e);
+  // slab boundaries in chunks: two leading slabs of nch / 32 chunks, then even slabs
+  std::vector<int64_t> bc(kSlabs + 1);
+  const int64_t lead = std::max<int64_t>(1, nch / 32);
+  bc[0] = 0;
+  bc[1] = std::min(nch, lead);
+  bc[2] = std::min(nch, 2 * lead);
+  for (int k = 3; k <= kSlabs; ++k) bc[k] = bc[2] + (nch - bc[2]) * (k - 2) / (kSlabs - 2);
+  c->slab_bnd.assign(kSlabs + 1, 0);
+  for (int k = 0; k <= kSlabs; ++k) c->slab_bnd[k] = std::min<int64_t>(c->n, bc[k] * 32);
   c->slab_need.assign(kSlabs, 0);
   for (int k = 0; k < kSlabs; ++k) {
-    const int64_t last = std::min<int64_t>(kSlabs - 1, (int64_t)h[k] / slab);
-    c->slab_need[k] = (int32_t)std::max<int64_t>(k, last);
+    int64_t far = -1;
+    for (int64_t q = bc[k]; q < bc[k + 1]; ++q) far = std::max<int64_t>(far, h[(size_t)q]);
+    int need = k;
+    while (need + 1 < kSlabs && far >= c->slab_bnd[need + 1]) ++need;
+    c->slab_need[k] = need;
   }
-  c->slab = slab;
   return PD_OK;
 }
 
 // Fp64Args restricted to slab k.
 static Fp64Args slab_args(const pd_ctx* c, const Fp64Args& a, int k) {
   Fp64Args r = a;
-  r.i0 = std::min<int64_t>(c->n, k * c->slab);
-  r.n = std::min<int64_t>(c->n, (k + 1) * c->slab);
+  r.i0 = c->slab_bnd[k];
+  r.n = c->slab_bnd[k + 1];
   return r;
 }
 
@@ -1240,8 +1253,11 @@ static cudaError_t enqueue_host_step(pd_ctx* c, int32_t nsteps, const double* u_
   const size_t b16 = sizeof(double2);
   ck(cudaEventRecord(ev[kEvStart], s));
   for (int q = 0; q < 3; ++q) ck(cudaStreamWaitEvent(io[q], ev[kEvStart], 0));
-  for (int k = 0; k < kSlabs; ++k) {  // import
-    const Fp64Args a = slab_args(c, plain, k);
+  // enqueued in dependency order (each pass A right after the import it waits for), so the
+  // first pass A is submitted before the host has issued the later imports
+  int next_a = 0;
+  for (int k = 0; k < kSlabs; ++k) {
+    const Fp64Args a = slab_args(c, plain, k);  // import slab k
     const size_t off = (size_t)a.i0, cnt = (size_t)(a.n - a.i0);
     if (cnt > 0) {
       ck(cudaMemcpyAsync(c->u + off, u_in + 2 * off, cnt * b16, cudaMemcpyHostToDevice, io[1]));
@@ -1252,11 +1268,11 @@ static cudaError_t enqueue_host_step(pd_ctx* c, int32_t nsteps, const double* u_
     ck(cudaStreamWaitEvent(io[0], ev[kEvCopy + k], 0));
     pd::launch_drift_fp64(a, io[0]);  // in place, on the device copy
     ck(cudaEventRecord(ev[kEvImport + k], io[0]));
-  }
-  for (int k = 0; k < kSlabs; ++k) {  // pass A of slab k once its neighbours are in
-    cudaStream_t sk = k % 2 ? io[2] : s;
-    ck(cudaStreamWaitEvent(sk, ev[kEvImport + c->slab_need[k]], 0));
-    pd::launch_pass_a_fp64(slab_args(c, plain, k), brk, sk);
+    for (; next_a < kSlabs && c->slab_need[next_a] <= k; ++next_a) {  // pass A of slabs whose neighbours are in
+      cudaStream_t sj = next_a % 2 ? io[2] : s;
+      ck(cudaStreamWaitEvent(sj, ev[kEvImport + c->slab_need[next_a]], 0));
+      pd::launch_pass_a_fp64(slab_args(c, plain, next_a), brk, sj);
+    }
   }
   ck(cudaEventRecord(ev[kEvJoin], io[2]));
   ck(cudaStreamWaitEvent(s, ev[kEvJoin], 0));
