@@ -206,9 +206,13 @@ class Server:
                 if q.rid not in futs:
                     futs[q.rid] = pool.submit(q.plate)
             # build the device contexts of arrived requests ahead of admission, in FIFO order,
-            # while their footprint fits next to the active and building ones
+            # while their footprint fits next to the active and building ones.  The requests
+            # being built stay a prefix of the queue (a parked request, restored at its
+            # admission, stops the scan), so their reserved memory never blocks the head.
             for q in list(queue)[: self.workers]:
-                if isinstance(q, _Parked) or q.rid in building:
+                if isinstance(q, _Parked):
+                    break
+                if q.rid in building:
                     continue
                 need = footprint(q.particles, self.precision)
                 if used + reserved + need > self.budget_bytes or len(active) + len(building) >= self.max_plates:
@@ -221,8 +225,15 @@ class Server:
                 if q.rid not in building:
                     if used + reserved + need > self.budget_bytes and active and self.preempt and \
                             not isinstance(q, _Parked):
-                        used -= self._preempt_for(q, need, used + reserved, active, batch, queue)
-                    if used + reserved + need > self.budget_bytes and (active or building):
+                        freed, parked = self._preempt_for(q, need, used + reserved, active, batch)
+                        used -= freed
+                        at = 1  # behind the head and the requests already being built
+                        while at < len(queue) and not isinstance(queue[at], _Parked) and queue[at].rid in building:
+                            at += 1
+                        for pk in reversed(parked):
+                            queue.insert(at, pk)
+                    # (a retired request still holds its memory until its results are read)
+                    if used + reserved + need > self.budget_bytes and (active or building or retired):
                         break
                 if isinstance(q, _Parked):
                     queue.popleft()
@@ -289,10 +300,10 @@ class Server:
             "preemptions": self.preemptions,
         }
 
-    def _preempt_for(self, q, need, used, active, batch, queue):
+    def _preempt_for(self, q, need, used, active, batch):
         """Checkpoints and frees active requests (largest remaining work first,
-        each with >= preempt_ratio x q's work) until q fits; they are queued
-        right behind q.  Returns the bytes freed."""
+        each with >= preempt_ratio x q's work) until q fits.  Returns the bytes
+        freed and the parked requests (the caller queues them behind q)."""
         work_q = q.steps * q.particles
         victims = sorted(active.items(), key=lambda kv: -kv[1][2] * kv[1][0].particles)
         freed, parked = 0.0, []
@@ -308,9 +319,7 @@ class Server:
             freed += a[4]
             del active[rid]
             self.preemptions += 1
-        for pk in reversed(parked):
-            queue.insert(1, pk)
-        return freed
+        return freed, parked
 
 
 def solo_digest(request, precision, device=0):
