@@ -2,8 +2,9 @@
 //
 // The reference positions are binned into square cells of side
 // q = sqrt(bbox area / n) (about one particle per cell; a lattice's cells are
-// its sites).  Cells are grouped in tiles of 32 cells x 8 rows:
-//   SELL positions  tile by tile (tiles row-major, bands of 8 rows), cells
+// its sites).  Cells are grouped in tiles of 32 cells x kTileRows rows
+// (kTileRows = kHaloBlock / 32, one visiting block of the mixed passes):
+//   SELL positions  tile by tile (tiles row-major, bands of kTileRows rows), cells
 //                   row-major inside a tile, equal cells by particle id; every
 //                   tile starts a new chunk, the tail of its last chunk is a
 //                   hole (member -1).  A chunk (32 positions) is then a row
@@ -31,6 +32,8 @@ namespace pd {
 namespace {
 
 constexpr int kTileSortCap = 2048;
+constexpr int64_t kTileRows = kHaloBlock / 32;
+static_assert(kHaloBlock % 32 == 0 && kHaloBlock <= 1024, "a visiting block is whole warps");
 
 struct CellGrid {
   double x0, y0, inv_q;
@@ -49,9 +52,9 @@ __global__ void k_spatial_keys(int64_t n, const double2* __restrict__ x, CellGri
   if (i >= n) return;
   const double2 p = x[i];
   const int64_t cx = cell_of(p.x, G.x0, G.inv_q, G.gx), cy = cell_of(p.y, G.y0, G.inv_q, G.gy);
-  const int64_t t = (cy >> 3) * G.tiles_x + (cx >> 5);
+  const int64_t t = (cy / kTileRows) * G.tiles_x + (cx >> 5);
   tile_of[i] = (int32_t)t;
-  local[i] = (uint16_t)((cy & 7) * 32 + (cx & 31));
+  local[i] = (uint16_t)((cy % kTileRows) * 32 + (cx & 31));
   rk[i] = ((uint64_t)(cy * G.gx + cx) << 31) | (uint64_t)i;
   atomicAdd(&tile_cnt[t], 1);
 }
@@ -120,7 +123,6 @@ cudaError_t alloc(T** p, size_t count, cudaStream_t s) {
 
 int build_spatial_order(int64_t n, const double2* d_x, const double* h_x, cudaStream_t s, SellLayout* L,
                         int32_t** d_blocks, int64_t* nblocks, std::string* msg) {
-  static_assert(kHaloBlock == 32 * 8, "a visiting block is one 32 x 8 tile");
   constexpr int kWarps = kHaloBlock / 32;
   *d_blocks = nullptr;
   *nblocks = 0;
@@ -147,7 +149,7 @@ int build_spatial_order(int64_t n, const double2* d_x, const double* h_x, cudaSt
   G.gx = std::min<int64_t>(cap, cell_of(std::isfinite(x1) ? x1 : 0.0, G.x0, G.inv_q, cap) + 1);
   G.gy = std::min<int64_t>(cap, cell_of(std::isfinite(y1) ? y1 : 0.0, G.y0, G.inv_q, cap) + 1);
   G.tiles_x = (G.gx + 31) / 32;
-  const int64_t ntiles = G.tiles_x * ((G.gy + 7) / 8);
+  const int64_t ntiles = G.tiles_x * ((G.gy + kTileRows - 1) / kTileRows);
   int32_t *tile_of = nullptr, *tile_cnt = nullptr, *cursor = nullptr, *bucket = nullptr;
   uint16_t* local = nullptr;
   int64_t *tile_start = nullptr, *tile_pos = nullptr;
