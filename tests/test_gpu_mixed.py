@@ -109,6 +109,33 @@ def test_mixed_shuffled_numbering_matches(pdg):
     assert np.array_equal(b.damage(), r.damage()[perm])
 
 
+def test_mixed_on_the_reference_mesh(pdg, hassa):
+    """The reference's own mesh (its Hassa test mesh: 4,064 particles,
+    irregular spacing) under the reference main's loading: every visiting
+    block of the spatial layout stages its halo, and the mixed form agrees
+    with the FP64 form within the mixed-form bar after 100 steps."""
+    n = hassa["x"].shape[0]
+    dx, hor, E, nu, rho, dt = hassa["params"]
+    g = np.zeros(n, np.uint8)
+    g[hassa["top"]] = 1
+    g[hassa["bottom"]] = 2
+    ctxs = []
+    for prec in (pdg.native.PD_FP64, pdg.native.PD_MIXED):
+        c = pdg.native.Context(pdg.default_params(E=E, nu=nu, rho=rho, dt=dt, s_c=0.0, precision=prec))
+        c.set_particles(hassa["x"], hassa["vol"])
+        c.build_families(1.01 * dx * hor)
+        c.set_bc([pdg.native.PD_BC_VELOCITY, pdg.native.PD_BC_FIXED], [[0.0, 5.0], [0.0, 0.0]], g)
+        ctxs.append(c)
+    a, b = ctxs
+    assert np.array_equal(a.families()[1], b.families()[1])
+    assert b.counters()["unstaged_blocks"] == 0
+    for c in ctxs:
+        c.step(100)
+    e = _errors(a, b)
+    print("reference mesh, mixed vs fp64:", e)
+    assert e["u_max"] < DISP_TOL
+
+
 def test_mixed_dense_cluster_unstaged_blocks(pdg):
     """A 120 x 120 plate with scrambled numbering and two lone particles 10 m
     apart: the layout's cells follow the bounding box, so each holds thousands
