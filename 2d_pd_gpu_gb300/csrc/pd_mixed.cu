@@ -709,10 +709,20 @@ __device__ __forceinline__ bool batch_phase_mixed(const MixedArgs* __restrict__ 
                                                   unsigned char* sm, uint64_t* bars) {
   const int phase = PHASE < 0 ? phase_rt : PHASE;
   bool ok = true;
+  // the tile's plate arguments, copied to shared memory once per tile (the block code
+  // reads them field by field; 2 % on the 256-plate batch)
+  __shared__ __align__(16) MixedArgs sp;
+  static_assert(sizeof(MixedArgs) % 8 == 0, "MixedArgs copies as int2");
   for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
     const BatchTile T = tiles[t];
-    const MixedArgs& p = plates[T.plate];
     __syncthreads();  // the previous tile's shared memory is no longer read
+    {
+      const int2* src = reinterpret_cast<const int2*>(plates + T.plate);
+      int2* dst = reinterpret_cast<int2*>(&sp);
+      for (int q = threadIdx.x; q < (int)(sizeof(MixedArgs) / 8); q += blockDim.x) dst[q] = src[q];
+    }
+    __syncthreads();
+    const MixedArgs& p = sp;
     if (phase == 0)
       drift_block(p, T.first);
     else if (phase == 1)  // the breaking pass also serves plates without breaking (their s2 is +inf)
