@@ -65,7 +65,7 @@ def _stale(target, deps):
 def build(verbose=False, force=False):
     os.makedirs(OUT, exist_ok=True)
     nv = nvcc()
-    headers = [os.path.join(CSRC, h) for h in ("pd_internal.h", "pd_walk.cuh", "pd_batch.cuh")] + \
+    headers = [os.path.join(CSRC, h) for h in ("pd_internal.h", "pd_walk.cuh", "pd_batch.cuh", "pd_stage.cuh")] + \
         [os.path.join(INCLUDE, "pd_gb300.h")]
     objs, jobs = [], []
     for src, extra in CUDA_UNITS:
