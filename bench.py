@@ -156,8 +156,8 @@ def byte_model(precision, n, nb):
 # and profiles/passes_mixed_plate600.txt), scaled to a launch by its bonds:
 # traffic grows with the bonds (and the particles, in the same proportion on
 # these plates).
-DRAM_BYTES_PER_BOND = {"fp64": {"pass_a": 265.60e6 / 10031592, "pass_b": 245.28e6 / 10031592},
-                       "mixed": {"pass_a": 43.32e6 / 10031592, "pass_b": 55.46e6 / 10031592}}
+DRAM_BYTES_PER_BOND = {"fp64": {"pass_a": 265.71e6 / 10031592, "pass_b": 245.49e6 / 10031592},
+                       "mixed": {"pass_a": 43.31e6 / 10031592, "pass_b": 55.54e6 / 10031592}}
 
 
 def fp64_ops(n, nb):
