@@ -405,11 +405,44 @@ __device__ __forceinline__ bool warp_stage_done(const MixedArgs& a, uint64_t* ba
   return true;
 }
 
+// Programmatic dependent launch: a pass launched with programmatic stream
+// serialization starts while the previous pass drains; grid_dep_sync() waits
+// until that pass has completed and its writes are visible, then lets the next
+// pass launch.  Without the launch attribute both instructions return at once.
+__device__ __forceinline__ void grid_dep_sync() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// The halo ids H[k0 + q kHaloBlock + t], q < kHaloBatch, that thread t
+// fetches (-1 past hn), and the calls f(k, id) for them: every thread loads
+// kHaloBatch ids before it issues their copies, so the id loads overlap.
+__device__ __forceinline__ void halo_ids(const int32_t* H, int hn, int k0, int (&g)[kHaloBatch]) {
+#pragma unroll
+  for (int q = 0; q < kHaloBatch; ++q) {
+    const int k = k0 + q * kHaloBlock + threadIdx.x;
+    g[q] = k < hn ? H[k] : -1;
+  }
+}
+
+template <typename F>
+__device__ __forceinline__ void for_halo(const int32_t* H, int hn, int (&g)[kHaloBatch], F f) {
+  for (int k0 = 0;;) {  // g holds the ids of the first batch
+#pragma unroll
+    for (int q = 0; q < kHaloBatch; ++q)
+      if (g[q] >= 0) f(k0 + q * kHaloBlock + threadIdx.x, g[q]);
+    k0 += kHaloBatch * kHaloBlock;
+    if (k0 >= hn) break;
+    halo_ids(H, hn, k0, g);
+  }
+}
+
 // Pass A of visiting block blk (kHaloBlock / 32 chunks) of plate a.  Every
 // thread of the kHaloBlock-thread block calls it; sm = the pass's dynamic
-// shared memory.  False if
-// a staged copy timed out.
-template <bool BREAK>
+// shared memory.  False if a staged copy timed out.  PDL: the pass may start
+// before the previous one has finished; until grid_dep_sync() it reads only
+// the visit record and the first halo ids, which no step writes.
+template <bool BREAK, bool PDL = false>
 __device__ __forceinline__ bool pass_a_block(const MixedArgs& a, int64_t blk, unsigned char* sm, uint64_t* bars) {
   int64_t chunk = 0, base = 0;
   int w = 0, nlive = 0;
@@ -418,6 +451,11 @@ __device__ __forceinline__ bool pass_a_block(const MixedArgs& a, int64_t blk, un
   const int hn = a.halo_n ? a.halo_n[blk] : -1;
   const int64_t p = chunk * 32 + lane;  // SELL position
   const bool live = has && lane < nlive;
+  int g[kHaloBatch];
+  if (PDL) {
+    if (hn >= 0) halo_ids(a.halo + blk * a.halo_cap, hn, 0, g);
+    grid_dep_sync();
+  }
   PreA pre{};
   if (live) pre = load_a(a, p);  // in flight during the staging below
   if (hn < 0) {  // int32 indices staged per warp, neighbour data from L1/L2
@@ -432,22 +470,12 @@ __device__ __forceinline__ bool pass_a_block(const MixedArgs& a, int64_t blk, un
   const HaloSmem h = halo_smem(a, sm);
   halo_begin(a, h, bars, has, w, base);
   const int32_t* H = a.halo + blk * a.halo_cap;
-  for (int k0 = 0; k0 < hn; k0 += kHaloBatch * kHaloBlock) {
-    int g[kHaloBatch];
-#pragma unroll
-    for (int q = 0; q < kHaloBatch; ++q) {
-      const int k = k0 + q * kHaloBlock + threadIdx.x;
-      g[q] = k < hn ? H[k] : -1;
-    }
-#pragma unroll
-    for (int q = 0; q < kHaloBatch; ++q)
-      if (g[q] >= 0) {
-        const int k = k0 + q * kHaloBlock + threadIdx.x;
-        cp_async16(&h.q0[k], &a.us[g[q]]);
-        cp_async16(&h.q1[k], &a.xs[g[q]]);
-        cp_async4(&h.vh[k], &a.vh[g[q]]);
-      }
-  }
+  if (!PDL) halo_ids(H, hn, 0, g);
+  for_halo(H, hn, g, [&](int k, int j) {
+    cp_async16(&h.q0[k], &a.us[j]);
+    cp_async16(&h.q1[k], &a.xs[j]);
+    cp_async4(&h.vh[k], &a.vh[j]);
+  });
   cp_async_wait_all();
   __syncthreads();
   if (!has) return true;
@@ -462,7 +490,8 @@ __device__ __forceinline__ bool pass_a_block(const MixedArgs& a, int64_t blk, un
 }
 
 // Pass B (+ the next drift when DRIFT) of visiting block blk of plate a.
-template <bool DRIFT>
+// PDL: as for pass A.
+template <bool DRIFT, bool PDL = false>
 __device__ __forceinline__ bool pass_b_block(const MixedArgs& a, int64_t blk, unsigned char* sm, uint64_t* bars) {
   int64_t chunk = 0, base = 0;
   int w = 0, nlive = 0;
@@ -471,6 +500,11 @@ __device__ __forceinline__ bool pass_b_block(const MixedArgs& a, int64_t blk, un
   const int hn = a.halo_n ? a.halo_n[blk] : -1;
   const int64_t p = chunk * 32 + lane;  // SELL position
   const bool live = has && lane < nlive;
+  int g[kHaloBatch];
+  if (PDL) {
+    if (hn >= 0) halo_ids(a.halo + blk * a.halo_cap, hn, 0, g);
+    grid_dep_sync();
+  }
   PreB pre{};
   if (live) pre = load_b<DRIFT>(a, p);  // in flight during the staging below
   if (hn < 0) {
@@ -486,21 +520,11 @@ __device__ __forceinline__ bool pass_b_block(const MixedArgs& a, int64_t blk, un
   const HaloSmem h = halo_smem(a, sm);
   halo_begin(a, h, bars, has, w, base);
   const int32_t* H = a.halo + blk * a.halo_cap;
-  for (int k0 = 0; k0 < hn; k0 += kHaloBatch * kHaloBlock) {
-    int g[kHaloBatch];
-#pragma unroll
-    for (int q = 0; q < kHaloBatch; ++q) {
-      const int k = k0 + q * kHaloBlock + threadIdx.x;
-      g[q] = k < hn ? H[k] : -1;
-    }
-#pragma unroll
-    for (int q = 0; q < kHaloBatch; ++q)
-      if (g[q] >= 0) {
-        const int k = k0 + q * kHaloBlock + threadIdx.x;
-        cp_async16(&h.q0[k], &a.xs[g[q]]);
-        cp_async16(&h.q1[k], &a.ws[g[q]]);
-      }
-  }
+  if (!PDL) halo_ids(H, hn, 0, g);
+  for_halo(H, hn, g, [&](int k, int j) {
+    cp_async16(&h.q0[k], &a.xs[j]);
+    cp_async16(&h.q1[k], &a.ws[j]);
+  });
   BcOf bc{};
   if (DRIFT && live) bc = resolve_bc(a, pre.g);
   cp_async_wait_all();
@@ -528,14 +552,14 @@ template <bool BREAK>
 __global__ void __launch_bounds__(kHaloBlock, 1024 / kHaloBlock) k_pass_a_mixed(MixedArgs a) {  // <= 64 registers
   extern __shared__ __align__(128) unsigned char sm[];
   __shared__ uint64_t bars[kHaloBlock / 32];
-  pass_a_block<BREAK>(a, blockIdx.x, sm, bars);
+  pass_a_block<BREAK, true>(a, blockIdx.x, sm, bars);
 }
 
 template <bool DRIFT>
 __global__ void __launch_bounds__(kHaloBlock, 1024 / kHaloBlock) k_pass_b_mixed(MixedArgs a) {  // <= 64 registers
   extern __shared__ __align__(128) unsigned char sm[];
   __shared__ uint64_t bars[kHaloBlock / 32];
-  pass_b_block<DRIFT>(a, blockIdx.x, sm, bars);
+  pass_b_block<DRIFT, true>(a, blockIdx.x, sm, bars);
 }
 
 // Dynamic shared memory of the single-plate passes: the larger of the int32
@@ -702,7 +726,10 @@ __global__ void k_halo_relink(MixedArgs a, const uint16_t* __restrict__ loc0, co
 // drift, 3 pass B.  A mixed tile is one visiting block of one plate (tile.first
 // = the block index, tile.count = 256 particles at most), run by the same
 // block code as the single-plate passes, so every plate's result is the one it
-// gets alone.  False if a staged copy timed out.
+// gets alone.  False if a staged copy timed out.  The phase kernels of the
+// passes (PHASE > 0) are launched with programmatic stream serialization: the
+// tile records and plate arguments they read first are written before the
+// step's launches.
 template <int PHASE>  // PHASE < 0: the phase is the runtime argument
 __device__ __forceinline__ bool batch_phase_mixed(const MixedArgs* __restrict__ plates,
                                                   const BatchTile* __restrict__ tiles, int ntiles, int phase_rt,
@@ -726,11 +753,11 @@ __device__ __forceinline__ bool batch_phase_mixed(const MixedArgs* __restrict__ 
     if (phase == 0)
       drift_block(p, T.first);
     else if (phase == 1)  // the breaking pass also serves plates without breaking (their s2 is +inf)
-      ok = pass_a_block<true>(p, T.first, sm, bars);
+      ok = pass_a_block<true, (PHASE > 0)>(p, T.first, sm, bars);
     else if (phase == 2)
-      ok = pass_b_block<true>(p, T.first, sm, bars);
+      ok = pass_b_block<true, (PHASE > 0)>(p, T.first, sm, bars);
     else
-      ok = pass_b_block<false>(p, T.first, sm, bars);
+      ok = pass_b_block<false, (PHASE > 0)>(p, T.first, sm, bars);
     ok = __syncthreads_and(ok);
   }
   return ok;
@@ -860,12 +887,21 @@ cudaError_t launch_batch_mixed(const MixedArgs* d_plates, const BatchTile* d_til
   if (!cfg.persistent) {
     const unsigned g = (unsigned)ntiles;
     k_batch_phase_mixed<0><<<g, kHaloBlock, 0, s>>>(d_plates, d_tiles, ntiles);
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3(g);
+    lc.blockDim = dim3(kHaloBlock);
+    lc.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    lc.attrs = at;
+    lc.numAttrs = 1;
     for (int k = 0; k < nsteps; ++k) {
-      k_batch_phase_mixed<1><<<g, kHaloBlock, smem_a, s>>>(d_plates, d_tiles, ntiles);
-      if (k + 1 < nsteps)
-        k_batch_phase_mixed<2><<<g, kHaloBlock, smem_b, s>>>(d_plates, d_tiles, ntiles);
-      else
-        k_batch_phase_mixed<3><<<g, kHaloBlock, smem_b, s>>>(d_plates, d_tiles, ntiles);
+      lc.dynamicSmemBytes = smem_a;
+      cudaLaunchKernelEx(&lc, k_batch_phase_mixed<1>, d_plates, d_tiles, ntiles);
+      lc.dynamicSmemBytes = smem_b;
+      cudaLaunchKernelEx(&lc, k + 1 < nsteps ? k_batch_phase_mixed<2> : k_batch_phase_mixed<3>, d_plates, d_tiles,
+                         ntiles);
     }
     return cudaGetLastError();
   }
@@ -910,22 +946,31 @@ void launch_drift_mixed(const MixedArgs& a, cudaStream_t s) {
   if (a.n > 0) k_drift_mixed<<<(unsigned)blocks_for(a.npos), kBlock, 0, s>>>(a);
 }
 
+// The single-plate passes are launched with programmatic stream
+// serialization: a pass's blocks may start (and fetch what no step writes)
+// while the previous kernel on the stream drains.
+static void launch_pass_pdl(void (*kernel)(MixedArgs), const MixedArgs& a, size_t sm, cudaStream_t s) {
+  cudaLaunchConfig_t lc = {};
+  lc.gridDim = dim3((unsigned)a.nblocks);
+  lc.blockDim = dim3(kHaloBlock);
+  lc.dynamicSmemBytes = sm;
+  lc.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  lc.attrs = at;
+  lc.numAttrs = 1;
+  cudaLaunchKernelEx(&lc, kernel, a);
+}
+
 void launch_pass_a_mixed(const MixedArgs& a, bool breaking, cudaStream_t s) {
   if (a.n <= 0) return;
-  const size_t sm = pass_smem_bytes(a, true);
-  if (breaking)
-    k_pass_a_mixed<true><<<(unsigned)a.nblocks, kHaloBlock, sm, s>>>(a);
-  else
-    k_pass_a_mixed<false><<<(unsigned)a.nblocks, kHaloBlock, sm, s>>>(a);
+  launch_pass_pdl(breaking ? k_pass_a_mixed<true> : k_pass_a_mixed<false>, a, pass_smem_bytes(a, true), s);
 }
 
 void launch_pass_b_mixed(const MixedArgs& a, bool drift, cudaStream_t s) {
   if (a.n <= 0) return;
-  const size_t sm = pass_smem_bytes(a, false);
-  if (drift)
-    k_pass_b_mixed<true><<<(unsigned)a.nblocks, kHaloBlock, sm, s>>>(a);
-  else
-    k_pass_b_mixed<false><<<(unsigned)a.nblocks, kHaloBlock, sm, s>>>(a);
+  launch_pass_pdl(drift ? k_pass_b_mixed<true> : k_pass_b_mixed<false>, a, pass_smem_bytes(a, false), s);
 }
 
 void launch_to_mixed(const MixedArgs& a, const double2* u, const double2* v, const double2* f, cudaStream_t s) {
