@@ -157,7 +157,7 @@ def byte_model(precision, n, nb):
 # traffic grows with the bonds (and the particles, in the same proportion on
 # these plates).
 DRAM_BYTES_PER_BOND = {"fp64": {"pass_a": 265.71e6 / 10031592, "pass_b": 245.49e6 / 10031592},
-                       "mixed": {"pass_a": 43.31e6 / 10031592, "pass_b": 55.54e6 / 10031592}}
+                       "mixed": {"pass_a": 43.24e6 / 10031592, "pass_b": 55.43e6 / 10031592}}
 
 
 def fp64_ops(n, nb):
