@@ -850,7 +850,7 @@ struct Launcher {
     else if (bond_assoc(c))
       pd::launch_ba_pass_a(f, ba_args(c), s);
     else
-      pd::launch_pass_a_fp64(f, brk, s);
+      pd::launch_pass_a_fp64(f, brk, s, true);
   }
   void pass_b(bool next_drift, cudaStream_t s) {
     if (mixed(c))
@@ -858,7 +858,7 @@ struct Launcher {
     else if (bond_assoc(c))
       pd::launch_ba_pass_b(f, ba_args(c), next_drift ? 1 : 0, s);
     else
-      pd::launch_pass_b_fp64(f, next_drift ? 1 : 0, s);
+      pd::launch_pass_b_fp64(f, next_drift ? 1 : 0, s, true);
   }
 };
 

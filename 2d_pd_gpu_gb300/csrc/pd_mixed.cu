@@ -405,15 +405,6 @@ __device__ __forceinline__ bool warp_stage_done(const MixedArgs& a, uint64_t* ba
   return true;
 }
 
-// Programmatic dependent launch: a pass launched with programmatic stream
-// serialization starts while the previous pass drains; grid_dep_sync() waits
-// until that pass has completed and its writes are visible, then lets the next
-// pass launch.  Without the launch attribute both instructions return at once.
-__device__ __forceinline__ void grid_dep_sync() {
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
-
 // The halo ids H[k0 + q kHaloBlock + t], q < kHaloBatch, that thread t
 // fetches (-1 past hn), and the calls f(k, id) for them: every thread loads
 // kHaloBatch ids before it issues their copies, so the id loads overlap.

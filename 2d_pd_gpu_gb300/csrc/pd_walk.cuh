@@ -19,6 +19,15 @@
 
 namespace pd {
 
+// Programmatic dependent launch: a pass launched with programmatic stream
+// serialization starts while the previous pass drains; grid_dep_sync() waits
+// until that pass has completed and its writes are visible, then lets the next
+// pass launch.  Without the launch attribute both instructions return at once.
+__device__ __forceinline__ void grid_dep_sync() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 template <int U, typename Idx, typename Gather, typename Body>
 __device__ __forceinline__ void walk_bonds(int w, int64_t self, Idx idx, Gather gather, Body body) {
   using G = decltype(gather(0));
