@@ -1,7 +1,8 @@
 """Autotuner for batched stepping (pd_batch launch shape).
 
 Chooses, by measurement on this GPU, the launch mode (one persistent
-cooperative kernel, or a graph of phase kernels), threads per block,
+cooperative kernel, a graph of phase kernels, or every plate's own
+single-plate kernels on one stream per plate), threads per block,
 particles per work tile, and persistent blocks per SM.  Mixed-form batches
 always run 256-thread blocks over the plates' visiting blocks (the
 shared-memory halo code of the single-plate passes), so for them only the
@@ -31,9 +32,11 @@ CANDIDATES = (
     [dict(persistent=1, block=b, tile=t, blocks_per_sm=s) for b in (128, 256) for t in (256, 1024, 4096)
      for s in (1, 2, 4)]
     + [dict(persistent=0, block=b, tile=t, blocks_per_sm=1) for b in (128, 256) for t in (256, 1024)]
+    + [dict(persistent=2, block=256, tile=256, blocks_per_sm=1)]
 )
 MIXED_CANDIDATES = ([dict(persistent=1, block=256, tile=256, blocks_per_sm=s) for s in (1, 2, 3, 4)]
-                    + [dict(persistent=0, block=256, tile=256, blocks_per_sm=1)])
+                    + [dict(persistent=0, block=256, tile=256, blocks_per_sm=1)]
+                    + [dict(persistent=2, block=256, tile=256, blocks_per_sm=1)])
 
 
 def candidates_for(precision):

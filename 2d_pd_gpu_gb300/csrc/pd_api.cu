@@ -81,6 +81,7 @@ struct pd_batch {
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
   cudaEvent_t t0 = nullptr, t1 = nullptr;  // around the last pd_batch_step's GPU work
+  cudaEvent_t join = nullptr;               // persistent == 2: a member's chain ends
   std::string err;
   std::vector<pd_ctx*> members;
   pd::BatchLaunch cfg;
@@ -1522,6 +1523,90 @@ cudaError_t batch_enqueue(pd_batch* b, int32_t nsteps) {
                                b->d_bar, b->nsm, b->stream);
 }
 
+// persistent == 2: every member steps with its own single-plate kernels (arguments in
+// parameter space, programmatic launches between its passes) on its own stream, forked from
+// and joined back to the batch stream.  m steps; first: the call's opening drift; last: the
+// call's closing pass B (no drift after it).  Each member gets exactly the launch sequence of
+// pd_step.
+cudaError_t enqueue_plates(pd_batch* b, int32_t m, bool first, bool last) {
+  cudaError_t e = cudaEventRecord(b->done, b->stream);
+  for (pd_ctx* c : b->members) {
+    if (e != cudaSuccess) break;
+    if (c->n == 0) continue;
+    e = cudaStreamWaitEvent(c->stream, b->done, 0);
+    if (e != cudaSuccess) break;
+    Launcher L(c);
+    if (first) L.drift(c->stream);
+    for (int32_t k = 0; k < m; ++k) {
+      L.pass_a(c->stream);
+      L.pass_b(!(last && k + 1 == m), c->stream);
+    }
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaEventRecord(b->join, c->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->join, 0);
+  }
+  return e;
+}
+
+// Steps of at most this many are captured in one per-member graph; the plates meet only where
+// one graph launch ends and the next begins.
+constexpr int32_t kPlateChunk = 10;
+
+// The graph of nsteps steps of the persistent kernel (persistent == 1) or the phase kernels
+// (0), captured on first use.  A runtime that refuses to capture the cooperative launch
+// leaves b->direct set and no graph: the kernel is then launched directly.
+int batch_graph(pd_batch* b, int32_t nsteps) {
+  if ((b->cfg.persistent && b->direct) || b->graphs.count(nsteps)) return PD_OK;
+  cudaGraph_t g;
+  PD_BCK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  const cudaError_t le = batch_enqueue(b, nsteps);
+  const cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+  if (le != cudaSuccess || ce != cudaSuccess) {
+    if (ce == cudaSuccess) cudaGraphDestroy(g);
+    cudaGetLastError();
+    if (!b->cfg.persistent)
+      return bfail(b, PD_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(le != cudaSuccess ? le : ce));
+    b->direct = true;
+    return PD_OK;
+  }
+  cudaGraphExec_t ge;
+  const cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
+  cudaGraphDestroy(g);
+  if (ie != cudaSuccess) return bfail(b, PD_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(ie));
+  if (b->graphs.size() > 16) clear_batch_graphs(b);
+  b->graphs.emplace(nsteps, ge);
+  return PD_OK;
+}
+
+// Captures (launch = false) or launches the graphs of nsteps per-member steps.
+int batch_step_plates(pd_batch* b, int32_t nsteps, bool launch) {
+  for (int32_t k0 = 0; k0 < nsteps; k0 += kPlateChunk) {
+    const int32_t m = std::min(kPlateChunk, nsteps - k0);
+    const bool first = k0 == 0, last = k0 + m == nsteps;
+    const int32_t key = -1 - (4 * m + (first ? 2 : 0) + (last ? 1 : 0));  // apart from the nsteps keys
+    auto it = b->graphs.find(key);
+    if (it == b->graphs.end()) {
+      if (b->graphs.size() > 16) clear_batch_graphs(b);
+      cudaGraph_t g;
+      PD_BCK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+      const cudaError_t le = enqueue_plates(b, m, first, last);
+      const cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+      if (le != cudaSuccess || ce != cudaSuccess) {
+        if (ce == cudaSuccess) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return bfail(b, PD_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(le != cudaSuccess ? le : ce));
+      }
+      cudaGraphExec_t ge;
+      const cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
+      cudaGraphDestroy(g);
+      if (ie != cudaSuccess) return bfail(b, PD_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(ie));
+      it = b->graphs.emplace(key, ge).first;
+    }
+    if (launch) PD_BCK(b, cudaGraphLaunch(it->second, b->stream));
+  }
+  return PD_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1545,6 +1630,7 @@ int pd_batch_create(int32_t device, int32_t precision, pd_batch** out) {
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreate(&b->t0);
   if (e == cudaSuccess) e = cudaEventCreate(&b->t1);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMalloc(&b->d_bar, sizeof(pd::GridBarrier));
   if (e == cudaSuccess) e = cudaMemsetAsync(b->d_bar, 0, sizeof(pd::GridBarrier), b->stream);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->nsm, cudaDevAttrMultiProcessorCount, device);
@@ -1569,6 +1655,7 @@ int pd_batch_destroy(pd_batch* b) {
   if (b->done) cudaEventDestroy(b->done);
   if (b->t0) cudaEventDestroy(b->t0);
   if (b->t1) cudaEventDestroy(b->t1);
+  if (b->join) cudaEventDestroy(b->join);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
   return PD_OK;
@@ -1621,7 +1708,7 @@ int pd_batch_info(const pd_batch* b, int32_t* nplates, int64_t* particles, int64
 int pd_batch_set_config(pd_batch* b, const pd_batch_config* cfg) {
   if (!b || !cfg) return PD_ERR_ARG;
   if (cfg->block < 32 || cfg->block > 256 || cfg->block % 32 || cfg->tile < 32 || cfg->tile % 32 ||
-      cfg->blocks_per_sm < 1 || (cfg->persistent != 0 && cfg->persistent != 1))
+      cfg->blocks_per_sm < 1 || cfg->persistent < 0 || cfg->persistent > 2)
     return bfail(b, PD_ERR_ARG, "invalid batch configuration");
   PD_BCK(b, cudaSetDevice(b->device));
   PD_BCK(b, cudaStreamSynchronize(b->stream));
@@ -1655,33 +1742,18 @@ int pd_batch_step(pd_batch* b, int32_t nsteps) {
     PD_BCK(b, cudaEventRecord(b->done, c->stream));
     PD_BCK(b, cudaStreamWaitEvent(b->stream, b->done, 0));
   }
+  // graphs first (host work), so that t0 .. t1 is the GPU's
+  rc = b->cfg.persistent == 2 ? batch_step_plates(b, nsteps, false) : batch_graph(b, nsteps);
+  if (rc != PD_OK) return rc;
   PD_BCK(b, cudaEventRecord(b->t0, b->stream));
-  if (b->cfg.persistent && b->direct) {
-    PD_BCK(b, batch_enqueue(b, nsteps));
+  if (b->cfg.persistent == 2) {
+    rc = batch_step_plates(b, nsteps, true);
+    if (rc != PD_OK) return rc;
   } else {
-    auto it = b->graphs.find(nsteps);
-    if (it == b->graphs.end()) {
-      cudaGraph_t g;
-      PD_BCK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-      cudaError_t le = batch_enqueue(b, nsteps);
-      cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
-      if (le != cudaSuccess || ce != cudaSuccess) {
-        if (ce == cudaSuccess) cudaGraphDestroy(g);
-        cudaGetLastError();
-        if (!b->cfg.persistent)
-          return bfail(b, PD_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(le != cudaSuccess ? le : ce));
-        b->direct = true;  // this runtime does not capture cooperative launches: launch directly
-        PD_BCK(b, batch_enqueue(b, nsteps));
-      } else {
-        cudaGraphExec_t ge;
-        cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
-        cudaGraphDestroy(g);
-        if (ie != cudaSuccess) return bfail(b, PD_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(ie));
-        if (b->graphs.size() > 16) clear_batch_graphs(b);
-        it = b->graphs.emplace(nsteps, ge).first;
-      }
-    }
-    if (!(b->cfg.persistent && b->direct)) PD_BCK(b, cudaGraphLaunch(it->second, b->stream));
+    if (b->cfg.persistent && b->direct)
+      PD_BCK(b, batch_enqueue(b, nsteps));
+    else
+      PD_BCK(b, cudaGraphLaunch(b->graphs.at(nsteps), b->stream));
   }
   PD_BCK(b, cudaEventRecord(b->t1, b->stream));
   PD_BCK(b, cudaEventRecord(b->done, b->stream));
@@ -1722,6 +1794,10 @@ int pd_batch_step_timed(pd_batch* b, int32_t nsteps, float* ms) {
   for (pd_ctx* c : b->members) {
     PD_BCK(b, cudaEventRecord(b->done, c->stream));
     PD_BCK(b, cudaStreamWaitEvent(b->stream, b->done, 0));
+  }
+  if (nsteps > 0 && !b->members.empty()) {  // graphs captured before the clock starts
+    rc = b->cfg.persistent == 2 ? batch_step_plates(b, nsteps, false) : batch_graph(b, nsteps);
+    if (rc != PD_OK) return rc;
   }
   PD_BCK(b, cudaEventRecord(e0, b->stream));
   rc = pd_batch_step(b, nsteps);

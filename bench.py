@@ -319,7 +319,8 @@ def run_batch(args, pdg, device):
                      "steps": args.batch_steps, "setup_s": setup, "config": best,
                      "candidates_ms": {k: round(v, 4) for k, v in sorted(timings.items(), key=lambda kv: kv[1])[:6]},
                      "achieved_gbs_step_model": ach, "frac_hbm": ach / peaks["hbm_gbs"],
-                     "gpu_launches": 1 if best["persistent"] else 1 + 2 * args.batch_steps}
+                     "gpu_launches": {0: 1 + 2 * args.batch_steps, 1: 1,
+                                      2: info["plates"] * (1 + 2 * args.batch_steps)}[best["persistent"]]}
         b.close()
         for c in ctxs:
             c.close()

@@ -31,7 +31,8 @@ def _solo(pdg, plates, precision, steps):
 @pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("cfg", [dict(persistent=1, block=256, tile=1024, blocks_per_sm=2),
                                  dict(persistent=1, block=128, tile=256, blocks_per_sm=1),
-                                 dict(persistent=0, block=256, tile=512, blocks_per_sm=1)])
+                                 dict(persistent=0, block=256, tile=512, blocks_per_sm=1),
+                                 dict(persistent=2, block=256, tile=256, blocks_per_sm=1)])
 def test_batch_equals_solo(pdg, precision, cfg):
     plates = _plates(pdg)
     steps = 23
