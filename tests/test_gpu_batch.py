@@ -57,12 +57,15 @@ def test_batch_equals_solo(pdg, precision, cfg):
     assert broke > 0
 
 
-def test_batch_membership_changes(pdg):
+@pytest.mark.parametrize("mode", [None, 2])  # the default launch mode; per-member kernels
+def test_batch_membership_changes(pdg, mode):
     """Continuous batching: members join and leave between steps; everyone's
     trajectory is still its solo trajectory."""
     plates = _plates(pdg)
     solo = _solo(pdg, plates, 0, 20)
     b = pdg.Batch(precision=0)
+    if mode is not None:
+        b.set_config(persistent=mode)
     ctxs = [p.context() for p in plates]
     b.add(ctxs[0])
     b.add(ctxs[1])
