@@ -81,7 +81,7 @@ struct pd_batch {
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
   cudaEvent_t t0 = nullptr, t1 = nullptr;  // around the last pd_batch_step's GPU work
-  cudaEvent_t join = nullptr;               // persistent == 2: a member's chain ends
+  cudaEvent_t join = nullptr;               // persistent == 2: a member's step graph ends
   std::string err;
   std::vector<pd_ctx*> members;
   pd::BatchLaunch cfg;
@@ -881,6 +881,29 @@ int check_after_step(pd_ctx* c) {
   return PD_OK;
 }
 
+// The graph of nsteps steps of c (enqueue_steps' launches), captured on c's stream on first use.
+int step_graph(pd_ctx* c, int32_t nsteps, cudaGraphExec_t* out) {
+  auto it = c->graphs.find(nsteps);
+  if (it == c->graphs.end()) {
+    cudaGraph_t g;
+    PD_CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_steps(c, nsteps, c->stream);
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (e != cudaSuccess) return cuda_fail(c, e, "graph capture");
+    cudaGraphExec_t ge;
+    e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(c, e, "graph instantiate");
+    if (c->graphs.size() > 16) {  // a bound on the cache (the arguments are not stale)
+      for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+      c->graphs.clear();
+    }
+    it = c->graphs.emplace(nsteps, ge).first;
+  }
+  *out = it->second;
+  return PD_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -894,21 +917,10 @@ int pd_step(pd_ctx* c, int32_t nsteps) {
     return PD_OK;
   }
   PD_CK(c, cudaSetDevice(c->p.device));
-  auto it = c->graphs.find(nsteps);
-  if (it == c->graphs.end()) {
-    cudaGraph_t g;
-    PD_CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    enqueue_steps(c, nsteps, c->stream);
-    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
-    if (e != cudaSuccess) return cuda_fail(c, e, "graph capture");
-    cudaGraphExec_t ge;
-    e = cudaGraphInstantiate(&ge, g, 0);
-    cudaGraphDestroy(g);
-    if (e != cudaSuccess) return cuda_fail(c, e, "graph instantiate");
-    if (c->graphs.size() > 16) clear_graphs(c);
-    it = c->graphs.emplace(nsteps, ge).first;
-  }
-  PD_CK(c, cudaGraphLaunch(it->second, c->stream));
+  cudaGraphExec_t ge = nullptr;
+  const int rc = step_graph(c, nsteps, &ge);
+  if (rc != PD_OK) return rc;
+  PD_CK(c, cudaGraphLaunch(ge, c->stream));
   c->steps += nsteps;
   return check_after_step(c);
 }
@@ -1523,35 +1535,6 @@ cudaError_t batch_enqueue(pd_batch* b, int32_t nsteps) {
                                b->d_bar, b->nsm, b->stream);
 }
 
-// persistent == 2: every member steps with its own single-plate kernels (arguments in
-// parameter space, programmatic launches between its passes) on its own stream, forked from
-// and joined back to the batch stream.  m steps; first: the call's opening drift; last: the
-// call's closing pass B (no drift after it).  Each member gets exactly the launch sequence of
-// pd_step.
-cudaError_t enqueue_plates(pd_batch* b, int32_t m, bool first, bool last) {
-  cudaError_t e = cudaEventRecord(b->done, b->stream);
-  for (pd_ctx* c : b->members) {
-    if (e != cudaSuccess) break;
-    if (c->n == 0) continue;
-    e = cudaStreamWaitEvent(c->stream, b->done, 0);
-    if (e != cudaSuccess) break;
-    Launcher L(c);
-    if (first) L.drift(c->stream);
-    for (int32_t k = 0; k < m; ++k) {
-      L.pass_a(c->stream);
-      L.pass_b(!(last && k + 1 == m), c->stream);
-    }
-    e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaEventRecord(b->join, c->stream);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->join, 0);
-  }
-  return e;
-}
-
-// Steps of at most this many are captured in one per-member graph; the plates meet only where
-// one graph launch ends and the next begins.
-constexpr int32_t kPlateChunk = 10;
-
 // The graph of nsteps steps of the persistent kernel (persistent == 1) or the phase kernels
 // (0), captured on first use.  A runtime that refuses to capture the cooperative launch
 // leaves b->direct set and no graph: the kernel is then launched directly.
@@ -1578,31 +1561,25 @@ int batch_graph(pd_batch* b, int32_t nsteps) {
   return PD_OK;
 }
 
-// Captures (launch = false) or launches the graphs of nsteps per-member steps.
-int batch_step_plates(pd_batch* b, int32_t nsteps, bool launch) {
-  for (int32_t k0 = 0; k0 < nsteps; k0 += kPlateChunk) {
-    const int32_t m = std::min(kPlateChunk, nsteps - k0);
-    const bool first = k0 == 0, last = k0 + m == nsteps;
-    const int32_t key = -1 - (4 * m + (first ? 2 : 0) + (last ? 1 : 0));  // apart from the nsteps keys
-    auto it = b->graphs.find(key);
-    if (it == b->graphs.end()) {
-      if (b->graphs.size() > 16) clear_batch_graphs(b);
-      cudaGraph_t g;
-      PD_BCK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-      const cudaError_t le = enqueue_plates(b, m, first, last);
-      const cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
-      if (le != cudaSuccess || ce != cudaSuccess) {
-        if (ce == cudaSuccess) cudaGraphDestroy(g);
-        cudaGetLastError();
-        return bfail(b, PD_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(le != cudaSuccess ? le : ce));
-      }
-      cudaGraphExec_t ge;
-      const cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
-      cudaGraphDestroy(g);
-      if (ie != cudaSuccess) return bfail(b, PD_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(ie));
-      it = b->graphs.emplace(key, ge).first;
-    }
-    if (launch) PD_BCK(b, cudaGraphLaunch(it->second, b->stream));
+// persistent == 2: every member runs its own step graph (pd_step's: the single-plate kernels,
+// arguments in parameter space, programmatic launches between its passes) on its own stream,
+// forked from and joined back to the batch stream, so the plates meet only at the call's end.
+// launch = false captures the members' graphs only.
+int batch_step_members(pd_batch* b, int32_t nsteps, bool launch) {
+  std::vector<cudaGraphExec_t> ge(b->members.size(), nullptr);
+  for (size_t k = 0; k < b->members.size(); ++k) {
+    pd_ctx* c = b->members[k];
+    if (c->n > 0 && step_graph(c, nsteps, &ge[k]) != PD_OK) return bfail(b, PD_ERR_CUDA, c->err);
+  }
+  if (!launch) return PD_OK;
+  PD_BCK(b, cudaEventRecord(b->done, b->stream));
+  for (size_t k = 0; k < b->members.size(); ++k) {
+    if (!ge[k]) continue;
+    cudaStream_t cs = b->members[k]->stream;
+    PD_BCK(b, cudaStreamWaitEvent(cs, b->done, 0));
+    PD_BCK(b, cudaGraphLaunch(ge[k], cs));
+    PD_BCK(b, cudaEventRecord(b->join, cs));
+    PD_BCK(b, cudaStreamWaitEvent(b->stream, b->join, 0));
   }
   return PD_OK;
 }
@@ -1743,11 +1720,11 @@ int pd_batch_step(pd_batch* b, int32_t nsteps) {
     PD_BCK(b, cudaStreamWaitEvent(b->stream, b->done, 0));
   }
   // graphs first (host work), so that t0 .. t1 is the GPU's
-  rc = b->cfg.persistent == 2 ? batch_step_plates(b, nsteps, false) : batch_graph(b, nsteps);
+  rc = b->cfg.persistent == 2 ? batch_step_members(b, nsteps, false) : batch_graph(b, nsteps);
   if (rc != PD_OK) return rc;
   PD_BCK(b, cudaEventRecord(b->t0, b->stream));
   if (b->cfg.persistent == 2) {
-    rc = batch_step_plates(b, nsteps, true);
+    rc = batch_step_members(b, nsteps, true);
     if (rc != PD_OK) return rc;
   } else {
     if (b->cfg.persistent && b->direct)
@@ -1796,7 +1773,7 @@ int pd_batch_step_timed(pd_batch* b, int32_t nsteps, float* ms) {
     PD_BCK(b, cudaStreamWaitEvent(b->stream, b->done, 0));
   }
   if (nsteps > 0 && !b->members.empty()) {  // graphs captured before the clock starts
-    rc = b->cfg.persistent == 2 ? batch_step_plates(b, nsteps, false) : batch_graph(b, nsteps);
+    rc = b->cfg.persistent == 2 ? batch_step_members(b, nsteps, false) : batch_graph(b, nsteps);
     if (rc != PD_OK) return rc;
   }
   PD_BCK(b, cudaEventRecord(e0, b->stream));

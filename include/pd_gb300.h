@@ -275,8 +275,8 @@ typedef struct pd_batch_config {
   int32_t blocks_per_sm;  /* persistent grid = SMs x this (capped at occupancy) */
   int32_t persistent;     /* 1: one cooperative persistent kernel per call; 0: phase kernels
                              (the default for PD_MIXED batches, 1 for PD_FP64); 2: every
-                             member's own single-plate kernels, on one stream per member, in
-                             graphs of up to 10 steps (block, tile, blocks_per_sm unused) */
+                             member's own pd_step graph on its own stream, the members' graphs
+                             running concurrently (block, tile, blocks_per_sm unused) */
   int32_t tile;           /* particles per work item (multiple of 32) */
 } pd_batch_config;
 int pd_batch_create(int32_t device, int32_t precision, pd_batch** out);
