@@ -26,6 +26,7 @@ rank time.
 from __future__ import annotations
 
 import argparse
+import contextlib
 import importlib
 import json
 import os
@@ -50,8 +51,22 @@ def load_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
+# (start, end) of every timed region, perf_counter seconds: the clock record is taken over these
+TIMED_WINDOWS = []
+
+
+@contextlib.contextmanager
+def timed():
+    t0 = time.perf_counter()
+    try:
+        yield
+    finally:
+        TIMED_WINDOWS.append((t0, time.perf_counter()))
+
+
 class ClockSampler:
-    """nvidia-smi sampling of SM clock and throttle reasons during a region."""
+    """nvidia-smi sampling of SM clock and throttle reasons while the run goes on; the
+    record covers the samples taken inside timed regions (every sample if none fell in one)."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -76,7 +91,7 @@ class ClockSampler:
         for line in self.proc.stdout:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) >= 9:
-                self.rows.append(parts)
+                self.rows.append((time.perf_counter(), parts))
 
     def stop(self):
         if self.proc is None:
@@ -87,16 +102,19 @@ class ClockSampler:
         except Exception:
             self.proc.kill()
         self.t.join(timeout=2)
-        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        inside = [r for t, r in self.rows if any(a <= t <= b for a, b in TIMED_WINDOWS)]
+        rows = inside if inside else [r for _, r in self.rows]
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
         reasons = set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for r in self.rows:
+        for r in rows:
             for k, nm in enumerate(names):
                 if r[5 + k].lower().startswith("active"):
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(self.rows)}
+                "reasons": sorted(reasons), "samples": len(rows), "samples_whole_run": len(self.rows),
+                "over": "timed regions" if inside else "whole run"}
 
 
 def dist_env():
@@ -225,7 +243,8 @@ def measure(ctx, prec, args, comm, sampler=None):
     ctx.step(args.warmup)
     ctx.synchronize()
     comm.barrier()
-    ms = ctx.step_timed(args.steps)
+    with timed():
+        ms = ctx.step_timed(args.steps)
     comm.barrier()
     ms_max = comm.max(ms)
     value = comm.sum(nb * args.steps) / (ms_max / 1e3)
@@ -309,7 +328,8 @@ def run_batch(args, pdg, device):
             c.reset()
         b.step(args.warmup)
         b.synchronize()
-        ms = b.step_timed(args.batch_steps)
+        with timed():
+            ms = b.step_timed(args.batch_steps)
         val = info["bonds"] * args.batch_steps / (ms / 1e3)
         model = byte_model(name, info["particles"], info["bonds"])["step"]
         peaks, _ = load_peaks()
@@ -344,7 +364,8 @@ def run_serve(args, pdg, device, capacity, configs):
         sample = sorted(reqs, key=lambda q: q.particles * q.steps)[:3] if prec == nat.PD_MIXED else []
         srv = serve.Server(precision=prec, device=device, budget_bytes=150e9, chunk=args.serve_chunk,
                            batch_config=configs.get(name), keep={q.rid for q in sample})
-        m = srv.run(reqs)
+        with timed():
+            m = srv.run(reqs)
         m.update({"arrival_rate_per_s": rate, "offered_load": 0.8, "capacity_bond_updates_per_s": capacity[name],
                   "particles_range": [min(q.particles for q in reqs), max(q.particles for q in reqs)]})
         if sample:
