@@ -78,8 +78,7 @@ __device__ __forceinline__ bool grid_sync(GridBarrier* b, unsigned nblocks) {
 struct BatchLaunch {
   int block = 256;          // threads per block
   int blocks_per_sm = 2;    // persistent grid = SMs x this (<= occupancy)
-  int persistent = 1;       // 1: cooperative persistent kernel, 0: phase kernels
-  int particles_per_thread = 1;
+  int persistent = 1;       // 1: cooperative persistent kernel, 0: phase kernels, 2: per-member graphs
 };
 
 }  // namespace pd
