@@ -1599,9 +1599,9 @@ int pd_batch_create(int32_t device, int32_t precision, pd_batch** out) {
   if (!b) return PD_ERR_CAPACITY;
   b->device = device;
   b->precision = precision;
-  // mixed batches: one graph of phase kernels (2.0 ms per step on the 256-plate batch against
-  // 2.75 ms for the persistent kernel, whose registers and shared memory allow 2 blocks per SM)
-  if (precision == PD_MIXED) b->cfg.persistent = 0;
+  // every member's own step graph, concurrently (256-plate batch, ms per step: mixed 1.40 against
+  // 1.79 for the phase kernels and 1.89 for the persistent kernel; FP64 10.6 against 11.4 / 11.5)
+  b->cfg.persistent = 2;
   cudaError_t e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);

@@ -393,8 +393,9 @@ class Context:
 
 
 class Batch:
-    """Many contexts stepped together (pd_batch): one persistent kernel or one
-    graph of phase kernels advances every member; results equal solo runs."""
+    """Many contexts stepped together (pd_batch): every member's own step graph
+    on its own stream (the default), one persistent kernel, or one graph of
+    phase kernels advances every member; results equal solo runs."""
 
     def __init__(self, precision=PD_FP64, device=0):
         self._h = _vp()

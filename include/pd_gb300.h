@@ -273,10 +273,10 @@ typedef struct pd_batch pd_batch;
 typedef struct pd_batch_config {
   int32_t block;          /* threads per block (64..256) */
   int32_t blocks_per_sm;  /* persistent grid = SMs x this (capped at occupancy) */
-  int32_t persistent;     /* 1: one cooperative persistent kernel per call; 0: phase kernels
-                             (the default for PD_MIXED batches, 1 for PD_FP64); 2: every
-                             member's own pd_step graph on its own stream, the members' graphs
-                             running concurrently (block, tile, blocks_per_sm unused) */
+  int32_t persistent;     /* 1: one cooperative persistent kernel per call; 0: phase kernels;
+                             2 (the default): every member's own pd_step graph on its own
+                             stream, the members' graphs running concurrently (block, tile,
+                             blocks_per_sm unused) */
   int32_t tile;           /* particles per work item (multiple of 32) */
 } pd_batch_config;
 int pd_batch_create(int32_t device, int32_t precision, pd_batch** out);

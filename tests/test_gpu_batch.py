@@ -57,15 +57,14 @@ def test_batch_equals_solo(pdg, precision, cfg):
     assert broke > 0
 
 
-@pytest.mark.parametrize("mode", [None, 2])  # the default launch mode; per-member kernels
+@pytest.mark.parametrize("mode", [1, 2])  # the persistent kernel; per-member graphs (the default)
 def test_batch_membership_changes(pdg, mode):
     """Continuous batching: members join and leave between steps; everyone's
     trajectory is still its solo trajectory."""
     plates = _plates(pdg)
     solo = _solo(pdg, plates, 0, 20)
     b = pdg.Batch(precision=0)
-    if mode is not None:
-        b.set_config(persistent=mode)
+    b.set_config(persistent=mode)
     ctxs = [p.context() for p in plates]
     b.add(ctxs[0])
     b.add(ctxs[1])

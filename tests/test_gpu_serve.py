@@ -26,13 +26,13 @@ def test_footprint_admission_math(pdg):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("precision", [0, 1])
-@pytest.mark.parametrize("mode", [None, 2])  # the batch's default launch mode; per-member kernels
+@pytest.mark.parametrize("mode", [0, 2])  # phase kernels; per-member graphs (the default)
 def test_served_results_equal_solo(pdg, precision, mode):
     serve = __import__("importlib").import_module("2d_pd_gpu_gb300.serve")
     reqs = serve.make_requests(10, seed=7, lo=2e3, hi=6e4, steps_lo=20, steps_hi=120, rate=400.0)
     # a budget that forces some requests to wait for memory
     budget = 2.5 * max(serve.footprint(q.particles, precision) for q in reqs)
-    cfg = None if mode is None else dict(persistent=mode, block=256, tile=256, blocks_per_sm=1)
+    cfg = dict(persistent=mode, block=256, tile=256, blocks_per_sm=1)
     srv = serve.Server(precision=precision, budget_bytes=budget, max_plates=4, chunk=16, workers=2,
                        batch_config=cfg)
     m = srv.run(reqs)
