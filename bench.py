@@ -337,6 +337,8 @@ def run_batch(args, pdg, device):
         out[name] = {"value": val, "unit": "bond-updates/s", "ms_per_step": ms / args.batch_steps,
                      "plates": info["plates"], "particles": info["particles"], "bonds": info["bonds"],
                      "steps": args.batch_steps, "setup_s": setup, "config": best,
+                     "mode": {0: "graph of phase kernels", 1: "persistent cooperative kernel",
+                              2: "every plate's own step graph, concurrently"}[best["persistent"]],
                      "candidates_ms": {k: round(v, 4) for k, v in sorted(timings.items(), key=lambda kv: kv[1])[:6]},
                      "achieved_gbs_step_model": ach, "frac_hbm": ach / peaks["hbm_gbs"],
                      "gpu_launches": {0: 1 + 2 * args.batch_steps, 1: 1,
