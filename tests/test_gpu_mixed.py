@@ -41,6 +41,25 @@ def test_mixed_config1_100_steps(pdg):
     assert e["mask_mismatch"] == 0
 
 
+@pytest.mark.parametrize("nx,ny", [(160, 80), (70, 140)])
+def test_mixed_rectangular_plates(pdg, nx, ny):
+    """2:1 plates (the serving workload's other shape; tiles cut both edges) with an
+    angled pre-crack and breaking: the mixed form stays within the bar of FP64 with the
+    same broken-bond mask."""
+    mat = pdg.plates.Material()
+    mat.s_c = 2e-4  # bonds break within the run
+    p = pdg.plates.make_plate(nx, ny, seed=5, crack=(0.0, 0.0, 0.4 * min(nx, ny) * 1e-3, 0.35), material=mat,
+                              v_load=1.5)
+    a, b = _pair(pdg, p)
+    a.step(300)
+    b.step(300)
+    e = _errors(a, b)
+    print(f"mixed vs fp64, {nx}x{ny}, 300 steps:", e)
+    assert e["u_max"] < DISP_TOL
+    assert e["mask_mismatch"] == 0
+    assert int((a.bond_mask() == 0).sum()) > 0  # the run did break bonds
+
+
 def test_mixed_200_cut_to_1000_steps(pdg):
     """The 200 x 200 cut of the scale plate (same generator), errors at steps 100/500/1000."""
     p = pdg.plates.config_plate_scale(side=200, seed=0)
