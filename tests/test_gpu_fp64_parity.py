@@ -101,6 +101,22 @@ def test_gpu_fp64_bit_exact_vs_oracle(pdg, po, side, seed, s_c, steps):
         assert ctx.counters()["bonds_broken"] == int((sim.mask == 0).sum())
 
 
+@pytest.mark.parametrize("nx,ny", [(80, 40), (36, 72)])
+def test_gpu_fp64_rectangular_angled_crack_bit_exact(pdg, po, nx, ny):
+    """2:1 plates with an angled pre-crack off the centre (the serving workload's shapes)."""
+    mat = pdg.plates.Material()
+    mat.s_c = 2e-4
+    p = pdg.plates.make_plate(nx, ny, seed=9, crack=(0.004, -0.002, 0.4 * min(nx, ny) * 1e-3, -0.4), material=mat,
+                              v_load=1.5)
+    ctx = p.context()
+    sim = plate_oracle(po, p)
+    for chunk in (5, 45):
+        ctx.step(chunk)
+        sim.step(chunk)
+        _assert_same(ctx, sim)
+    assert sim.mask.min() == 0, "the case is meant to break bonds"
+
+
 def test_gpu_config1_plate_100_steps_bit_exact(pdg, po):
     """The CPU-runnable plate: 100x100, centred half-width crack, s_c = 5e-4, 100 steps."""
     p = pdg.plates.config_plate_100(seed=0)
