@@ -59,6 +59,40 @@ def test_tiny_and_partial_chunks_bit_exact(pdg, po, n):
         b.free()
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_batch_with_degenerate_members(pdg, precision, mode):
+    """A batch whose members include an empty problem, single particles and partial
+    chunks next to a cracked plate: every member equals its solo run in every launch mode."""
+    base = pdg.plates.make_plate(20, seed=6, crack="centre-half")
+    base.material.s_c = 2e-4
+    plates = [_subset(base, np.arange(n)) for n in (1, 2, 33, 257)] + [base]
+    steps = 12
+    solo = []
+    for p in plates:
+        c = p.context(precision=precision)
+        c.step(steps)
+        solo.append((*c.state(), c.bond_mask()))
+        c.close()
+    b = pdg.Batch(precision=precision)
+    b.set_config(persistent=mode)
+    empty = pdg.native.Context(pdg.default_params(precision=precision))
+    empty.set_particles(np.zeros((0, 2)), np.zeros(0))
+    empty.build_families(1.0)
+    b.add(empty)
+    ctxs = [p.context(precision=precision) for p in plates]
+    for c in ctxs:
+        b.add(c)
+    b.step(5)
+    b.step(steps - 5)
+    b.synchronize()
+    for c, ref in zip(ctxs, solo):
+        for g, r in zip((*c.state(), c.bond_mask()), ref):
+            assert np.array_equal(g, r)
+    assert empty.state()[0].shape == (0, 2)
+    b.close()
+
+
 def test_ragged_families_with_holes(pdg, po):
     """Two circular holes and a slot: families from 0 to 28 bonds, particles
     with no neighbours (singular), SELL chunks of very different widths."""
