@@ -227,14 +227,20 @@ def run_reference(args, comm):
     v = nb * args.steps / secs
     sample = f"{args.steps} full steps of the {args.side}x{args.side} FP64 plate ({nb} bonds), {nth} threads"
     print(json.dumps({
-        "impl": "reference", "metric": "bond-updates/s", "value": v, "unit": "bond-updates/s", "n_gpus": args.gpus,
+        "impl": "reference", "metric": "bond-updates/s", "value": v, "unit": "bond-updates/s", "n_gpus": comm.world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"plate{args.side}x{args.side}-fp64-crack-sc5e-4", "particles": plate.n, "bonds": nb,
-                   "precision": "fp64", "parallelism": "host threads"},
+        "config": workload_config(args, plate.n, nb),
+        "parallelism": f"{nth} host threads on rank 0 of {comm.world}",
         "cpu_baseline": {"value": v, "unit": "bond-updates/s", "cores": nth, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": "bond-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
+
+
+def workload_config(args, particles, bonds):
+    """The workload both arms measure (identical dicts in both JSON lines)."""
+    return {"workload": f"plate{args.side}x{args.side}-fp64-crack-sc5e-4", "particles": particles, "bonds": bonds,
+            "precision": "fp64", "l2": "inputs larger than L2 (~2 GB state vs 129 MB L2), no flush"}
 
 
 def measure(ctx, prec, args, comm, sampler=None):
@@ -404,9 +410,8 @@ def run_ours(args, comm):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded plate generator)",
-        "config": {"workload": f"plate{args.side}x{args.side}-fp64-crack-sc5e-4", "particles": n, "bonds": nb,
-                   "precision": "fp64", "parallelism": f"replicas x{comm.world}",
-                   "l2": "inputs larger than L2 (~2 GB state vs 129 MB L2)"},
+        "config": workload_config(args, n, nb),
+        "parallelism": f"replicas x{comm.world} (one independent plate per GPU)",
         "gpu_launches": 1 + 2 * args.steps,
         "roofline": roof,
         "kernels": kernels,
@@ -481,6 +486,20 @@ def run_ours(args, comm):
         print(json.dumps(result), flush=True)
 
 
+def relaunch(n):
+    """--gpus N without a launcher: start N ranks (one per GPU) under
+    torch.distributed.run on this node, rendezvous on 127.0.0.1; returns
+    the launcher's exit status."""
+    import socket
+
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr", "127.0.0.1", f"--master-port={port}", os.path.abspath(__file__)] + sys.argv[1:]
+    return subprocess.run(cmd).returncode
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -504,6 +523,11 @@ def main():
     ap.add_argument("--serve-chunk", type=int, default=50)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    launched = os.environ.get("WORLD_SIZE")
+    if launched is None and args.gpus > 1:
+        sys.exit(relaunch(args.gpus))
+    if int(launched or 1) != args.gpus:
+        sys.exit(f"bench.py: --gpus {args.gpus} but WORLD_SIZE={launched}: launch one rank per GPU")
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     comm = Comm()
     try:

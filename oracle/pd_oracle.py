@@ -227,6 +227,19 @@ def ref_available():
     return os.path.exists(REF_HARNESS)
 
 
+def reference_dir():
+    """The reference checkout: PD_REFERENCE_DIR, else the one oracle/_ref was
+    built from (recorded by oracle/Makefile), else None."""
+    d = os.environ.get("PD_REFERENCE_DIR")
+    if d:
+        return d
+    rec = os.path.join(HERE, "_ref", "REFERENCE_DIR")
+    if os.path.exists(rec):
+        d = open(rec).read().strip()
+        return d or None
+    return None
+
+
 def run_ref_mazars(mesh_dir, n1, n2, out):
     """The reference's computeDamageStatus on the Hassa mesh at two imposed
     displacement levels (oracle/ref_harness.cpp, mode `mazars`)."""
@@ -291,17 +304,23 @@ def read_ref_output(path, n_hint=None, hassa=False):
     return out
 
 
-def write_ref_input(path, x, vol, params, nsteps, dump_every=1, families=None, vbc=(), fixed=()):
-    """Write the plate-mode input of pd_ref_harness.  vbc: [(idx, (vx, vy))]."""
+def write_ref_input(path, x, vol, params, nsteps, dump_every=1, families=None, vbc=(), fixed=(), state=None):
+    """Write the plate-mode input of pd_ref_harness.  vbc: [(idx, (vx, vy))];
+    state: None (start at rest) or (u0, v0), the initial displacement and
+    velocity, [n][2] each (input format version 2)."""
     n = x.shape[0]
     with open(path, "wb") as fh:
         fh.write(b"PDRF")
-        fh.write(struct.pack("<iii", 1, n, 1 if families is not None else 0))
+        fh.write(struct.pack("<iii", 1 if state is None else 2, n, 1 if families is not None else 0))
         fh.write(struct.pack("<8d", params["dx"], params["horizon"], params.get("n1", 0.0), params.get("n2", 0.0),
                              params["E"], params["nu"], params["rho"], params["dt"]))
         fh.write(struct.pack("<ii", nsteps, dump_every))
         fh.write(np.ascontiguousarray(x, dtype="<f8").tobytes())
         fh.write(np.ascontiguousarray(vol, dtype="<f8").tobytes())
+        if state is not None:
+            fh.write(struct.pack("<i", 1))
+            fh.write(np.ascontiguousarray(state[0], dtype="<f8").tobytes())
+            fh.write(np.ascontiguousarray(state[1], dtype="<f8").tobytes())
         if families is not None:
             fh.write(np.ascontiguousarray(families[0], dtype="<i8").tobytes())
             fh.write(np.ascontiguousarray(families[1], dtype="<i4").tobytes())

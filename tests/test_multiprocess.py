@@ -70,3 +70,31 @@ def test_reference_arm_under_torchrun():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] == "port"
+
+
+def test_gpus_flag_starts_the_ranks_itself():
+    """`bench.py --gpus 2` with no launcher relaunches itself under
+    torch.distributed.run: two ranks join (n_gpus counts the ranks in the
+    process group), rank 0 alone prints; the config dict is the shared one."""
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--gpus", "2", "--side", "60", "--steps", "1",
+                        "--warmup", "3"], cwd=ROOT, capture_output=True, text=True, timeout=600,
+                       env={k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")})
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["n_gpus"] == 2 and "rank 0 of 2" in d["parallelism"]
+    sys.path.insert(0, ROOT)
+    import argparse
+
+    import bench
+
+    want = bench.workload_config(argparse.Namespace(side=60), d["config"]["particles"], d["config"]["bonds"])
+    assert d["config"] == want
+
+
+def test_gpus_flag_must_match_the_launcher():
+    env = dict(os.environ, WORLD_SIZE="1", RANK="0", LOCAL_RANK="0")
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--gpus", "2", "--side", "40"], cwd=ROOT,
+                       capture_output=True, text=True, timeout=120, env=env)
+    assert r.returncode != 0 and "WORLD_SIZE=1" in r.stderr

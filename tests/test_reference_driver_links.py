@@ -9,14 +9,16 @@ maintainer's machine has the real ones).
 import os
 import subprocess
 
+import pd_oracle
 import pytest
 
 from conftest import ROOT
 
-REF = os.environ.get("PD_REFERENCE_DIR", "/root/reference")
+REF = pd_oracle.reference_dir()  # PD_REFERENCE_DIR, or the checkout oracle/_ref was built from
 
 
-@pytest.mark.skipif(not os.path.exists(os.path.join(REF, "src", "main.cu")), reason="reference checkout absent")
+@pytest.mark.skipif(not REF or not os.path.exists(os.path.join(REF, "src", "main.cu")),
+                    reason="reference checkout absent (set PD_REFERENCE_DIR)")
 def test_reference_main_cu_links_against_dropin(pdg, tmp_path):
     libdir = os.path.dirname(pdg.native.LIB_PATH)
     exe = str(tmp_path / "ref_main_on_gb300")
