@@ -1682,6 +1682,17 @@ int pd_batch_info(const pd_batch* b, int32_t* nplates, int64_t* particles, int64
   return PD_OK;
 }
 
+int pd_batch_set_barrier_limits(pd_batch* b, uint64_t spin_limit, uint32_t hold_ns) {
+  if (!b) return PD_ERR_ARG;
+  if (hold_ns > pd::kBarrierHoldMaxNs) return bfail(b, PD_ERR_ARG, "hold_ns above 100 ms");
+  PD_BCK(b, cudaSetDevice(b->device));
+  PD_BCK(b, cudaStreamSynchronize(b->stream));
+  b->cfg.limits.spins = spin_limit;
+  b->cfg.limits.hold_ns = hold_ns;
+  clear_batch_graphs(b);  // the limits are launch arguments
+  return PD_OK;
+}
+
 int pd_batch_set_config(pd_batch* b, const pd_batch_config* cfg) {
   if (!b || !cfg) return PD_ERR_ARG;
   if (cfg->block < 32 || cfg->block > 256 || cfg->block % 32 || cfg->tile < 32 || cfg->tile % 32 ||

@@ -294,13 +294,13 @@ __device__ __forceinline__ void batch_phase(const Fp64Args* __restrict__ plates,
 
 __global__ void __launch_bounds__(256) k_batch_persistent(const Fp64Args* __restrict__ plates,
                                                           const BatchTile* __restrict__ tiles, int ntiles, int nsteps,
-                                                          GridBarrier* bar) {
+                                                          GridBarrier* bar, const BarrierLimits lim) {
   const unsigned nb = gridDim.x;
   batch_phase(plates, tiles, ntiles, 0);
   for (int s = 0; s < nsteps; ++s) {
-    if (!grid_sync(bar, nb)) return;
+    if (!grid_sync(bar, nb, lim)) return;
     batch_phase(plates, tiles, ntiles, 1);
-    if (!grid_sync(bar, nb)) return;
+    if (!grid_sync(bar, nb, lim)) return;
     batch_phase(plates, tiles, ntiles, s + 1 < nsteps ? 2 : 3);
   }
 }
@@ -346,7 +346,7 @@ cudaError_t launch_batch_fp64(const Fp64Args* d_plates, const BatchTile* d_tiles
   at[0].val.cooperative = 1;
   lc.attrs = at;
   lc.numAttrs = 1;
-  return cudaLaunchKernelEx(&lc, k_batch_persistent, d_plates, d_tiles, ntiles, nsteps, d_bar);
+  return cudaLaunchKernelEx(&lc, k_batch_persistent, d_plates, d_tiles, ntiles, nsteps, d_bar, cfg.limits);
 }
 
 namespace {

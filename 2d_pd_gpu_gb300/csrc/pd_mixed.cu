@@ -756,16 +756,17 @@ __device__ __forceinline__ bool batch_phase_mixed(const MixedArgs* __restrict__ 
 
 __global__ void __launch_bounds__(kHaloBlock) k_batch_persistent_mixed(const MixedArgs* __restrict__ plates,
                                                                    const BatchTile* __restrict__ tiles, int ntiles,
-                                                                   int nsteps, GridBarrier* bar) {
+                                                                   int nsteps, GridBarrier* bar,
+                                                                   const BarrierLimits lim) {
   extern __shared__ __align__(128) unsigned char sm[];
   __shared__ uint64_t bars[kHaloBlock / 32];
   const unsigned nb = gridDim.x;
   bool ok = batch_phase_mixed<-1>(plates, tiles, ntiles, 0, sm, bars);
   for (int s = 0; s < nsteps && ok; ++s) {
-    if (!grid_sync(bar, nb)) return;
+    if (!grid_sync(bar, nb, lim)) return;
     ok = batch_phase_mixed<-1>(plates, tiles, ntiles, 1, sm, bars);
     if (!ok) break;
-    if (!grid_sync(bar, nb)) return;
+    if (!grid_sync(bar, nb, lim)) return;
     ok = batch_phase_mixed<-1>(plates, tiles, ntiles, s + 1 < nsteps ? 2 : 3, sm, bars);
   }
   if (!ok && threadIdx.x == 0) atomicExch(&bar->err, 1);  // releases the other blocks' barrier waits
@@ -913,7 +914,7 @@ cudaError_t launch_batch_mixed(const MixedArgs* d_plates, const BatchTile* d_til
   at[0].val.cooperative = 1;
   lc.attrs = at;
   lc.numAttrs = 1;
-  return cudaLaunchKernelEx(&lc, k_batch_persistent_mixed, d_plates, d_tiles, ntiles, nsteps, d_bar);
+  return cudaLaunchKernelEx(&lc, k_batch_persistent_mixed, d_plates, d_tiles, ntiles, nsteps, d_bar, cfg.limits);
 }
 
 void launch_init_geometry_mixed(const MixedArgs& a, cudaStream_t s) {

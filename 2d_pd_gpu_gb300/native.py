@@ -135,6 +135,7 @@ _SIGS = {
     "pd_batch_step": [_vp, ctypes.c_int32],
     "pd_batch_synchronize": [_vp],
     "pd_batch_step_timed": [_vp, ctypes.c_int32, ctypes.POINTER(ctypes.c_float)],
+    "pd_batch_set_barrier_limits": [_vp, ctypes.c_uint64, ctypes.c_uint32],
     "pd_batch_last_step_ms": [_vp, ctypes.POINTER(ctypes.c_float)],
     "pd_probe_fma_rates": [ctypes.c_int32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
     "pd_host_alloc": [ctypes.c_int64, ctypes.POINTER(_vp)],
@@ -441,6 +442,10 @@ class Batch:
 
     def synchronize(self):
         self._ck(lib().pd_batch_synchronize(self._h))
+
+    def set_barrier_limits(self, spin_limit=0, hold_ns=0):
+        """Persistent-kernel barrier controls (0, 0: the defaults); see pd_gb300.h."""
+        self._ck(lib().pd_batch_set_barrier_limits(self._h, int(spin_limit), int(hold_ns)))
 
     def step_timed(self, nsteps):
         ms = ctypes.c_float(0.0)

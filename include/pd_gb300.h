@@ -246,16 +246,27 @@ int pd_compute_velocity(pd_ctx* ctx, const double* u, double* velocity, double* 
  * CSR families row_ptr[n+1] / col[row_ptr[n]] (every bond intact; no bond
  * breaking here), u[n][2] (displacement), velocity[n][2] and acce[n][2]
  * (read and written, as pd_compute_velocity), netF[n][2] (written).  p
- * gives E, nu, rho, dt, det_guard, k_hg (plane stress).  stream is a cudaStream_t
+ * gives E, nu, rho, dt, det_guard, k_hg (plane stress); p->precision must be
+ * PD_FP64, n1 = n2 = 0 and s_c = 0 (anything else returns PD_ERR_ARG: this
+ * path has no mixed form, bond-associated weights or bond breaking), and
+ * damage_fail has no effect (no bond breaks, so no particle is damaged).
+ * The caller owns the families' validity: row_ptr[0] = 0, rows
+ * non-decreasing, col holding row_ptr[n] indices in [0, n).  The kernels
+ * check this as they walk it (the call itself does not read device
+ * memory): a particle whose row or indices break it reads nothing out of
+ * range and gets NaN in its velocity, acce and netF, as do particles whose
+ * families reach it.  stream is a cudaStream_t
  * (NULL: the legacy default stream); the call only enqueues work, so results
  * are ready once that stream is synchronised.  The per-particle scratch
  * between its two kernels lives in a static device array sized for
  * PD_NOALLOC_MAX_PARTICLES particles (4 MiB on every device that loads the
  * library, until exit): larger n returns PD_ERR_CAPACITY.  Every call
  * shares that array, so calls that overlap on the GPU race.  The first call
- * on a device looks up the array's device address (cudaGetSymbolAddress);
- * make that first call before any stream capture.  errbuf (may be NULL)
- * receives a message on failure. */
+ * in a CUDA context (normally once per device; again after cudaDeviceReset
+ * replaces the device's context) looks up the array's device address
+ * (cudaGetSymbolAddress) and caches it for that context; make that first
+ * call before any stream capture.  errbuf (may be NULL) receives a message
+ * on failure. */
 #define PD_NOALLOC_MAX_PARTICLES 65536
 int pd_compute_velocity_noalloc(int64_t n, const double* x, const double* vol, const int64_t* row_ptr,
                                 const int32_t* col, const double* u, double* velocity, double* acce, double* netF,
@@ -292,6 +303,15 @@ int pd_batch_get_config(const pd_batch* b, pd_batch_config* cfg);
 int pd_batch_step(pd_batch* b, int32_t nsteps);
 int pd_batch_synchronize(pd_batch* b);
 int pd_batch_step_timed(pd_batch* b, int32_t nsteps, float* ms);
+/* The persistent kernel's grid-barrier controls (persistent = 1; no
+ * reference counterpart -- the reference has no device waits).  spin_limit:
+ * polls before a barrier wait gives up and the call reports PD_ERR_TIMEOUT
+ * (0: the default, >= 4 s of waiting).  hold_ns: block 0 sleeps this long
+ * before it arrives at every barrier (0: never; at most 100 ms) -- a
+ * fault-injection control, so a test can make the other blocks' waits run
+ * out without faulting anything.  After a timeout the members' state is not
+ * trustworthy: pd_reset them (or restore a checkpoint). */
+int pd_batch_set_barrier_limits(pd_batch* b, uint64_t spin_limit, uint32_t hold_ns);
 /* GPU time of the last pd_batch_step call's kernels (CUDA events on the
  * batch stream, from its first kernel to its last; waits for them). */
 int pd_batch_last_step_ms(pd_batch* b, float* ms);

@@ -96,3 +96,38 @@ def test_batch_rejects_mixed_precisions(pdg):
     b = pdg.Batch(precision=0)
     with pytest.raises(pdg.PdError):
         b.add(p.context(precision=1))
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_barrier_wait_runs_out_and_the_batch_recovers(pdg, precision):
+    """A bounded device wait that runs out, without any fault: block 0 of the
+    persistent kernel holds 2 ms before every grid barrier while the others
+    may poll 16 times, so their waits give up; every block returns (the
+    kernel ends, the stream stays usable), pd_batch_synchronize reports
+    PD_ERR_TIMEOUT, and after pd_reset the same batch steps bit-identically
+    to the solo runs."""
+    plates = _plates(pdg)
+    steps = 5
+    solo = _solo(pdg, plates, precision, steps)
+    b = pdg.Batch(precision=precision)
+    b.set_config(persistent=1, block=256, tile=256, blocks_per_sm=1)
+    ctxs = [p.context(precision=precision) for p in plates]
+    for c in ctxs:
+        b.add(c)
+    b.set_barrier_limits(spin_limit=16, hold_ns=2_000_000)
+    b.step(3)
+    with pytest.raises(pdg.native.PdError) as err:
+        b.synchronize()
+    assert err.value.code == -7 and "grid-barrier" in str(err.value)
+    b.set_barrier_limits(0, 0)
+    for c in ctxs:
+        c.reset()
+    b.step(steps)
+    b.synchronize()
+    for c, ref in zip(ctxs, solo):
+        got = (*c.state(), c.bond_mask(), c.damage())
+        for g, r in zip(got, ref):
+            assert np.array_equal(g, r)
+    b.close()
+    for c in ctxs:
+        c.close()
