@@ -119,7 +119,7 @@ struct Problem {
   vector<int> fixed_idx;
 };
 
-int run_steps(Problem& pb, int nsteps, int dump_every, Writer& w, bool dump_fam) {
+int run_steps(Problem& pb, int nsteps, int dump_every, Writer& w, bool dump_fam, const vector<double>* v0) {
   const int n = (int)pb.P.size();
   unordered_map<int, int> g2l;
   defineParticleIDmap(pb.P, g2l);
@@ -128,6 +128,8 @@ int run_steps(Problem& pb, int nsteps, int dump_every, Writer& w, bool dump_fam)
   matrix C = getStiffnessTensor(pb.ndim, pb.E, pb.nu);
   vector<vector<long double>> netF(n, vector<long double>(2, 0.0)), vel(n, vector<long double>(2, 0.0)),
       acce(n, vector<long double>(2, 0.0));
+  if (v0)
+    for (int i = 0; i < n; ++i) { vel[i][0] = (*v0)[2 * i]; vel[i][1] = (*v0)[2 * i + 1]; }
   vector<vector<double>> bondDamage(n + 1);
   for (int i = 0; i < n; ++i) bondDamage[i].resize(NL[i].size(), 0.0);
   bondDamage[n].resize(30, 0.0);
@@ -231,13 +233,16 @@ int main(int argc, char** argv) {
     //   char[4] "PDRF", int32 version(=1), int32 n, int32 families_from_file,
     //   double dx, horizon, n1, n2, E, nu, rho, dt, int32 nsteps, int32 dump_every,
     //   double x_ref[n][2], double vol[n],
+    //   version 2 only: int32 has_state; if has_state: double u0[n][2], v0[n][2]
+    //     (initial displacement and velocity; version 1 starts at rest),
     //   if families_from_file: int64 row_ptr[n+1], int32 col[row_ptr[n]],
     //   int32 n_vbc; n_vbc x { int32 cnt, double vx, vy, int32 idx[cnt] },
     //   int32 n_fixed, int32 idx[n_fixed]
     char magic[4];
     r.arr(magic, 4);
     if (memcmp(magic, "PDRF", 4) != 0) { fprintf(stderr, "bad magic\n"); return 2; }
-    if (r.get<int32_t>() != 1) { fprintf(stderr, "bad version\n"); return 2; }
+    const int version = r.get<int32_t>();
+    if (version != 1 && version != 2) { fprintf(stderr, "bad version\n"); return 2; }
     Problem pb;
     const int n = r.get<int32_t>();
     const int fam_from_file = r.get<int32_t>();
@@ -247,6 +252,13 @@ int main(int argc, char** argv) {
     vector<double> x(2 * (size_t)n), vol(n);
     r.arr(x.data(), x.size());
     r.arr(vol.data(), vol.size());
+    vector<double> u0, v0;
+    if (version == 2 && r.get<int32_t>() != 0) {
+      u0.resize(2 * (size_t)n);
+      v0.resize(2 * (size_t)n);
+      r.arr(u0.data(), u0.size());
+      r.arr(v0.data(), v0.size());
+    }
     pb.P.resize(n);
     for (int i = 0; i < n; ++i) {
       Particle& p = pb.P[i];
@@ -254,6 +266,10 @@ int main(int argc, char** argv) {
       p.volume = vol[i];
       p.initialPositions = {x[2 * i], x[2 * i + 1]};
       p.currentPositions = p.initialPositions;
+      if (!u0.empty()) {  // current = reference + u0 in long double, so u = u0 exactly
+        p.currentPositions[0] += (long double)u0[2 * i];
+        p.currentPositions[1] += (long double)u0[2 * i + 1];
+      }
     }
     if (fam_from_file) {
       vector<int64_t> rp(n + 1);
@@ -281,7 +297,7 @@ int main(int argc, char** argv) {
     if (!fo) { perror("out"); return 2; }
     Writer w{fo};
     w.put<int32_t>(n);
-    run_steps(pb, nsteps, dump_every, w, true);
+    run_steps(pb, nsteps, dump_every, w, true, v0.empty() ? nullptr : &v0);
     fclose(fo);
     return 0;
   }

@@ -3,8 +3,11 @@
 Run here, where the reference checkout exists (it does not exist on the GPU
 machine, which only reads the committed .npz files):
 
-    make -C oracle ref oracle
-    python tests/golden/make_golden.py [--reference /root/reference]
+    make -C oracle ref oracle REF=<reference checkout>
+    python tests/golden/make_golden.py [--reference <checkout>] [--only mazars|plates]
+
+(--reference defaults to PD_REFERENCE_DIR, else the checkout oracle/_ref was
+built from.)
 
 Steps, each recorded in manifest.json:
  1. Hassa mesh (the reference's only input, 2D_Hassa_test_mesh.dat): the
@@ -25,6 +28,16 @@ Steps, each recorded in manifest.json:
  5. The reference's Mazars damage (computeDamageStatus) on the Hassa mesh,
     classic and n1 = n2 = 10 weights, at two imposed displacement fields in
     turn -> mazars_ref.npz.  `--only mazars` regenerates just this one.
+ 6. The reference's own step with its own model (no zero-energy-mode
+    penalty, no bond breaking) on the benchmark plates (`--only plates`):
+    the config-1 100 x 100 plate (plates.config_plate_100(seed=0)) for 3
+    steps from rest, and again from a seeded preloaded state (preload_state
+    below: every particle displaced and moving, so the crack and the whole
+    interior carry load from the first step); and the 200 x 200 cut of the
+    1M-particle workload (plates.config_plate_scale(side=200, seed=0)) for 2
+    steps from rest -> config1_ref.npz, plate200_ref.npz.  Families are the
+    crack-cut restatement families (the reference's findNeighbor has no crack
+    rule for plates); their sha256 is stored so a test can check its own.
 """
 from __future__ import annotations
 
@@ -62,14 +75,95 @@ def sha(path):
     return hashlib.sha256(open(path, "rb").read()).hexdigest()
 
 
+def families_sha(row_ptr, col):
+    """sha256 of the CSR families as little-endian int64 row_ptr then int32 col."""
+    h = hashlib.sha256(np.ascontiguousarray(row_ptr, dtype="<i8").tobytes())
+    h.update(np.ascontiguousarray(col, dtype="<i4").tobytes())
+    return h.hexdigest()
+
+
+def preload_state(p, seed=5):
+    """A seeded initial displacement and velocity for plate p ([n][2] each).
+
+    Polynomials of the reference coordinates plus splitmix64 noise: plain
+    IEEE additions and multiplications (no transcendental functions), so every
+    machine regenerates the same bits.  Displacement: a stretch-shear of
+    strain 2e-4, a quadratic bend and +-2e-7 m noise; velocity: a linear
+    field of up to ~0.5 m/s and +-0.05 m/s noise."""
+    x = p.x
+    cx = p.meta["x0"] + 0.5 * (p.nx - 1) * p.dx
+    cy = p.meta["y0"] + 0.5 * (p.ny - 1) * p.dx
+    X = (x[:, 0] - cx) / p.dx
+    Y = (x[:, 1] - cy) / p.dx
+    r = plates.uniform(seed, 3, np.arange(4 * p.n)).reshape(p.n, 4) * 2.0 - 1.0
+    u0 = np.empty((p.n, 2))
+    u0[:, 0] = p.dx * (2e-4 * (X + 0.3 * Y) + 1e-6 * X * Y) + 2e-7 * r[:, 0]
+    u0[:, 1] = p.dx * (-0.8e-4 * Y + 1.5e-6 * X * X) + 2e-7 * r[:, 1]
+    v0 = np.empty((p.n, 2))
+    v0[:, 0] = 0.01 * X + 0.05 * r[:, 2]
+    v0[:, 1] = -0.005 * Y + 0.05 * r[:, 3]
+    return u0, v0
+
+
+def state_sha(u0, v0):
+    h = hashlib.sha256(np.ascontiguousarray(u0, dtype="<f8").tobytes())
+    h.update(np.ascontiguousarray(v0, dtype="<f8").tobytes())
+    return h.hexdigest()
+
+
+def _ref_plate_run(p, td, tag, nsteps, state=None):
+    """The reference's own step (k_hg = 0, no breaking) on plate p with the
+    crack-cut restatement families; returns (row_ptr, col, harness output)."""
+    rp, col = po.build_families(p.x, p.cutoff, p.cracks)
+    prm = {"dx": p.dx, "horizon": 3.015, "E": p.material.E, "nu": p.material.nu, "rho": p.material.rho,
+           "dt": p.dt}
+    vbc = [(np.nonzero(p.group_of == 1)[0], p.group_val[0]), (np.nonzero(p.group_of == 2)[0], p.group_val[1])]
+    fin = os.path.join(td, f"{tag}.bin")
+    po.write_ref_input(fin, p.x, p.vol, prm, nsteps, families=(rp, col), vbc=vbc, state=state)
+    return rp, col, po.run_ref_plate(fin, os.path.join(td, f"{tag}.out"), timeout=4 * 3600)
+
+
+def fixtures_plates(td, man):
+    import time
+    p = plates.config_plate_100(seed=0)
+    t0 = time.time()
+    rp, col, rest = _ref_plate_run(p, td, "c1_rest", 3)
+    t_rest = time.time() - t0
+    u0, v0 = preload_state(p)
+    _, _, pre = _ref_plate_run(p, td, "c1_pre", 3, state=(u0, v0))
+    out = {"families_sha": np.array(families_sha(rp, col)), "state_sha": np.array(state_sha(u0, v0))}
+    for s in (1, 3):
+        for k in ("u", "v", "f"):
+            out[f"rest_{k}{s}"] = rest["steps"][s][k]
+    for k in ("u", "v", "f"):
+        out[f"pre_{k}3"] = pre["steps"][3][k]
+    np.savez_compressed(os.path.join(HERE, "config1_ref.npz"), **out)
+    man["config1"] = {"generator": "plates.config_plate_100(seed=0)", "n": int(p.n), "bonds": int(rp[-1]),
+                      "model": "reference (k_hg=0, s_c=0, damage_fail=1)", "steps": {"rest": [1, 3], "preloaded": [3]},
+                      "preload": "make_golden.preload_state(plate, seed=5)",
+                      "reference_seconds_per_step": round(t_rest / 3, 1)}
+    p2 = plates.config_plate_scale(side=200, seed=0)
+    t0 = time.time()
+    rp2, col2, r2 = _ref_plate_run(p2, td, "p200_rest", 2)
+    t2 = time.time() - t0
+    out2 = {"families_sha": np.array(families_sha(rp2, col2))}
+    for s in (1, 2):
+        for k in ("u", "v", "f"):
+            out2[f"rest_{k}{s}"] = r2["steps"][s][k]
+    np.savez_compressed(os.path.join(HERE, "plate200_ref.npz"), **out2)
+    man["plate200"] = {"generator": "plates.config_plate_scale(side=200, seed=0)", "n": int(p2.n),
+                       "bonds": int(rp2[-1]), "model": "reference (k_hg=0, s_c=0, damage_fail=1)",
+                       "steps": {"rest": [1, 2]}, "reference_seconds_per_step": round(t2 / 2, 1)}
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
-    ap.add_argument("--only", choices=["mazars"], default=None)
+    ap.add_argument("--reference", default=po.reference_dir())
+    ap.add_argument("--only", choices=["mazars", "plates"], default=None)
     args = ap.parse_args()
     ref = args.reference
-    if not po.ref_available():
-        sys.exit("build the reference oracle first: make -C oracle ref")
+    if not po.ref_available() or not ref:
+        sys.exit("build the reference oracle first: make -C oracle ref REF=<reference checkout>")
     man_path = os.path.join(HERE, "manifest.json")
     man = json.load(open(man_path)) if args.only and os.path.exists(man_path) else {}
     with tempfile.TemporaryDirectory() as td:
@@ -78,8 +172,21 @@ def main():
         os.makedirs(mesh_dir)
         mesh = os.path.join(mesh_dir, "2D_Hassa_test_mesh.dat")
         open(mesh, "w").write(hassa_mesh_lines())
-        if args.only != "mazars":
+        if args.only is None:
             fixtures_1_to_4(ref, td, mesh_dir, mesh, man)
+        if args.only in (None, "plates"):
+            fixtures_plates(td, man)
+        if args.only in (None, "mazars"):
+            fixtures_mazars(td, mesh_dir, man)
+    json.dump(man, open(man_path, "w"), indent=1, sort_keys=True)
+    print(json.dumps(man, indent=1, sort_keys=True))
+    bad = [k for k, v in man.items() if v is False]
+    if bad:
+        sys.exit(f"pinning failed: {bad}")
+
+
+def fixtures_mazars(td, mesh_dir, man):
+    if True:
         # 5. Mazars damage, classic and bond-associated weights
         out = {"kappa0": np.float64(np.longdouble(3.0) / np.longdouble(3.5e4))}
         for tag, w in (("c", 0), ("b", 10)):
@@ -95,11 +202,6 @@ def main():
                          "kappa0": "3.0L / 3.5e4L (tensileStrength / E, src/main_seq.cpp:659)",
                          "law": "a_t=0.87 b_t=20000 a_c=0.65 b_c=2150 (src/main_seq.cpp:481)",
                          "bonds_updated_level1": {"classic": out["c_updated1"], "bond_associated": out["b_updated1"]}}
-    json.dump(man, open(man_path, "w"), indent=1, sort_keys=True)
-    print(json.dumps(man, indent=1, sort_keys=True))
-    bad = [k for k, v in man.items() if v is False]
-    if bad:
-        sys.exit(f"pinning failed: {bad}")
 
 
 def fixtures_1_to_4(ref, td, mesh_dir, mesh, man):
