@@ -3,8 +3,10 @@
     python -m 2d_pd_gpu_gb300.build      (or __graft_entry__.build())
 
 produces 2d_pd_gpu_gb300/_build/libpd_gb300.so (CUDA kernels + C ABI, sm_103a
-only) and 2d_pd_gpu_gb300/_build/libpd_dropin.so (the C++ drop-in with the
-reference's function names, linked against libpd_gb300.so).  Translation
+only), 2d_pd_gpu_gb300/_build/libpd_dropin.so (the C++ drop-in with the
+reference's function names, linked against libpd_gb300.so) and
+2d_pd_gpu_gb300/_build/pd_hassa_timing (the drop-in timed on the reference's
+own published problem, see csrc/pd_hassa_timing.cpp).  Translation
 units compile in parallel.  Files whose results must match the FP64 oracle
 bit-for-bit are compiled with --fmad=false (only explicit fma() fuses).
 """
@@ -90,6 +92,12 @@ def build(verbose=False, force=False):
         if force or _stale(dlib, dsrc + dh + [lib]):
             _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", f"-I{INCLUDE}", "-o", dlib] + dsrc +
                  [f"-L{OUT}", "-lpd_gb300", "-Wl,-rpath,$ORIGIN"])
+        # the timing driver for the reference's published problem (bench.py's bond-associated leg)
+        tsrc = os.path.join(CSRC, "pd_hassa_timing.cpp")
+        texe = os.path.join(OUT, "pd_hassa_timing")
+        if force or _stale(texe, [tsrc, dlib] + dh + [os.path.join(INCLUDE, "pd_gb300.h")]):
+            _run(["g++", "-O2", "-std=c++17", f"-I{INCLUDE}", tsrc, "-o", texe, f"-L{OUT}", "-lpd_dropin",
+                  "-lpd_gb300", "-Wl,-rpath,$ORIGIN"])
     return lib
 
 

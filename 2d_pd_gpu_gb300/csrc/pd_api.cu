@@ -58,10 +58,16 @@ struct pd_ctx {
   int64_t* rslot = nullptr;
   int32_t max_family = 0;
   // pd_step_host's copy / compute pipeline (streams and events, see plan_slabs)
-  cudaStream_t io[3] = {nullptr, nullptr, nullptr};
+  cudaStream_t io[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   std::vector<cudaEvent_t> slab_ev;
   std::vector<int64_t> slab_bnd;    // slab k = particles slab_bnd[k] .. slab_bnd[k+1]; empty: not planned
   std::vector<int32_t> slab_need;   // slab k's pass A needs slabs 0 .. slab_need[k] imported
+  // the mixed form's: slab k = visiting blocks mslab_blk[k] .. mslab_blk[k+1], whose bonds
+  // reach slabs mslab_lo[k] .. mslab_hi[k]; id slab k = particles mslab_id[k] ..
+  // mslab_id[k+1], which slab k's import needs at the latest, and whose export waits for
+  // pass B of slabs 0 .. mslab_out[k]
+  std::vector<int64_t> mslab_blk, mslab_id;
+  std::vector<int32_t> mslab_lo, mslab_hi, mslab_out;
   // Mazars damage history (pd_mazars_*)
   double *mz_thr = nullptr, *mz_bd = nullptr, *mz_status = nullptr;
   pd_mazars_params mz{};
@@ -179,6 +185,11 @@ void free_families(pd_ctx* c) {
   c->sell = pd::SellLayout{};
   c->slab_bnd.clear();
   c->slab_need.clear();
+  c->mslab_blk.clear();
+  c->mslab_id.clear();
+  c->mslab_lo.clear();
+  c->mslab_hi.clear();
+  c->mslab_out.clear();
   c->nnz = 0;
   c->has_families = false;
   clear_graphs(c);
@@ -1198,19 +1209,26 @@ int pd_checkpoint_load(pd_ctx* c, const void* buf, int64_t bytes) {
 constexpr int kSlabs = 8;
 enum { kEvImport = 0, kEvCopy = kSlabs, kEvStart = 2 * kSlabs, kEvJoin = 2 * kSlabs + 1, kEvCount = 2 * kSlabs + 2 };
 
-static int plan_slabs(pd_ctx* c) {
-  if (!c->slab_bnd.empty()) return PD_OK;
+// The pipeline's streams (io[0], io[1] at high priority) and events.
+static int pipeline_streams(pd_ctx* c, int nev) {
   if (!c->io[0]) {
     int lo = 0, hi = 0;
     PD_CK(c, cudaDeviceGetStreamPriorityRange(&lo, &hi));
-    for (int q = 0; q < 2; ++q) PD_CK(c, cudaStreamCreateWithPriority(&c->io[q], cudaStreamNonBlocking, hi));
-    PD_CK(c, cudaStreamCreateWithFlags(&c->io[2], cudaStreamNonBlocking));
+    for (int q = 0; q < 6; ++q)
+      PD_CK(c, cudaStreamCreateWithPriority(&c->io[q], cudaStreamNonBlocking, q < 2 || q == 5 ? hi : lo));
   }
-  while ((int)c->slab_ev.size() < kEvCount) {
+  while ((int)c->slab_ev.size() < nev) {
     cudaEvent_t e;
     PD_CK(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     c->slab_ev.push_back(e);
   }
+  return PD_OK;
+}
+
+static int plan_slabs(pd_ctx* c) {
+  if (!c->slab_bnd.empty()) return PD_OK;
+  const int rs = pipeline_streams(c, kEvCount);
+  if (rs != PD_OK) return rs;
   // the largest neighbour id of every 32-particle chunk
   const int64_t nch = (c->n + 31) / 32;
   std::vector<int32_t> h((size_t)nch, 0);
@@ -1265,7 +1283,7 @@ static cudaError_t enqueue_host_step(pd_ctx* c, int32_t nsteps, const double* u_
   cudaStream_t* io = c->io;
   const size_t b16 = sizeof(double2);
   ck(cudaEventRecord(ev[kEvStart], s));
-  for (int q = 0; q < 3; ++q) ck(cudaStreamWaitEvent(io[q], ev[kEvStart], 0));
+  for (int q = 0; q < 4; ++q) ck(cudaStreamWaitEvent(io[q], ev[kEvStart], 0));
   // enqueued in dependency order (each pass A right after the import it waits for), so the
   // first pass A is submitted before the host has issued the later imports
   int next_a = 0;
@@ -1299,15 +1317,214 @@ static cudaError_t enqueue_host_step(pd_ctx* c, int32_t nsteps, const double* u_
   return e;
 }
 
+// pd_step_host pipeline, mixed form: a wavefront over slabs of visiting blocks
+// (spatial tiles in order; two small leading slabs, then even ones).  A slab is
+// a run of visiting blocks, and everything about it -- which positions it
+// imports, which slabs its bonds reach -- is taken through the blocks' visit
+// records, since a tile's last block holds fewer chunks than kHaloBlock / 32.
+// Moving the state is the cost here: 48 B per particle each way in FP64
+// against a step that takes ~0.1 us per 1k particles, over a CPU-GPU link of
+// ~200 GB/s each way.  Host <-> device traffic therefore goes through the copy
+// engines (which share the link in both directions better than SM loads and
+// stores do), by slabs of particle ids, through the context's FP64 staging
+// buffers (u, v, f):
+//   io[1]  copies id slab k in;
+//   io[0]  imports slab k (conversion to the scaled state + drift, from the
+//          staging buffers) once id slabs 0 .. k are in;
+//   main / io[2] alternately: pass A of slab k once the slabs its bonds reach
+//          are imported;
+//   io[3] / io[4] alternately (one-step calls): pass B of slab k once pass A
+//          of those slabs is done, writing the new FP64 state by particle id
+//          into the staging buffers;
+//   io[5]  copies id slab k out once pass B of every slab holding its ids is
+//          done -- while later slabs are still coming in.
+// Id slab k ends after the highest id of slabs 0 .. k, so slab k's import
+// needs id slabs 0 .. k only (a row-major numbering gives slabs of whole
+// rows; any numbering is correct, a scrambled one just pipelines less).
+constexpr int kMixedSlabs = 8;
+enum { kMEvIn = 0, kMEvImport = kMixedSlabs, kMEvA = 2 * kMixedSlabs, kMEvB = 3 * kMixedSlabs,
+       kMEvStart = 4 * kMixedSlabs, kMEvCount = 4 * kMixedSlabs + 1 };
+
+static int plan_slabs_mixed(pd_ctx* c) {
+  if (!c->mslab_blk.empty()) return PD_OK;
+  const int rs = pipeline_streams(c, std::max<int>(kEvCount, kMEvCount));
+  if (rs != PD_OK) return rs;
+  const int64_t nb = c->halo.nblocks;
+  std::vector<int64_t> h(5 * (size_t)nb);
+  int64_t* d = nullptr;
+  PD_CK(c, cudaMalloc(&d, h.size() * sizeof(int64_t)));
+  pd::launch_block_reach_mixed(mixed_args(c), d, d + nb, d + 2 * nb, d + 3 * nb, d + 4 * nb, c->stream);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = copy_sync(h.data(), d, h.size() * sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream);
+  cudaFree(d);
+  PD_CK(c, e);
+  const int64_t *lo = h.data(), *hi = lo + nb, *idlo = hi + nb, *idhi = idlo + nb, *cf = idhi + nb;
+  // visiting blocks hold ascending runs of chunks: the block of a SELL position is the last
+  // block whose first chunk is at or below the position's chunk
+  std::vector<int64_t> first((size_t)nb);
+  for (int64_t b = 0; b < nb; ++b) first[b] = cf[b] >= 0 ? cf[b] : (b ? first[b - 1] : 0);
+  auto block_of_pos = [&](int64_t p) {
+    const auto it = std::upper_bound(first.begin(), first.end(), p / 32);
+    return (int64_t)(it == first.begin() ? 0 : (it - first.begin()) - 1);
+  };
+  const int K = kMixedSlabs;
+  std::vector<int64_t> bc(K + 1);
+  const int64_t lead = std::max<int64_t>(1, nb / 32);
+  bc[0] = 0;
+  bc[1] = std::min(nb, lead);
+  bc[2] = std::min(nb, 2 * lead);
+  for (int k = 3; k <= K; ++k) bc[k] = bc[2] + (nb - bc[2]) * (k - 2) / (K - 2);
+  auto slab_of_block = [&](int64_t blk) {
+    int k = 0;
+    while (k + 1 < K && blk >= bc[k + 1]) ++k;
+    return k;
+  };
+  c->mslab_lo.assign(K, 0);
+  c->mslab_hi.assign(K, 0);
+  std::vector<int64_t> smin(K, -1), smax(K, -1);  // particle ids held by slab k
+  for (int k = 0; k < K; ++k) {
+    int l = k, u = k;
+    for (int64_t b = bc[k]; b < bc[k + 1]; ++b) {
+      if (lo[b] >= 0) {
+        l = std::min(l, slab_of_block(block_of_pos(lo[b])));
+        u = std::max(u, slab_of_block(block_of_pos(hi[b])));
+      }
+      if (idlo[b] >= 0) {
+        smin[k] = smin[k] < 0 ? idlo[b] : std::min(smin[k], idlo[b]);
+        smax[k] = std::max(smax[k], idhi[b]);
+      }
+    }
+    c->mslab_lo[k] = l;
+    c->mslab_hi[k] = u;
+  }
+  // id slab k ends after the highest id of slabs 0 .. k
+  c->mslab_id.assign(K + 1, 0);
+  for (int k = 0; k < K; ++k) c->mslab_id[k + 1] = std::max(c->mslab_id[k], smax[k] + 1);
+  c->mslab_id[K] = c->n;
+  // id slab j goes out after pass B of the last slab whose ids meet it
+  c->mslab_out.assign(K, 0);
+  for (int j = 0; j < K; ++j)
+    for (int k = 0; k < K; ++k)
+      if (smin[k] >= 0 && smin[k] < c->mslab_id[j + 1] && smax[k] >= c->mslab_id[j])
+        c->mslab_out[j] = std::max(c->mslab_out[j], k);
+  c->mslab_blk = bc;
+  return PD_OK;
+}
+
+static pd::MixedArgs mixed_slab(const pd_ctx* c, pd::MixedArgs a, int k) {
+  a.blk0 = c->mslab_blk[k];
+  a.nblocks = c->mslab_blk[k + 1];
+  return a;
+}
+
+static cudaError_t enqueue_host_step_mixed(pd_ctx* c, int32_t nsteps, const double* u_in, const double* v_in,
+                                           const double* f_in, double* u_out, double* v_out, double* f_out,
+                                           bool brk) {
+  cudaError_t e = cudaSuccess;
+  auto ck = [&](cudaError_t r) {
+    if (e == cudaSuccess) e = r;
+  };
+  cudaStream_t s = c->stream;
+  cudaEvent_t* ev = c->slab_ev.data();
+  cudaStream_t* io = c->io;
+  const int K = kMixedSlabs;
+  const size_t b16 = sizeof(double2);
+  pd::MixedArgs plain = mixed_args(c), out = plain;
+  out.out_u = c->u;  // pass B writes the FP64 state into the staging buffers
+  out.out_v = c->v;
+  out.out_f = c->f;
+  ck(cudaEventRecord(ev[kMEvStart], s));
+  for (int q = 0; q < 6; ++q) ck(cudaStreamWaitEvent(io[q], ev[kMEvStart], 0));
+  const bool one = nsteps == 1;
+  int next_a = 0, next_b = 0, next_out = 0, b_waited = -1;
+  auto export_ready = [&]() {  // copy out every id slab whose passes B are done
+    for (; one && next_out < K && c->mslab_out[next_out] < next_b; ++next_out) {
+      for (; b_waited < c->mslab_out[next_out]; ++b_waited) ck(cudaStreamWaitEvent(io[5], ev[kMEvB + b_waited + 1], 0));
+      const size_t off = (size_t)c->mslab_id[next_out], cnt = (size_t)(c->mslab_id[next_out + 1] - off);
+      if (cnt == 0) continue;
+      ck(cudaMemcpyAsync(u_out + 2 * off, c->u + off, cnt * b16, cudaMemcpyDeviceToHost, io[5]));
+      ck(cudaMemcpyAsync(v_out + 2 * off, c->v + off, cnt * b16, cudaMemcpyDeviceToHost, io[5]));
+      ck(cudaMemcpyAsync(f_out + 2 * off, c->f + off, cnt * b16, cudaMemcpyDeviceToHost, io[5]));
+    }
+  };
+  for (int k = 0; k < K; ++k) {  // enqueued in dependency order
+    const size_t off = (size_t)c->mslab_id[k], cnt = (size_t)(c->mslab_id[k + 1] - off);
+    if (cnt > 0) {
+      ck(cudaMemcpyAsync(c->u + off, u_in + 2 * off, cnt * b16, cudaMemcpyHostToDevice, io[1]));
+      ck(cudaMemcpyAsync(c->v + off, v_in + 2 * off, cnt * b16, cudaMemcpyHostToDevice, io[1]));
+      ck(cudaMemcpyAsync(c->f + off, f_in + 2 * off, cnt * b16, cudaMemcpyHostToDevice, io[1]));
+    }
+    ck(cudaEventRecord(ev[kMEvIn + k], io[1]));
+    ck(cudaStreamWaitEvent(io[0], ev[kMEvIn + k], 0));
+    pd::launch_import_drift_mixed(plain, c->mslab_blk[k], c->mslab_blk[k + 1], c->u, c->v, c->f, io[0]);
+    ck(cudaEventRecord(ev[kMEvImport + k], io[0]));
+    for (; next_a < K && c->mslab_hi[next_a] <= k; ++next_a) {
+      cudaStream_t sa = next_a % 2 ? io[2] : s;
+      ck(cudaStreamWaitEvent(sa, ev[kMEvImport + c->mslab_hi[next_a]], 0));
+      pd::launch_slab_pass_a_mixed(mixed_slab(c, plain, next_a), brk, sa);
+      ck(cudaEventRecord(ev[kMEvA + next_a], sa));
+      for (; one && next_b < next_a && c->mslab_hi[next_b] < next_a; ++next_b) {
+        cudaStream_t sb = next_b % 2 ? io[4] : io[3];
+        for (int q = c->mslab_lo[next_b]; q <= c->mslab_hi[next_b]; ++q) ck(cudaStreamWaitEvent(sb, ev[kMEvA + q], 0));
+        pd::launch_slab_pass_b_mixed(mixed_slab(c, out, next_b), true, sb);
+        ck(cudaEventRecord(ev[kMEvB + next_b], sb));
+      }
+      export_ready();
+    }
+  }
+  for (; one && next_b < K;) {
+    cudaStream_t sb = next_b % 2 ? io[4] : io[3];
+    for (int q = c->mslab_lo[next_b]; q <= c->mslab_hi[next_b]; ++q) ck(cudaStreamWaitEvent(sb, ev[kMEvA + q], 0));
+    pd::launch_slab_pass_b_mixed(mixed_slab(c, out, next_b), true, sb);
+    ck(cudaEventRecord(ev[kMEvB + next_b], sb));
+    ++next_b;
+    export_ready();
+  }
+  if (one && next_out != K) e = e == cudaSuccess ? cudaErrorLaunchFailure : e;  // every id slab is out (a plan bug)
+  // join every stream's work on the main stream (io[5] holds the last copies out)
+  cudaEvent_t join = ev[kMEvStart];
+  for (int q = 0; q < 6; ++q) {
+    ck(cudaEventRecord(join, io[q]));
+    ck(cudaStreamWaitEvent(s, join, 0));
+  }
+  if (!one) {  // the remaining steps on the whole plate; the last pass B exports
+    pd::launch_slab_pass_b_mixed(plain, false, s);  // (plain launch: it follows the join's event waits)
+    for (int32_t k = 1; k < nsteps; ++k) {
+      pd::launch_pass_a_mixed(plain, brk, s);
+      if (k + 1 < nsteps)
+        pd::launch_pass_b_mixed(plain, true, s);
+      else
+        pd::launch_slab_pass_b_mixed(out, true, s);
+    }
+    const size_t bytes = (size_t)c->n * b16;
+    ck(cudaMemcpyAsync(u_out, c->u, bytes, cudaMemcpyDeviceToHost, s));
+    ck(cudaMemcpyAsync(v_out, c->v, bytes, cudaMemcpyDeviceToHost, s));
+    ck(cudaMemcpyAsync(f_out, c->f, bytes, cudaMemcpyDeviceToHost, s));
+  }
+  ck(cudaGetLastError());
+  return e;
+}
+
 int pd_step_host(pd_ctx* c, int32_t nsteps, const double* u_in, const double* v_in, const double* f_in, double* u_out,
                  double* v_out, double* f_out) {
   if (!c) return PD_ERR_ARG;
   if (!c->has_families) return fail(c, PD_ERR_ORDER, "families first");
-  if (mixed(c)) return fail(c, PD_ERR_ARG, "pd_step_host: PD_FP64 contexts (use pd_set_state / pd_get_state)");
   if (nsteps < 1) return fail(c, PD_ERR_ARG, "pd_step_host: nsteps >= 1");
   if (!u_in || !v_in || !f_in || !u_out || !v_out || !f_out) return fail(c, PD_ERR_ARG, "pd_step_host: NULL buffer");
   if (c->n == 0) return PD_OK;
   PD_CK(c, cudaSetDevice(c->p.device));
+  if (mixed(c)) {
+    if (!mapped_host(u_in) || !mapped_host(v_in) || !mapped_host(f_in) || !mapped_host(u_out) ||
+        !mapped_host(v_out) || !mapped_host(f_out))
+      return fail(c, PD_ERR_ARG, "pd_step_host: buffers must be page-locked host memory (pd_host_alloc)");
+    const int rp = plan_slabs_mixed(c);
+    if (rp != PD_OK) return rp;
+    PD_CK(c, enqueue_host_step_mixed(c, nsteps, u_in, v_in, f_in, u_out, v_out, f_out, c->p.s_c > 0.0));
+    PD_CK(c, cudaGetLastError());
+    PD_CK(c, cudaStreamSynchronize(c->stream));
+    c->steps += nsteps;
+    return check_after_step(c);
+  }
   Fp64Args in = fp64_args(c), out = fp64_args(c);
   in.in_u = static_cast<const double2*>(mapped_host(u_in));
   in.in_v = static_cast<const double2*>(mapped_host(v_in));

@@ -171,6 +171,12 @@ struct MixedArgs {
   unsigned long long* counters;
   int32_t brk;  // bond breaking on (s_c > 0)
   int32_t wmax;  // widest SELL chunk (slot rows), sizes the staged passes' shared memory
+  // pd_step_host: a pass launch covers visiting blocks blk0 .. nblocks - 1 (0: all), and
+  // the exporting pass B writes the new FP64 state by particle id to these (host-mapped)
+  double2* out_u;
+  double2* out_v;
+  double2* out_f;
+  int64_t blk0;
 };
 
 // ---- family build (pd_family.cu)
@@ -267,6 +273,16 @@ void launch_drift_mixed(const MixedArgs& a, cudaStream_t s);
 void launch_pass_a_mixed(const MixedArgs& a, bool breaking, cudaStream_t s);
 void launch_pass_b_mixed(const MixedArgs& a, bool drift, cudaStream_t s);
 void launch_to_mixed(const MixedArgs& a, const double2* u, const double2* v, const double2* f, cudaStream_t s);
+// pd_step_host (mixed): slabbed passes over visiting blocks a.blk0 .. a.nblocks - 1 in plain
+// stream order; the fused import + drift of the positions of visiting blocks blk0 .. blk1 - 1
+// from FP64 state by particle id; and, per visiting block, the lowest / highest SELL position
+// its bonds reach, the lowest / highest particle id it holds and its first chunk.
+void launch_slab_pass_a_mixed(const MixedArgs& a, bool breaking, cudaStream_t s);
+void launch_slab_pass_b_mixed(const MixedArgs& a, bool exporting, cudaStream_t s);
+void launch_import_drift_mixed(const MixedArgs& a, int64_t blk0, int64_t blk1, const double2* u, const double2* v,
+                               const double2* f, cudaStream_t s);
+void launch_block_reach_mixed(const MixedArgs& a, int64_t* lo, int64_t* hi, int64_t* idlo, int64_t* idhi,
+                              int64_t* cfirst, cudaStream_t s);
 void launch_from_mixed(const MixedArgs& a, double2* u, double2* v, double2* f, cudaStream_t s);
 // mixed tiles: {plate, particles <= 256, first = visiting block}; smem = the
 // largest mixed_pass_smem of the batch's plates for pass A (smem_a) and pass B (smem_b)

@@ -62,6 +62,15 @@ __device__ __forceinline__ float2 tf_diff2(float4 j, float2 nhi, float2 nlo) {
   return add2(add2(f2(j.x, j.y), nhi), add2(f2(j.z, j.w), nlo));
 }
 
+// A SELL slot's neighbour: its particle id, broken bonds included (-1: padding).
+__device__ __forceinline__ int decode_nbr(int v) { return v >= 0 ? v : (v <= -2 ? -2 - v : -1); }
+
+// FP64 -> two-float (hi + lo) for the scaled state.
+__device__ __forceinline__ void split2(double v, float& hi, float& lo) {
+  hi = (float)v;
+  lo = (float)(v - (double)hi);
+}
+
 // K^-1 (FP64 inversion + guard) and m^ from the FP64 reference positions of
 // particle i at SELL position p, whose slots are s0 + 32 k, k < w.
 __device__ void kinv_update_mixed(const MixedArgs& a, int64_t i, int64_t p, int64_t s0, int w) {
@@ -260,7 +269,7 @@ struct PreB {
   int g;
 };
 
-template <bool DRIFT>
+template <bool DRIFT, bool EXPORT = false>
 __device__ __forceinline__ PreB load_b(const MixedArgs& a, int64_t q) {
   PreB p;
   p.wi = a.ws[q];
@@ -269,16 +278,25 @@ __device__ __forceinline__ PreB load_b(const MixedArgs& a, int64_t q) {
   p.h = a.hgs[q];
   p.fo = a.fs[q];
   p.v = a.vs[q];
-  if (DRIFT) {
-    p.u = a.us[q];
-    p.g = a.bc[q];
-  }
+  if (DRIFT || EXPORT) p.u = a.us[q];
+  if (DRIFT) p.g = a.bc[q];
   return p;
 }
 
+// The FP64 state of SELL position p written by particle id to the export
+// buffers (pd_step_host): the same conversions as pd_get_state (k_from_mixed).
+__device__ __forceinline__ void export_state(const MixedArgs& a, int64_t p, const float4& u, const float4& v, float fx,
+                                             float fy) {
+  const int64_t i = a.member[p];
+  if (i < 0) return;
+  a.out_u[i] = make_double2(((double)u.x + (double)u.z) / a.inv_ls, ((double)u.y + (double)u.w) / a.inv_ls);
+  a.out_v[i] = make_double2(((double)v.x + (double)v.z) / a.v_scale, ((double)v.y + (double)v.w) / a.v_scale);
+  a.out_f[i] = make_double2((double)fx / a.f_scale, (double)fy / a.f_scale);
+}
+
 // Pass B of the particle at SELL position p (force gather, kick, optional
-// next drift).
-template <bool DRIFT, typename Idx, typename Gather>
+// next drift, or -- EXPORT -- the new state written to host buffers).
+template <bool DRIFT, bool EXPORT = false, typename Idx, typename Gather>
 __device__ __forceinline__ void pass_b_core(const MixedArgs& a, int64_t p, const PreB& pre, const BcOf& bc, int w,
                                             Idx idx, Gather gather) {
   const float4 wi = pre.wi, xi = pre.xi;
@@ -309,6 +327,7 @@ __device__ __forceinline__ void pass_b_core(const MixedArgs& a, int64_t p, const
     a.us[p] = u;
   }
   a.vs[p] = v;
+  if (EXPORT) export_state(a, p, pre.u, v, fx, fy);
 }
 
 struct GatherB {  // neighbour data of particle j (unstaged blocks)
@@ -480,9 +499,9 @@ __device__ __forceinline__ bool pass_a_block(const MixedArgs& a, int64_t blk, un
   return true;
 }
 
-// Pass B (+ the next drift when DRIFT) of visiting block blk of plate a.
-// PDL: as for pass A.
-template <bool DRIFT, bool PDL = false>
+// Pass B (+ the next drift when DRIFT, or the export when EXPORT) of
+// visiting block blk of plate a.  PDL: as for pass A.
+template <bool DRIFT, bool PDL = false, bool EXPORT = false>
 __device__ __forceinline__ bool pass_b_block(const MixedArgs& a, int64_t blk, unsigned char* sm, uint64_t* bars) {
   int64_t chunk = 0, base = 0;
   int w = 0, nlive = 0;
@@ -497,7 +516,7 @@ __device__ __forceinline__ bool pass_b_block(const MixedArgs& a, int64_t blk, un
     grid_dep_sync();
   }
   PreB pre{};
-  if (live) pre = load_b<DRIFT>(a, p);  // in flight during the staging below
+  if (live) pre = load_b<DRIFT, EXPORT>(a, p);  // in flight during the staging below
   if (hn < 0) {
     if (!has) return true;
     int32_t* mine = reinterpret_cast<int32_t*>(sm) + warp * a.wmax * 32;
@@ -505,7 +524,8 @@ __device__ __forceinline__ bool pass_b_block(const MixedArgs& a, int64_t blk, un
     __syncwarp();
     if (!warp_stage_done(a, &bars[warp], w)) return false;
     if (live)
-      pass_b_core<DRIFT>(a, p, pre, DRIFT ? resolve_bc(a, pre.g) : BcOf{}, w, SharedIdx{mine, lane}, GatherB{&a});
+      pass_b_core<DRIFT, EXPORT>(a, p, pre, DRIFT ? resolve_bc(a, pre.g) : BcOf{}, w, SharedIdx{mine, lane},
+                                 GatherB{&a});
     return true;
   }
   const HaloSmem h = halo_smem(a, sm);
@@ -525,8 +545,8 @@ __device__ __forceinline__ bool pass_b_block(const MixedArgs& a, int64_t blk, un
   if (!live) return true;
   const float4* q0 = h.q0;
   const float4* q1 = h.q1;
-  pass_b_core<DRIFT>(a, p, pre, bc, w, SharedHaloIdx{h.li + warp * a.wmax * 32, lane},
-                     [=](int64_t l) { return NbB{q0[l], q1[l]}; });
+  pass_b_core<DRIFT, EXPORT>(a, p, pre, bc, w, SharedHaloIdx{h.li + warp * a.wmax * 32, lane},
+                             [=](int64_t l) { return NbB{q0[l], q1[l]}; });
   return true;
 }
 
@@ -543,14 +563,117 @@ template <bool BREAK>
 __global__ void __launch_bounds__(kHaloBlock, 1024 / kHaloBlock) k_pass_a_mixed(MixedArgs a) {  // <= 64 registers
   extern __shared__ __align__(128) unsigned char sm[];
   __shared__ uint64_t bars[kHaloBlock / 32];
-  pass_a_block<BREAK, true>(a, blockIdx.x, sm, bars);
+  pass_a_block<BREAK, true>(a, a.blk0 + blockIdx.x, sm, bars);
 }
 
 template <bool DRIFT>
 __global__ void __launch_bounds__(kHaloBlock, 1024 / kHaloBlock) k_pass_b_mixed(MixedArgs a) {  // <= 64 registers
   extern __shared__ __align__(128) unsigned char sm[];
   __shared__ uint64_t bars[kHaloBlock / 32];
-  pass_b_block<DRIFT, true>(a, blockIdx.x, sm, bars);
+  pass_b_block<DRIFT, true>(a, a.blk0 + blockIdx.x, sm, bars);
+}
+
+// The last pass B of pd_step_host: no drift, the new state written by
+// particle id to the host buffers a.out_u / out_v / out_f.
+__global__ void __launch_bounds__(kHaloBlock, 1024 / kHaloBlock) k_pass_b_mixed_export(MixedArgs a) {
+  extern __shared__ __align__(128) unsigned char sm[];
+  __shared__ uint64_t bars[kHaloBlock / 32];
+  pass_b_block<false, true, true>(a, a.blk0 + blockIdx.x, sm, bars);
+}
+
+// pd_step_host's import: the positions of visiting blocks blk0 .. blk1 - 1
+// take the FP64 state of their particles from u, v, f (by particle id; the
+// same conversions as pd_set_state, k_to_mixed) and drift, as pd_set_state
+// followed by a step's first drift (k_drift_mixed).  One thread per lane of
+// each block's warps, as in the passes; holes keep their zeros.
+__global__ void __launch_bounds__(kHaloBlock) k_import_drift_mixed(MixedArgs a, int64_t blk0,
+                                                                 const double2* __restrict__ u,
+                                                                 const double2* __restrict__ v,
+                                                                 const double2* __restrict__ f) {
+  int64_t chunk = 0, base = 0;
+  int w = 0, nlive = 0;
+  const int lane = threadIdx.x & 31;
+  if (!warp_chunk(a, blk0 + blockIdx.x, &chunk, &w, &base, &nlive) || lane >= nlive) return;
+  const int64_t p = chunk * 32 + lane;
+  const int64_t i = a.member[p];
+  if (i < 0) return;
+  const double2 qu = u[i], qv = v[i], qf = f[i];
+  float4 uu, vv;
+  split2(qu.x * a.inv_ls, uu.x, uu.z);
+  split2(qu.y * a.inv_ls, uu.y, uu.w);
+  split2(qv.x * a.v_scale, vv.x, vv.z);
+  split2(qv.y * a.v_scale, vv.y, vv.w);
+  const float2 ff = make_float2((float)(qf.x * a.f_scale), (float)(qf.y * a.f_scale));
+  a.fs[p] = ff;
+  drift_mixed(a, p, vv, uu, a.tau2 * ff.x, a.tau2 * ff.y);
+  a.vs[p] = vv;
+  a.us[p] = uu;
+}
+
+// Per visiting block: the lowest and highest SELL position its bonds reach
+// (its own positions included), the lowest and highest particle id it holds,
+// and its first chunk (-1: none), for pd_step_host's slab plan.  A block's
+// positions are those of its warps' chunks (visit records), not a fixed
+// range: a tile's last block may hold fewer than kHaloBlock / 32 chunks.
+// Staged blocks read their halo list (which holds their own positions); the
+// others their slots.
+__global__ void __launch_bounds__(kHaloBlock) k_block_reach_mixed(MixedArgs a, int64_t* lo, int64_t* hi,
+                                                                 int64_t* idlo, int64_t* idhi, int64_t* cfirst) {
+  __shared__ unsigned long long s_lo, s_hi, s_idlo, s_idhi, s_c;
+  const int64_t blk = blockIdx.x;
+  if (threadIdx.x == 0) {
+    s_lo = ~0ull;
+    s_hi = 0ull;
+    s_idlo = ~0ull;
+    s_idhi = 0ull;
+    s_c = ~0ull;
+  }
+  __syncthreads();
+  int64_t chunk = 0, base = 0;
+  int w = 0, nlive = 0;
+  const int lane = threadIdx.x & 31;
+  const bool has = warp_chunk(a, blk, &chunk, &w, &base, &nlive);
+  unsigned long long mn = ~0ull, mx = 0ull;
+  if (has) {
+    if (lane == 0) atomicMin(&s_c, (unsigned long long)chunk);
+    if (lane < nlive) {
+      const int64_t p = chunk * 32 + lane;
+      const int64_t i = a.member[p];
+      if (i >= 0) {
+        atomicMin(&s_idlo, (unsigned long long)i);
+        atomicMax(&s_idhi, (unsigned long long)i);
+      }
+      mn = (unsigned long long)p;
+      mx = (unsigned long long)p;
+    }
+  }
+  const int hn = a.halo_n ? a.halo_n[blk] : -1;
+  if (hn >= 0) {
+    for (int k = threadIdx.x; k < hn; k += blockDim.x) {
+      const unsigned long long q = (unsigned long long)a.halo[blk * a.halo_cap + k];
+      mn = q < mn ? q : mn;
+      mx = q > mx ? q : mx;
+    }
+  } else if (has && lane < nlive) {
+    for (int k = 0; k < w; ++k) {
+      const int j = decode_nbr(a.nbr[base + lane + (int64_t)k * kChunk]);
+      if (j < 0) continue;
+      const unsigned long long q = (unsigned long long)a.pos_of[j];
+      mn = q < mn ? q : mn;
+      mx = q > mx ? q : mx;
+    }
+  }
+  if (mn != ~0ull) atomicMin(&s_lo, mn);
+  if (mn != ~0ull) atomicMax(&s_hi, mx);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const bool none = s_lo == ~0ull;  // a block without positions reaches nothing
+    lo[blk] = none ? -1 : (int64_t)s_lo;
+    hi[blk] = none ? -1 : (int64_t)s_hi;
+    idlo[blk] = s_idlo == ~0ull ? -1 : (int64_t)s_idlo;  // -1: no particle (holes only)
+    idhi[blk] = s_idlo == ~0ull ? -1 : (int64_t)s_idhi;
+    cfirst[blk] = s_c == ~0ull ? -1 : (int64_t)s_c;
+  }
 }
 
 // Dynamic shared memory of the single-plate passes: the larger of the int32
@@ -569,7 +692,6 @@ inline size_t pass_smem_bytes(const MixedArgs& a, bool pass_a) {
 // shared-memory hash set (open addressing, linear probing), their keys
 // compacted, sorted (bitonic) and looked up by binary search; a block with
 // more than kHaloCap distinct particles is not staged.
-__device__ __forceinline__ int decode_nbr(int v) { return v >= 0 ? v : (v <= -2 ? -2 - v : -1); }
 
 constexpr int kHaloHashBits = 12;
 constexpr int kHaloHash = 1 << kHaloHashBits;
@@ -782,11 +904,7 @@ __global__ void __launch_bounds__(kHaloBlock, 1024 / kHaloBlock)
   batch_phase_mixed<PHASE>(plates, tiles, ntiles, PHASE, sm, bars);
 }
 
-// FP64 <-> scaled two-float conversions (set/get state; not per step)
-__device__ __forceinline__ void split2(double v, float& hi, float& lo) {
-  hi = (float)v;
-  lo = (float)(v - (double)hi);
-}
+// FP64 <-> scaled two-float conversions (set/get state; not per step): split2 above
 
 // (per particle i; the scaled state of i sits at SELL position pos_of[i])
 __global__ void k_to_mixed(MixedArgs a, const double2* u, const double2* v, const double2* f) {
@@ -941,9 +1059,11 @@ void launch_drift_mixed(const MixedArgs& a, cudaStream_t s) {
 // The single-plate passes are launched with programmatic stream
 // serialization: a pass's blocks may start (and fetch what no step writes)
 // while the previous kernel on the stream drains.
-static void launch_pass_pdl(void (*kernel)(MixedArgs), const MixedArgs& a, size_t sm, cudaStream_t s) {
+static void launch_pass_pdl(void (*kernel)(MixedArgs), const MixedArgs& a, size_t sm, cudaStream_t s,
+                            bool pdl = true) {
+  if (a.nblocks <= a.blk0) return;
   cudaLaunchConfig_t lc = {};
-  lc.gridDim = dim3((unsigned)a.nblocks);
+  lc.gridDim = dim3((unsigned)(a.nblocks - a.blk0));
   lc.blockDim = dim3(kHaloBlock);
   lc.dynamicSmemBytes = sm;
   lc.stream = s;
@@ -951,7 +1071,7 @@ static void launch_pass_pdl(void (*kernel)(MixedArgs), const MixedArgs& a, size_
   at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   at[0].val.programmaticStreamSerializationAllowed = 1;
   lc.attrs = at;
-  lc.numAttrs = 1;
+  lc.numAttrs = pdl ? 1 : 0;
   cudaLaunchKernelEx(&lc, kernel, a);
 }
 
@@ -963,6 +1083,29 @@ void launch_pass_a_mixed(const MixedArgs& a, bool breaking, cudaStream_t s) {
 void launch_pass_b_mixed(const MixedArgs& a, bool drift, cudaStream_t s) {
   if (a.n <= 0) return;
   launch_pass_pdl(drift ? k_pass_b_mixed<true> : k_pass_b_mixed<false>, a, pass_smem_bytes(a, false), s);
+}
+
+// pd_step_host's slabbed launches: plain stream order (each waits on events of
+// other streams), visiting blocks a.blk0 .. a.nblocks - 1.
+void launch_slab_pass_a_mixed(const MixedArgs& a, bool breaking, cudaStream_t s) {
+  if (a.n <= 0) return;
+  launch_pass_pdl(breaking ? k_pass_a_mixed<true> : k_pass_a_mixed<false>, a, pass_smem_bytes(a, true), s, false);
+}
+
+void launch_slab_pass_b_mixed(const MixedArgs& a, bool exporting, cudaStream_t s) {
+  if (a.n <= 0) return;
+  launch_pass_pdl(exporting ? k_pass_b_mixed_export : k_pass_b_mixed<true>, a, pass_smem_bytes(a, false), s,
+                  false);
+}
+
+void launch_import_drift_mixed(const MixedArgs& a, int64_t blk0, int64_t blk1, const double2* u, const double2* v,
+                               const double2* f, cudaStream_t s) {
+  if (blk1 > blk0) k_import_drift_mixed<<<(unsigned)(blk1 - blk0), kHaloBlock, 0, s>>>(a, blk0, u, v, f);
+}
+
+void launch_block_reach_mixed(const MixedArgs& a, int64_t* lo, int64_t* hi, int64_t* idlo, int64_t* idhi,
+                              int64_t* cfirst, cudaStream_t s) {
+  if (a.nblocks > 0) k_block_reach_mixed<<<(unsigned)a.nblocks, kHaloBlock, 0, s>>>(a, lo, hi, idlo, idhi, cfirst);
 }
 
 void launch_to_mixed(const MixedArgs& a, const double2* u, const double2* v, const double2* f, cudaStream_t s) {

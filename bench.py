@@ -297,6 +297,90 @@ def accuracy(pdg, plate, device, checkpoints=(100, 500, 1000)):
     return out
 
 
+def e2e_leg(ctx, nat, comm, esteps):
+    """The step end to end through the public API: pd_step_host(1) with the
+    state in page-locked host buffers every step (read and written over the
+    CPU-GPU link inside the timed region), and the same through the
+    three-call sequence pd_set_state -> pd_step(1) -> pd_get_state."""
+    n, nb = ctx.n, ctx.nnz
+    bufs = [nat.PinnedArray((n, 2)) for _ in range(3)]
+    u, v, f = (b.array for b in bufs)
+    u[:], v[:], f[:] = ctx.state()
+    ctx.step_host(1, u, v, f)  # plans the pipeline (once per context), outside the timed region
+    comm.barrier()
+    with timed():
+        t0 = time.perf_counter()
+        for _ in range(esteps):
+            ctx.step_host(1, u, v, f)
+        secs = comm.max(time.perf_counter() - t0)
+    out = {"value": comm.sum(nb * esteps) / secs, "unit": "bond-updates/s", "ms_per_step": 1e3 * secs / esteps,
+           "h2d_bytes_per_step": 3 * 16 * n, "d2h_bytes_per_step": 3 * 16 * n, "steps": esteps,
+           "api": "pd_step_host(1): u, v, f (FP64) read from and written back to page-locked host buffers "
+                  "by the step's own kernels, every step"}
+    comm.barrier()
+    t0 = time.perf_counter()
+    for _ in range(esteps):
+        ctx._ck(nat.lib().pd_set_state(ctx.handle, nat.ptr(u), nat.ptr(v), nat.ptr(f)))
+        ctx._ck(nat.lib().pd_step(ctx.handle, 1))
+        ctx._ck(nat.lib().pd_get_state(ctx.handle, nat.ptr(u), nat.ptr(v), nat.ptr(f)))
+    secs = comm.max(time.perf_counter() - t0)
+    out["copies_api"] = {"value": comm.sum(nb * esteps) / secs, "api": "pd_set_state -> pd_step(1) -> pd_get_state"}
+    for b in bufs:
+        b.free()
+    return out
+
+
+# The reference's only published timings: one call of its velocity step on the
+# Hassa mesh (4,064 particles, 107,996 bonds) with its default bond-associated
+# weights n1 = n2 = 10 -- output/cpu_output.txt:9 (sequential computeVelocity)
+# and output/gpu_output.txt:9 (compute_velocity_GPU_host, including its
+# per-call cudaMalloc / copies / free; that kernel's results are wrong,
+# include/mechanics.cuh:165 uses the initial instead of the current position).
+REFERENCE_HASSA_CPU_S = 69.967052
+REFERENCE_HASSA_GPU_S = 0.609138
+
+
+def hassa_mesh_text():
+    """2D_Hassa_test_mesh.dat by its rule: a 70 x 60 unit grid, x in
+    [-34.5, 34.5], y in [-29.5, 29.5], unit area, x the outer loop."""
+    rows = ["Center_X Center_Y Area"]
+    for ix in range(70):
+        for iy in range(60):
+            rows.append(f"{ix - 34.5:.6f} {iy - 29.5:.6f} {1.0:.6f}")
+    return "\n".join(rows) + "\n"
+
+
+def run_bond_assoc(pdg, calls=6):
+    """The reference's published problem through the drop-in: the Hassa mesh,
+    n1 = n2 = 10, the reference GPU main's call sequence, compute_velocity_GPU_host
+    timed per call with host buffers (as the reference times it), and the same
+    step device-resident (pd_step_timed)."""
+    import tempfile
+
+    exe = os.path.join(os.path.dirname(pdg.native.LIB_PATH), "pd_hassa_timing")
+    with tempfile.TemporaryDirectory() as td:
+        open(os.path.join(td, "2D_Hassa_test_mesh.dat"), "w").write(hassa_mesh_text())
+        r = subprocess.run([exe, "10", "10", str(calls)], cwd=td, capture_output=True, text=True, timeout=600)
+    if r.returncode != 0:
+        return {"error": r.stderr[-500:]}
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    nb = d["bonds"]
+    call_s = d["median_call_s"]
+    dev_s = d["device_step_ms_median"] / 1e3
+    return {"workload": "hassa-mesh-4064-bond-associated-n1=n2=10", "particles": d["particles"], "bonds": nb,
+            "e2e": {"value": nb / call_s, "unit": "bond-updates/s", "seconds_per_call": call_s,
+                    "first_call_s": d["first_call_s"], "calls": d["calls"],
+                    "api": "compute_velocity_GPU_host (C++ drop-in, host vectors in and out every call)"},
+            "device": {"value": nb / dev_s, "unit": "bond-updates/s", "ms_per_step": d["device_step_ms_median"],
+                       "api": "pd_step_timed(1), CUDA events"},
+            "reference_published": {"cpu_s": REFERENCE_HASSA_CPU_S, "gpu_s": REFERENCE_HASSA_GPU_S,
+                                    "gpu_parity": "not parity-correct (wrong results, up to 78% off the CPU path)",
+                                    "source": "output/cpu_output.txt:9, output/gpu_output.txt:9"},
+            "speedup_e2e_vs_reference_cpu": REFERENCE_HASSA_CPU_S / call_s,
+            "speedup_e2e_vs_reference_gpu": REFERENCE_HASSA_GPU_S / call_s,
+            "speedup_first_call_vs_reference_gpu": REFERENCE_HASSA_GPU_S / d["first_call_s"]}
+
+
 def run_mixed_scale(args, pdg, device, comm):
     """The mixed form on a scale_side x scale_side plate (16M particles at 4000):
     how the bandwidth-class path holds up when nothing of the state fits L2."""
@@ -430,44 +514,25 @@ def run_ours(args, comm):
                                             "per bond take ~8x longer than the step's algorithmic HBM bytes"}
     # end to end through the public API with pinned host buffers, every step
     if not args.no_e2e:
-        esteps = min(args.steps, args.e2e_steps)
-        bufs = [nat.PinnedArray((n, 2)) for _ in range(3)]
-        u, v, f = (b.array for b in bufs)
-        got = ctx.state()
-        u[:], v[:], f[:] = got
-        comm.barrier()
-        t0 = time.perf_counter()
-        for _ in range(esteps):
-            ctx.step_host(1, u, v, f)
-        secs = comm.max(time.perf_counter() - t0)
-        result["e2e"] = {"value": comm.sum(nb * esteps) / secs, "unit": "bond-updates/s",
-                         "h2d_bytes_per_step": 3 * 16 * n, "d2h_bytes_per_step": 3 * 16 * n, "steps": esteps,
-                         "api": "pd_step_host(1): u, v, f read from and written back to page-locked host buffers "
-                                "by the step's own kernels, every step"}
-        # the same through the three-call sequence with staged copies
-        comm.barrier()
-        t0 = time.perf_counter()
-        for _ in range(esteps):
-            ctx._ck(nat.lib().pd_set_state(ctx.handle, nat.ptr(u), nat.ptr(v), nat.ptr(f)))
-            ctx._ck(nat.lib().pd_step(ctx.handle, 1))
-            ctx._ck(nat.lib().pd_get_state(ctx.handle, nat.ptr(u), nat.ptr(v), nat.ptr(f)))
-        secs = comm.max(time.perf_counter() - t0)
-        result["e2e"]["copies_api"] = {"value": comm.sum(nb * esteps) / secs,
-                                       "api": "pd_set_state -> pd_step(1) -> pd_get_state"}
-        for b in bufs:
-            b.free()
+        result["e2e"] = e2e_leg(ctx, nat, comm, min(args.steps, args.e2e_steps))
     ctx.close()
     if not args.no_mixed:
         mctx = plate.context(precision=nat.PD_MIXED, device=device)
         mvalue, mstep_ms, mkernels, mroof = measure(mctx, "mixed", args, comm)
-        mctx.close()
         result["mixed"] = {"value": mvalue, "unit": "bond-updates/s", "ms_per_step": mstep_ms,
                            "speedup_vs_fp64": mvalue / value, "dtype": "f32 bonds + f64 K^-1/det",
                            "roofline": mroof, "kernels": mkernels, "gpu_launches": 1 + 2 * args.steps}
+        if not args.no_e2e:
+            me2e = e2e_leg(mctx, nat, comm, min(args.steps, args.e2e_steps))
+            me2e["speedup_vs_fp64_e2e"] = me2e["value"] / result["e2e"]["value"] if "e2e" in result else None
+            result["mixed"]["e2e"] = me2e
+        mctx.close()
         if not args.no_accuracy and comm.rank == 0:
             result["mixed"]["accuracy_vs_fp64"] = accuracy(pdg, plate, device)
         if args.scale_side > 0:
             result["mixed_scale"] = run_mixed_scale(args, pdg, device, comm)
+    if comm.rank == 0 and not args.no_bond_assoc:
+        result["bond_assoc"] = run_bond_assoc(pdg)
     if not args.no_batch and comm.rank == 0:
         result["batch"] = run_batch(args, pdg, device)
         if not args.no_serve:
@@ -516,6 +581,7 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-bond-assoc", action="store_true")
     ap.add_argument("--scale-side", type=int, default=4000, help="mixed form on this plate too (0: skip)")
     ap.add_argument("--batch-plates", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=500)

@@ -237,3 +237,44 @@ def test_checkpoint_rejects_other_problems(pdg):
     c = p.context(precision=pdg.native.PD_MIXED)
     c.restore(blob)  # the matching context accepts it
     assert c.counters()["steps"] == 3
+
+
+@pytest.mark.parametrize("shuffle", [False, True])
+def test_mixed_step_host_equals_staged_copies(pdg, shuffle):
+    """pd_step_host on a mixed context (import + drift of each slab read over
+    the CPU-GPU link, passes in a wavefront of slabs, the last pass B writing
+    the FP64 state to the host buffers) is pd_set_state + pd_step +
+    pd_get_state, bit for bit, call after call while bonds break -- with the
+    plate numbered row-major (slabs reach their neighbours only) and randomly
+    (every slab reaches every other one)."""
+    import dataclasses
+    p = pdg.plates.make_plate(240, seed=4, crack="centre-half")
+    p.material.s_c = 2e-4
+    if shuffle:
+        perm = np.random.default_rng(3).permutation(p.n)
+        p = dataclasses.replace(p, x=np.ascontiguousarray(p.x[perm]), vol=np.ascontiguousarray(p.vol[perm]),
+                                group_of=np.ascontiguousarray(p.group_of[perm]))
+    a = p.context(precision=pdg.native.PD_MIXED)
+    b = p.context(precision=pdg.native.PD_MIXED)
+    a.step(7)
+    b.step(7)
+    u, v, f = a.state()
+    bufs = [pdg.native.PinnedArray((p.n, 2)) for _ in range(6)]
+    hu, hv, hf, ou, ov, of = (x.array for x in bufs)
+    hu[:], hv[:], hf[:] = u, v, f
+    broke = 0
+    for call, nsteps in enumerate((1, 1, 3, 1, 2, 1)):
+        a.set_state(u=hu, v=hv, f=hf)
+        a.step(nsteps)
+        ua, va, fa = a.state()
+        if call % 2:  # separate output buffers, then in place
+            b.step_host(nsteps, hu, hv, hf, ou, ov, of)
+            hu[:], hv[:], hf[:] = ou, ov, of
+        else:
+            b.step_host(nsteps, hu, hv, hf)
+        assert np.array_equal(ua, hu) and np.array_equal(va, hv) and np.array_equal(fa, hf), (call, nsteps)
+        assert np.array_equal(a.bond_mask(), b.bond_mask())
+        broke = int((b.bond_mask() == 0).sum())
+    assert broke > 0
+    for x in bufs:
+        x.free()
