@@ -334,6 +334,29 @@ def write_ref_input(path, x, vol, params, nsteps, dump_every=1, families=None, v
         fh.write(fixed.tobytes())
 
 
+def read_grid_dump(path):
+    """The `grid` dump of computeInitialPositions (oracle/ref_harness.cpp; the
+    drop-in's tests/grid_main.cpp writes the same format): each long double
+    as the pair (hi, lo) of doubles."""
+    b = open(path, "rb").read()
+    n, nd = struct.unpack_from("<ii", b, 0)
+    o = 8
+    box = np.frombuffer(b, "<f8", 4 * nd, o).reshape(2 * nd, 2).copy()
+    o += 8 * 4 * nd
+    rec = np.dtype([("gid", "<i4"), ("part", "<i4"), ("x0", "<f8", (nd, 2)), ("x", "<f8", (nd, 2)),
+                    ("vol", "<f8", (2,))])
+    r = np.frombuffer(b, rec, n, o)
+    return {"n": n, "ndim": nd, "boxlimit": box, "gid": r["gid"].copy(), "part": r["part"].copy(),
+            "x0": r["x0"].copy(), "x": r["x"].copy(), "vol": r["vol"].copy()}
+
+
+def run_ref_grid(rows, dx, ndim, out_path):
+    """The reference's computeInitialPositions (oracle/ref_harness.cpp, mode `grid`)."""
+    subprocess.run([REF_HARNESS, "grid", str(rows), repr(dx), str(ndim), out_path], check=True,
+                   capture_output=True)
+    return read_grid_dump(out_path)
+
+
 def run_ref_plate(in_path, out_path, timeout=3600):
     subprocess.run([REF_HARNESS, "plate", in_path, out_path], check=True, timeout=timeout,
                    stdout=subprocess.DEVNULL)

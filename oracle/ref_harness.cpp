@@ -26,6 +26,13 @@
 //       main does (tensileStrength / E, :659-673), called on two imposed
 //       displacement fields in turn (mazars_field below); dumps u, the bond
 //       thresholds, bond damage and damageStatus after each call.
+//   grid <numParticlesRow> <dx> <ndim> <out.bin>
+//       the reference's computeInitialPositions (src/SetupParticleSystem.cpp:
+//       62-98); dumps int32 n, int32 ndim, then boxlimit[2 ndim], and per
+//       particle int32 globalID, int32 partitionID, initialPositions[ndim],
+//       currentPositions[ndim], volume -- every long double v as two doubles
+//       hi = (double)v, lo = (double)(v - hi) (exact for x86's 64-bit
+//       extended mantissa).
 //
 // Never part of the product: only tests/ and the fixture script run it.
 #include <cstdint>
@@ -220,6 +227,33 @@ int main(int argc, char** argv) {
         outputLocalParticlesPositions(0, pb.P, 2, 0);
       }
       dump_step(w, s + 1, pb.P, vel, netF, acce);
+    }
+    fclose(fo);
+    return 0;
+  }
+  if (mode == "grid") {
+    if (argc != 6) { fprintf(stderr, "grid <numParticlesRow> <dx> <ndim> <out.bin>\n"); return 2; }
+    const int rows = atoi(argv[2]), ndim = atoi(argv[4]);
+    const long double dx = strtold(argv[3], nullptr);
+    vector<long double> boxlimit(2 * ndim);
+    vector<Particle> P = computeInitialPositions(rows, dx, ndim, boxlimit);
+    FILE* fo = fopen(argv[5], "wb");
+    if (!fo) { perror("out"); return 2; }
+    Writer w{fo};
+    auto ld = [&](long double v) {
+      const double hi = (double)v;
+      w.put<double>(hi);
+      w.put<double>((double)(v - (long double)hi));
+    };
+    w.put<int32_t>((int32_t)P.size());
+    w.put<int32_t>(ndim);
+    for (long double b : boxlimit) ld(b);
+    for (const auto& p : P) {
+      w.put<int32_t>(p.globalID);
+      w.put<int32_t>(p.partitionID);
+      for (int d = 0; d < ndim; ++d) ld(p.initialPositions[d]);
+      for (int d = 0; d < ndim; ++d) ld(p.currentPositions[d]);
+      ld(p.volume);
     }
     fclose(fo);
     return 0;

@@ -28,6 +28,10 @@ Steps, each recorded in manifest.json:
  5. The reference's Mazars damage (computeDamageStatus) on the Hassa mesh,
     classic and n1 = n2 = 10 weights, at two imposed displacement fields in
     turn -> mazars_ref.npz.  `--only mazars` regenerates just this one.
+ 7. The reference's computeInitialPositions (src/SetupParticleSystem.cpp:62-98)
+    on grids of 1, 2 and 3 dimensions, odd and even rows (`--only grid`)
+    -> grid_ref.npz: every particle's ids, positions and volume and the box
+    limits, long doubles as (hi, lo) double pairs.
  6. The reference's own step with its own model (no zero-energy-mode
     penalty, no bond breaking) on the benchmark plates (`--only plates`):
     the config-1 100 x 100 plate (plates.config_plate_100(seed=0)) for 3
@@ -159,7 +163,7 @@ def fixtures_plates(td, man):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=po.reference_dir())
-    ap.add_argument("--only", choices=["mazars", "plates"], default=None)
+    ap.add_argument("--only", choices=["mazars", "plates", "grid"], default=None)
     args = ap.parse_args()
     ref = args.reference
     if not po.ref_available() or not ref:
@@ -178,11 +182,30 @@ def main():
             fixtures_plates(td, man)
         if args.only in (None, "mazars"):
             fixtures_mazars(td, mesh_dir, man)
+        if args.only in (None, "grid"):
+            fixtures_grid(td, man)
     json.dump(man, open(man_path, "w"), indent=1, sort_keys=True)
     print(json.dumps(man, indent=1, sort_keys=True))
     bad = [k for k, v in man.items() if v is False]
     if bad:
         sys.exit(f"pinning failed: {bad}")
+
+
+# (numParticlesRow, dx, ndim): the config-1 plate's 100 x 100 at 1e-3, odd
+# and even rows, dx not a power of two, and the 1D and 3D branches
+GRID_CASES = [(100, 1e-3, 2), (7, 0.5, 2), (8, 0.3, 2), (5, 1.0, 1), (5, 0.1, 3), (4, 2.5e-4, 3)]
+
+
+def fixtures_grid(td, man):
+    out = {}
+    for k, (rows, dx, nd) in enumerate(GRID_CASES):
+        r = po.run_ref_grid(rows, dx, nd, os.path.join(td, f"grid{k}.bin"))
+        for key in ("boxlimit", "gid", "part", "x0", "x", "vol"):
+            out[f"c{k}_{key}"] = r[key]
+    out["cases"] = np.array(GRID_CASES, dtype=object).astype(str)
+    np.savez_compressed(os.path.join(HERE, "grid_ref.npz"), **out)
+    man["grid"] = {"function": "computeInitialPositions (src/SetupParticleSystem.cpp:62-98)",
+                   "cases": [list(c) for c in GRID_CASES], "long_double": "(hi, lo) double pairs"}
 
 
 def fixtures_mazars(td, mesh_dir, man):

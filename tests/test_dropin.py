@@ -55,6 +55,36 @@ def test_dropin_driver_compiles(pdg, tmp_path):
     assert os.path.exists(_build_driver(pdg, str(tmp_path)))
 
 
+def test_dropin_compute_initial_positions_matches_reference(pdg, tmp_path):
+    """computeInitialPositions against the reference function's own output
+    (tests/golden/grid_ref.npz, src/SetupParticleSystem.cpp:62-98): ids,
+    initial and current positions, volumes and box limits at full long double
+    precision, on 1D, 2D and 3D grids with odd and even rows.  No GPU call."""
+    import platform
+
+    import pd_oracle as po
+
+    g = np.load(os.path.join(GOLDEN, "grid_ref.npz"))
+    exe = os.path.join(str(tmp_path), "grid_main")
+    libdir = os.path.dirname(pdg.native.LIB_PATH)
+    subprocess.run(["g++", "-O2", "-std=c++17", f"-I{os.path.join(ROOT, 'include')}",
+                    os.path.join(ROOT, "tests", "grid_main.cpp"), "-o", exe, f"-L{libdir}", "-lpd_dropin",
+                    "-lpd_gb300", f"-Wl,-rpath,{libdir}"], check=True)
+    # the fixture's (hi, lo) pairs hold x86's 64-bit extended mantissa exactly; elsewhere long
+    # double differs, so only the double-rounded values (hi) must agree
+    full = platform.machine() in ("x86_64", "AMD64")
+    for k, case in enumerate(g["cases"]):
+        rows, dx, nd = int(case[0]), case[1], int(case[2])
+        out = os.path.join(str(tmp_path), f"grid{k}.bin")
+        subprocess.run([exe, str(rows), dx, str(nd), out], check=True)
+        r = po.read_grid_dump(out)
+        assert r["n"] == rows ** nd and r["ndim"] == nd
+        assert np.array_equal(r["gid"], g[f"c{k}_gid"]) and np.array_equal(r["part"], g[f"c{k}_part"])
+        for key in ("boxlimit", "x0", "x", "vol"):
+            a, b = r[key], g[f"c{k}_{key}"]
+            assert np.array_equal(a if full else a[..., 0], b if full else b[..., 0]), (case, key)
+
+
 @pytest.mark.gpu
 def test_dropin_reference_default_weights(pdg, hassa, tmp_path):
     """The reference main's own defaults, n1 = n2 = 10 (bond-associated), one
