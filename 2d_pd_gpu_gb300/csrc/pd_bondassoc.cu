@@ -10,13 +10,22 @@
 // with the net force f_i = sum_j (T_ij - T_ji) V_j (computeVelocity :396-470).
 // The reference recomputes sigma_b K_b^-1 inside the (i, j) loop (O(n^3) per
 // particle).  Here pass A forms P_b = sigma_b K_b^-1 once per bond and T_ij
-// once per bond (O(n^2) per particle, family <= 64 bonds, kept in local
-// memory), storing T per bond slot; pass B reads T_ji through the reverse
-// slot index and applies the kick (+ the next drift) as the classic form.
-// Arithmetic follows the oracle's ba_pass_a / ba_pass_b (--fmad=false, the
-// same explicit fma() calls); exp/pow are CUDA's, so the two agree to
-// rounding (not bit for bit) in this mode.  No bond breaking here (the
-// reference has none).
+// once per bond (O(n^2) per particle), storing T per bond slot; pass B reads
+// T_ji through the reverse slot index and applies the kick (+ the next
+// drift) as the classic form.
+//
+// Pass A runs one warp per particle and one lane per bond (families <= 64
+// bonds, two per lane): the family's bond data is staged in shared memory,
+// lane q sums K_q and D_q over k in family order (the oracle's order), and,
+// once the P_b of every bond are in shared memory, lane j sums T_ij over b.
+// The weight is evaluated in factored form: exp(-n1 |L_b - L_k| / l) =
+// e+(min L) e-(max L) with e+-(L) = exp(+-n1 L / l) per bond, the cosine as
+// (xi_b . xi_k) (1/L_b)(1/L_k), and an integer n2 <= 64 by repeated squaring
+// (pow otherwise; the direct exp where n1 L / l could overflow).  The terms
+// are those of the oracle's ba_pass_a (--fmad=false, explicit fma()); the
+// weights differ from its libm exp / pow / division by a few ulp, so GPU and
+// oracle agree to rounding (1e-12 normwise), not bit for bit.  No bond
+// breaking here (the reference has none).
 #include "pd_internal.h"
 
 namespace pd {
@@ -24,59 +33,108 @@ namespace pd {
 namespace {
 
 constexpr int kBaMax = 64;
+constexpr int kBaWarps = 4;  // particles per block of pass A
 
-__device__ __forceinline__ double ba_weight(double n1, double n2, double inv_wlen, double bx, double by, double lb,
-                                            double kx, double ky, double lk) {
-  double c = (bx * kx + by * ky) / (lb * lk);
-  if (c > 1.0) c = 1.0;
-  else if (c < -1.0) c = -1.0;
-  const double lr = fabs(lb - lk) * inv_wlen;
-  return exp(-n1 * lr) * pow(0.5 + 0.5 * c, n2);
-}
+struct BaFamily {  // one particle's bonds, in family order
+  double ex[kBaMax], ey[kBaMax], rl[kBaMax], len[kBaMax], ep[kBaMax], em[kBaMax], vv[kBaMax], dx[kBaMax],
+      dy[kBaMax];
+  double P[kBaMax][4];
+  int64_t slot[kBaMax];
+};
 
-__global__ void __launch_bounds__(128) k_ba_pass_a(Fp64Args a, BondAssoc b) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
+struct BaWeight {
+  double n1, inv_wlen, n2;
+  int n2i;      // n2 as a small integer (-1: use pow)
+  bool direct;  // exp(-n1 |L_b - L_k| / l) evaluated directly (the factors could overflow)
+  __device__ __forceinline__ double operator()(const BaFamily& F, int b, int k) const {
+    double c = fma(F.ex[b], F.ex[k], F.ey[b] * F.ey[k]) * (F.rl[b] * F.rl[k]);
+    c = c > 1.0 ? 1.0 : (c < -1.0 ? -1.0 : c);
+    const double x = fma(0.5, c, 0.5);
+    double pw;
+    if (n2i >= 0) {
+      pw = 1.0;
+      double base = x;
+      for (int e = n2i; e; e >>= 1) {
+        if (e & 1) pw *= base;
+        base *= base;
+      }
+    } else {
+      pw = pow(x, n2);
+    }
+    double ew;
+    if (direct)
+      ew = exp(-n1 * (fabs(F.len[b] - F.len[k]) * inv_wlen));
+    else
+      ew = F.len[b] >= F.len[k] ? F.ep[k] * F.em[b] : F.ep[b] * F.em[k];
+    return ew * pw;
+  }
+};
+
+__global__ void __launch_bounds__(32 * kBaWarps) k_ba_pass_a(Fp64Args a, BondAssoc b) {
+  __shared__ BaFamily fam[kBaWarps];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t i = (int64_t)blockIdx.x * kBaWarps + warp;
+  if (i >= a.n) return;  // warp-uniform
+  BaFamily& F = fam[warp];
   const int64_t c0 = i >> 5;
   const int w = a.chunk_w[c0];
   const int64_t s0 = a.chunk_base[c0] + (i & 31);
-  double ex[kBaMax], ey[kBaMax], el[kBaMax], vv[kBaMax], dx[kBaMax], dy[kBaMax], P[kBaMax][4];
-  int64_t slot[kBaMax];
   const double2 ui = a.u[i];
-  double vh = 0.0;
+  BaWeight wf;
+  wf.n1 = b.n1;
+  wf.inv_wlen = b.inv_wlen;
+  wf.n2 = b.n2;
+  wf.n2i = (b.n2 >= 0.0 && b.n2 <= 64.0 && b.n2 == floor(b.n2)) ? (int)b.n2 : -1;
+  // stage the family (slots k = lane, lane + 32, compacted past empty slots in order)
   int n = 0;
-  for (int k = 0; k < w && n < kBaMax; ++k) {
+  double lmax = 0.0;
+  for (int k0 = 0; k0 < w; k0 += 32) {
+    const int k = k0 + lane;
     const int64_t s = s0 + (int64_t)k * kChunk;
-    const int j = a.nbr[s];
-    if (j < 0) continue;
-    const double2 e = a.bxi[s];
-    const double2 uj = a.u[j];
-    ex[n] = e.x;
-    ey[n] = e.y;
-    el[n] = sqrt(e.x * e.x + e.y * e.y);
-    vv[n] = a.vol[j];
-    dx[n] = uj.x - ui.x;
-    dy[n] = uj.y - ui.y;
-    vh = vh + vv[n];
-    slot[n] = s;
-    ++n;
+    const int j = k < w ? a.nbr[s] : -1;
+    const unsigned m = __ballot_sync(0xffffffffu, j >= 0);
+    const int q = n + __popc(m & ((1u << lane) - 1u));
+    if (j >= 0 && q < kBaMax) {
+      const double2 e = a.bxi[s];
+      const double2 uj = a.u[j];
+      const double l = sqrt(e.x * e.x + e.y * e.y);
+      F.ex[q] = e.x;
+      F.ey[q] = e.y;
+      F.len[q] = l;
+      F.rl[q] = 1.0 / l;
+      F.ep[q] = exp(b.n1 * (l * b.inv_wlen));
+      F.em[q] = exp(-b.n1 * (l * b.inv_wlen));
+      F.vv[q] = a.vol[j];
+      F.dx[q] = uj.x - ui.x;
+      F.dy[q] = uj.y - ui.y;
+      F.slot[q] = s;
+      lmax = fmax(lmax, l);
+    }
+    n += __popc(m);
   }
-  for (int q = 0; q < n; ++q) {
+  n = n < kBaMax ? n : kBaMax;
+  for (int o = 16; o; o >>= 1) lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+  wf.direct = !(fabs(b.n1) * lmax * b.inv_wlen < 600.0);
+  __syncwarp();
+  // P_b = sigma_b K_b^-1 of bond q
+  for (int q = lane; q < n; q += 32) {
     double k11 = 0.0, k12 = 0.0, k22 = 0.0, d11 = 0.0, d12 = 0.0, d21 = 0.0, d22 = 0.0;
     for (int k = 0; k < n; ++k) {
-      const double wv = ba_weight(b.n1, b.n2, b.inv_wlen, ex[q], ey[q], el[q], ex[k], ey[k], el[k]) * vv[k];
-      const double t0 = wv * ex[k], t1 = wv * ey[k];
-      k11 = fma(t0, ex[k], k11);
-      k12 = fma(t0, ey[k], k12);
-      k22 = fma(t1, ey[k], k22);
-      d11 = fma(dx[k], t0, d11);
-      d12 = fma(dx[k], t1, d12);
-      d21 = fma(dy[k], t0, d21);
-      d22 = fma(dy[k], t1, d22);
+      const double wv = wf(F, q, k) * F.vv[k];
+      const double ekx = F.ex[k], eky = F.ey[k];
+      const double t0 = wv * ekx, t1 = wv * eky;
+      k11 = fma(t0, ekx, k11);
+      k12 = fma(t0, eky, k12);
+      k22 = fma(t1, eky, k22);
+      const double dkx = F.dx[k], dky = F.dy[k];
+      d11 = fma(dkx, t0, d11);
+      d12 = fma(dkx, t1, d12);
+      d21 = fma(dky, t0, d21);
+      d22 = fma(dky, t1, d22);
     }
     const double det = fma(k11, k22, -(k12 * k12));
     if (!(det > a.det_guard * (k11 * k22))) {
-      P[q][0] = P[q][1] = P[q][2] = P[q][3] = 0.0;
+      F.P[q][0] = F.P[q][1] = F.P[q][2] = F.P[q][3] = 0.0;
       continue;
     }
     const double r = 1.0 / det;
@@ -87,22 +145,27 @@ __global__ void __launch_bounds__(128) k_ba_pass_a(Fp64Args a, BondAssoc b) {
     const double s11 = fma(a.c11, e11, a.c12 * e22);
     const double s22 = fma(a.c12, e11, a.c11 * e22);
     const double s12 = a.c33 * e12;
-    P[q][0] = fma(s11, q11, s12 * q12);
-    P[q][1] = fma(s11, q12, s12 * q22);
-    P[q][2] = fma(s12, q11, s22 * q12);
-    P[q][3] = fma(s12, q12, s22 * q22);
+    F.P[q][0] = fma(s11, q11, s12 * q12);
+    F.P[q][1] = fma(s11, q12, s12 * q22);
+    F.P[q][2] = fma(s12, q11, s22 * q12);
+    F.P[q][3] = fma(s12, q12, s22 * q22);
   }
+  // V_h in family order (as the oracle), then T_ij of bond jj
+  double vh = 0.0;
+  for (int k = 0; k < n; ++k) vh = vh + F.vv[k];
+  __syncwarp();
   const double rv = 1.0 / vh;
-  for (int jj = 0; jj < n; ++jj) {
+  for (int jj = lane; jj < n; jj += 32) {
     double m11 = 0.0, m12 = 0.0, m21 = 0.0, m22 = 0.0;
     for (int q = 0; q < n; ++q) {
-      const double wv = ba_weight(b.n1, b.n2, b.inv_wlen, ex[jj], ey[jj], el[jj], ex[q], ey[q], el[q]) * vv[q];
-      m11 = fma(wv, P[q][0], m11);
-      m12 = fma(wv, P[q][1], m12);
-      m21 = fma(wv, P[q][2], m21);
-      m22 = fma(wv, P[q][3], m22);
+      const double wv = wf(F, jj, q) * F.vv[q];
+      m11 = fma(wv, F.P[q][0], m11);
+      m12 = fma(wv, F.P[q][1], m12);
+      m21 = fma(wv, F.P[q][2], m21);
+      m22 = fma(wv, F.P[q][3], m22);
     }
-    b.tb[slot[jj]] = make_double2(fma(m11 * rv, ex[jj], (m12 * rv) * ey[jj]), fma(m21 * rv, ex[jj], (m22 * rv) * ey[jj]));
+    const double ex = F.ex[jj], ey = F.ey[jj];
+    b.tb[F.slot[jj]] = make_double2(fma(m11 * rv, ex, (m12 * rv) * ey), fma(m21 * rv, ex, (m22 * rv) * ey));
   }
 }
 
@@ -198,7 +261,7 @@ void launch_ba_reverse(const Fp64Args& a, const BondAssoc& b, cudaStream_t s) {
 }
 
 void launch_ba_pass_a(const Fp64Args& a, const BondAssoc& b, cudaStream_t s) {
-  if (a.n > 0) k_ba_pass_a<<<(unsigned)blocks_for(a.n, 128), 128, 0, s>>>(a, b);
+  if (a.n > 0) k_ba_pass_a<<<(unsigned)((a.n + kBaWarps - 1) / kBaWarps), 32 * kBaWarps, 0, s>>>(a, b);
 }
 
 void launch_ba_pass_b(const Fp64Args& a, const BondAssoc& b, int mode, cudaStream_t s) {

@@ -138,6 +138,8 @@ _SIGS = {
     "pd_batch_set_barrier_limits": [_vp, ctypes.c_uint64, ctypes.c_uint32],
     "pd_batch_last_step_ms": [_vp, ctypes.POINTER(ctypes.c_float)],
     "pd_probe_fma_rates": [ctypes.c_int32, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
+    "pd_probe_link_rates": [ctypes.c_int32, ctypes.c_int64, ctypes.POINTER(ctypes.c_double),
+                            ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
     "pd_host_alloc": [ctypes.c_int64, ctypes.POINTER(_vp)],
     "pd_host_free": [_vp],
 }
@@ -206,6 +208,16 @@ def probe_fma_rates(device=0):
     if rc != PD_OK:
         raise PdError(rc, "pd_probe_fma_rates failed")
     return a.value, b.value
+
+
+def probe_link_rates(nbytes, device=0):
+    """Measured copy-engine GB/s of nbytes between page-locked host memory and
+    the device: (host to device, device to host, each while both run)."""
+    a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    rc = lib().pd_probe_link_rates(device, int(nbytes), ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+    if rc != PD_OK:
+        raise PdError(rc, "pd_probe_link_rates failed")
+    return a.value, b.value, c.value
 
 
 class Context:

@@ -297,7 +297,7 @@ def accuracy(pdg, plate, device, checkpoints=(100, 500, 1000)):
     return out
 
 
-def e2e_leg(ctx, nat, comm, esteps):
+def e2e_leg(ctx, nat, comm, esteps, device):
     """The step end to end through the public API: pd_step_host(1) with the
     state in page-locked host buffers every step (read and written over the
     CPU-GPU link inside the timed region), and the same through the
@@ -327,6 +327,11 @@ def e2e_leg(ctx, nat, comm, esteps):
     out["copies_api"] = {"value": comm.sum(nb * esteps) / secs, "api": "pd_set_state -> pd_step(1) -> pd_get_state"}
     for b in bufs:
         b.free()
+    # the link bound: the step's bytes each way at the measured concurrent copy rate
+    h2d, d2h, both = nat.probe_link_rates(3 * 16 * n, device)
+    out["link"] = {"h2d_gbs": h2d, "d2h_gbs": d2h, "both_gbs_per_direction": both,
+                   "bound_ms_per_step": 3 * 16 * n / (both * 1e9) * 1e3,
+                   "source": "pd_probe_link_rates: copy engines, page-locked buffers of the step's size"}
     return out
 
 
@@ -514,7 +519,7 @@ def run_ours(args, comm):
                                             "per bond take ~8x longer than the step's algorithmic HBM bytes"}
     # end to end through the public API with pinned host buffers, every step
     if not args.no_e2e:
-        result["e2e"] = e2e_leg(ctx, nat, comm, min(args.steps, args.e2e_steps))
+        result["e2e"] = e2e_leg(ctx, nat, comm, min(args.steps, args.e2e_steps), device)
     ctx.close()
     if not args.no_mixed:
         mctx = plate.context(precision=nat.PD_MIXED, device=device)
@@ -523,7 +528,7 @@ def run_ours(args, comm):
                            "speedup_vs_fp64": mvalue / value, "dtype": "f32 bonds + f64 K^-1/det",
                            "roofline": mroof, "kernels": mkernels, "gpu_launches": 1 + 2 * args.steps}
         if not args.no_e2e:
-            me2e = e2e_leg(mctx, nat, comm, min(args.steps, args.e2e_steps))
+            me2e = e2e_leg(mctx, nat, comm, min(args.steps, args.e2e_steps), device)
             me2e["speedup_vs_fp64_e2e"] = me2e["value"] / result["e2e"]["value"] if "e2e" in result else None
             result["mixed"]["e2e"] = me2e
         mctx.close()

@@ -342,6 +342,12 @@ int pd_profile_steps(pd_ctx* ctx, int32_t nsteps, double* ms, int64_t* launches)
  * counterpart. */
 int pd_probe_fma_rates(int32_t device, double* fp64_fma_per_s, double* fp32_fma_per_s);
 
+/* Measured copy-engine rates (GB/s) of `bytes` (16 B .. 4 GiB) between
+ * page-locked host memory and the device: host to device alone, device to
+ * host alone, and each direction while both run at once -- the link bound of
+ * pd_step_host.  Allocates its own buffers.  No reference counterpart. */
+int pd_probe_link_rates(int32_t device, int64_t bytes, double* h2d_gbs, double* d2h_gbs, double* both_gbs);
+
 /* Algorithmic bytes per step of the dominant kernels (fixed byte model:
  * FP64 248 B/particle + 11 B/bond, mixed 148 B/particle + 11 B/bond). */
 int pd_model_bytes(const pd_ctx* ctx, double* bytes_per_step);
