@@ -26,6 +26,7 @@ struct pd_ctx {
   double cutoff = 0.0;        // family cutoff (0 if families came from the host)
   // mixed-form scales: lengths / Ls, volumes / Vs, stresses / Es
   double ls = 1.0, vs_scale = 1.0;
+  bool uniform_v = false;  // mixed form: every (float)(V_i / Vs) is exactly 1
 
   // per particle
   double2 *x = nullptr, *u = nullptr, *v = nullptr, *f = nullptr, *acc = nullptr;
@@ -330,6 +331,7 @@ pd::MixedArgs mixed_args(pd_ctx* c) {
   a.k_hg = (float)(c->p.k_hg * c->vs_scale * c->ls * c->ls / es);
   a.inv_ls = 1.0 / c->ls;
   a.inv_vs = 1.0 / c->vs_scale;
+  a.uniform_v = c->uniform_v ? 1 : 0;
   a.v_scale = c->p.dt / c->ls;
   a.f_scale = c->ls / es;
   a.det_guard = c->p.det_guard;
@@ -427,6 +429,13 @@ int finish_families(pd_ctx* c) {
     for (double v : c->h_vol) vsum += v;
     c->ls = ls;
     c->vs_scale = c->n > 0 ? vsum / (double)c->n : 1.0;
+    // the scaled volumes as k_positions_mixed forms them: (float)(V_i * (1 / Vs))
+    c->uniform_v = c->n > 0;
+    for (double v : c->h_vol)
+      if ((float)(v * (1.0 / c->vs_scale)) != 1.0f) {
+        c->uniform_v = false;
+        break;
+      }
     const int rch = pd::build_halo_mixed(mixed_args(c), c->sell.nslots, nblocks, blocks.p, c->sell.rk, s, &c->halo,
                                          &msg);
     if (rch != PD_OK) return fail(c, rch, msg);

@@ -177,6 +177,7 @@ struct MixedArgs {
   double2* out_v;
   double2* out_f;
   int64_t blk0;
+  int32_t uniform_v;  // every particle's V^ is exactly 1 (pass A leaves the V^ gathers out)
 };
 
 // ---- family build (pd_family.cu)

@@ -193,12 +193,16 @@ __device__ __forceinline__ PreA load_a(const MixedArgs& a, int64_t p) {
 // gives a slot's neighbour (a particle id, -1 for padding or broken; or, when
 // the data is staged, a halo entry, the particle's own for padding or
 // broken) and gather(j) its data.
-template <bool BREAK, typename Idx, typename Gather>
+// UV: every particle's V^ is 1 (uniform volumes; the host checks that
+// (float)(V_i / Vs) == 1 for all i): the V^ gathers and products are left
+// out, which changes no result -- x * 1 and fma(1, x, y) are exact.
+template <bool BREAK, bool UV, typename Idx, typename Gather>
 __device__ __forceinline__ void pass_a_core(const MixedArgs& a, int64_t p, const PreA& pre, int w, int64_t s0, Idx idx,
                                             Gather gather) {
   const float4 ui = pre.ui, xi = pre.xi;
   int newly = 0;
   const float2 nxh = f2(-xi.x, -xi.y), nxl = f2(-xi.z, -xi.w), nuh = f2(-ui.x, -ui.y), nul = f2(-ui.z, -ui.w);
+  const float2 ns2 = f2(-a.s2, -a.s2);
   float2 D1 = f2(0.f, 0.f), D2 = f2(0.f, 0.f), A = f2(0.f, 0.f);  // (d11, d12), (d21, d22), (ax, ay)
   // 2 slots at a time: the halo walk reads shared memory, whose short latency needs less
   // memory-level parallelism than global gathers did, and at 64 registers 4 blocks fit an
@@ -206,10 +210,9 @@ __device__ __forceinline__ void pass_a_core(const MixedArgs& a, int64_t p, const
   walk_bonds<2>(w, 0, idx, gather, [&](int k, int j, const NbA& nb) {
     const float2 e = tf_diff2(nb.x, nxh, nxl);  // xi^
     const float2 d = tf_diff2(nb.u, nuh, nul);  // du^
-    if (BREAK) {
-      const float2 q = mul2(d, fma2(f2(2.f, 2.f), e, d));  // d . (2 xi + d)
-      const float2 ee = mul2(e, e);
-      if (q.x + q.y > a.s2 * (ee.x + ee.y)) {
+    if (BREAK) {  // d . (2 xi + d) - s2 xi . xi > 0, per component with one rounding
+      const float2 r = fma2(ns2, mul2(e, e), mul2(d, fma2(f2(2.f, 2.f), e, d)));
+      if (r.x + r.y > 0.f) {
         const int64_t s = s0 + (int64_t)k * kChunk;
         a.nbr[s] = -2 - a.nbr[s];  // the particle id of slot s (j may be a halo position)
         if (a.loc) a.loc[s] = (uint16_t)pre.self_l;  // the slot now adds exact zeros
@@ -217,11 +220,17 @@ __device__ __forceinline__ void pass_a_core(const MixedArgs& a, int64_t p, const
         return;
       }
     }
-    const float2 vv = f2(nb.v, nb.v);
-    const float2 t = mul2(vv, e);
-    D1 = fma2(f2(d.x, d.x), t, D1);
-    D2 = fma2(f2(d.y, d.y), t, D2);
-    A = fma2(vv, d, A);
+    if (UV) {
+      D1 = fma2(f2(d.x, d.x), e, D1);
+      D2 = fma2(f2(d.y, d.y), e, D2);
+      A = add2(A, d);
+    } else {
+      const float2 vv = f2(nb.v, nb.v);
+      const float2 t = mul2(vv, e);
+      D1 = fma2(f2(d.x, d.x), t, D1);
+      D2 = fma2(f2(d.y, d.y), t, D2);
+      A = fma2(vv, d, A);
+    }
   });
   const float d11 = D1.x, d12 = D1.y, d21 = D2.x, d22 = D2.y;
   a.hgs[p] = make_float2(2.f * a.k_hg * A.x, 2.f * a.k_hg * A.y);
@@ -302,18 +311,19 @@ __device__ __forceinline__ void pass_b_core(const MixedArgs& a, int64_t p, const
   const float4 wi = pre.wi, xi = pre.xi;
   const float2 m = pre.m, h = pre.h;
   // W columns c1 = (W11, W21), c2 = (W12, W22): W v = c1 v.x + c2 v.y
-  // compensated (TwoSum) sums S + C of both components at once
+  // compensated (Kahan) sums S - C of both components at once: C carries
+  // the rounding error of every addition into the next term
   float2 S = fma2(f2(wi.x, wi.y), f2(m.x, m.x), fma2(f2(wi.z, wi.w), f2(m.y, m.y), h)), C = f2(0.f, 0.f);
   const float2 nxh = f2(-xi.x, -xi.y), nxl = f2(-xi.z, -xi.w);
   walk_bonds<4>(w, 0, idx, gather, [&](int, int, const NbB& nb) {
     const float2 e = tf_diff2(nb.x, nxh, nxl);
     const float2 p = fma2(f2(nb.w.x, nb.w.y), f2(e.x, e.x), mul2(f2(nb.w.z, nb.w.w), f2(e.y, e.y)));
-    const float2 s = add2(S, p);
-    const float2 z = sub2(s, S);
-    C = add2(C, add2(sub2(S, sub2(s, z)), sub2(p, z)));
-    S = s;
+    const float2 y = sub2(p, C);
+    const float2 t = add2(S, y);
+    C = sub2(sub2(t, S), y);
+    S = t;
   });
-  const float fx = S.x + C.x, fy = S.y + C.y;
+  const float fx = S.x - C.x, fy = S.y - C.y;
   const float2 fo = pre.fo;
   const float aox = a.tau2 * fo.x, aoy = a.tau2 * fo.y;
   const float anx = a.tau2 * fx, any = a.tau2 * fy;
@@ -452,7 +462,7 @@ __device__ __forceinline__ void for_halo(const int32_t* H, int hn, int (&g)[kHal
 // shared memory.  False if a staged copy timed out.  PDL: the pass may start
 // before the previous one has finished; until grid_dep_sync() it reads only
 // the visit record and the first halo ids, which no step writes.
-template <bool BREAK, bool PDL = false>
+template <bool BREAK, bool PDL = false, bool UV = false>
 __device__ __forceinline__ bool pass_a_block(const MixedArgs& a, int64_t blk, unsigned char* sm, uint64_t* bars) {
   int64_t chunk = 0, base = 0;
   int w = 0, nlive = 0;
@@ -474,7 +484,7 @@ __device__ __forceinline__ bool pass_a_block(const MixedArgs& a, int64_t blk, un
     if (w > 0 && lane == 0) stage_issue(mine, a.nbr + base, (uint32_t)w * 128u, &bars[warp]);
     __syncwarp();
     if (!warp_stage_done(a, &bars[warp], w)) return false;
-    if (live) pass_a_core<BREAK>(a, p, pre, w, base + lane, SharedIdx{mine, lane}, GatherA{&a});
+    if (live) pass_a_core<BREAK, UV>(a, p, pre, w, base + lane, SharedIdx{mine, lane}, GatherA{&a});
     return true;
   }
   const HaloSmem h = halo_smem(a, sm);
@@ -484,7 +494,7 @@ __device__ __forceinline__ bool pass_a_block(const MixedArgs& a, int64_t blk, un
   for_halo(H, hn, g, [&](int k, int j) {
     cp_async16(&h.q0[k], &a.us[j]);
     cp_async16(&h.q1[k], &a.xs[j]);
-    cp_async4(&h.vh[k], &a.vh[j]);
+    if (!UV) cp_async4(&h.vh[k], &a.vh[j]);
   });
   cp_async_wait_all();
   __syncthreads();
@@ -494,7 +504,7 @@ __device__ __forceinline__ bool pass_a_block(const MixedArgs& a, int64_t blk, un
   const float4* q0 = h.q0;
   const float4* q1 = h.q1;
   const float* vh = h.vh;
-  pass_a_core<BREAK>(a, p, pre, w, base + lane, SharedHaloIdx{h.li + warp * a.wmax * 32, lane},
+  pass_a_core<BREAK, UV>(a, p, pre, w, base + lane, SharedHaloIdx{h.li + warp * a.wmax * 32, lane},
                      [=](int64_t l) { return NbA{q0[l], q1[l], vh[l]}; });
   return true;
 }
@@ -559,11 +569,11 @@ __device__ __forceinline__ void drift_block(const MixedArgs& a, int64_t blk) {
   if (lane < nlive) drift_particle_mixed(a, chunk * 32 + lane);
 }
 
-template <bool BREAK>
+template <bool BREAK, bool UV>
 __global__ void __launch_bounds__(kHaloBlock, 1024 / kHaloBlock) k_pass_a_mixed(MixedArgs a) {  // <= 64 registers
   extern __shared__ __align__(128) unsigned char sm[];
   __shared__ uint64_t bars[kHaloBlock / 32];
-  pass_a_block<BREAK, true>(a, a.blk0 + blockIdx.x, sm, bars);
+  pass_a_block<BREAK, true, UV>(a, a.blk0 + blockIdx.x, sm, bars);
 }
 
 template <bool DRIFT>
@@ -1039,8 +1049,10 @@ void launch_init_geometry_mixed(const MixedArgs& a, cudaStream_t s) {
   if (a.n <= 0) return;
   // the passes may take up to kHaloCap x 36 B + one PD_MAX_FAMILY x 64 B index chunk per warp of shared memory
   const int mx = kHaloCap * 36 + (kHaloBlock / 32) * PD_MAX_FAMILY * 64;
-  cudaFuncSetAttribute(k_pass_a_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-  cudaFuncSetAttribute(k_pass_a_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_pass_a_mixed<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_pass_a_mixed<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_pass_a_mixed<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_pass_a_mixed<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   cudaFuncSetAttribute(k_pass_b_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   cudaFuncSetAttribute(k_pass_b_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   cudaFuncSetAttribute(k_batch_persistent_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
@@ -1059,6 +1071,11 @@ void launch_drift_mixed(const MixedArgs& a, cudaStream_t s) {
 // The single-plate passes are launched with programmatic stream
 // serialization: a pass's blocks may start (and fetch what no step writes)
 // while the previous kernel on the stream drains.
+static void (*pass_a_kernel(const MixedArgs& a, bool breaking))(MixedArgs) {
+  if (a.uniform_v) return breaking ? k_pass_a_mixed<true, true> : k_pass_a_mixed<false, true>;
+  return breaking ? k_pass_a_mixed<true, false> : k_pass_a_mixed<false, false>;
+}
+
 static void launch_pass_pdl(void (*kernel)(MixedArgs), const MixedArgs& a, size_t sm, cudaStream_t s,
                             bool pdl = true) {
   if (a.nblocks <= a.blk0) return;
@@ -1077,7 +1094,7 @@ static void launch_pass_pdl(void (*kernel)(MixedArgs), const MixedArgs& a, size_
 
 void launch_pass_a_mixed(const MixedArgs& a, bool breaking, cudaStream_t s) {
   if (a.n <= 0) return;
-  launch_pass_pdl(breaking ? k_pass_a_mixed<true> : k_pass_a_mixed<false>, a, pass_smem_bytes(a, true), s);
+  launch_pass_pdl(pass_a_kernel(a, breaking), a, pass_smem_bytes(a, true), s);
 }
 
 void launch_pass_b_mixed(const MixedArgs& a, bool drift, cudaStream_t s) {
@@ -1089,7 +1106,7 @@ void launch_pass_b_mixed(const MixedArgs& a, bool drift, cudaStream_t s) {
 // other streams), visiting blocks a.blk0 .. a.nblocks - 1.
 void launch_slab_pass_a_mixed(const MixedArgs& a, bool breaking, cudaStream_t s) {
   if (a.n <= 0) return;
-  launch_pass_pdl(breaking ? k_pass_a_mixed<true> : k_pass_a_mixed<false>, a, pass_smem_bytes(a, true), s, false);
+  launch_pass_pdl(pass_a_kernel(a, breaking), a, pass_smem_bytes(a, true), s, false);
 }
 
 void launch_slab_pass_b_mixed(const MixedArgs& a, bool exporting, cudaStream_t s) {
