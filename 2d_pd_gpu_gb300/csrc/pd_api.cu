@@ -2,6 +2,7 @@
 // state, family/bond set-up, step launches captured in CUDA graphs.
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -60,9 +61,12 @@ struct pd_ctx {
   int32_t max_family = 0;
   // pd_step_host's copy / compute pipeline (streams and events, see plan_slabs)
   cudaStream_t io[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  std::vector<cudaStream_t> ps;  // pd_step_host: one stream per slab's pass A, then one per slab's pass B
   std::vector<cudaEvent_t> slab_ev;
   std::vector<int64_t> slab_bnd;    // slab k = particles slab_bnd[k] .. slab_bnd[k+1]; empty: not planned
   std::vector<int32_t> slab_need;   // slab k's pass A needs slabs 0 .. slab_need[k] imported
+  std::vector<int32_t> slab_low;    // the first slab holding a neighbour of slab k (its pass B waits on
+                                    // pass A of slabs slab_low[k] .. slab_need[k])
   // the mixed form's: slab k = visiting blocks mslab_blk[k] .. mslab_blk[k+1], whose bonds
   // reach slabs mslab_lo[k] .. mslab_hi[k]; id slab k = particles mslab_id[k] ..
   // mslab_id[k+1], which slab k's import needs at the latest, and whose export waits for
@@ -186,6 +190,7 @@ void free_families(pd_ctx* c) {
   c->sell = pd::SellLayout{};
   c->slab_bnd.clear();
   c->slab_need.clear();
+  c->slab_low.clear();
   c->mslab_blk.clear();
   c->mslab_id.clear();
   c->mslab_lo.clear();
@@ -531,6 +536,7 @@ int pd_destroy(pd_ctx* c) {
   for (cudaEvent_t e : c->slab_ev) cudaEventDestroy(e);
   for (cudaStream_t q : c->io)
     if (q) cudaStreamDestroy(q);
+  for (cudaStream_t q : c->ps) cudaStreamDestroy(q);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return PD_OK;
@@ -1206,25 +1212,46 @@ int pd_checkpoint_load(pd_ctx* c, const void* buf, int64_t bytes) {
 
 
 // pd_step_host pipeline (FP64 form).  The particles are cut into kSlabs index
-// ranges (multiples of 32; the first two small, so the first pass A starts
-// early, the rest even); slab_need[k] = the last slab holding slab k's
-// particles or any of their neighbours.  Streams (io[0], io[1] at high
-// priority): io[1] copies u, v, f in slab by slab (host-to-device copies
-// share one path, ~200 GB/s, so slab order is what matters), io[0] runs each
-// slab's drift as its copy lands, and pass A of slab k starts, on the main
-// stream or io[2] alternately, as soon as slabs 0 .. slab_need[k] are in.
-// The last pass B writes the state back to the host buffers itself, which
-// hides the export under the pass (separate copies measured slower).
-constexpr int kSlabs = 8;
-enum { kEvImport = 0, kEvCopy = kSlabs, kEvStart = 2 * kSlabs, kEvJoin = 2 * kSlabs + 1, kEvCount = 2 * kSlabs + 2 };
+// ranges (multiples of 32) of geometric sizes -- 1/128, 1/128, 1/64, 1/32,
+// 1/16, 1/8 of the plate, then six of 1/8 -- so the first pass A starts
+// after a few microseconds of copying and the later copies stay ahead of it;
+// slab_need[k] / slab_low[k] = the last / first slab holding a neighbour of
+// slab k's particles.  Streams (io[0], io[1] at high priority): io[1] copies
+// u, v, f in slab by slab, io[0] runs each slab's drift as its copy lands,
+// pass A of slab k starts on its own stream once slabs 0 .. slab_need[k] are
+// in, and, in one-step calls, pass B of slab k (its own stream) once pass A
+// of slabs slab_low[k] .. slab_need[k] is done, writing the slab's new state
+// straight to the host buffers -- so the device-to-host traffic runs under
+// the later slabs' pass A instead of after it.  One stream per launch: an
+// FP64 pass A block runs for ~70 us whatever the slab's size (one thread per
+// particle, FP64-latency bound when the SM is not full), so slab launches
+// queued on shared streams would wait out each other's tails.
+constexpr int kSlabs = 12;
+enum {
+  kEvImport = 0,
+  kEvCopy = kSlabs,
+  kEvA = 2 * kSlabs,
+  kEvB = 3 * kSlabs,
+  kEvStart = 4 * kSlabs,
+  kEvJoin = 4 * kSlabs + 1,
+  kEvCount = 4 * kSlabs + 2
+};
 
-// The pipeline's streams (io[0], io[1] at high priority) and events.
+constexpr int kMaxSlabs = 16;  // the most slabs either form's pipeline uses
+
+// The pipeline's streams (io[0], io[1], io[5] at high priority; the per-slab
+// pass streams at low priority) and events.
 static int pipeline_streams(pd_ctx* c, int nev) {
   if (!c->io[0]) {
     int lo = 0, hi = 0;
     PD_CK(c, cudaDeviceGetStreamPriorityRange(&lo, &hi));
     for (int q = 0; q < 6; ++q)
       PD_CK(c, cudaStreamCreateWithPriority(&c->io[q], cudaStreamNonBlocking, q < 2 || q == 5 ? hi : lo));
+    while ((int)c->ps.size() < 2 * kMaxSlabs) {
+      cudaStream_t q;
+      PD_CK(c, cudaStreamCreateWithPriority(&q, cudaStreamNonBlocking, lo));
+      c->ps.push_back(q);
+    }
   }
   while ((int)c->slab_ev.size() < nev) {
     cudaEvent_t e;
@@ -1238,35 +1265,45 @@ static int plan_slabs(pd_ctx* c) {
   if (!c->slab_bnd.empty()) return PD_OK;
   const int rs = pipeline_streams(c, kEvCount);
   if (rs != PD_OK) return rs;
-  // the largest neighbour id of every 32-particle chunk
+  // the largest and smallest neighbour id of every 32-particle chunk
   const int64_t nch = (c->n + 31) / 32;
-  std::vector<int32_t> h((size_t)nch, 0);
+  std::vector<int32_t> h((size_t)nch, 0), hl((size_t)nch, 0);
   int32_t* reach = nullptr;
-  PD_CK(c, cudaMalloc(&reach, h.size() * sizeof(int32_t)));
+  PD_CK(c, cudaMalloc(&reach, 2 * h.size() * sizeof(int32_t)));
   cudaError_t e = cudaMemsetAsync(reach, 0, h.size() * sizeof(int32_t), c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(reach + nch, 0x7f, h.size() * sizeof(int32_t), c->stream);
   if (e == cudaSuccess) {
-    pd::launch_slab_reach(c->n, c->row_ptr, c->col, 32, reach, c->stream);
+    pd::launch_slab_reach(c->n, c->row_ptr, c->col, 32, reach, reach + nch, c->stream);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = copy_sync(h.data(), reach, h.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess)
+    e = copy_sync(hl.data(), reach + nch, hl.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
   cudaFree(reach);
   PD_CK(c, e);
-  // slab boundaries in chunks: two leading slabs of nch / 32 chunks, then even slabs
-  std::vector<int64_t> bc(kSlabs + 1);
-  const int64_t lead = std::max<int64_t>(1, nch / 32);
-  bc[0] = 0;
-  bc[1] = std::min(nch, lead);
-  bc[2] = std::min(nch, 2 * lead);
-  for (int k = 3; k <= kSlabs; ++k) bc[k] = bc[2] + (nch - bc[2]) * (k - 2) / (kSlabs - 2);
+  // slab boundaries in chunks: 1/128, 1/128, 1/64, 1/32, 1/16, 1/8, then six of 1/8
+  static const int kShare[kSlabs] = {2, 2, 4, 8, 16, 32, 32, 32, 32, 32, 32, 32};  // of 256
+  std::vector<int64_t> bc(kSlabs + 1, 0);
+  int acc = 0;
+  for (int k = 0; k < kSlabs; ++k) {
+    acc += kShare[k];
+    bc[k + 1] = k + 1 == kSlabs ? nch : std::min<int64_t>(nch, std::max<int64_t>(bc[k] + 1, nch * acc / 256));
+  }
   c->slab_bnd.assign(kSlabs + 1, 0);
   for (int k = 0; k <= kSlabs; ++k) c->slab_bnd[k] = std::min<int64_t>(c->n, bc[k] * 32);
   c->slab_need.assign(kSlabs, 0);
+  c->slab_low.assign(kSlabs, 0);
   for (int k = 0; k < kSlabs; ++k) {
-    int64_t far = -1;
-    for (int64_t q = bc[k]; q < bc[k + 1]; ++q) far = std::max<int64_t>(far, h[(size_t)q]);
-    int need = k;
+    int64_t far = -1, near = INT64_MAX;
+    for (int64_t q = bc[k]; q < bc[k + 1]; ++q) {
+      far = std::max<int64_t>(far, h[(size_t)q]);
+      near = std::min<int64_t>(near, hl[(size_t)q]);
+    }
+    int need = k, low = k;
     while (need + 1 < kSlabs && far >= c->slab_bnd[need + 1]) ++need;
+    while (low > 0 && near < c->slab_bnd[low]) --low;
     c->slab_need[k] = need;
+    c->slab_low[k] = low;
   }
   return PD_OK;
 }
@@ -1292,10 +1329,14 @@ static cudaError_t enqueue_host_step(pd_ctx* c, int32_t nsteps, const double* u_
   cudaStream_t* io = c->io;
   const size_t b16 = sizeof(double2);
   ck(cudaEventRecord(ev[kEvStart], s));
-  for (int q = 0; q < 4; ++q) ck(cudaStreamWaitEvent(io[q], ev[kEvStart], 0));
-  // enqueued in dependency order (each pass A right after the import it waits for), so the
-  // first pass A is submitted before the host has issued the later imports
-  int next_a = 0;
+  for (int q = 0; q < 2; ++q) ck(cudaStreamWaitEvent(io[q], ev[kEvStart], 0));
+  cudaStream_t* pa = c->ps.data();           // pass A of slab k: pa[k]
+  cudaStream_t* pb = c->ps.data() + kMaxSlabs;  // pass B of slab k: pb[k]
+  // enqueued in dependency order (each pass A right after the import it waits for, each
+  // pass B right after the last pass A it waits for), so the first pass A is submitted
+  // before the host has issued the later imports
+  const bool one = nsteps == 1;
+  int next_a = 0, next_b = 0;
   for (int k = 0; k < kSlabs; ++k) {
     const Fp64Args a = slab_args(c, plain, k);  // import slab k
     const size_t off = (size_t)a.i0, cnt = (size_t)(a.n - a.i0);
@@ -1309,19 +1350,34 @@ static cudaError_t enqueue_host_step(pd_ctx* c, int32_t nsteps, const double* u_
     pd::launch_drift_fp64(a, io[0]);  // in place, on the device copy
     ck(cudaEventRecord(ev[kEvImport + k], io[0]));
     for (; next_a < kSlabs && c->slab_need[next_a] <= k; ++next_a) {  // pass A of slabs whose neighbours are in
-      cudaStream_t sj = next_a % 2 ? io[2] : s;
-      ck(cudaStreamWaitEvent(sj, ev[kEvImport + c->slab_need[next_a]], 0));
+      cudaStream_t sj = pa[next_a];
+      ck(cudaStreamWaitEvent(sj, ev[kEvImport + c->slab_need[next_a]], 0));  // (after the call's start)
       pd::launch_pass_a_fp64(slab_args(c, plain, next_a), brk, sj);
+      ck(cudaEventRecord(ev[kEvA + next_a], sj));
+      // one-step calls: pass B (with the write-back) of every slab whose neighbours' pass A is in
+      for (; one && next_b < kSlabs && c->slab_need[next_b] <= next_a; ++next_b) {
+        cudaStream_t sb = pb[next_b];
+        for (int q = c->slab_low[next_b]; q <= c->slab_need[next_b]; ++q) ck(cudaStreamWaitEvent(sb, ev[kEvA + q], 0));
+        pd::launch_pass_b_fp64(slab_args(c, out, next_b), 0, sb);
+        ck(cudaEventRecord(ev[kEvB + next_b], sb));
+      }
     }
   }
-  ck(cudaEventRecord(ev[kEvJoin], io[2]));
-  ck(cudaStreamWaitEvent(s, ev[kEvJoin], 0));
-  ck(cudaStreamWaitEvent(s, ev[kEvImport + kSlabs - 1], 0));
-  for (int32_t k = 0; k < nsteps; ++k) {
-    const bool last = k + 1 == nsteps;
-    if (k > 0) pd::launch_pass_a_fp64(plain, brk, s);
-    pd::launch_pass_b_fp64(last ? out : plain, last ? 0 : 1, s);  // the last writes the state back
-  }
+  if (one && next_b != kSlabs) e = e == cudaSuccess ? cudaErrorLaunchFailure : e;  // (a plan bug)
+  // join every stream's work on the main stream
+  auto join = [&](cudaStream_t q) {
+    ck(cudaEventRecord(ev[kEvJoin], q));
+    ck(cudaStreamWaitEvent(s, ev[kEvJoin], 0));
+  };
+  join(io[0]);
+  for (int k = 0; k < kSlabs; ++k) join(pa[k]);
+  for (int k = 0; one && k < kSlabs; ++k) join(pb[k]);
+  if (!one)
+    for (int32_t k = 0; k < nsteps; ++k) {
+      const bool last = k + 1 == nsteps;
+      if (k > 0) pd::launch_pass_a_fp64(plain, brk, s);
+      pd::launch_pass_b_fp64(last ? out : plain, last ? 0 : 1, s);  // the last writes the state back
+    }
   ck(cudaGetLastError());
   return e;
 }
@@ -1333,24 +1389,26 @@ static cudaError_t enqueue_host_step(pd_ctx* c, int32_t nsteps, const double* u_
 // records, since a tile's last block holds fewer chunks than kHaloBlock / 32.
 // Moving the state is the cost here: 48 B per particle each way in FP64
 // against a step that takes ~0.1 us per 1k particles, over a CPU-GPU link of
-// ~200 GB/s each way.  Host <-> device traffic therefore goes through the copy
-// engines (which share the link in both directions better than SM loads and
-// stores do), by slabs of particle ids, through the context's FP64 staging
-// buffers (u, v, f):
+// ~200 GB/s each way (~165 GB/s each way when both run).  Host <-> device
+// traffic therefore goes through the copy engines (which share the link in
+// both directions better than SM loads and stores do; an import kernel
+// reading the host buffers directly measured 0.67 against 0.64-0.65 ms per
+// one-step call on the 1M-particle plate), by slabs of particle ids, through
+// the context's FP64 staging buffers (u, v, f):
 //   io[1]  copies id slab k in;
 //   io[0]  imports slab k (conversion to the scaled state + drift, from the
 //          staging buffers) once id slabs 0 .. k are in;
-//   main / io[2] alternately: pass A of slab k once the slabs its bonds reach
-//          are imported;
-//   io[3] / io[4] alternately (one-step calls): pass B of slab k once pass A
-//          of those slabs is done, writing the new FP64 state by particle id
-//          into the staging buffers;
+//   its own stream: pass A of slab k once the slabs its bonds reach are
+//          imported;
+//   its own stream (one-step calls): pass B of slab k once pass A of those
+//          slabs is done, writing the new FP64 state by particle id into the
+//          staging buffers;
 //   io[5]  copies id slab k out once pass B of every slab holding its ids is
 //          done -- while later slabs are still coming in.
 // Id slab k ends after the highest id of slabs 0 .. k, so slab k's import
 // needs id slabs 0 .. k only (a row-major numbering gives slabs of whole
 // rows; any numbering is correct, a scrambled one just pipelines less).
-constexpr int kMixedSlabs = 8;
+constexpr int kMixedSlabs = 16;
 enum { kMEvIn = 0, kMEvImport = kMixedSlabs, kMEvA = 2 * kMixedSlabs, kMEvB = 3 * kMixedSlabs,
        kMEvStart = 4 * kMixedSlabs, kMEvCount = 4 * kMixedSlabs + 1 };
 
@@ -1376,13 +1434,15 @@ static int plan_slabs_mixed(pd_ctx* c) {
     const auto it = std::upper_bound(first.begin(), first.end(), p / 32);
     return (int64_t)(it == first.begin() ? 0 : (it - first.begin()) - 1);
   };
+  // slabs of visiting blocks: 1/64, 1/64, 1/32 of the plate, then 13 even ones (the first
+  // copies out start after a few percent of the plate is in)
   const int K = kMixedSlabs;
   std::vector<int64_t> bc(K + 1);
-  const int64_t lead = std::max<int64_t>(1, nb / 32);
   bc[0] = 0;
-  bc[1] = std::min(nb, lead);
-  bc[2] = std::min(nb, 2 * lead);
-  for (int k = 3; k <= K; ++k) bc[k] = bc[2] + (nb - bc[2]) * (k - 2) / (K - 2);
+  bc[1] = std::min(nb, std::max<int64_t>(1, nb / 64));
+  bc[2] = std::min(nb, std::max<int64_t>(bc[1], 2 * (nb / 64)));
+  bc[3] = std::min(nb, std::max<int64_t>(bc[2], 4 * (nb / 64)));
+  for (int k = 4; k <= K; ++k) bc[k] = bc[3] + (nb - bc[3]) * (k - 3) / (K - 3);
   auto slab_of_block = [&](int64_t blk) {
     int k = 0;
     while (k + 1 < K && blk >= bc[k + 1]) ++k;
@@ -1444,6 +1504,8 @@ static cudaError_t enqueue_host_step_mixed(pd_ctx* c, int32_t nsteps, const doub
   out.out_f = c->f;
   ck(cudaEventRecord(ev[kMEvStart], s));
   for (int q = 0; q < 6; ++q) ck(cudaStreamWaitEvent(io[q], ev[kMEvStart], 0));
+  cudaStream_t* pa = c->ps.data();           // pass A of slab k: pa[k]
+  cudaStream_t* pb = c->ps.data() + kMaxSlabs;  // pass B of slab k: pb[k]
   const bool one = nsteps == 1;
   int next_a = 0, next_b = 0, next_out = 0, b_waited = -1;
   auto export_ready = [&]() {  // copy out every id slab whose passes B are done
@@ -1468,12 +1530,12 @@ static cudaError_t enqueue_host_step_mixed(pd_ctx* c, int32_t nsteps, const doub
     pd::launch_import_drift_mixed(plain, c->mslab_blk[k], c->mslab_blk[k + 1], c->u, c->v, c->f, io[0]);
     ck(cudaEventRecord(ev[kMEvImport + k], io[0]));
     for (; next_a < K && c->mslab_hi[next_a] <= k; ++next_a) {
-      cudaStream_t sa = next_a % 2 ? io[2] : s;
+      cudaStream_t sa = pa[next_a];
       ck(cudaStreamWaitEvent(sa, ev[kMEvImport + c->mslab_hi[next_a]], 0));
       pd::launch_slab_pass_a_mixed(mixed_slab(c, plain, next_a), brk, sa);
       ck(cudaEventRecord(ev[kMEvA + next_a], sa));
       for (; one && next_b < next_a && c->mslab_hi[next_b] < next_a; ++next_b) {
-        cudaStream_t sb = next_b % 2 ? io[4] : io[3];
+        cudaStream_t sb = pb[next_b];
         for (int q = c->mslab_lo[next_b]; q <= c->mslab_hi[next_b]; ++q) ck(cudaStreamWaitEvent(sb, ev[kMEvA + q], 0));
         pd::launch_slab_pass_b_mixed(mixed_slab(c, out, next_b), true, sb);
         ck(cudaEventRecord(ev[kMEvB + next_b], sb));
@@ -1482,7 +1544,7 @@ static cudaError_t enqueue_host_step_mixed(pd_ctx* c, int32_t nsteps, const doub
     }
   }
   for (; one && next_b < K;) {
-    cudaStream_t sb = next_b % 2 ? io[4] : io[3];
+    cudaStream_t sb = pb[next_b];
     for (int q = c->mslab_lo[next_b]; q <= c->mslab_hi[next_b]; ++q) ck(cudaStreamWaitEvent(sb, ev[kMEvA + q], 0));
     pd::launch_slab_pass_b_mixed(mixed_slab(c, out, next_b), true, sb);
     ck(cudaEventRecord(ev[kMEvB + next_b], sb));
@@ -1491,11 +1553,13 @@ static cudaError_t enqueue_host_step_mixed(pd_ctx* c, int32_t nsteps, const doub
   }
   if (one && next_out != K) e = e == cudaSuccess ? cudaErrorLaunchFailure : e;  // every id slab is out (a plan bug)
   // join every stream's work on the main stream (io[5] holds the last copies out)
-  cudaEvent_t join = ev[kMEvStart];
-  for (int q = 0; q < 6; ++q) {
-    ck(cudaEventRecord(join, io[q]));
-    ck(cudaStreamWaitEvent(s, join, 0));
-  }
+  auto join = [&](cudaStream_t q) {
+    ck(cudaEventRecord(ev[kMEvStart], q));
+    ck(cudaStreamWaitEvent(s, ev[kMEvStart], 0));
+  };
+  for (int q = 0; q < 6; ++q) join(io[q]);
+  for (int k = 0; k < K; ++k) join(pa[k]);
+  for (int k = 0; one && k < K; ++k) join(pb[k]);
   if (!one) {  // the remaining steps on the whole plate; the last pass B exports
     pd::launch_slab_pass_b_mixed(plain, false, s);  // (plain launch: it follows the join's event waits)
     for (int32_t k = 1; k < nsteps; ++k) {

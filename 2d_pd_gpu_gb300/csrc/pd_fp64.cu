@@ -353,20 +353,25 @@ namespace {
 }  // namespace
 
 namespace {
-// reach[k] = the largest neighbour id of slab k (particles k*slab .. k*slab + slab - 1)
+// reach[k] / low[k] = the largest / smallest id among slab k's particles
+// (k*slab .. k*slab + slab - 1) and their neighbours
 __global__ void k_slab_reach(int64_t n, const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
-                             int64_t slab, int32_t* reach) {
+                             int64_t slab, int32_t* reach, int32_t* low) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  int32_t m = (int32_t)i;
-  for (int64_t k = row_ptr[i]; k < row_ptr[i + 1]; ++k) m = col[k] > m ? col[k] : m;
+  int32_t m = (int32_t)i, l = (int32_t)i;
+  for (int64_t k = row_ptr[i]; k < row_ptr[i + 1]; ++k) {
+    m = col[k] > m ? col[k] : m;
+    l = col[k] < l ? col[k] : l;
+  }
   atomicMax(&reach[i / slab], m);
+  atomicMin(&low[i / slab], l);
 }
 }  // namespace
 
 void launch_slab_reach(int64_t n, const int64_t* row_ptr, const int32_t* col, int64_t slab, int32_t* reach,
-                       cudaStream_t s) {
-  if (n > 0) k_slab_reach<<<(unsigned)blocks_for(n), kBlock, 0, s>>>(n, row_ptr, col, slab, reach);
+                       int32_t* low, cudaStream_t s) {
+  if (n > 0) k_slab_reach<<<(unsigned)blocks_for(n), kBlock, 0, s>>>(n, row_ptr, col, slab, reach, low);
 }
 
 void launch_init_geometry_fp64(const Fp64Args& a, cudaStream_t s) {

@@ -226,7 +226,7 @@ void launch_drift_fp64(const Fp64Args& a, cudaStream_t s);
 void launch_shadow_fp64(const Fp64Args& a, cudaStream_t s);  // u32 := (float)u
 // reach[k] := max(reach[k], largest neighbour id of slab k); reach zeroed by the caller
 void launch_slab_reach(int64_t n, const int64_t* row_ptr, const int32_t* col, int64_t slab, int32_t* reach,
-                       cudaStream_t s);
+                       int32_t* low, cudaStream_t s);
 // hourglass term if a.k_hg != 0; pdl: programmatic stream serialization (the plain step loop)
 void launch_pass_a_fp64(const Fp64Args& a, bool breaking, cudaStream_t s, bool pdl = false);
 // mode 0: kick; 1: kick + next step's drift; 2: drop-in kick (acc array in/out)
