@@ -150,6 +150,8 @@ class Server:
     chunk: int = 50
     batch_config: dict | None = None
     workers: int = 4
+    builder_threads: int = 3  # device contexts built ahead of admission
+    reader_threads: int = 2  # finished requests' results read (and their memory freed) off the loop
     preempt: bool = True
     preempt_ratio: float = 4.0
     keep: set = field(default_factory=set)  # request ids whose final (u, mask) the results keep
@@ -164,7 +166,8 @@ class Server:
         pending = deque(sorted(requests, key=lambda q: q.arrival))
         queue, active, used = deque(), {}, 0.0
         pool = ThreadPoolExecutor(max_workers=self.workers)  # host plates
-        builders = ThreadPoolExecutor(max_workers=2)  # device contexts, built while the GPU steps the batch
+        builders = ThreadPoolExecutor(max_workers=self.builder_threads)  # built while the GPU steps the batch
+        readers = ThreadPoolExecutor(max_workers=self.reader_threads)  # results read while the loop goes on
         futs, building, reserved = {}, {}, 0.0
         t0 = time.perf_counter()
         busy = 0.0
@@ -180,21 +183,35 @@ class Server:
             building[q.rid] = (builders.submit(build, q, futs.pop(q.rid)), need)
             reserved += need
 
-        # finished requests whose results are read (and memory freed) while the next chunk runs
-        retired = []
+        # finished requests: their results are read (and their memory freed) on reader threads
+        # while the loop admits and steps; `used` drops when a read completes (harvest)
+        retired, reading = [], []
+
+        def read(q, ctx, admitted, fin):
+            dig, broken = state_digest(ctx)
+            kept = (ctx.state()[0], ctx.bond_mask()) if q.rid in self.keep else None
+            res = Result(q.rid, q.arrival, admitted, fin, q.particles, ctx.nnz, q.steps, dig, broken, kept)
+            ctx.close()
+            return res
+
+        def harvest(wait=False):
+            nonlocal used
+            keep = []
+            for fut, need in reading:
+                if wait or fut.done():
+                    self.results.append(fut.result())
+                    used -= need
+                else:
+                    keep.append((fut, need))
+            reading[:] = keep
 
         def finish():
-            nonlocal used
             for q, ctx, admitted, fin, need in retired:
-                dig, broken = state_digest(ctx)
-                kept = (ctx.state()[0], ctx.bond_mask()) if q.rid in self.keep else None
-                self.results.append(Result(q.rid, q.arrival, admitted, fin, q.particles, ctx.nnz, q.steps, dig,
-                                           broken, kept))
-                ctx.close()
-                used -= need
+                reading.append((readers.submit(read, q, ctx, admitted, fin), need))
             retired.clear()
 
         while pending or queue or active:
+            harvest()
             now = time.perf_counter() - t0
             while pending and pending[0].arrival <= now:
                 q = pending.popleft()
@@ -233,7 +250,7 @@ class Server:
                         for pk in reversed(parked):
                             queue.insert(at, pk)
                     # (a retired request still holds its memory until its results are read)
-                    if used + reserved + need > self.budget_bytes and (active or building or retired):
+                    if used + reserved + need > self.budget_bytes and (active or building or retired or reading):
                         break
                 if isinstance(q, _Parked):
                     queue.popleft()
@@ -257,6 +274,9 @@ class Server:
                 active[q.rid] = [q, ctx, q.steps, time.perf_counter() - t0, need, p]
             if not active:
                 finish()
+                if reading and used + reserved > 0 and queue:
+                    harvest(wait=True)  # the head may be waiting for memory that a read frees
+                    continue
                 if pending:
                     time.sleep(max(0.0, min(0.01, pending[0].arrival - (time.perf_counter() - t0))))
                 continue
@@ -278,7 +298,9 @@ class Server:
             if stop_after and done >= stop_after:
                 break
         finish()
+        harvest(wait=True)
         makespan = time.perf_counter() - t0
+        readers.shutdown()
         pool.shutdown()
         for fut, _ in building.values():  # stopped early: contexts built ahead of admission
             fut.result()[1].close()
@@ -286,13 +308,20 @@ class Server:
         batch.close()
         lat = np.array([r.latency for r in self.results])
         wait = np.array([r.admitted - r.arrival for r in self.results])
+        arr = np.array([r.arrival for r in self.results])
+        pct = (lambda a, q: float(np.percentile(a, q)) if a.size else None)
         return {
             "requests": len(self.results),
+            "latency_samples": int(lat.size),
             "precision": "fp64" if self.precision == native.PD_FP64 else "mixed",
-            "p50_latency_s": float(np.percentile(lat, 50)) if lat.size else None,
-            "p99_latency_s": float(np.percentile(lat, 99)) if lat.size else None,
+            "p50_latency_s": pct(lat, 50),
+            "p95_latency_s": pct(lat, 95),
+            "p99_latency_s": pct(lat, 99),
+            "max_latency_s": float(lat.max()) if lat.size else None,
             "mean_latency_s": float(lat.mean()) if lat.size else None,
-            "p50_queue_s": float(np.percentile(wait, 50)) if wait.size else None,
+            "p50_queue_s": pct(wait, 50),
+            "p99_queue_s": pct(wait, 99),
+            "arrival_window_s": float(arr.max() - arr.min()) if arr.size else None,
             "makespan_s": makespan,
             "gpu_busy_frac": busy / makespan if makespan > 0 else None,
             "bond_updates_per_s": bond_steps / makespan if makespan > 0 else None,

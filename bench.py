@@ -451,11 +451,11 @@ def run_serve(args, pdg, device, capacity, configs):
     nat = pdg.native
     serve = importlib.import_module("2d_pd_gpu_gb300.serve")
     out = {}
-    for name, prec, count in (("mixed", nat.PD_MIXED, args.serve_requests),
-                              ("fp64", nat.PD_FP64, max(4, args.serve_requests // 4))):
+    fp64_count = args.serve_fp64_requests or max(4, args.serve_requests // 4)
+    for name, prec, count in (("mixed", nat.PD_MIXED, args.serve_requests), ("fp64", nat.PD_FP64, fp64_count)):
         probe = serve.make_requests(count, seed=args.seed + 17)
         work = float(np.mean([27.9 * q.particles * q.steps for q in probe]))
-        rate = 0.8 * capacity[name] / work
+        rate = args.serve_load * capacity[name] / work
         reqs = serve.make_requests(count, seed=args.seed + 17, rate=rate)
         # the mixed results' error against the FP64 form, on the three smallest requests
         sample = sorted(reqs, key=lambda q: q.particles * q.steps)[:3] if prec == nat.PD_MIXED else []
@@ -463,7 +463,11 @@ def run_serve(args, pdg, device, capacity, configs):
                            batch_config=configs.get(name), keep={q.rid for q in sample})
         with timed():
             m = srv.run(reqs)
-        m.update({"arrival_rate_per_s": rate, "offered_load": 0.8, "capacity_bond_updates_per_s": capacity[name],
+        # the load the stream actually offered: its bond updates over its arrival window, against capacity
+        window = max(q.arrival for q in reqs) - min(q.arrival for q in reqs)
+        offered = m["bond_updates"] / window / capacity[name] if window > 0 else None
+        m.update({"arrival_rate_per_s": rate, "offered_load_target": args.serve_load,
+                  "offered_load_achieved": offered, "capacity_bond_updates_per_s": capacity[name],
                   "particles_range": [min(q.particles for q in reqs), max(q.particles for q in reqs)]})
         if sample:
             by = {r.rid: r for r in srv.results}
@@ -484,7 +488,29 @@ def run_serve(args, pdg, device, capacity, configs):
     return out
 
 
+def run_serve_only(args, comm):
+    """The batch leg (capacity, autotuned launch shape) and the serve leg alone:
+    long request streams whose percentiles need more time than the default run."""
+    pdg = importlib.import_module("2d_pd_gpu_gb300")
+    device = comm.local
+    sampler = ClockSampler(device)
+    sampler.start()
+    result = {"metric": "served bond-updates/s and completion latency", "n_gpus": 1, "data": "synthetic",
+              "config": {"workload": "serve: Poisson stream, plates 10k-2M particles log-uniform, 200-2000 steps, "
+                                     "150 GB HBM budget"}}
+    if comm.rank == 0:
+        result["batch"] = run_batch(args, pdg, device)
+        cap = {k: v["value"] for k, v in result["batch"].items()}
+        cfgs = {k: v["config"] for k, v in result["batch"].items()}
+        result["serve"] = run_serve(args, pdg, device, cap, cfgs)
+    result["clocks"] = sampler.stop()
+    if comm.rank == 0:
+        print(json.dumps(result), flush=True)
+
+
 def run_ours(args, comm):
+    if args.serve_only:
+        return run_serve_only(args, comm)
     pdg = importlib.import_module("2d_pd_gpu_gb300")
     nat = pdg.native
     plate = replica_plate(pdg, args.side, args.seed, comm.rank)
@@ -590,7 +616,11 @@ def main():
     ap.add_argument("--scale-side", type=int, default=4000, help="mixed form on this plate too (0: skip)")
     ap.add_argument("--batch-plates", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=500)
-    ap.add_argument("--serve-requests", type=int, default=64)
+    ap.add_argument("--serve-requests", type=int, default=64, help="mixed requests in the serve leg")
+    ap.add_argument("--serve-fp64-requests", type=int, default=0, help="FP64 requests (0: a quarter of the mixed)")
+    ap.add_argument("--serve-load", type=float, default=0.8, help="offered load, of the measured batch capacity")
+    ap.add_argument("--serve-only", action="store_true",
+                    help="only the batch leg (for the capacity) and the serve leg; prints their JSON line")
     ap.add_argument("--serve-chunk", type=int, default=50)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
