@@ -212,15 +212,18 @@ int pd_mazars_set(pd_ctx* ctx, const double* threshold, const double* bond_damag
  * src/main_seq.cpp:686-699 (applyVelocityBC, updatePositions, applyFixedBC,
  * computeVelocity).  Asynchronous unless an error check needs the host. */
 int pd_step(pd_ctx* ctx, int32_t nsteps);
-/* nsteps steps from a host state to a host state, FP64 contexts (no
+/* nsteps steps from a host state to a host state, both precisions (no
  * reference counterpart; the end-to-end form of the reference's per-call
  * host-buffer contract, include/mechanics.cuh:867-881).  u_in, v_in, f_in
  * ([n][2] doubles, page-locked: pd_host_alloc) are copied in by slabs of
- * particles while the first pass runs on the slabs already in; the last
- * kernel writes the new state to u_out, v_out, f_out directly over the
- * CPU-GPU link.  In and out may be the same buffers.  Synchronous; the
- * device state is updated as by pd_set_state + pd_step + pd_get_state, bit
- * for bit. */
+ * particles while the first pass runs on the slabs already in.  FP64
+ * contexts: in one-step calls each slab's pass B writes its new state to
+ * u_out, v_out, f_out directly over the CPU-GPU link while later slabs'
+ * pass A runs (in longer calls, the last pass B does).  Mixed contexts: each
+ * slab's state goes out by copy engine as soon as the slabs holding its
+ * particles have their pass B.  In and out may be the same buffers.
+ * Synchronous; the device state and the outputs are those of pd_set_state +
+ * pd_step + pd_get_state, bit for bit. */
 int pd_step_host(pd_ctx* ctx, int32_t nsteps, const double* u_in, const double* v_in, const double* f_in,
                  double* u_out, double* v_out, double* f_out);
 /* Waits for the context's stream.  PD_ERR_TIMEOUT if a bounded device wait
