@@ -17,7 +17,9 @@
 // Pass A runs one warp per particle and one lane per bond (families <= 64
 // bonds, two per lane): the family's bond data is staged in shared memory,
 // lane q sums K_q and D_q over k in family order (the oracle's order), and,
-// once the P_b of every bond are in shared memory, lane j sums T_ij over b.
+// once the P_b of every bond are in shared memory, lane j sums T_ij over b
+// (re-reading, for its first bond, the weight row it formed for K_q: the
+// weight matrix is symmetric, and lane j's row j is what both sums use).
 // The weight is evaluated in factored form: exp(-n1 |L_b - L_k| / l) =
 // e+(min L) e-(max L) with e+-(L) = exp(+-n1 L / l) per bond, the cosine as
 // (xi_b . xi_k) (1/L_b)(1/L_k), and an integer n2 <= 64 by repeated squaring
@@ -33,13 +35,14 @@ namespace pd {
 namespace {
 
 constexpr int kBaMax = 64;
-constexpr int kBaWarps = 4;  // particles per block of pass A
+constexpr int kBaWarps = 2;  // particles per block of pass A (30 KB of shared memory per block)
 
 struct BaFamily {  // one particle's bonds, in family order
   double ex[kBaMax], ey[kBaMax], rl[kBaMax], len[kBaMax], ep[kBaMax], em[kBaMax], vv[kBaMax], dx[kBaMax],
       dy[kBaMax];
   double P[kBaMax][4];
   int64_t slot[kBaMax];
+  double wrow[32][32];  // wrow[k][l] = w(l, k): lane l's weight row for its first bond, kept for the T_ij sums
 };
 
 struct BaWeight {
@@ -120,7 +123,9 @@ __global__ void __launch_bounds__(32 * kBaWarps) k_ba_pass_a(Fp64Args a, BondAss
   for (int q = lane; q < n; q += 32) {
     double k11 = 0.0, k12 = 0.0, k22 = 0.0, d11 = 0.0, d12 = 0.0, d21 = 0.0, d22 = 0.0;
     for (int k = 0; k < n; ++k) {
-      const double wv = wf(F, q, k) * F.vv[k];
+      const double wqk = wf(F, q, k);
+      if (q < 32) F.wrow[k][q] = wqk;  // (q == lane: the thread's own row, read back below)
+      const double wv = wqk * F.vv[k];
       const double ekx = F.ex[k], eky = F.ey[k];
       const double t0 = wv * ekx, t1 = wv * eky;
       k11 = fma(t0, ekx, k11);
@@ -158,7 +163,8 @@ __global__ void __launch_bounds__(32 * kBaWarps) k_ba_pass_a(Fp64Args a, BondAss
   for (int jj = lane; jj < n; jj += 32) {
     double m11 = 0.0, m12 = 0.0, m21 = 0.0, m22 = 0.0;
     for (int q = 0; q < n; ++q) {
-      const double wv = wf(F, jj, q) * F.vv[q];
+      // w(jj, q) = w(q, jj): the row this thread kept for its first bond, recomputed for the second
+      const double wv = (jj < 32 ? F.wrow[q][jj] : wf(F, jj, q)) * F.vv[q];
       m11 = fma(wv, F.P[q][0], m11);
       m12 = fma(wv, F.P[q][1], m12);
       m21 = fma(wv, F.P[q][2], m21);
