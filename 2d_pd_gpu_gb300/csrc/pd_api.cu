@@ -69,10 +69,9 @@ struct pd_ctx {
                                     // pass A of slabs slab_low[k] .. slab_need[k])
   // the mixed form's: slab k = visiting blocks mslab_blk[k] .. mslab_blk[k+1], whose bonds
   // reach slabs mslab_lo[k] .. mslab_hi[k]; id slab k = particles mslab_id[k] ..
-  // mslab_id[k+1], which slab k's import needs at the latest, and whose export waits for
-  // pass B of slabs 0 .. mslab_out[k]
+  // mslab_id[k+1], which slab k's import needs at the latest
   std::vector<int64_t> mslab_blk, mslab_id;
-  std::vector<int32_t> mslab_lo, mslab_hi, mslab_out;
+  std::vector<int32_t> mslab_lo, mslab_hi;
   // Mazars damage history (pd_mazars_*)
   double *mz_thr = nullptr, *mz_bd = nullptr, *mz_status = nullptr;
   pd_mazars_params mz{};
@@ -195,7 +194,6 @@ void free_families(pd_ctx* c) {
   c->mslab_id.clear();
   c->mslab_lo.clear();
   c->mslab_hi.clear();
-  c->mslab_out.clear();
   c->nnz = 0;
   c->has_families = false;
   clear_graphs(c);
@@ -1389,25 +1387,25 @@ static cudaError_t enqueue_host_step(pd_ctx* c, int32_t nsteps, const double* u_
 // records, since a tile's last block holds fewer chunks than kHaloBlock / 32.
 // Moving the state is the cost here: 48 B per particle each way in FP64
 // against a step that takes ~0.1 us per 1k particles, over a CPU-GPU link of
-// ~200 GB/s each way (~165 GB/s each way when both run).  Host <-> device
-// traffic therefore goes through the copy engines (which share the link in
-// both directions better than SM loads and stores do; an import kernel
-// reading the host buffers directly measured 0.67 against 0.64-0.65 ms per
-// one-step call on the 1M-particle plate), by slabs of particle ids, through
-// the context's FP64 staging buffers (u, v, f):
+// ~200 GB/s each way (~165 GB/s each way when both run).  The input comes in
+// by copy engine, by slabs of particle ids, into the context's FP64 staging
+// buffers (u, v, f); the output goes straight from each slab's pass B to the
+// output buffers (on the 1M-particle plate: 0.56 ms per one-step call,
+// against 0.63 with pass B writing the staging buffers and copy engines taking
+// id slabs out, and 0.67 with an import kernel reading the host buffers):
 //   io[1]  copies id slab k in;
 //   io[0]  imports slab k (conversion to the scaled state + drift, from the
 //          staging buffers) once id slabs 0 .. k are in;
 //   its own stream: pass A of slab k once the slabs its bonds reach are
 //          imported;
 //   its own stream (one-step calls): pass B of slab k once pass A of those
-//          slabs is done, writing the new FP64 state by particle id into the
-//          staging buffers;
-//   io[5]  copies id slab k out once pass B of every slab holding its ids is
-//          done -- while later slabs are still coming in.
+//          slabs is done, writing the new FP64 state by particle id to the
+//          output buffers over the link -- while later slabs are still coming in.
 // Id slab k ends after the highest id of slabs 0 .. k, so slab k's import
 // needs id slabs 0 .. k only (a row-major numbering gives slabs of whole
-// rows; any numbering is correct, a scrambled one just pipelines less).
+// rows; any numbering is correct, a scrambled one just pipelines less).  With
+// the input and output buffers the same, slab k's pass B overwrites only ids
+// of id slabs 0 .. k, whose copies in are complete before its import.
 constexpr int kMixedSlabs = 16;
 enum { kMEvIn = 0, kMEvImport = kMixedSlabs, kMEvA = 2 * kMixedSlabs, kMEvB = 3 * kMixedSlabs,
        kMEvStart = 4 * kMixedSlabs, kMEvCount = 4 * kMixedSlabs + 1 };
@@ -1450,7 +1448,7 @@ static int plan_slabs_mixed(pd_ctx* c) {
   };
   c->mslab_lo.assign(K, 0);
   c->mslab_hi.assign(K, 0);
-  std::vector<int64_t> smin(K, -1), smax(K, -1);  // particle ids held by slab k
+  std::vector<int64_t> smax(K, -1);  // the highest particle id held by slab k
   for (int k = 0; k < K; ++k) {
     int l = k, u = k;
     for (int64_t b = bc[k]; b < bc[k + 1]; ++b) {
@@ -1458,10 +1456,7 @@ static int plan_slabs_mixed(pd_ctx* c) {
         l = std::min(l, slab_of_block(block_of_pos(lo[b])));
         u = std::max(u, slab_of_block(block_of_pos(hi[b])));
       }
-      if (idlo[b] >= 0) {
-        smin[k] = smin[k] < 0 ? idlo[b] : std::min(smin[k], idlo[b]);
-        smax[k] = std::max(smax[k], idhi[b]);
-      }
+      if (idlo[b] >= 0) smax[k] = std::max(smax[k], idhi[b]);
     }
     c->mslab_lo[k] = l;
     c->mslab_hi[k] = u;
@@ -1470,12 +1465,6 @@ static int plan_slabs_mixed(pd_ctx* c) {
   c->mslab_id.assign(K + 1, 0);
   for (int k = 0; k < K; ++k) c->mslab_id[k + 1] = std::max(c->mslab_id[k], smax[k] + 1);
   c->mslab_id[K] = c->n;
-  // id slab j goes out after pass B of the last slab whose ids meet it
-  c->mslab_out.assign(K, 0);
-  for (int j = 0; j < K; ++j)
-    for (int k = 0; k < K; ++k)
-      if (smin[k] >= 0 && smin[k] < c->mslab_id[j + 1] && smax[k] >= c->mslab_id[j])
-        c->mslab_out[j] = std::max(c->mslab_out[j], k);
   c->mslab_blk = bc;
   return PD_OK;
 }
@@ -1499,25 +1488,16 @@ static cudaError_t enqueue_host_step_mixed(pd_ctx* c, int32_t nsteps, const doub
   const int K = kMixedSlabs;
   const size_t b16 = sizeof(double2);
   pd::MixedArgs plain = mixed_args(c), out = plain;
-  out.out_u = c->u;  // pass B writes the FP64 state into the staging buffers
-  out.out_v = c->v;
-  out.out_f = c->f;
+  // the exporting pass B writes the new FP64 state straight to the (page-locked) output buffers
+  out.out_u = static_cast<double2*>(mapped_host(u_out));
+  out.out_v = static_cast<double2*>(mapped_host(v_out));
+  out.out_f = static_cast<double2*>(mapped_host(f_out));
   ck(cudaEventRecord(ev[kMEvStart], s));
   for (int q = 0; q < 6; ++q) ck(cudaStreamWaitEvent(io[q], ev[kMEvStart], 0));
   cudaStream_t* pa = c->ps.data();           // pass A of slab k: pa[k]
   cudaStream_t* pb = c->ps.data() + kMaxSlabs;  // pass B of slab k: pb[k]
   const bool one = nsteps == 1;
-  int next_a = 0, next_b = 0, next_out = 0, b_waited = -1;
-  auto export_ready = [&]() {  // copy out every id slab whose passes B are done
-    for (; one && next_out < K && c->mslab_out[next_out] < next_b; ++next_out) {
-      for (; b_waited < c->mslab_out[next_out]; ++b_waited) ck(cudaStreamWaitEvent(io[5], ev[kMEvB + b_waited + 1], 0));
-      const size_t off = (size_t)c->mslab_id[next_out], cnt = (size_t)(c->mslab_id[next_out + 1] - off);
-      if (cnt == 0) continue;
-      ck(cudaMemcpyAsync(u_out + 2 * off, c->u + off, cnt * b16, cudaMemcpyDeviceToHost, io[5]));
-      ck(cudaMemcpyAsync(v_out + 2 * off, c->v + off, cnt * b16, cudaMemcpyDeviceToHost, io[5]));
-      ck(cudaMemcpyAsync(f_out + 2 * off, c->f + off, cnt * b16, cudaMemcpyDeviceToHost, io[5]));
-    }
-  };
+  int next_a = 0, next_b = 0;
   for (int k = 0; k < K; ++k) {  // enqueued in dependency order
     const size_t off = (size_t)c->mslab_id[k], cnt = (size_t)(c->mslab_id[k + 1] - off);
     if (cnt > 0) {
@@ -1540,7 +1520,6 @@ static cudaError_t enqueue_host_step_mixed(pd_ctx* c, int32_t nsteps, const doub
         pd::launch_slab_pass_b_mixed(mixed_slab(c, out, next_b), true, sb);
         ck(cudaEventRecord(ev[kMEvB + next_b], sb));
       }
-      export_ready();
     }
   }
   for (; one && next_b < K;) {
@@ -1549,10 +1528,8 @@ static cudaError_t enqueue_host_step_mixed(pd_ctx* c, int32_t nsteps, const doub
     pd::launch_slab_pass_b_mixed(mixed_slab(c, out, next_b), true, sb);
     ck(cudaEventRecord(ev[kMEvB + next_b], sb));
     ++next_b;
-    export_ready();
   }
-  if (one && next_out != K) e = e == cudaSuccess ? cudaErrorLaunchFailure : e;  // every id slab is out (a plan bug)
-  // join every stream's work on the main stream (io[5] holds the last copies out)
+  // join every stream's work on the main stream
   auto join = [&](cudaStream_t q) {
     ck(cudaEventRecord(ev[kMEvStart], q));
     ck(cudaStreamWaitEvent(s, ev[kMEvStart], 0));
@@ -1569,10 +1546,6 @@ static cudaError_t enqueue_host_step_mixed(pd_ctx* c, int32_t nsteps, const doub
       else
         pd::launch_slab_pass_b_mixed(out, true, s);
     }
-    const size_t bytes = (size_t)c->n * b16;
-    ck(cudaMemcpyAsync(u_out, c->u, bytes, cudaMemcpyDeviceToHost, s));
-    ck(cudaMemcpyAsync(v_out, c->v, bytes, cudaMemcpyDeviceToHost, s));
-    ck(cudaMemcpyAsync(f_out, c->f, bytes, cudaMemcpyDeviceToHost, s));
   }
   ck(cudaGetLastError());
   return e;

@@ -219,9 +219,9 @@ int pd_step(pd_ctx* ctx, int32_t nsteps);
  * particles while the first pass runs on the slabs already in.  FP64
  * contexts: in one-step calls each slab's pass B writes its new state to
  * u_out, v_out, f_out directly over the CPU-GPU link while later slabs'
- * pass A runs (in longer calls, the last pass B does).  Mixed contexts: each
- * slab's state goes out by copy engine as soon as the slabs holding its
- * particles have their pass B.  In and out may be the same buffers.
+ * pass A runs (in longer calls, the last pass B does); mixed contexts the
+ * same, through the mixed form's own slabs of spatial tiles.  In and out may
+ * be the same buffers.
  * Synchronous; the device state and the outputs are those of pd_set_state +
  * pd_step + pd_get_state, bit for bit. */
 int pd_step_host(pd_ctx* ctx, int32_t nsteps, const double* u_in, const double* v_in, const double* f_in,
