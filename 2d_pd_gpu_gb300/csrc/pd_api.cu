@@ -1210,9 +1210,11 @@ int pd_checkpoint_load(pd_ctx* c, const void* buf, int64_t bytes) {
 
 
 // pd_step_host pipeline (FP64 form).  The particles are cut into kSlabs index
-// ranges (multiples of 32) of geometric sizes -- 1/128, 1/128, 1/64, 1/32,
-// 1/16, 1/8 of the plate, then six of 1/8 -- so the first pass A starts
-// after a few microseconds of copying and the later copies stay ahead of it;
+// ranges (multiples of 32): 1/64 and 3/64 of the plate, then seven of 1/8, so
+// the first pass A starts after a few microseconds of copying and the later
+// copies stay ahead of it (1M-particle plate, ms per one-step call: these
+// slabs 0.840; 1/128, 1/128, 1/64, 1/32, 1/16, then seven of 1/8 0.862;
+// 1/32, 3/32, 1/8, then four of 3/16 0.862; five of 3/16 after 1/16 0.874);
 // slab_need[k] / slab_low[k] = the last / first slab holding a neighbour of
 // slab k's particles.  Streams (io[0], io[1] at high priority): io[1] copies
 // u, v, f in slab by slab, io[0] runs each slab's drift as its copy lands,
@@ -1224,7 +1226,7 @@ int pd_checkpoint_load(pd_ctx* c, const void* buf, int64_t bytes) {
 // FP64 pass A block runs for ~70 us whatever the slab's size (one thread per
 // particle, FP64-latency bound when the SM is not full), so slab launches
 // queued on shared streams would wait out each other's tails.
-constexpr int kSlabs = 12;
+constexpr int kSlabs = 9;
 enum {
   kEvImport = 0,
   kEvCopy = kSlabs,
@@ -1279,8 +1281,8 @@ static int plan_slabs(pd_ctx* c) {
     e = copy_sync(hl.data(), reach + nch, hl.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
   cudaFree(reach);
   PD_CK(c, e);
-  // slab boundaries in chunks: 1/128, 1/128, 1/64, 1/32, 1/16, 1/8, then six of 1/8
-  static const int kShare[kSlabs] = {2, 2, 4, 8, 16, 32, 32, 32, 32, 32, 32, 32};  // of 256
+  // slab boundaries in chunks: 1/64, 3/64, then seven of 1/8
+  static const int kShare[kSlabs] = {4, 12, 32, 32, 32, 32, 32, 32, 32};  // of 256
   std::vector<int64_t> bc(kSlabs + 1, 0);
   int acc = 0;
   for (int k = 0; k < kSlabs; ++k) {
