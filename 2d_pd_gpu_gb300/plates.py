@@ -146,6 +146,18 @@ def make_plate(nx, ny=None, *, dx=1e-3, thickness=1e-3, jitter=0.01, seed=0, hor
                  material, dt, steps, name, {"seed": seed, "x0": x0, "y0": y0})
 
 
+def hassa_mesh_text():
+    """The reference's only input mesh, 2D_Hassa_test_mesh.dat, written by its
+    rule: a 70 x 60 grid of unit cells, centres x in [-34.5, 34.5], y in
+    [-29.5, 29.5], area 1, x the outer loop, six decimals, one header line.
+    (tests/golden/make_golden.py checks it equals the reference's file.)"""
+    rows = ["Center_X Center_Y Area"]
+    for ix in range(70):
+        for iy in range(60):
+            rows.append(f"{ix - 34.5:.6f} {iy - 29.5:.6f} {1.0:.6f}")
+    return "\n".join(rows) + "\n"
+
+
 def config_plate_100(seed=0):
     """100 x 100 FP64 plate, centred half-width horizontal pre-crack, 100 steps."""
     return make_plate(100, seed=seed, crack="centre-half", steps=100, name="plate100x100-fp64")

@@ -347,16 +347,6 @@ REFERENCE_HASSA_CPU_S = 69.967052
 REFERENCE_HASSA_GPU_S = 0.609138
 
 
-def hassa_mesh_text():
-    """2D_Hassa_test_mesh.dat by its rule: a 70 x 60 unit grid, x in
-    [-34.5, 34.5], y in [-29.5, 29.5], unit area, x the outer loop."""
-    rows = ["Center_X Center_Y Area"]
-    for ix in range(70):
-        for iy in range(60):
-            rows.append(f"{ix - 34.5:.6f} {iy - 29.5:.6f} {1.0:.6f}")
-    return "\n".join(rows) + "\n"
-
-
 def run_bond_assoc(pdg, calls=6):
     """The reference's published problem through the drop-in: the Hassa mesh,
     n1 = n2 = 10, the reference GPU main's call sequence, compute_velocity_GPU_host
@@ -366,7 +356,7 @@ def run_bond_assoc(pdg, calls=6):
 
     exe = os.path.join(os.path.dirname(pdg.native.LIB_PATH), "pd_hassa_timing")
     with tempfile.TemporaryDirectory() as td:
-        open(os.path.join(td, "2D_Hassa_test_mesh.dat"), "w").write(hassa_mesh_text())
+        open(os.path.join(td, "2D_Hassa_test_mesh.dat"), "w").write(pdg.plates.hassa_mesh_text())
         r = subprocess.run([exe, "10", "10", str(calls)], cwd=td, capture_output=True, text=True, timeout=600)
     if r.returncode != 0:
         return {"error": r.stderr[-500:]}

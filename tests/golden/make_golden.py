@@ -66,15 +66,6 @@ import pd_oracle as po  # noqa: E402
 plates = importlib.import_module("2d_pd_gpu_gb300.plates")
 
 
-def hassa_mesh_lines():
-    """The Hassa mesh file content by rule (x outer loop, y inner)."""
-    lines = ["Center_X Center_Y Area"]
-    for ix in range(70):
-        for iy in range(60):
-            lines.append(f"{ix - 34.5:.6f} {iy - 29.5:.6f} {1.0:.6f}")
-    return "\n".join(lines) + "\n"
-
-
 def sha(path):
     return hashlib.sha256(open(path, "rb").read()).hexdigest()
 
@@ -175,7 +166,7 @@ def main():
         mesh_dir = os.path.join(td, "mesh")
         os.makedirs(mesh_dir)
         mesh = os.path.join(mesh_dir, "2D_Hassa_test_mesh.dat")
-        open(mesh, "w").write(hassa_mesh_lines())
+        open(mesh, "w").write(plates.hassa_mesh_text())
         if args.only is None:
             fixtures_1_to_4(ref, td, mesh_dir, mesh, man)
         if args.only in (None, "plates"):

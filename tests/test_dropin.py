@@ -35,11 +35,9 @@ def test_dropin_exports_reference_names(pdg):
 
 
 def _hassa_mesh(path):
-    with open(path, "w") as fh:
-        fh.write("Center_X Center_Y Area\n")
-        for ix in range(70):
-            for iy in range(60):
-                fh.write(f"{ix - 34.5:.6f} {iy - 29.5:.6f} {1.0:.6f}\n")
+    import importlib
+
+    open(path, "w").write(importlib.import_module("2d_pd_gpu_gb300.plates").hassa_mesh_text())
 
 
 def _build_driver(pdg, tmp):

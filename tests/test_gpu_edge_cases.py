@@ -147,3 +147,17 @@ def test_bad_particles_rejected(pdg):
         ctx.set_particles(np.array([[0.0, 0.0], [1.0, 1.0]]), np.array([1.0, 0.0]))
     with pytest.raises(pdg.PdError):
         ctx.step(1)  # no families yet
+
+
+def test_probes_report_plausible_rates(pdg):
+    """The measured denominators the bench reports: the FP64 / FP32 FMA rates
+    (FP64 well below FP32 on this part) and the copy-engine link rates
+    (positive, below any CPU-GPU link's nominal peak), and bad arguments are
+    refused."""
+    fp64, fp32 = pdg.native.probe_fma_rates(0)
+    assert 0 < fp64 < fp32
+    h2d, d2h, both = pdg.native.probe_link_rates(16 << 20, 0)
+    for r in (h2d, d2h, both):
+        assert 1.0 < r < 2000.0
+    with pytest.raises(pdg.PdError):
+        pdg.native.probe_link_rates(8, 0)
