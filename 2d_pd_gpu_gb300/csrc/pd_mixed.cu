@@ -1055,6 +1055,7 @@ void launch_init_geometry_mixed(const MixedArgs& a, cudaStream_t s) {
   cudaFuncSetAttribute(k_pass_a_mixed<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   cudaFuncSetAttribute(k_pass_b_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   cudaFuncSetAttribute(k_pass_b_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+  cudaFuncSetAttribute(k_pass_b_mixed_export, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   cudaFuncSetAttribute(k_batch_persistent_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   cudaFuncSetAttribute(k_batch_phase_mixed<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
   cudaFuncSetAttribute(k_batch_phase_mixed<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);

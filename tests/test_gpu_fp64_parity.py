@@ -234,6 +234,39 @@ def test_gpu_step_host_equals_staged_copies(pdg):
         x.free()
 
 
+@pytest.mark.parametrize("case", ["one_chunk", "shuffled"])
+def test_gpu_step_host_edge_layouts(pdg, case):
+    """pd_step_host where the slab plan degenerates: 20 particles (one chunk, all
+    but the first slab empty) and a randomly numbered plate (every slab's bonds
+    reach every other slab, so each pass A waits for the whole import and each
+    pass B for every pass A) -- bit for bit pd_set_state + pd_step + pd_get_state."""
+    import dataclasses
+    if case == "one_chunk":
+        p = pdg.plates.make_plate(5, 4, seed=2, bc_rows=1)
+    else:
+        p = pdg.plates.make_plate(70, seed=4, crack="centre-half")
+        perm = np.random.default_rng(7).permutation(p.n)
+        p = dataclasses.replace(p, x=np.ascontiguousarray(p.x[perm]), vol=np.ascontiguousarray(p.vol[perm]),
+                                group_of=np.ascontiguousarray(p.group_of[perm]))
+    p.material.s_c = 2e-4
+    a = p.context()
+    b = p.context()
+    a.step(4)
+    b.step(4)
+    bufs = [pdg.native.PinnedArray((p.n, 2)) for _ in range(3)]
+    hu, hv, hf = (x.array for x in bufs)
+    hu[:], hv[:], hf[:] = a.state()
+    for nsteps in (1, 2, 1):
+        a.set_state(u=hu, v=hv, f=hf)
+        a.step(nsteps)
+        ua, va, fa = a.state()
+        b.step_host(nsteps, hu, hv, hf)
+        assert np.array_equal(ua, hu) and np.array_equal(va, hv) and np.array_equal(fa, hf), (case, nsteps)
+        assert np.array_equal(a.bond_mask(), b.bond_mask())
+    for x in bufs:
+        x.free()
+
+
 def test_gpu_scale_plate_200_cut_1000_steps_bit_exact(pdg, po):
     """The 1000 x 1000 workload's generator at 200 x 200 (same seed rule,
     seeded crack), 1000 steps with bond breaking: bit-exact damage mask,

@@ -278,3 +278,43 @@ def test_mixed_step_host_equals_staged_copies(pdg, shuffle):
     assert broke > 0
     for x in bufs:
         x.free()
+
+
+@pytest.mark.parametrize("case", ["tiny", "one_row_of_tiles", "dense_cluster"])
+def test_mixed_step_host_edge_layouts(pdg, case):
+    """pd_step_host on layouts that stress the slab plan: a plate of one visiting
+    block (most slabs empty), a plate one tile high (every slab a run of
+    neighbouring tiles), and a scrambled plate whose blocks are not staged
+    (they gather from HBM; their bonds reach across every slab) -- each equal,
+    bit for bit, to pd_set_state + pd_step + pd_get_state, one step and three."""
+    import dataclasses
+    if case == "tiny":
+        p = pdg.plates.make_plate(9, seed=3)
+    elif case == "one_row_of_tiles":
+        p = pdg.plates.make_plate(512, 8, seed=3, bc_rows=2)
+    else:
+        p = pdg.plates.make_plate(120, seed=5, crack="centre-half")
+        perm = np.random.default_rng(11).permutation(p.n)
+        far = np.array([[-5.0, -5.0], [5.0, 5.0]])
+        p = dataclasses.replace(p, x=np.ascontiguousarray(np.vstack([p.x[perm], far])),
+                                vol=np.ascontiguousarray(np.concatenate([p.vol[perm], p.vol[:2]])),
+                                group_of=np.ascontiguousarray(np.concatenate([p.group_of[perm],
+                                                                              np.zeros(2, p.group_of.dtype)])))
+    a = p.context(precision=pdg.native.PD_MIXED)
+    b = p.context(precision=pdg.native.PD_MIXED)
+    if case == "dense_cluster":
+        assert b.counters()["unstaged_blocks"] > 0
+    a.step(5)
+    b.step(5)
+    bufs = [pdg.native.PinnedArray((p.n, 2)) for _ in range(3)]
+    hu, hv, hf = (x.array for x in bufs)
+    hu[:], hv[:], hf[:] = a.state()
+    for nsteps in (1, 3, 1):
+        a.set_state(u=hu, v=hv, f=hf)
+        a.step(nsteps)
+        ua, va, fa = a.state()
+        b.step_host(nsteps, hu, hv, hf)
+        assert np.array_equal(ua, hu) and np.array_equal(va, hv) and np.array_equal(fa, hf), (case, nsteps)
+        assert np.array_equal(a.bond_mask(), b.bond_mask())
+    for x in bufs:
+        x.free()
