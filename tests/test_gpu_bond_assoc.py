@@ -74,3 +74,25 @@ def test_bond_assoc_rejects_breaking_and_mixed(pdg):
         pdg.native.Context(pdg.default_params(n1=10.0, n2=10.0, weight_len=3.0, s_c=5e-4))
     with pytest.raises(pdg.PdError):
         pdg.native.Context(pdg.default_params(n1=10.0, n2=10.0, weight_len=3.0, precision=1))
+
+
+def test_bond_assoc_step_host_equals_staged_copies(pdg, hassa):
+    """pd_step_host in the bond-associated mode (the drift reads the host
+    buffers, the last pass B writes them) is pd_set_state + pd_step +
+    pd_get_state, bit for bit, for one step and for two."""
+    a = _ctx(pdg, hassa)
+    b = _ctx(pdg, hassa)
+    a.step(2)
+    b.step(2)
+    n = hassa["x"].shape[0]
+    bufs = [pdg.native.PinnedArray((n, 2)) for _ in range(3)]
+    hu, hv, hf = (x.array for x in bufs)
+    hu[:], hv[:], hf[:] = a.state()
+    for nsteps in (1, 2):
+        a.set_state(u=hu, v=hv, f=hf)
+        a.step(nsteps)
+        ua, va, fa = a.state()
+        b.step_host(nsteps, hu, hv, hf)
+        assert np.array_equal(ua, hu) and np.array_equal(va, hv) and np.array_equal(fa, hf), nsteps
+    for x in bufs:
+        x.free()
