@@ -317,8 +317,8 @@ def e2e_leg(ctx, nat, comm, esteps, device):
         secs = comm.max(time.perf_counter() - t0)
     out = {"value": comm.sum(nb * esteps) / secs, "unit": "bond-updates/s", "ms_per_step": 1e3 * secs / esteps,
            "h2d_bytes_per_step": 3 * 16 * n, "d2h_bytes_per_step": 3 * 16 * n, "steps": esteps,
-           "api": "pd_step_host(1): u, v, f (FP64) read from and written back to page-locked host buffers "
-                  "by the step's own kernels, every step"}
+           "api": "pd_step_host(1): u, v, f (FP64) copied in from page-locked host buffers slab by slab under "
+                  "the first pass, and written back to them by each slab's last pass, every step"}
     comm.barrier()
     t0 = time.perf_counter()
     for _ in range(esteps):
