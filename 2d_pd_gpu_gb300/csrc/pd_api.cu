@@ -1227,6 +1227,10 @@ int pd_checkpoint_load(pd_ctx* c, const void* buf, int64_t bytes) {
 // particle, FP64-latency bound when the SM is not full), so slab launches
 // queued on shared streams would wait out each other's tails.
 constexpr int kSlabs = 9;
+// the first slabs are imported by their drift kernel reading the page-locked input directly
+// (no copy-engine start-up before the first pass A can begin: 0.852-0.855 -> 0.843-0.846 ms
+// per one-step call on the 1M-particle plate); the rest by copy engine
+constexpr int kZeroCopySlabs = 2;
 enum {
   kEvImport = 0,
   kEvCopy = kSlabs,
@@ -1340,14 +1344,22 @@ static cudaError_t enqueue_host_step(pd_ctx* c, int32_t nsteps, const double* u_
   for (int k = 0; k < kSlabs; ++k) {
     const Fp64Args a = slab_args(c, plain, k);  // import slab k
     const size_t off = (size_t)a.i0, cnt = (size_t)(a.n - a.i0);
-    if (cnt > 0) {
-      ck(cudaMemcpyAsync(c->u + off, u_in + 2 * off, cnt * b16, cudaMemcpyHostToDevice, io[1]));
-      ck(cudaMemcpyAsync(c->v + off, v_in + 2 * off, cnt * b16, cudaMemcpyHostToDevice, io[1]));
-      ck(cudaMemcpyAsync(c->f + off, f_in + 2 * off, cnt * b16, cudaMemcpyHostToDevice, io[1]));
+    if (k < kZeroCopySlabs) {  // the drift reads the page-locked input itself
+      Fp64Args z = a;
+      z.in_u = static_cast<const double2*>(mapped_host(u_in));
+      z.in_v = static_cast<const double2*>(mapped_host(v_in));
+      z.in_f = static_cast<const double2*>(mapped_host(f_in));
+      pd::launch_drift_fp64(z, io[0]);
+    } else {
+      if (cnt > 0) {
+        ck(cudaMemcpyAsync(c->u + off, u_in + 2 * off, cnt * b16, cudaMemcpyHostToDevice, io[1]));
+        ck(cudaMemcpyAsync(c->v + off, v_in + 2 * off, cnt * b16, cudaMemcpyHostToDevice, io[1]));
+        ck(cudaMemcpyAsync(c->f + off, f_in + 2 * off, cnt * b16, cudaMemcpyHostToDevice, io[1]));
+      }
+      ck(cudaEventRecord(ev[kEvCopy + k], io[1]));
+      ck(cudaStreamWaitEvent(io[0], ev[kEvCopy + k], 0));
+      pd::launch_drift_fp64(a, io[0]);  // in place, on the device copy
     }
-    ck(cudaEventRecord(ev[kEvCopy + k], io[1]));
-    ck(cudaStreamWaitEvent(io[0], ev[kEvCopy + k], 0));
-    pd::launch_drift_fp64(a, io[0]);  // in place, on the device copy
     ck(cudaEventRecord(ev[kEvImport + k], io[0]));
     for (; next_a < kSlabs && c->slab_need[next_a] <= k; ++next_a) {  // pass A of slabs whose neighbours are in
       cudaStream_t sj = pa[next_a];
