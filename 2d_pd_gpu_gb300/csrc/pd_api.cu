@@ -1217,7 +1217,8 @@ int pd_checkpoint_load(pd_ctx* c, const void* buf, int64_t bytes) {
 // 1/32, 3/32, 1/8, then four of 3/16 0.862; five of 3/16 after 1/16 0.874);
 // slab_need[k] / slab_low[k] = the last / first slab holding a neighbour of
 // slab k's particles.  Streams (io[0], io[1] at high priority): io[1] copies
-// u, v, f in slab by slab, io[0] runs each slab's drift as its copy lands,
+// u, v, f in slab by slab, io[0] runs each slab's drift as its copy lands (the
+// first kZeroCopySlabs slabs' drifts read the input buffers directly),
 // pass A of slab k starts on its own stream once slabs 0 .. slab_need[k] are
 // in, and, in one-step calls, pass B of slab k (its own stream) once pass A
 // of slabs slab_low[k] .. slab_need[k] is done, writing the slab's new state
