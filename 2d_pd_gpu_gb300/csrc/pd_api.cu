@@ -1210,11 +1210,14 @@ int pd_checkpoint_load(pd_ctx* c, const void* buf, int64_t bytes) {
 
 
 // pd_step_host pipeline (FP64 form).  The particles are cut into kSlabs index
-// ranges (multiples of 32): 1/64 and 3/64 of the plate, then seven of 1/8, so
-// the first pass A starts after a few microseconds of copying and the later
-// copies stay ahead of it (1M-particle plate, ms per one-step call: these
-// slabs 0.840; 1/128, 1/128, 1/64, 1/32, 1/16, then seven of 1/8 0.862;
-// 1/32, 3/32, 1/8, then four of 3/16 0.862; five of 3/16 after 1/16 0.874);
+// ranges (multiples of 32): 1/64 and 3/64 of the plate, six of 1/8, then 3/32,
+// 1/16 and 1/32, so the first pass A starts after a few microseconds of
+// copying, the later copies stay ahead of it, and the last slabs, whose pass
+// B and write-back end the call, are short (1M-particle plate, ms per one-step
+// call: these slabs 0.844-0.848 against 0.864-0.887 for seven of 1/8 after the
+// same two; 1/128, 1/128, 1/64, 1/32, 1/16, then seven of 1/8 0.862; 1/32,
+// 3/32, 1/8, then four of 3/16 0.862; five of 3/16 after 1/16 0.874; trailing
+// 1/16, 1/16, 1/32, 1/64, 1/64 or 3/32, 3/32, 1/16, 1/32, 1/32 0.857-0.866);
 // slab_need[k] / slab_low[k] = the last / first slab holding a neighbour of
 // slab k's particles.  Streams (io[0], io[1] at high priority): io[1] copies
 // u, v, f in slab by slab, io[0] runs each slab's drift as its copy lands (the
@@ -1227,7 +1230,7 @@ int pd_checkpoint_load(pd_ctx* c, const void* buf, int64_t bytes) {
 // FP64 pass A block runs for ~70 us whatever the slab's size (one thread per
 // particle, FP64-latency bound when the SM is not full), so slab launches
 // queued on shared streams would wait out each other's tails.
-constexpr int kSlabs = 9;
+constexpr int kSlabs = 11;
 // the first slabs are imported by their drift kernel reading the page-locked input directly
 // (no copy-engine start-up before the first pass A can begin: 0.852-0.855 -> 0.843-0.846 ms
 // per one-step call on the 1M-particle plate); the rest by copy engine
@@ -1243,6 +1246,7 @@ enum {
 };
 
 constexpr int kMaxSlabs = 16;  // the most slabs either form's pipeline uses
+static_assert(kSlabs <= kMaxSlabs, "one pass stream pair per slab");
 
 // The pipeline's streams (io[0], io[1], io[5] at high priority; the per-slab
 // pass streams at low priority) and events.
@@ -1286,8 +1290,8 @@ static int plan_slabs(pd_ctx* c) {
     e = copy_sync(hl.data(), reach + nch, hl.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
   cudaFree(reach);
   PD_CK(c, e);
-  // slab boundaries in chunks: 1/64, 3/64, then seven of 1/8
-  static const int kShare[kSlabs] = {4, 12, 32, 32, 32, 32, 32, 32, 32};  // of 256
+  // slab boundaries in chunks: 1/64, 3/64, six of 1/8, then 3/32, 1/16, 1/32
+  static const int kShare[kSlabs] = {4, 12, 32, 32, 32, 32, 32, 32, 24, 16, 8};  // of 256
   std::vector<int64_t> bc(kSlabs + 1, 0);
   int acc = 0;
   for (int k = 0; k < kSlabs; ++k) {
@@ -1422,6 +1426,7 @@ static cudaError_t enqueue_host_step(pd_ctx* c, int32_t nsteps, const double* u_
 // the input and output buffers the same, slab k's pass B overwrites only ids
 // of id slabs 0 .. k, whose copies in are complete before its import.
 constexpr int kMixedSlabs = 16;
+static_assert(kMixedSlabs <= kMaxSlabs, "one pass stream pair per slab");
 enum { kMEvIn = 0, kMEvImport = kMixedSlabs, kMEvA = 2 * kMixedSlabs, kMEvB = 3 * kMixedSlabs,
        kMEvStart = 4 * kMixedSlabs, kMEvCount = 4 * kMixedSlabs + 1 };
 
