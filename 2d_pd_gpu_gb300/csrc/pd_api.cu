@@ -1400,7 +1400,7 @@ static cudaError_t enqueue_host_step(pd_ctx* c, int32_t nsteps, const double* u_
 }
 
 // pd_step_host pipeline, mixed form: a wavefront over slabs of visiting blocks
-// (spatial tiles in order; two small leading slabs, then even ones).  A slab is
+// (spatial tiles in order, eight even slabs).  A slab is
 // a run of visiting blocks, and everything about it -- which positions it
 // imports, which slabs its bonds reach -- is taken through the blocks' visit
 // records, since a tile's last block holds fewer chunks than kHaloBlock / 32.
@@ -1411,7 +1411,11 @@ static cudaError_t enqueue_host_step(pd_ctx* c, int32_t nsteps, const double* u_
 // buffers (u, v, f); the output goes straight from each slab's pass B to the
 // output buffers (on the 1M-particle plate: 0.56 ms per one-step call,
 // against 0.63 with pass B writing the staging buffers and copy engines taking
-// id slabs out, and 0.67 with an import kernel reading the host buffers):
+// id slabs out, and 0.67 with an import kernel reading the host buffers).
+// Each slab costs three copies in: 8 even slabs measured 0.556-0.566 ms per
+// call (a Python harness) against 0.599-0.603 for 16 (two of 1/64, one of 1/32, then even); 9 or
+// 10 slabs with short leading or trailing ones the same as 8, 7 slabs 0.579,
+// 6 0.609, 4 0.605 (each a bit-identical result).  The streams:
 //   io[1]  copies id slab k in;
 //   io[0]  imports slab k (conversion to the scaled state + drift, from the
 //          staging buffers) once id slabs 0 .. k are in;
@@ -1425,7 +1429,7 @@ static cudaError_t enqueue_host_step(pd_ctx* c, int32_t nsteps, const double* u_
 // rows; any numbering is correct, a scrambled one just pipelines less).  With
 // the input and output buffers the same, slab k's pass B overwrites only ids
 // of id slabs 0 .. k, whose copies in are complete before its import.
-constexpr int kMixedSlabs = 16;
+constexpr int kMixedSlabs = 8;
 static_assert(kMixedSlabs <= kMaxSlabs, "one pass stream pair per slab");
 enum { kMEvIn = 0, kMEvImport = kMixedSlabs, kMEvA = 2 * kMixedSlabs, kMEvB = 3 * kMixedSlabs,
        kMEvStart = 4 * kMixedSlabs, kMEvCount = 4 * kMixedSlabs + 1 };
@@ -1452,15 +1456,10 @@ static int plan_slabs_mixed(pd_ctx* c) {
     const auto it = std::upper_bound(first.begin(), first.end(), p / 32);
     return (int64_t)(it == first.begin() ? 0 : (it - first.begin()) - 1);
   };
-  // slabs of visiting blocks: 1/64, 1/64, 1/32 of the plate, then 13 even ones (the first
-  // copies out start after a few percent of the plate is in)
+  // even slabs of visiting blocks (a plate of fewer blocks than slabs leaves some empty)
   const int K = kMixedSlabs;
   std::vector<int64_t> bc(K + 1);
-  bc[0] = 0;
-  bc[1] = std::min(nb, std::max<int64_t>(1, nb / 64));
-  bc[2] = std::min(nb, std::max<int64_t>(bc[1], 2 * (nb / 64)));
-  bc[3] = std::min(nb, std::max<int64_t>(bc[2], 4 * (nb / 64)));
-  for (int k = 4; k <= K; ++k) bc[k] = bc[3] + (nb - bc[3]) * (k - 3) / (K - 3);
+  for (int k = 0; k <= K; ++k) bc[k] = nb * k / K;
   auto slab_of_block = [&](int64_t blk) {
     int k = 0;
     while (k + 1 < K && blk >= bc[k + 1]) ++k;
