@@ -1327,8 +1327,13 @@ static Fp64Args slab_args(const pd_ctx* c, const Fp64Args& a, int k) {
 
 // Enqueues pd_step_host's pipeline (slabs planned) on the main stream.  (A
 // CUDA graph of it measured the same: the GPU, not the enqueue, sets the pace.)
+// dropin: pd_compute_velocity's one call instead (nsteps 1; f_in is acce):
+// each slab's import takes u, velocity and acce and forms the FP32 shadow
+// (no drift), and pass B is the drop-in kick (mode 2), writing velocity,
+// acce and the force to out's buffers.
 static cudaError_t enqueue_host_step(pd_ctx* c, int32_t nsteps, const double* u_in, const double* v_in,
-                                     const double* f_in, const Fp64Args& plain, const Fp64Args& out, bool brk) {
+                                     const double* f_in, const Fp64Args& plain, const Fp64Args& out, bool brk,
+                                     bool dropin = false) {
   cudaError_t e = cudaSuccess;
   auto ck = [&](cudaError_t r) {
     if (e == cudaSuccess) e = r;
@@ -1349,21 +1354,30 @@ static cudaError_t enqueue_host_step(pd_ctx* c, int32_t nsteps, const double* u_
   for (int k = 0; k < kSlabs; ++k) {
     const Fp64Args a = slab_args(c, plain, k);  // import slab k
     const size_t off = (size_t)a.i0, cnt = (size_t)(a.n - a.i0);
-    if (k < kZeroCopySlabs) {  // the drift reads the page-locked input itself
+    if (k < kZeroCopySlabs) {  // the import kernel reads the page-locked input itself
       Fp64Args z = a;
       z.in_u = static_cast<const double2*>(mapped_host(u_in));
       z.in_v = static_cast<const double2*>(mapped_host(v_in));
-      z.in_f = static_cast<const double2*>(mapped_host(f_in));
-      pd::launch_drift_fp64(z, io[0]);
+      if (dropin) {
+        z.in_a = static_cast<const double2*>(mapped_host(f_in));
+        pd::launch_shadow_fp64(z, io[0]);
+      } else {
+        z.in_f = static_cast<const double2*>(mapped_host(f_in));
+        pd::launch_drift_fp64(z, io[0]);
+      }
     } else {
       if (cnt > 0) {
         ck(cudaMemcpyAsync(c->u + off, u_in + 2 * off, cnt * b16, cudaMemcpyHostToDevice, io[1]));
         ck(cudaMemcpyAsync(c->v + off, v_in + 2 * off, cnt * b16, cudaMemcpyHostToDevice, io[1]));
-        ck(cudaMemcpyAsync(c->f + off, f_in + 2 * off, cnt * b16, cudaMemcpyHostToDevice, io[1]));
+        ck(cudaMemcpyAsync((dropin ? c->acc : c->f) + off, f_in + 2 * off, cnt * b16, cudaMemcpyHostToDevice,
+                           io[1]));
       }
       ck(cudaEventRecord(ev[kEvCopy + k], io[1]));
       ck(cudaStreamWaitEvent(io[0], ev[kEvCopy + k], 0));
-      pd::launch_drift_fp64(a, io[0]);  // in place, on the device copy
+      if (dropin)
+        pd::launch_shadow_fp64(a, io[0]);  // on the device copy
+      else
+        pd::launch_drift_fp64(a, io[0]);  // in place, on the device copy
     }
     ck(cudaEventRecord(ev[kEvImport + k], io[0]));
     for (; next_a < kSlabs && c->slab_need[next_a] <= k; ++next_a) {  // pass A of slabs whose neighbours are in
@@ -1375,7 +1389,7 @@ static cudaError_t enqueue_host_step(pd_ctx* c, int32_t nsteps, const double* u_
       for (; one && next_b < kSlabs && c->slab_need[next_b] <= next_a; ++next_b) {
         cudaStream_t sb = pb[next_b];
         for (int q = c->slab_low[next_b]; q <= c->slab_need[next_b]; ++q) ck(cudaStreamWaitEvent(sb, ev[kEvA + q], 0));
-        pd::launch_pass_b_fp64(slab_args(c, out, next_b), 0, sb);
+        pd::launch_pass_b_fp64(slab_args(c, out, next_b), dropin ? 2 : 0, sb);
         ck(cudaEventRecord(ev[kEvB + next_b], sb));
       }
     }
@@ -1640,6 +1654,22 @@ int pd_compute_velocity(pd_ctx* c, const double* u, double* velocity, double* ac
   PD_CK(c, cudaSetDevice(c->p.device));
   const size_t b = (size_t)c->n * sizeof(double2);
   cudaStream_t s = c->stream;
+  if (!bond_assoc(c) && mapped_host(u) && mapped_host(velocity) && mapped_host(acce) && mapped_host(netF)) {
+    // page-locked buffers (pd_host_alloc): pd_step_host's slab pipeline, the
+    // copies in overlapping pass A and each slab's pass B writing its results
+    // back while later slabs compute; the same results as the staged call
+    const int rp = plan_slabs(c);
+    if (rp != PD_OK) return rp;
+    Fp64Args out = fp64_args(c);
+    out.out_v = static_cast<double2*>(mapped_host(velocity));
+    out.out_a = static_cast<double2*>(mapped_host(acce));
+    out.out_f = static_cast<double2*>(mapped_host(netF));
+    PD_CK(c, enqueue_host_step(c, 1, u, velocity, acce, fp64_args(c), out, c->p.s_c > 0.0, true));
+    PD_CK(c, cudaGetLastError());
+    PD_CK(c, cudaStreamSynchronize(s));
+    c->steps += 1;
+    return check_after_step(c);
+  }
   PD_CK(c, cudaMemcpyAsync(c->u, u, b, cudaMemcpyHostToDevice, s));
   PD_CK(c, cudaMemcpyAsync(c->v, velocity, b, cudaMemcpyHostToDevice, s));
   PD_CK(c, cudaMemcpyAsync(c->acc, acce, b, cudaMemcpyHostToDevice, s));

@@ -101,10 +101,16 @@ __global__ void __launch_bounds__(kBlock) k_drift(Fp64Args a) {
   if (i < a.n) drift_particle(a, i);
 }
 
+// The FP32 shadow of u for particles i0 <= i < n; with in_u / in_v / in_a
+// set (pd_compute_velocity on page-locked buffers), u, velocity and acce are
+// first read from host memory into the device state.
 __global__ void __launch_bounds__(kBlock) k_shadow(Fp64Args a) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t i = a.i0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
-  const double2 u = a.u[i];
+  const double2 u = a.in_u ? a.in_u[i] : a.u[i];
+  if (a.in_u) a.u[i] = u;
+  if (a.in_v) a.v[i] = a.in_v[i];
+  if (a.in_a) a.acc[i] = a.in_a[i];
   a.u32[i] = make_float2((float)u.x, (float)u.y);
 }
 
@@ -251,8 +257,11 @@ __device__ __forceinline__ void pass_b_particle(const Fp64Args& a, int64_t i) {
     a.u32[i] = make_float2((float)u.x, (float)u.y);
   }
   a.v[i] = v;
-  if (a.out_v) {  // pd_step_host's last pass: the state straight to host memory
-    a.out_u[i] = a.u[i];
+  if (a.out_v) {  // pd_step_host's last pass, or the drop-in call: the results straight to host memory
+    if (MODE == 2)
+      a.out_a[i] = make_double2(anx, any);
+    else
+      a.out_u[i] = a.u[i];
     a.out_v[i] = v;
     a.out_f[i] = make_double2(fx, fy);
   }
@@ -383,7 +392,7 @@ void launch_drift_fp64(const Fp64Args& a, cudaStream_t s) {
 }
 
 void launch_shadow_fp64(const Fp64Args& a, cudaStream_t s) {
-  if (a.n > 0) k_shadow<<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a);
+  if (a.n > a.i0) k_shadow<<<(unsigned)blocks_for(a.n - a.i0), kBlock, 0, s>>>(a);
 }
 
 // pdl: launched with programmatic stream serialization (the blocks start

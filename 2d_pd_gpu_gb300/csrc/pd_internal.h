@@ -89,13 +89,17 @@ struct Fp64Args {
   double2* hg;  // 2 k_hg sum_j V_j (u_j - u_i), pass A -> pass B
   // pd_step_host: the drift takes the state from page-locked host memory
   // (read over the CPU-GPU link by the kernel itself) and the last pass B
-  // writes it back there; null otherwise
+  // writes it back there; pd_compute_velocity with page-locked buffers: the
+  // import (k_shadow) takes u, velocity, acce (in_a) from there and pass B
+  // (mode 2) writes velocity, acce (out_a) and the force back; null otherwise
   const double2* in_u;
   const double2* in_v;
   const double2* in_f;
+  const double2* in_a;
   double2* out_u;
   double2* out_v;
   double2* out_f;
+  double2* out_a;
   double c11, c12, c33;
   double dt, dt2, inv_rho, det_guard, k_hg, damage_fail;
   unsigned long long* counters;
@@ -223,7 +227,7 @@ void scan_exclusive_i64(const int64_t* in, int64_t* out, int64_t n, cudaStream_t
 // ---- FP64 step (pd_fp64.cu)
 void launch_init_geometry_fp64(const Fp64Args& a, cudaStream_t s);
 void launch_drift_fp64(const Fp64Args& a, cudaStream_t s);
-void launch_shadow_fp64(const Fp64Args& a, cudaStream_t s);  // u32 := (float)u
+void launch_shadow_fp64(const Fp64Args& a, cudaStream_t s);  // [import in_u, in_v, in_a,] u32 := (float)u; i0 <= i < n
 // reach[k] := max(reach[k], largest neighbour id of slab k); reach zeroed by the caller
 void launch_slab_reach(int64_t n, const int64_t* row_ptr, const int32_t* col, int64_t slab, int32_t* reach,
                        int32_t* low, cudaStream_t s);

@@ -381,10 +381,13 @@ class Context:
     def synchronize(self):
         self._ck(lib().pd_synchronize(self._h))
 
-    def compute_velocity(self, u, velocity, acce):
-        """The reference GPU wrapper's one-call contract on host arrays (in place)."""
+    def compute_velocity(self, u, velocity, acce, netf=None):
+        """The reference GPU wrapper's one-call contract on host arrays (velocity
+        and acce in place; the force into netf, a new array when None).  With
+        every buffer page-locked (PinnedArray.array) the call is pipelined."""
         u = np.ascontiguousarray(u, dtype=np.float64)
-        netf = np.zeros_like(velocity)
+        if netf is None:
+            netf = np.zeros_like(velocity)
         self._ck(lib().pd_compute_velocity(self._h, ptr(u), ptr(velocity), ptr(acce), ptr(netf)))
         return netf
 

@@ -237,7 +237,11 @@ int pd_synchronize(pd_ctx* ctx);
  * reference position), velocity[n][2] and acce[n][2]; writes
  * velocity += 0.5 (acce + f/rho) dt, acce = f/rho and netF = f.  Device
  * buffers stay allocated between calls.  The bond mask persists across calls
- * and breaks bonds as in pd_step when s_c > 0. */
+ * and breaks bonds as in pd_step when s_c > 0.  When all four buffers are
+ * page-locked (pd_host_alloc) and the context is in the plain mode, the call
+ * runs pd_step_host's slab pipeline: the copies in overlap the first pass,
+ * and each slab's results go back while later slabs compute; the results are
+ * the same bit for bit. */
 int pd_compute_velocity(pd_ctx* ctx, const double* u, double* velocity, double* acce, double* netF);
 
 /* One FP64 force + kick, pd_compute_velocity's arithmetic, on CALLER-OWNED

@@ -267,6 +267,47 @@ def test_gpu_step_host_edge_layouts(pdg, case):
         x.free()
 
 
+@pytest.mark.parametrize("case", ["plate", "one_chunk", "shuffled"])
+def test_gpu_compute_velocity_pinned_equals_staged(pdg, case):
+    """pd_compute_velocity on page-locked buffers (pd_step_host's slab pipeline,
+    each slab's pass B writing velocity, acce and the force back) against the
+    same calls on pageable buffers (whole-array copies): bit for bit, velocity
+    and acce in place, over repeated calls that break bonds, on a 300 x 300
+    plate and on the layouts where the slab plan degenerates."""
+    import dataclasses
+    if case == "plate":
+        p = pdg.plates.make_plate(300, seed=3, crack="centre-half")
+    elif case == "one_chunk":
+        p = pdg.plates.make_plate(5, 4, seed=2, bc_rows=1)
+    else:
+        p = pdg.plates.make_plate(70, seed=4, crack="centre-half")
+        perm = np.random.default_rng(7).permutation(p.n)
+        p = dataclasses.replace(p, x=np.ascontiguousarray(p.x[perm]), vol=np.ascontiguousarray(p.vol[perm]),
+                                group_of=np.ascontiguousarray(p.group_of[perm]))
+    p.material.s_c = 2e-4
+    run = p.context()
+    run.step(40)  # a strained state, so that the calls below break bonds
+    u, v, f = run.state()
+    run.close()
+    acc = f / p.material.rho
+    a = p.context()
+    b = p.context()
+    bufs = [pdg.native.PinnedArray((p.n, 2)) for _ in range(4)]
+    hu, hv, ha, hf = (x.array for x in bufs)
+    hu[:], hv[:], ha[:] = u, v, acc
+    for _ in range(4):
+        fa = a.compute_velocity(u, v, acc)  # pageable buffers: staged copies
+        b.compute_velocity(hu, hv, ha, netf=hf)  # page-locked buffers: the slab pipeline
+        assert np.array_equal(v, hv) and np.array_equal(acc, ha) and np.array_equal(fa, hf), case
+        assert np.array_equal(a.bond_mask(), b.bond_mask()) and np.array_equal(a.damage(), b.damage())
+        u = u + v * p.dt + 0.5 * acc * p.dt ** 2  # the reference host loop's drift, the same for both
+        hu[:] = u
+    if case != "one_chunk":
+        assert int((a.bond_mask() == 0).sum()) > 0, "the calls are meant to break bonds"
+    for x in bufs:
+        x.free()
+
+
 def test_gpu_scale_plate_200_cut_1000_steps_bit_exact(pdg, po):
     """The 1000 x 1000 workload's generator at 200 x 200 (same seed rule,
     seeded crack), 1000 steps with bond breaking: bit-exact damage mask,
