@@ -299,11 +299,14 @@ def accuracy(pdg, plate, device, checkpoints=(100, 500, 1000)):
     return out
 
 
-def e2e_leg(ctx, nat, comm, esteps, device):
+def e2e_leg(ctx, nat, comm, esteps, device, dropin=False):
     """The step end to end through the public API: pd_step_host(1) with the
     state in page-locked host buffers every step (read and written over the
     CPU-GPU link inside the timed region), and the same through the
-    three-call sequence pd_set_state -> pd_step(1) -> pd_get_state."""
+    three-call sequence pd_set_state -> pd_step(1) -> pd_get_state.  dropin
+    (FP64 contexts): also pd_compute_velocity, the reference GPU wrapper's
+    one-call contract, on page-locked buffers (it changes the context's state:
+    run it last)."""
     n, nb = ctx.n, ctx.nnz
     bufs = [nat.PinnedArray((n, 2)) for _ in range(3)]
     u, v, f = (b.array for b in bufs)
@@ -329,6 +332,25 @@ def e2e_leg(ctx, nat, comm, esteps, device):
     out["copies_api"] = {"value": comm.sum(nb * esteps) / secs, "api": "pd_set_state -> pd_step(1) -> pd_get_state"}
     for b in bufs:
         b.free()
+    if dropin:
+        bufs = [nat.PinnedArray((n, 2)) for _ in range(4)]
+        u, v, a, f = (b.array for b in bufs)
+        u[:], v[:], _ = ctx.state()
+        a[:] = 0.0
+        ctx.compute_velocity(u, v, a, netf=f)  # outside the timed region
+        comm.barrier()
+        t0 = time.perf_counter()
+        for _ in range(esteps):
+            ctx.compute_velocity(u, v, a, netf=f)
+        secs = comm.max(time.perf_counter() - t0)
+        out["dropin_api"] = {"value": comm.sum(nb * esteps) / secs, "unit": "bond-updates/s",
+                             "ms_per_step": 1e3 * secs / esteps, "h2d_bytes_per_step": 3 * 16 * n,
+                             "d2h_bytes_per_step": 3 * 16 * n, "steps": esteps,
+                             "api": "pd_compute_velocity (compute_velocity_GPU_host's contract, one force + kick "
+                                    "per call): u, velocity, acce in from page-locked buffers, velocity, acce, "
+                                    "netF back, by the same slab pipeline"}
+        for b in bufs:
+            b.free()
     # the link bound: the step's bytes each way at the measured concurrent copy rate
     h2d, d2h, both = nat.probe_link_rates(3 * 16 * n, device)
     out["link"] = {"h2d_gbs": h2d, "d2h_gbs": d2h, "both_gbs_per_direction": both,
@@ -537,7 +559,7 @@ def run_ours(args, comm):
                                             "per bond take ~8x longer than the step's algorithmic HBM bytes"}
     # end to end through the public API with pinned host buffers, every step
     if not args.no_e2e:
-        result["e2e"] = e2e_leg(ctx, nat, comm, min(args.steps, args.e2e_steps), device)
+        result["e2e"] = e2e_leg(ctx, nat, comm, min(args.steps, args.e2e_steps), device, dropin=True)
     ctx.close()
     if not args.no_mixed:
         mctx = plate.context(precision=nat.PD_MIXED, device=device)

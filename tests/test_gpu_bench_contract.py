@@ -40,6 +40,8 @@ def test_bench_line_keys_on_a_small_plate():
         n = d["config"]["particles"]
         assert e["value"] > 0 and e["h2d_bytes_per_step"] == e["d2h_bytes_per_step"] == 48 * n
         assert 0 < e["link"]["bound_ms_per_step"] < e["ms_per_step"]
+    dr = d["e2e"]["dropin_api"]
+    assert dr["value"] > 0 and dr["h2d_bytes_per_step"] == dr["d2h_bytes_per_step"] == 48 * d["config"]["particles"]
     assert {"sm_mhz", "sm_max_mhz", "reasons"} <= set(d["clocks"])
     assert d["bond_assoc"]["device"]["ms_per_step"] > 0 and d["bond_assoc"]["particles"] == 4064
 
