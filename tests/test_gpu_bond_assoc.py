@@ -69,6 +69,32 @@ def test_bond_assoc_compute_velocity_dropin(pdg, hassa):
     assert normwise(f, hassa["b_f1"]) < F_TOL
 
 
+def test_bond_assoc_compute_velocity_pinned_equals_staged(pdg, hassa):
+    """pd_compute_velocity in the bond-associated mode on page-locked buffers
+    (what the C++ drop-in passes) against pageable buffers: bit for bit over
+    three calls with the reference's drift."""
+    a = _ctx(pdg, hassa)
+    b = _ctx(pdg, hassa)
+    n = hassa["x"].shape[0]
+    dt = hassa["params"][5]
+    v = np.zeros((n, 2))
+    v[hassa["top"]] = [0.0, 5.0]
+    u = v * dt
+    u[hassa["bottom"]] = 0.0
+    acc = np.zeros((n, 2))
+    bufs = [pdg.native.PinnedArray((n, 2)) for _ in range(4)]
+    hu, hv, ha, hf = (x.array for x in bufs)
+    hu[:], hv[:], ha[:] = u, v, acc
+    for _ in range(3):
+        fa = a.compute_velocity(u, v, acc)
+        b.compute_velocity(hu, hv, ha, netf=hf)
+        assert np.array_equal(v, hv) and np.array_equal(acc, ha) and np.array_equal(fa, hf)
+        u = u + v * dt + 0.5 * acc * dt ** 2
+        hu[:] = u
+    for x in bufs:
+        x.free()
+
+
 def test_bond_assoc_rejects_breaking_and_mixed(pdg):
     with pytest.raises(pdg.PdError):
         pdg.native.Context(pdg.default_params(n1=10.0, n2=10.0, weight_len=3.0, s_c=5e-4))
