@@ -17,9 +17,12 @@
 // Pass A runs one warp per particle and one lane per bond (families <= 64
 // bonds, two per lane): the family's bond data is staged in shared memory,
 // lane q sums K_q and D_q over k in family order (the oracle's order), and,
-// once the P_b of every bond are in shared memory, lane j sums T_ij over b
-// (re-reading, for its first bond, the weight row it formed for K_q: the
-// weight matrix is symmetric, and lane j's row j is what both sums use).
+// once the P_b of every bond are in shared memory, lane j sums T_ij over b.
+// The weight matrix is symmetric bit for bit (its products commute, and the
+// exponential factor is ordered by the two lengths), so a family of <= 32
+// bonds evaluates its lower triangle once, spread over all 32 lanes, into
+// shared memory, and both sums read it there; a larger family evaluates each
+// lane's row inside the K_q loop and keeps the rows of the first 32 bonds.
 // The weight is evaluated in factored form: exp(-n1 |L_b - L_k| / l) =
 // e+(min L) e-(max L) with e+-(L) = exp(+-n1 L / l) per bond, the cosine as
 // (xi_b . xi_k) (1/L_b)(1/L_k), and an integer n2 <= 64 by repeated squaring
@@ -42,7 +45,7 @@ struct BaFamily {  // one particle's bonds, in family order
       dy[kBaMax];
   double P[kBaMax][4];
   int64_t slot[kBaMax];
-  double wrow[32][32];  // wrow[k][l] = w(l, k): lane l's weight row for its first bond, kept for the T_ij sums
+  double wrow[32][32];  // wrow[k][l] = w(l, k) for bonds l, k < 32
 };
 
 struct BaWeight {
@@ -119,12 +122,31 @@ __global__ void __launch_bounds__(32 * kBaWarps) k_ba_pass_a(Fp64Args a, BondAss
   for (int o = 16; o; o >>= 1) lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
   wf.direct = !(fabs(b.n1) * lmax * b.inv_wlen < 600.0);
   __syncwarp();
+  const bool tri = n <= 32;
+  if (tri) {  // pair p = k (k + 1) / 2 + q, q <= k, of the lower triangle
+    const int npair = n * (n + 1) / 2;
+    for (int p = lane; p < npair; p += 32) {
+      int k = (int)((sqrtf(8.0f * (float)p + 1.0f) - 1.0f) * 0.5f);
+      if ((k + 1) * (k + 2) / 2 <= p) ++k;
+      if (k * (k + 1) / 2 > p) --k;
+      const int q = p - k * (k + 1) / 2;
+      const double wqk = wf(F, q, k);
+      F.wrow[k][q] = wqk;
+      F.wrow[q][k] = wqk;
+    }
+    __syncwarp();
+  }
   // P_b = sigma_b K_b^-1 of bond q
   for (int q = lane; q < n; q += 32) {
     double k11 = 0.0, k12 = 0.0, k22 = 0.0, d11 = 0.0, d12 = 0.0, d21 = 0.0, d22 = 0.0;
     for (int k = 0; k < n; ++k) {
-      const double wqk = wf(F, q, k);
-      if (q < 32) F.wrow[k][q] = wqk;  // (q == lane: the thread's own row, read back below)
+      double wqk;
+      if (tri) {
+        wqk = F.wrow[k][q];
+      } else {
+        wqk = wf(F, q, k);
+        if (q < 32 && k < 32) F.wrow[k][q] = wqk;  // (q == lane: the thread's own row, read back below)
+      }
       const double wv = wqk * F.vv[k];
       const double ekx = F.ex[k], eky = F.ey[k];
       const double t0 = wv * ekx, t1 = wv * eky;
@@ -163,8 +185,8 @@ __global__ void __launch_bounds__(32 * kBaWarps) k_ba_pass_a(Fp64Args a, BondAss
   for (int jj = lane; jj < n; jj += 32) {
     double m11 = 0.0, m12 = 0.0, m21 = 0.0, m22 = 0.0;
     for (int q = 0; q < n; ++q) {
-      // w(jj, q) = w(q, jj): the row this thread kept for its first bond, recomputed for the second
-      const double wv = (jj < 32 ? F.wrow[q][jj] : wf(F, jj, q)) * F.vv[q];
+      // w(jj, q) = w(q, jj), kept for pairs of bonds < 32, recomputed for the others
+      const double wv = (jj < 32 && q < 32 ? F.wrow[q][jj] : wf(F, jj, q)) * F.vv[q];
       m11 = fma(wv, F.P[q][0], m11);
       m12 = fma(wv, F.P[q][1], m12);
       m21 = fma(wv, F.P[q][2], m21);

@@ -55,6 +55,30 @@ def test_bond_assoc_matches_oracle_over_steps(pdg, po, hassa):
     assert normwise(u, sim.u) < 1e-12 and normwise(v, sim.v) < 1e-12 and normwise(f, sim.f) < 1e-11
 
 
+@pytest.mark.parametrize("horizon", [3.2, 3.6, 4.4])
+def test_bond_assoc_wide_families_match_oracle(pdg, po, horizon):
+    """Families around and above 32 bonds (up to ~32, ~40 and ~61 at these
+    horizons), where pass A switches from evaluating the weight matrix's lower
+    triangle to per-lane rows with a partial cache: against the oracle over
+    3 steps, to the same tolerance as on the reference's mesh."""
+    p = pdg.plates.make_plate(26, seed=5, horizon=horizon)
+    rp, col = po.build_families(p.x, p.cutoff, p.cracks)
+    deg = np.diff(rp)
+    assert deg.max() <= 64
+    assert (deg > 32).any() and (deg <= 32).any()
+    ctx = pdg.native.Context(pdg.default_params(E=p.material.E, nu=p.material.nu, rho=p.material.rho, dt=p.dt,
+                                                s_c=0.0, n1=4.0, n2=3.0, weight_len=p.cutoff))
+    ctx.set_particles(p.x, p.vol)
+    ctx.set_families(rp, col)
+    ctx.set_bc(p.group_kind, p.group_val, p.group_of)
+    sim = po.OracleSim(p.x, p.vol, rp, col, E=p.material.E, nu=p.material.nu, rho=p.material.rho, dt=p.dt, s_c=0.0,
+                       n1=4.0, n2=3.0, wlen=p.cutoff, bc=p.group_of, group_kind=p.group_kind, group_val=p.group_val)
+    ctx.step(3)
+    sim.step(3)
+    u, v, f = ctx.state()
+    assert normwise(u, sim.u) < 1e-12 and normwise(v, sim.v) < 1e-12 and normwise(f, sim.f) < 1e-11
+
+
 def test_bond_assoc_compute_velocity_dropin(pdg, hassa):
     """pd_compute_velocity in the bond-associated mode after the reference's host drift."""
     ctx = _ctx(pdg, hassa)
