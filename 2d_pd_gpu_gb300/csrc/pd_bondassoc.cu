@@ -26,8 +26,11 @@
 // The weight is evaluated in factored form: exp(-n1 |L_b - L_k| / l) =
 // e+(min L) e-(max L) with e+-(L) = exp(+-n1 L / l) per bond, the cosine as
 // (xi_b . xi_k) (1/L_b)(1/L_k), and an integer n2 <= 64 by repeated squaring
-// (pow otherwise; the direct exp where n1 L / l could overflow).  The terms
-// are those of the oracle's ba_pass_a (--fmad=false, explicit fma()); the
+// (pow otherwise; the direct exp where n1 L / l could overflow).  The sums
+// run in the oracle's order (ba_pass_a; --fmad=false, explicit fma()), but
+// the per-bond products V_k xi_k (x) xi_k, V_k d_k (x) xi_k and V_b P_b are
+// formed once per bond and then weighted (the oracle weights V_k first:
+// 7 + 4 FP64 operations per ordered pair here against 10 + 5), and the
 // weights differ from its libm exp / pow / division by a few ulp, so GPU and
 // oracle agree to rounding (1e-12 normwise), not bit for bit.  No bond
 // breaking here (the reference has none).
@@ -38,12 +41,13 @@ namespace pd {
 namespace {
 
 constexpr int kBaMax = 64;
-constexpr int kBaWarps = 2;  // particles per block of pass A (30 KB of shared memory per block)
+constexpr int kBaWarps = 2;  // particles per block of pass A (35 KB of shared memory per block)
 
 struct BaFamily {  // one particle's bonds, in family order
-  double ex[kBaMax], ey[kBaMax], rl[kBaMax], len[kBaMax], ep[kBaMax], em[kBaMax], vv[kBaMax], dx[kBaMax],
-      dy[kBaMax];
-  double P[kBaMax][4];
+  double ex[kBaMax], ey[kBaMax], rl[kBaMax], len[kBaMax], ep[kBaMax], em[kBaMax], vv[kBaMax];
+  double M[kBaMax][3];  // V_k xi_k (x) xi_k: (xx, xy, yy)
+  double N[kBaMax][4];  // V_k d_k (x) xi_k: (dx xx, dx xy, dy xx, dy xy) with xy = the xi components
+  double P[kBaMax][4];  // V_b sigma_b K_b^-1
   int64_t slot[kBaMax];
   double wrow[32][32];  // wrow[k][l] = w(l, k) for bonds l, k < 32
 };
@@ -110,9 +114,16 @@ __global__ void __launch_bounds__(32 * kBaWarps) k_ba_pass_a(Fp64Args a, BondAss
       F.rl[q] = 1.0 / l;
       F.ep[q] = exp(b.n1 * (l * b.inv_wlen));
       F.em[q] = exp(-b.n1 * (l * b.inv_wlen));
-      F.vv[q] = a.vol[j];
-      F.dx[q] = uj.x - ui.x;
-      F.dy[q] = uj.y - ui.y;
+      const double vj = a.vol[j], dx = uj.x - ui.x, dy = uj.y - ui.y;
+      const double t0 = vj * e.x, t1 = vj * e.y;
+      F.vv[q] = vj;
+      F.M[q][0] = t0 * e.x;
+      F.M[q][1] = t0 * e.y;
+      F.M[q][2] = t1 * e.y;
+      F.N[q][0] = dx * t0;
+      F.N[q][1] = dx * t1;
+      F.N[q][2] = dy * t0;
+      F.N[q][3] = dy * t1;
       F.slot[q] = s;
       lmax = fmax(lmax, l);
     }
@@ -147,17 +158,13 @@ __global__ void __launch_bounds__(32 * kBaWarps) k_ba_pass_a(Fp64Args a, BondAss
         wqk = wf(F, q, k);
         if (q < 32 && k < 32) F.wrow[k][q] = wqk;  // (q == lane: the thread's own row, read back below)
       }
-      const double wv = wqk * F.vv[k];
-      const double ekx = F.ex[k], eky = F.ey[k];
-      const double t0 = wv * ekx, t1 = wv * eky;
-      k11 = fma(t0, ekx, k11);
-      k12 = fma(t0, eky, k12);
-      k22 = fma(t1, eky, k22);
-      const double dkx = F.dx[k], dky = F.dy[k];
-      d11 = fma(dkx, t0, d11);
-      d12 = fma(dkx, t1, d12);
-      d21 = fma(dky, t0, d21);
-      d22 = fma(dky, t1, d22);
+      k11 = fma(wqk, F.M[k][0], k11);
+      k12 = fma(wqk, F.M[k][1], k12);
+      k22 = fma(wqk, F.M[k][2], k22);
+      d11 = fma(wqk, F.N[k][0], d11);
+      d12 = fma(wqk, F.N[k][1], d12);
+      d21 = fma(wqk, F.N[k][2], d21);
+      d22 = fma(wqk, F.N[k][3], d22);
     }
     const double det = fma(k11, k22, -(k12 * k12));
     if (!(det > a.det_guard * (k11 * k22))) {
@@ -172,10 +179,11 @@ __global__ void __launch_bounds__(32 * kBaWarps) k_ba_pass_a(Fp64Args a, BondAss
     const double s11 = fma(a.c11, e11, a.c12 * e22);
     const double s22 = fma(a.c12, e11, a.c11 * e22);
     const double s12 = a.c33 * e12;
-    F.P[q][0] = fma(s11, q11, s12 * q12);
-    F.P[q][1] = fma(s11, q12, s12 * q22);
-    F.P[q][2] = fma(s12, q11, s22 * q12);
-    F.P[q][3] = fma(s12, q12, s22 * q22);
+    const double vq = F.vv[q];
+    F.P[q][0] = vq * fma(s11, q11, s12 * q12);
+    F.P[q][1] = vq * fma(s11, q12, s12 * q22);
+    F.P[q][2] = vq * fma(s12, q11, s22 * q12);
+    F.P[q][3] = vq * fma(s12, q12, s22 * q22);
   }
   // V_h in family order (as the oracle), then T_ij of bond jj
   double vh = 0.0;
@@ -186,11 +194,11 @@ __global__ void __launch_bounds__(32 * kBaWarps) k_ba_pass_a(Fp64Args a, BondAss
     double m11 = 0.0, m12 = 0.0, m21 = 0.0, m22 = 0.0;
     for (int q = 0; q < n; ++q) {
       // w(jj, q) = w(q, jj), kept for pairs of bonds < 32, recomputed for the others
-      const double wv = (jj < 32 && q < 32 ? F.wrow[q][jj] : wf(F, jj, q)) * F.vv[q];
-      m11 = fma(wv, F.P[q][0], m11);
-      m12 = fma(wv, F.P[q][1], m12);
-      m21 = fma(wv, F.P[q][2], m21);
-      m22 = fma(wv, F.P[q][3], m22);
+      const double w = jj < 32 && q < 32 ? F.wrow[q][jj] : wf(F, jj, q);
+      m11 = fma(w, F.P[q][0], m11);
+      m12 = fma(w, F.P[q][1], m12);
+      m21 = fma(w, F.P[q][2], m21);
+      m22 = fma(w, F.P[q][3], m22);
     }
     const double ex = F.ex[jj], ey = F.ey[jj];
     b.tb[F.slot[jj]] = make_double2(fma(m11 * rv, ex, (m12 * rv) * ey), fma(m21 * rv, ex, (m22 * rv) * ey));
