@@ -56,17 +56,28 @@ struct BaWeight {
   double n1, inv_wlen, n2;
   int n2i;      // n2 as a small integer (-1: use pow)
   bool direct;  // exp(-n1 |L_b - L_k| / l) evaluated directly (the factors could overflow)
+  // The comparisons run on the integer pipe, on the bit patterns (the FP64 pipe
+  // is the kernel's bound): c is finite, so |c| > 1 exactly when its magnitude
+  // bits exceed those of 1.0, and lengths are >= 0, whose bit patterns order as
+  // their values.  The power starts from its first factor and skips the last,
+  // unused squaring: the same products as pw = 1, pw *= base for each set bit.
   __device__ __forceinline__ double operator()(const BaFamily& F, int b, int k) const {
     double c = fma(F.ex[b], F.ex[k], F.ey[b] * F.ey[k]) * (F.rl[b] * F.rl[k]);
-    c = c > 1.0 ? 1.0 : (c < -1.0 ? -1.0 : c);
+    const long long cb = __double_as_longlong(c);
+    if ((cb & 0x7FFFFFFFFFFFFFFFll) > 0x3FF0000000000000ll) c = cb < 0 ? -1.0 : 1.0;
     const double x = fma(0.5, c, 0.5);
     double pw;
     if (n2i >= 0) {
       pw = 1.0;
       double base = x;
-      for (int e = n2i; e; e >>= 1) {
-        if (e & 1) pw *= base;
-        base *= base;
+      bool first = true;
+      for (int e = n2i; e;) {
+        if (e & 1) {
+          pw = first ? base : pw * base;
+          first = false;
+        }
+        e >>= 1;
+        if (e) base *= base;
       }
     } else {
       pw = pow(x, n2);
@@ -75,7 +86,8 @@ struct BaWeight {
     if (direct)
       ew = exp(-n1 * (fabs(F.len[b] - F.len[k]) * inv_wlen));
     else
-      ew = F.len[b] >= F.len[k] ? F.ep[k] * F.em[b] : F.ep[b] * F.em[k];
+      ew = __double_as_longlong(F.len[b]) >= __double_as_longlong(F.len[k]) ? F.ep[k] * F.em[b]
+                                                                          : F.ep[b] * F.em[k];
     return ew * pw;
   }
 };
