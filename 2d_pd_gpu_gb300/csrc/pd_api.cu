@@ -58,6 +58,8 @@ struct pd_ctx {
   // bond-associated mode
   double2* tb = nullptr;
   int64_t* rslot = nullptr;
+  double2* ba_lr = nullptr;  // bond-associated mode, per slot: |xi|, 1/|xi|
+  double2* ba_ex = nullptr;  // and exp(+-n1 |xi| / l)
   int32_t max_family = 0;
   // pd_step_host's copy / compute pipeline (streams and events, see plan_slabs)
   cudaStream_t io[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -186,6 +188,8 @@ void free_families(pd_ctx* c) {
   dfree(c->br2);
   dfree(c->tb);
   dfree(c->rslot);
+  dfree(c->ba_lr);
+  dfree(c->ba_ex);
   c->sell = pd::SellLayout{};
   c->slab_bnd.clear();
   c->slab_need.clear();
@@ -272,15 +276,26 @@ pd::BondAssoc ba_args(pd_ctx* c) {
   b.inv_wlen = c->p.weight_len > 0.0 ? 1.0 / c->p.weight_len : 0.0;
   b.tb = c->tb;
   b.rslot = c->rslot;
+  b.lr = c->ba_lr;
+  b.ex = c->ba_ex;
   return b;
 }
 
-// Buffers and reverse-slot index of the bond-associated mode.
+// Buffers and reverse-slot index of the bond-associated mode, and its
+// per-bond constants for the current weights (recomputed on every call: the
+// parameters may have changed).
 int ensure_ba(pd_ctx* c) {
   if (!bond_assoc(c) || !c->has_families) return PD_OK;
   if (c->max_family > 64) return fail(c, PD_ERR_CAPACITY, "bond-associated mode: families are limited to 64 bonds");
-  if (c->tb) return PD_OK;
   const size_t ns = (size_t)(c->sell.nslots > 0 ? c->sell.nslots : 1);
+  if (c->tb) {
+    pd::launch_ba_bonds(fp64_args(c), ba_args(c), c->sell.nslots, c->stream);
+    PD_CK(c, cudaGetLastError());
+    return PD_OK;
+  }
+  PD_CK(c, cudaMalloc(&c->ba_lr, ns * sizeof(double2)));
+  PD_CK(c, cudaMalloc(&c->ba_ex, ns * sizeof(double2)));
+  pd::launch_ba_bonds(fp64_args(c), ba_args(c), c->sell.nslots, c->stream);
   PD_CK(c, cudaMalloc(&c->tb, ns * sizeof(double2)));
   PD_CK(c, cudaMalloc(&c->rslot, ns * sizeof(int64_t)));
   PD_CK(c, cudaMemsetAsync(c->tb, 0, ns * sizeof(double2), c->stream));

@@ -119,13 +119,14 @@ __global__ void __launch_bounds__(32 * kBaWarps) k_ba_pass_a(Fp64Args a, BondAss
     if (j >= 0 && q < kBaMax) {
       const double2 e = a.bxi[s];
       const double2 uj = a.u[j];
-      const double l = sqrt(e.x * e.x + e.y * e.y);
+      const double2 lr = b.lr[s], ee = b.ex[s];  // k_ba_bonds
+      const double l = lr.x;
       F.ex[q] = e.x;
       F.ey[q] = e.y;
       F.len[q] = l;
-      F.rl[q] = 1.0 / l;
-      F.ep[q] = exp(b.n1 * (l * b.inv_wlen));
-      F.em[q] = exp(-b.n1 * (l * b.inv_wlen));
+      F.rl[q] = lr.y;
+      F.ep[q] = ee.x;
+      F.em[q] = ee.y;
       const double vj = a.vol[j], dx = uj.x - ui.x, dy = uj.y - ui.y;
       const double t0 = vj * e.x, t1 = vj * e.y;
       F.vv[q] = vj;
@@ -274,6 +275,17 @@ __global__ void __launch_bounds__(kBlock) k_ba_pass_b(Fp64Args a, BondAssoc b) {
   }
 }
 
+// The per-bond constants of the weights, once per slot (they depend on the
+// reference geometry and on n1 and l only): |xi|, 1/|xi|, exp(+-n1 |xi| / l).
+__global__ void k_ba_bonds(Fp64Args a, BondAssoc b, int64_t nslots) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nslots || a.nbr[s] < 0) return;
+  const double2 e = a.bxi[s];
+  const double l = sqrt(e.x * e.x + e.y * e.y);
+  b.lr[s] = make_double2(l, 1.0 / l);
+  b.ex[s] = make_double2(exp(b.n1 * (l * b.inv_wlen)), exp(-b.n1 * (l * b.inv_wlen)));
+}
+
 // rslot[s] = slot of (j, i) in j's SELL rows, for every slot s = (i, j).
 __global__ void k_ba_reverse(Fp64Args a, BondAssoc b, unsigned long long* counters) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -306,6 +318,10 @@ __global__ void k_ba_reverse(Fp64Args a, BondAssoc b, unsigned long long* counte
 
 void launch_ba_reverse(const Fp64Args& a, const BondAssoc& b, cudaStream_t s) {
   if (a.n > 0) k_ba_reverse<<<(unsigned)blocks_for(a.n), kBlock, 0, s>>>(a, b, a.counters);
+}
+
+void launch_ba_bonds(const Fp64Args& a, const BondAssoc& b, int64_t nslots, cudaStream_t s) {
+  if (nslots > 0) k_ba_bonds<<<(unsigned)((nslots + kBlock - 1) / kBlock), kBlock, 0, s>>>(a, b, nslots);
 }
 
 void launch_ba_pass_a(const Fp64Args& a, const BondAssoc& b, cudaStream_t s) {

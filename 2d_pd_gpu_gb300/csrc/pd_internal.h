@@ -112,6 +112,8 @@ struct BondAssoc {
   double n1, n2, inv_wlen;
   double2* tb;     // T_ij per bond slot
   int64_t* rslot;  // slot of the reverse bond (j, i)
+  double2* lr;     // per bond slot: |xi|, 1 / |xi|
+  double2* ex;     // per bond slot: exp(n1 |xi| / l), exp(-n1 |xi| / l) (for the weights n1, l of the call)
 };
 
 // Mazars damage (pd_mazars.cu): law constants and per-slot history.
@@ -243,6 +245,7 @@ int batch_occupancy_fp64(const BatchLaunch& cfg);  // resident persistent blocks
 
 // ---- bond-associated FP64 step (pd_bondassoc.cu); families <= 64 bonds
 void launch_ba_reverse(const Fp64Args& a, const BondAssoc& b, cudaStream_t s);
+void launch_ba_bonds(const Fp64Args& a, const BondAssoc& b, int64_t nslots, cudaStream_t s);  // lr, ex
 void launch_ba_pass_a(const Fp64Args& a, const BondAssoc& b, cudaStream_t s);
 void launch_ba_pass_b(const Fp64Args& a, const BondAssoc& b, int mode, cudaStream_t s);
 

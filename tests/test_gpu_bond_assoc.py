@@ -79,6 +79,25 @@ def test_bond_assoc_wide_families_match_oracle(pdg, po, horizon):
     assert normwise(u, sim.u) < 1e-12 and normwise(v, sim.v) < 1e-12 and normwise(f, sim.f) < 1e-11
 
 
+def test_bond_assoc_weights_follow_set_params(pdg, hassa):
+    """The per-bond weight constants (|xi|, 1/|xi|, exp(+-n1 |xi| / l)) are formed
+    once per slot; pd_set_params with other weights re-forms them: a context
+    switched from n1 = 4, n2 = 3 (and a longer weight length) to the reference's
+    n1 = n2 = 10 steps bit for bit as one created with them."""
+    dx, hor = hassa["params"][0], hassa["params"][1]
+    a = _ctx(pdg, hassa, n1=4.0, n2=3.0)
+    a.set_params(weight_len=1.5 * hor * dx)
+    a.step(2)  # the constants formed for the first weights
+    a.set_params(n1=10.0, n2=10.0, weight_len=hor * dx)
+    b = _ctx(pdg, hassa)
+    u, v, f = a.state()
+    b.set_state(u=u, v=v, f=f)
+    a.step(2)
+    b.step(2)
+    for x, y in zip(a.state(), b.state()):
+        assert np.array_equal(x, y)
+
+
 def test_bond_assoc_compute_velocity_dropin(pdg, hassa):
     """pd_compute_velocity in the bond-associated mode after the reference's host drift."""
     ctx = _ctx(pdg, hassa)
