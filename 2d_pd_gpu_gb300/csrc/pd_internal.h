@@ -174,6 +174,7 @@ struct MixedArgs {
   float s2, tau2;       // stretch limit factor, Es dt^2 / (rho Ls^2)
   float k_hg;           // k Vs Ls^2 / Es
   double inv_ls, inv_vs, v_scale, f_scale, det_guard, damage_fail;
+  double ls, v_unscale, f_unscale;  // 1 / inv_ls, 1 / v_scale, 1 / f_scale: the FP64 state out by products
   unsigned long long* counters;
   int32_t brk;  // bond breaking on (s_c > 0)
   int32_t wmax;  // widest SELL chunk (slot rows), sizes the staged passes' shared memory

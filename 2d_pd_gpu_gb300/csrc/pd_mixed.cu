@@ -298,9 +298,9 @@ __device__ __forceinline__ void export_state(const MixedArgs& a, int64_t p, cons
                                              float fy) {
   const int64_t i = a.member[p];
   if (i < 0) return;
-  a.out_u[i] = make_double2(((double)u.x + (double)u.z) / a.inv_ls, ((double)u.y + (double)u.w) / a.inv_ls);
-  a.out_v[i] = make_double2(((double)v.x + (double)v.z) / a.v_scale, ((double)v.y + (double)v.w) / a.v_scale);
-  a.out_f[i] = make_double2((double)fx / a.f_scale, (double)fy / a.f_scale);
+  a.out_u[i] = make_double2(((double)u.x + (double)u.z) * a.ls, ((double)u.y + (double)u.w) * a.ls);
+  a.out_v[i] = make_double2(((double)v.x + (double)v.z) * a.v_unscale, ((double)v.y + (double)v.w) * a.v_unscale);
+  a.out_f[i] = make_double2((double)fx * a.f_unscale, (double)fy * a.f_unscale);
 }
 
 // Pass B of the particle at SELL position p (force gather, kick, optional
@@ -946,15 +946,15 @@ __global__ void k_from_mixed(MixedArgs a, double2* u, double2* v, double2* f) {
   const int64_t p = a.pos_of[i];
   if (u) {
     const float4 q = a.us[p];
-    u[i] = make_double2(((double)q.x + (double)q.z) / a.inv_ls, ((double)q.y + (double)q.w) / a.inv_ls);
+    u[i] = make_double2(((double)q.x + (double)q.z) * a.ls, ((double)q.y + (double)q.w) * a.ls);
   }
   if (v) {
     const float4 q = a.vs[p];
-    v[i] = make_double2(((double)q.x + (double)q.z) / a.v_scale, ((double)q.y + (double)q.w) / a.v_scale);
+    v[i] = make_double2(((double)q.x + (double)q.z) * a.v_unscale, ((double)q.y + (double)q.w) * a.v_unscale);
   }
   if (f) {
     const float2 q = a.fs[p];
-    f[i] = make_double2((double)q.x / a.f_scale, (double)q.y / a.f_scale);
+    f[i] = make_double2((double)q.x * a.f_unscale, (double)q.y * a.f_unscale);
   }
 }
 
