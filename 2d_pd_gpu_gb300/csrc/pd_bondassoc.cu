@@ -16,8 +16,10 @@
 //
 // Pass A runs one warp per particle and one lane per bond (families <= 64
 // bonds, two per lane): the family's bond data is staged in shared memory,
-// lane q sums K_q and D_q over k in family order (the oracle's order), and,
-// once the P_b of every bond are in shared memory, lane j sums T_ij over b.
+// lane q sums D_q over k in family order (the oracle's order), and, once the
+// P_b of every bond are in shared memory, lane j sums T_ij over b.  The mode
+// breaks no bond, so each K_q (summed the same way) and its inverse are formed
+// once per slot at set-up and on every parameter change (k_ba_pass_a<true>).
 // The weight matrix is symmetric bit for bit (its products commute, and the
 // exponential factor is ordered by the two lengths), so a family of <= 32
 // bonds evaluates its lower triangle once, spread over all 32 lanes, into
@@ -41,12 +43,12 @@ namespace pd {
 namespace {
 
 constexpr int kBaMax = 64;
-constexpr int kBaWarps = 2;  // particles per block of pass A (35 KB of shared memory per block)
+constexpr int kBaWarps = 2;  // particles per block of pass A (32 KB of shared memory per block)
 
 struct BaFamily {  // one particle's bonds, in family order
   double ex[kBaMax], ey[kBaMax], rl[kBaMax], len[kBaMax], ep[kBaMax], em[kBaMax], vv[kBaMax];
-  double M[kBaMax][3];  // V_k xi_k (x) xi_k: (xx, xy, yy)
-  double N[kBaMax][4];  // V_k d_k (x) xi_k: (dx xx, dx xy, dy xx, dy xy) with xy = the xi components
+  // pass A: V_k d_k (x) xi_k (dx xi_x, dx xi_y, dy xi_x, dy xi_y); the K table: V_k xi_k (x) xi_k (xx, xy, yy)
+  double S[kBaMax][4];
   double P[kBaMax][4];  // V_b sigma_b K_b^-1
   int64_t slot[kBaMax];
   double wrow[32][32];  // wrow[k][l] = w(l, k) for bonds l, k < 32
@@ -92,6 +94,11 @@ struct BaWeight {
   }
 };
 
+// KTAB: the set-up form (launch_ba_bonds), which forms every bond's weighted
+// shape tensor K_b and writes K_b^-1 and its det-guard flag per slot (the
+// mode breaks no bond, so K_b is fixed); the same operations in the same
+// order as the pass itself would, so reading them back changes no result.
+template <bool KTAB>
 __global__ void __launch_bounds__(32 * kBaWarps) k_ba_pass_a(Fp64Args a, BondAssoc b) {
   __shared__ BaFamily fam[kBaWarps];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -118,7 +125,6 @@ __global__ void __launch_bounds__(32 * kBaWarps) k_ba_pass_a(Fp64Args a, BondAss
     const int q = n + __popc(m & ((1u << lane) - 1u));
     if (j >= 0 && q < kBaMax) {
       const double2 e = a.bxi[s];
-      const double2 uj = a.u[j];
       const double2 lr = b.lr[s], ee = b.ex[s];  // k_ba_bonds
       const double l = lr.x;
       F.ex[q] = e.x;
@@ -127,16 +133,21 @@ __global__ void __launch_bounds__(32 * kBaWarps) k_ba_pass_a(Fp64Args a, BondAss
       F.rl[q] = lr.y;
       F.ep[q] = ee.x;
       F.em[q] = ee.y;
-      const double vj = a.vol[j], dx = uj.x - ui.x, dy = uj.y - ui.y;
+      const double vj = a.vol[j];
       const double t0 = vj * e.x, t1 = vj * e.y;
       F.vv[q] = vj;
-      F.M[q][0] = t0 * e.x;
-      F.M[q][1] = t0 * e.y;
-      F.M[q][2] = t1 * e.y;
-      F.N[q][0] = dx * t0;
-      F.N[q][1] = dx * t1;
-      F.N[q][2] = dy * t0;
-      F.N[q][3] = dy * t1;
+      if (KTAB) {
+        F.S[q][0] = t0 * e.x;
+        F.S[q][1] = t0 * e.y;
+        F.S[q][2] = t1 * e.y;
+      } else {
+        const double2 uj = a.u[j];
+        const double dx = uj.x - ui.x, dy = uj.y - ui.y;
+        F.S[q][0] = dx * t0;
+        F.S[q][1] = dx * t1;
+        F.S[q][2] = dy * t0;
+        F.S[q][3] = dy * t1;
+      }
       F.slot[q] = s;
       lmax = fmax(lmax, l);
     }
@@ -160,9 +171,9 @@ __global__ void __launch_bounds__(32 * kBaWarps) k_ba_pass_a(Fp64Args a, BondAss
     }
     __syncwarp();
   }
-  // P_b = sigma_b K_b^-1 of bond q
+  // P_b = sigma_b K_b^-1 of bond q (KTAB: K_b^-1)
   for (int q = lane; q < n; q += 32) {
-    double k11 = 0.0, k12 = 0.0, k22 = 0.0, d11 = 0.0, d12 = 0.0, d21 = 0.0, d22 = 0.0;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;  // KTAB: k11, k12, k22; else d11, d12, d21, d22
     for (int k = 0; k < n; ++k) {
       double wqk;
       if (tri) {
@@ -171,21 +182,32 @@ __global__ void __launch_bounds__(32 * kBaWarps) k_ba_pass_a(Fp64Args a, BondAss
         wqk = wf(F, q, k);
         if (q < 32 && k < 32) F.wrow[k][q] = wqk;  // (q == lane: the thread's own row, read back below)
       }
-      k11 = fma(wqk, F.M[k][0], k11);
-      k12 = fma(wqk, F.M[k][1], k12);
-      k22 = fma(wqk, F.M[k][2], k22);
-      d11 = fma(wqk, F.N[k][0], d11);
-      d12 = fma(wqk, F.N[k][1], d12);
-      d21 = fma(wqk, F.N[k][2], d21);
-      d22 = fma(wqk, F.N[k][3], d22);
+      s0 = fma(wqk, F.S[k][0], s0);
+      s1 = fma(wqk, F.S[k][1], s1);
+      s2 = fma(wqk, F.S[k][2], s2);
+      if (!KTAB) s3 = fma(wqk, F.S[k][3], s3);
     }
-    const double det = fma(k11, k22, -(k12 * k12));
-    if (!(det > a.det_guard * (k11 * k22))) {
+    const int64_t sl = F.slot[q];
+    if (KTAB) {
+      const double k11 = s0, k12 = s1, k22 = s2;
+      const double det = fma(k11, k22, -(k12 * k12));
+      if (!(det > a.det_guard * (k11 * k22))) {
+        b.kq0[sl] = make_double2(0.0, 0.0);
+        b.kq1[sl] = make_double2(0.0, 1.0);
+        continue;
+      }
+      const double r = 1.0 / det;
+      b.kq0[sl] = make_double2(k22 * r, -k12 * r);
+      b.kq1[sl] = make_double2(k11 * r, 0.0);
+      continue;
+    }
+    const double d11 = s0, d12 = s1, d21 = s2, d22 = s3;
+    const double2 kq0 = b.kq0[sl], kq1 = b.kq1[sl];
+    if (__double_as_longlong(kq1.y) != 0) {  // K_b failed the det guard
       F.P[q][0] = F.P[q][1] = F.P[q][2] = F.P[q][3] = 0.0;
       continue;
     }
-    const double r = 1.0 / det;
-    const double q11 = k22 * r, q12 = -k12 * r, q22 = k11 * r;
+    const double q11 = kq0.x, q12 = kq0.y, q22 = kq1.x;
     const double g11 = fma(d11, q11, d12 * q12), g12 = fma(d11, q12, d12 * q22);
     const double g21 = fma(d21, q11, d22 * q12), g22 = fma(d21, q12, d22 * q22);
     const double e11 = g11, e22 = g22, e12 = 0.5 * (g12 + g21);
@@ -198,6 +220,7 @@ __global__ void __launch_bounds__(32 * kBaWarps) k_ba_pass_a(Fp64Args a, BondAss
     F.P[q][2] = vq * fma(s12, q11, s22 * q12);
     F.P[q][3] = vq * fma(s12, q12, s22 * q22);
   }
+  if (KTAB) return;
   // V_h in family order (as the oracle), then T_ij of bond jj
   double vh = 0.0;
   for (int k = 0; k < n; ++k) vh = vh + F.vv[k];
@@ -322,10 +345,11 @@ void launch_ba_reverse(const Fp64Args& a, const BondAssoc& b, cudaStream_t s) {
 
 void launch_ba_bonds(const Fp64Args& a, const BondAssoc& b, int64_t nslots, cudaStream_t s) {
   if (nslots > 0) k_ba_bonds<<<(unsigned)((nslots + kBlock - 1) / kBlock), kBlock, 0, s>>>(a, b, nslots);
+  if (a.n > 0) k_ba_pass_a<true><<<(unsigned)((a.n + kBaWarps - 1) / kBaWarps), 32 * kBaWarps, 0, s>>>(a, b);
 }
 
 void launch_ba_pass_a(const Fp64Args& a, const BondAssoc& b, cudaStream_t s) {
-  if (a.n > 0) k_ba_pass_a<<<(unsigned)((a.n + kBaWarps - 1) / kBaWarps), 32 * kBaWarps, 0, s>>>(a, b);
+  if (a.n > 0) k_ba_pass_a<false><<<(unsigned)((a.n + kBaWarps - 1) / kBaWarps), 32 * kBaWarps, 0, s>>>(a, b);
 }
 
 void launch_ba_pass_b(const Fp64Args& a, const BondAssoc& b, int mode, cudaStream_t s) {

@@ -114,6 +114,8 @@ struct BondAssoc {
   int64_t* rslot;  // slot of the reverse bond (j, i)
   double2* lr;     // per bond slot: |xi|, 1 / |xi|
   double2* ex;     // per bond slot: exp(n1 |xi| / l), exp(-n1 |xi| / l) (for the weights n1, l of the call)
+  double2* kq0;    // per bond slot: K_b^-1 (q11, q12)
+  double2* kq1;    // per bond slot: (q22, 1 if K_b fails the det guard else 0)
 };
 
 // Mazars damage (pd_mazars.cu): law constants and per-slot history.
@@ -246,7 +248,8 @@ int batch_occupancy_fp64(const BatchLaunch& cfg);  // resident persistent blocks
 
 // ---- bond-associated FP64 step (pd_bondassoc.cu); families <= 64 bonds
 void launch_ba_reverse(const Fp64Args& a, const BondAssoc& b, cudaStream_t s);
-void launch_ba_bonds(const Fp64Args& a, const BondAssoc& b, int64_t nslots, cudaStream_t s);  // lr, ex
+// lr, ex, then kq0, kq1 (the weighted shape tensors' inverses: the mode breaks no bond, so K_b is fixed)
+void launch_ba_bonds(const Fp64Args& a, const BondAssoc& b, int64_t nslots, cudaStream_t s);
 void launch_ba_pass_a(const Fp64Args& a, const BondAssoc& b, cudaStream_t s);
 void launch_ba_pass_b(const Fp64Args& a, const BondAssoc& b, int mode, cudaStream_t s);
 
