@@ -60,8 +60,9 @@ struct pd_ctx {
   int64_t* rslot = nullptr;
   double2* ba_lr = nullptr;  // bond-associated mode, per slot: |xi|, 1/|xi|
   double2* ba_ex = nullptr;  // exp(+-n1 |xi| / l)
-  double2* ba_kq0 = nullptr;  // and K_b^-1 with its det-guard flag
+  double2* ba_kq0 = nullptr;  // K_b^-1 with its det-guard flag
   double2* ba_kq1 = nullptr;
+  double* ba_wtri = nullptr;  // and, per particle, its weight matrix's lower triangle
   int32_t max_family = 0;
   // pd_step_host's copy / compute pipeline (streams and events, see plan_slabs)
   cudaStream_t io[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -194,6 +195,7 @@ void free_families(pd_ctx* c) {
   dfree(c->ba_ex);
   dfree(c->ba_kq0);
   dfree(c->ba_kq1);
+  dfree(c->ba_wtri);
   c->sell = pd::SellLayout{};
   c->slab_bnd.clear();
   c->slab_need.clear();
@@ -284,6 +286,7 @@ pd::BondAssoc ba_args(pd_ctx* c) {
   b.ex = c->ba_ex;
   b.kq0 = c->ba_kq0;
   b.kq1 = c->ba_kq1;
+  b.wtri = c->ba_wtri;
   return b;
 }
 
@@ -303,6 +306,7 @@ int ensure_ba(pd_ctx* c) {
   PD_CK(c, cudaMalloc(&c->ba_ex, ns * sizeof(double2)));
   PD_CK(c, cudaMalloc(&c->ba_kq0, ns * sizeof(double2)));
   PD_CK(c, cudaMalloc(&c->ba_kq1, ns * sizeof(double2)));
+  PD_CK(c, cudaMalloc(&c->ba_wtri, (size_t)(c->n > 0 ? c->n : 1) * (size_t)pd::kBaTri * sizeof(double)));
   pd::launch_ba_bonds(fp64_args(c), ba_args(c), c->sell.nslots, c->stream);
   PD_CK(c, cudaMalloc(&c->tb, ns * sizeof(double2)));
   PD_CK(c, cudaMalloc(&c->rslot, ns * sizeof(int64_t)));

@@ -18,8 +18,9 @@
 // bonds, two per lane): the family's bond data is staged in shared memory,
 // lane q sums D_q over k in family order (the oracle's order), and, once the
 // P_b of every bond are in shared memory, lane j sums T_ij over b.  The mode
-// breaks no bond, so each K_q (summed the same way) and its inverse are formed
-// once per slot at set-up and on every parameter change (k_ba_pass_a<true>).
+// breaks no bond, so the weights of families of <= 32 bonds, each K_q (summed
+// the same way) and its inverse are formed once, at set-up and on every
+// parameter change (k_ba_pass_a<true>).
 // The weight matrix is symmetric bit for bit (its products commute, and the
 // exponential factor is ordered by the two lengths), so a family of <= 32
 // bonds evaluates its lower triangle once, spread over all 32 lanes, into
@@ -94,9 +95,11 @@ struct BaWeight {
   }
 };
 
-// KTAB: the set-up form (launch_ba_bonds), which forms every bond's weighted
+// KTAB: the set-up form (launch_ba_bonds), which evaluates the weights (kept
+// per particle for families of <= 32 bonds), forms every bond's weighted
 // shape tensor K_b and writes K_b^-1 and its det-guard flag per slot (the
-// mode breaks no bond, so K_b is fixed); the same operations in the same
+// mode breaks no bond and the weights depend on the reference geometry and
+// the parameters only, so both are fixed); the same operations in the same
 // order as the pass itself would, so reading them back changes no result.
 template <bool KTAB>
 __global__ void __launch_bounds__(32 * kBaWarps) k_ba_pass_a(Fp64Args a, BondAssoc b) {
@@ -159,13 +162,21 @@ __global__ void __launch_bounds__(32 * kBaWarps) k_ba_pass_a(Fp64Args a, BondAss
   __syncwarp();
   const bool tri = n <= 32;
   if (tri) {  // pair p = k (k + 1) / 2 + q, q <= k, of the lower triangle
+    // (the set-up form evaluates it and keeps it per particle; the step reads it back)
     const int npair = n * (n + 1) / 2;
+    double* wt = b.wtri + i * kBaTri;
     for (int p = lane; p < npair; p += 32) {
       int k = (int)((sqrtf(8.0f * (float)p + 1.0f) - 1.0f) * 0.5f);
       if ((k + 1) * (k + 2) / 2 <= p) ++k;
       if (k * (k + 1) / 2 > p) --k;
       const int q = p - k * (k + 1) / 2;
-      const double wqk = wf(F, q, k);
+      double wqk;
+      if (KTAB) {
+        wqk = wf(F, q, k);
+        wt[p] = wqk;
+      } else {
+        wqk = wt[p];
+      }
       F.wrow[k][q] = wqk;
       F.wrow[q][k] = wqk;
     }
@@ -299,7 +310,8 @@ __global__ void __launch_bounds__(kBlock) k_ba_pass_b(Fp64Args a, BondAssoc b) {
 }
 
 // The per-bond constants of the weights, once per slot (they depend on the
-// reference geometry and on n1 and l only): |xi|, 1/|xi|, exp(+-n1 |xi| / l).
+// reference geometry and on n1 and l only): |xi|, 1/|xi|, exp(+-n1 |xi| / l);
+// k_ba_pass_a<true> then forms the weights and K_b^-1 from them.
 __global__ void k_ba_bonds(Fp64Args a, BondAssoc b, int64_t nslots) {
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nslots || a.nbr[s] < 0) return;

@@ -116,7 +116,9 @@ struct BondAssoc {
   double2* ex;     // per bond slot: exp(n1 |xi| / l), exp(-n1 |xi| / l) (for the weights n1, l of the call)
   double2* kq0;    // per bond slot: K_b^-1 (q11, q12)
   double2* kq1;    // per bond slot: (q22, 1 if K_b fails the det guard else 0)
+  double* wtri;    // per particle with <= 32 bonds: its weight matrix's lower triangle (kBaTri doubles)
 };
+constexpr int64_t kBaTri = 32 * 33 / 2;
 
 // Mazars damage (pd_mazars.cu): law constants and per-slot history.
 struct MazarsArgs {
