@@ -302,14 +302,16 @@ int ensure_ba(pd_ctx* c) {
     PD_CK(c, cudaGetLastError());
     return PD_OK;
   }
-  PD_CK(c, cudaMalloc(&c->ba_lr, ns * sizeof(double2)));
-  PD_CK(c, cudaMalloc(&c->ba_ex, ns * sizeof(double2)));
-  PD_CK(c, cudaMalloc(&c->ba_kq0, ns * sizeof(double2)));
-  PD_CK(c, cudaMalloc(&c->ba_kq1, ns * sizeof(double2)));
-  PD_CK(c, cudaMalloc(&c->ba_wtri, (size_t)(c->n > 0 ? c->n : 1) * (size_t)pd::kBaTri * sizeof(double)));
+  // (each allocated once: a call that failed part-way is retried without leaking)
+  if (!c->ba_lr) PD_CK(c, cudaMalloc(&c->ba_lr, ns * sizeof(double2)));
+  if (!c->ba_ex) PD_CK(c, cudaMalloc(&c->ba_ex, ns * sizeof(double2)));
+  if (!c->ba_kq0) PD_CK(c, cudaMalloc(&c->ba_kq0, ns * sizeof(double2)));
+  if (!c->ba_kq1) PD_CK(c, cudaMalloc(&c->ba_kq1, ns * sizeof(double2)));
+  if (!c->ba_wtri)
+    PD_CK(c, cudaMalloc(&c->ba_wtri, (size_t)(c->n > 0 ? c->n : 1) * (size_t)pd::kBaTri * sizeof(double)));
   pd::launch_ba_bonds(fp64_args(c), ba_args(c), c->sell.nslots, c->stream);
+  if (!c->rslot) PD_CK(c, cudaMalloc(&c->rslot, ns * sizeof(int64_t)));
   PD_CK(c, cudaMalloc(&c->tb, ns * sizeof(double2)));
-  PD_CK(c, cudaMalloc(&c->rslot, ns * sizeof(int64_t)));
   PD_CK(c, cudaMemsetAsync(c->tb, 0, ns * sizeof(double2), c->stream));
   PD_CK(c, cudaMemsetAsync(c->counters + pd::CNT_ERROR, 0, sizeof(unsigned long long), c->stream));
   pd::launch_ba_reverse(fp64_args(c), ba_args(c), c->stream);

@@ -138,6 +138,17 @@ def test_bond_assoc_compute_velocity_pinned_equals_staged(pdg, hassa):
         x.free()
 
 
+def test_bond_assoc_rejects_asymmetric_families(pdg):
+    """The mode pairs every bond with its reverse: caller-supplied families in
+    which 1 lists 2 but 2 does not list 1 are refused (the unmatched bond is
+    made inert on the device, so nothing reads outside the families)."""
+    x = np.array([[0.0, 0.0], [1e-3, 0.0], [2e-3, 0.0]])
+    ctx = pdg.native.Context(pdg.default_params(s_c=0.0, n1=10.0, n2=10.0, weight_len=3e-3))
+    ctx.set_particles(x, np.full(3, 1e-9))
+    with pytest.raises(pdg.PdError, match="symmetric"):
+        ctx.set_families(np.array([0, 1, 3, 3]), np.array([1, 0, 2]))
+
+
 def test_bond_assoc_rejects_breaking_and_mixed(pdg):
     with pytest.raises(pdg.PdError):
         pdg.native.Context(pdg.default_params(n1=10.0, n2=10.0, weight_len=3.0, s_c=5e-4))
