@@ -14,29 +14,33 @@
 // T_ji through the reverse slot index and applies the kick (+ the next
 // drift) as the classic form.
 //
+// The mode breaks no bond, and the weights depend on the reference geometry
+// and the parameters only, so what does not involve the displacements is
+// formed once, at set-up and on every parameter change, by the set-up form of
+// pass A (k_ba_pass_a<true>, after k_ba_bonds): per slot |xi|, 1/|xi|,
+// exp(+-n1 |xi| / l) and K_b^-1 with its det-guard flag; per particle with
+// <= 32 bonds, the lower triangle of its weight matrix.
+//
 // Pass A runs one warp per particle and one lane per bond (families <= 64
 // bonds, two per lane): the family's bond data is staged in shared memory,
-// lane q sums D_q over k in family order (the oracle's order), and, once the
-// P_b of every bond are in shared memory, lane j sums T_ij over b.  The mode
-// breaks no bond, so the weights of families of <= 32 bonds, each K_q (summed
-// the same way) and its inverse are formed once, at set-up and on every
-// parameter change (k_ba_pass_a<true>).
+// the weight triangle is loaded into a 32 x 32 matrix there, lane q sums D_q
+// over k in family order (the oracle's order) and forms V_q P_q, and, once
+// every P_b is in shared memory, lane j sums T_ij over b: 8 FP64 fma per
+// ordered pair of bonds.  A family of more than 32 bonds evaluates each lane's
+// weight row inside its D_q loop and keeps the rows of the first 32 bonds.
 // The weight matrix is symmetric bit for bit (its products commute, and the
-// exponential factor is ordered by the two lengths), so a family of <= 32
-// bonds evaluates its lower triangle once, spread over all 32 lanes, into
-// shared memory, and both sums read it there; a larger family evaluates each
-// lane's row inside the K_q loop and keeps the rows of the first 32 bonds.
-// The weight is evaluated in factored form: exp(-n1 |L_b - L_k| / l) =
-// e+(min L) e-(max L) with e+-(L) = exp(+-n1 L / l) per bond, the cosine as
-// (xi_b . xi_k) (1/L_b)(1/L_k), and an integer n2 <= 64 by repeated squaring
-// (pow otherwise; the direct exp where n1 L / l could overflow).  The sums
-// run in the oracle's order (ba_pass_a; --fmad=false, explicit fma()), but
-// the per-bond products V_k xi_k (x) xi_k, V_k d_k (x) xi_k and V_b P_b are
-// formed once per bond and then weighted (the oracle weights V_k first:
-// 7 + 4 FP64 operations per ordered pair here against 10 + 5), and the
-// weights differ from its libm exp / pow / division by a few ulp, so GPU and
-// oracle agree to rounding (1e-12 normwise), not bit for bit.  No bond
-// breaking here (the reference has none).
+// exponential factor is ordered by the two lengths), so only its lower
+// triangle is evaluated, spread over all 32 lanes.  The weight is evaluated in
+// factored form: exp(-n1 |L_b - L_k| / l) = e+(min L) e-(max L) with
+// e+-(L) = exp(+-n1 L / l) per bond, the cosine as (xi_b . xi_k) (1/L_b)(1/L_k),
+// and an integer n2 <= 64 by repeated squaring (pow otherwise; the direct exp
+// where n1 L / l could overflow).  The sums run in the oracle's order
+// (ba_pass_a; --fmad=false, explicit fma()), but the per-bond products
+// V_k xi_k (x) xi_k, V_k d_k (x) xi_k and V_b P_b are formed once per bond and
+// then weighted (the oracle weights V_k first), and the weights differ from
+// its libm exp / pow / division by a few ulp, so GPU and oracle agree to
+// rounding (1e-12 normwise), not bit for bit.  No bond breaking here (the
+// reference has none).
 #include "pd_internal.h"
 
 namespace pd {
