@@ -48,10 +48,10 @@ namespace pd {
 namespace {
 
 constexpr int kBaMax = 64;
-constexpr int kBaWarps = 2;  // particles per block of pass A (32 KB of shared memory per block)
+constexpr int kBaWarps = 2;  // particles per block of pass A (28 KB of shared memory per block: 7 per SM)
 
 struct BaFamily {  // one particle's bonds, in family order
-  double ex[kBaMax], ey[kBaMax], rl[kBaMax], len[kBaMax], ep[kBaMax], em[kBaMax], vv[kBaMax];
+  double ex[kBaMax], ey[kBaMax], vv[kBaMax];
   // pass A: V_k d_k (x) xi_k (dx xi_x, dx xi_y, dy xi_x, dy xi_y); the K table: V_k xi_k (x) xi_k (xx, xy, yy)
   double S[kBaMax][4];
   double P[kBaMax][4];  // V_b sigma_b K_b^-1
@@ -61,6 +61,8 @@ struct BaFamily {  // one particle's bonds, in family order
 
 struct BaWeight {
   double n1, inv_wlen, n2;
+  const double2* __restrict__ lr;  // per slot: |xi|, 1/|xi|
+  const double2* __restrict__ ex;  // per slot: exp(+-n1 |xi| / l)
   int n2i;      // n2 as a small integer (-1: use pow)
   bool direct;  // exp(-n1 |L_b - L_k| / l) evaluated directly (the factors could overflow)
   // The comparisons run on the integer pipe, on the bit patterns (the FP64 pipe
@@ -69,7 +71,9 @@ struct BaWeight {
   // their values.  The power starts from its first factor and skips the last,
   // unused squaring: the same products as pw = 1, pw *= base for each set bit.
   __device__ __forceinline__ double operator()(const BaFamily& F, int b, int k) const {
-    double c = fma(F.ex[b], F.ex[k], F.ey[b] * F.ey[k]) * (F.rl[b] * F.rl[k]);
+    const int64_t sb = F.slot[b], sk = F.slot[k];
+    const double2 lb = lr[sb], lk = lr[sk];  // |xi|, 1/|xi| (k_ba_bonds)
+    double c = fma(F.ex[b], F.ex[k], F.ey[b] * F.ey[k]) * (lb.y * lk.y);
     const long long cb = __double_as_longlong(c);
     if ((cb & 0x7FFFFFFFFFFFFFFFll) > 0x3FF0000000000000ll) c = cb < 0 ? -1.0 : 1.0;
     const double x = fma(0.5, c, 0.5);
@@ -91,10 +95,9 @@ struct BaWeight {
     }
     double ew;
     if (direct)
-      ew = exp(-n1 * (fabs(F.len[b] - F.len[k]) * inv_wlen));
+      ew = exp(-n1 * (fabs(lb.x - lk.x) * inv_wlen));
     else
-      ew = __double_as_longlong(F.len[b]) >= __double_as_longlong(F.len[k]) ? F.ep[k] * F.em[b]
-                                                                          : F.ep[b] * F.em[k];
+      ew = __double_as_longlong(lb.x) >= __double_as_longlong(lk.x) ? ex[sk].x * ex[sb].y : ex[sb].x * ex[sk].y;
     return ew * pw;
   }
 };
@@ -120,6 +123,8 @@ __global__ void __launch_bounds__(32 * kBaWarps) k_ba_pass_a(Fp64Args a, BondAss
   wf.n1 = b.n1;
   wf.inv_wlen = b.inv_wlen;
   wf.n2 = b.n2;
+  wf.lr = b.lr;
+  wf.ex = b.ex;
   wf.n2i = (b.n2 >= 0.0 && b.n2 <= 64.0 && b.n2 == floor(b.n2)) ? (int)b.n2 : -1;
   // stage the family (slots k = lane, lane + 32, compacted past empty slots in order)
   int n = 0;
@@ -132,14 +137,9 @@ __global__ void __launch_bounds__(32 * kBaWarps) k_ba_pass_a(Fp64Args a, BondAss
     const int q = n + __popc(m & ((1u << lane) - 1u));
     if (j >= 0 && q < kBaMax) {
       const double2 e = a.bxi[s];
-      const double2 lr = b.lr[s], ee = b.ex[s];  // k_ba_bonds
-      const double l = lr.x;
+      const double l = b.lr[s].x;  // k_ba_bonds
       F.ex[q] = e.x;
       F.ey[q] = e.y;
-      F.len[q] = l;
-      F.rl[q] = lr.y;
-      F.ep[q] = ee.x;
-      F.em[q] = ee.y;
       const double vj = a.vol[j];
       const double t0 = vj * e.x, t1 = vj * e.y;
       F.vv[q] = vj;
